@@ -1,0 +1,281 @@
+/*
+ * neofiz.h -- C ABI of libneofiz_gpu.so, a GB300 (sm_103a) implementation of the Neofiz
+ * explicit central-difference timestep.
+ *
+ * The reference has no FFI of its own: its surface is the Java class
+ * org.neofiz.solver.ExplicitSolver (src/main/java/org/neofiz/solver/ExplicitSolver.java)
+ * with its collaborators RigidWall and Contact. Each entry point below replaces one method
+ * of that surface and cites it. A Java caller binds these through java.lang.foreign; the
+ * binding is plain C: scalars, pointers to caller-owned host arrays, sizes.
+ *
+ * Ownership: nf_create deep-copies every mesh and material array to the device; nothing
+ * passed in is retained. Reads copy device -> caller buffer only when asked. A handle is
+ * single-owner and not thread-safe (as ExplicitSolver is); distinct handles may be driven from
+ * distinct host threads. Each handle owns one CUDA stream.
+ *
+ * Errors: every function returns an nf_status. NF_EINVAL corresponds to the reference's
+ * IllegalArgumentException and NF_ESTATE to IllegalStateException, with the same messages,
+ * readable through nf_last_error. Numerical faults detected on the device (a non-finite
+ * nodal value, a bounded wait that ran out) are reported through nf_status_word, never by
+ * trapping.
+ */
+#ifndef NEOFIZ_H
+#define NEOFIZ_H
+
+#include <stddef.h>
+#include <stdint.h>
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+typedef enum {
+    NF_OK = 0,
+    NF_EINVAL = 1,     /* IllegalArgumentException */
+    NF_ESTATE = 2,     /* IllegalStateException */
+    NF_EDEVICE = 3,    /* CUDA error, no device, or a device-side status bit */
+    NF_ETIMEOUT = 4,   /* a bounded device-side wait gave up */
+    NF_ENOMEM = 5
+} nf_status;
+
+/* core/Formulation.java:16-23 */
+enum { NF_AXISYMMETRIC = 0, NF_PLANE_STRAIN = 1, NF_PLANE_STRESS = 2 };
+/* solver/Integration.java:11-27 */
+enum { NF_FULL = 0, NF_REDUCED = 1 };
+/* solver/Kinematics.java:11-34 */
+enum { NF_SMALL_STRAIN = 0, NF_FINITE_STRAIN = 1 };
+
+/* mesh/QuadMesh.java:17-54: flat structure-of-arrays mesh, CCW element winding. */
+typedef struct {
+    int32_t node_count;
+    int32_t element_count;
+    int32_t pressure_edge_count;     /* edges, not ints */
+    const double *r;                 /* [node_count] reference radial coordinate, m */
+    const double *z;                 /* [node_count] reference axial coordinate, m */
+    const int32_t *conn;             /* [4 * element_count] */
+    const int32_t *pressure_edges;   /* [2 * pressure_edge_count], may be NULL if none */
+} nf_mesh;
+
+/* core/Material.java:20-21 and core/JohnsonCook.java:66-69. yield_stress = +inf is an
+ * elastic material (Material.java:61-63). */
+typedef struct {
+    double youngs_modulus;
+    double poisson_ratio;
+    double density;
+    double yield_stress;
+    double isotropic_hardening;
+    double kinematic_hardening;
+    int32_t has_johnson_cook;
+    int32_t reserved;
+    double jc_a, jc_b, jc_n, jc_c, jc_m;
+    double jc_reference_strain_rate;
+    double jc_room_temperature;
+    double jc_melt_temperature;
+    double jc_specific_heat;
+    double jc_taylor_quinney;
+} nf_material;
+
+typedef struct nf_solver nf_solver;
+
+/* Scalar state of the integrator (ExplicitSolver.java:191-234, getters :622-652, :825-840). */
+typedef struct {
+    double time;
+    double timestep;
+    double timestep_previous;
+    double reference_timestep;       /* dt0 */
+    double mass_scale;
+    double min_edge_squared;
+    double fastest_wave;
+    double eroded_energy;
+    double bore_pressure;            /* pressureAt(time), :826-828 */
+    int64_t steps;
+    int32_t eroded_elements;
+    int32_t inverted_elements;
+    int32_t node_count;
+    int32_t element_count;
+    int32_t points_per_element;
+    int32_t pressure_edge_count;
+} nf_state;
+
+/* Energy, momentum and damage audits (ExplicitSolver.java:875-886, :1610-1860). */
+typedef struct {
+    double kinetic_energy;
+    double centred_kinetic_energy;
+    double strain_energy;
+    double plastic_dissipation;
+    double hourglass_energy;
+    double fracture_dissipation;
+    double axial_momentum;
+    double radial_momentum;
+    double max_plastic_strain;
+    double yielded_fraction;
+    double max_damage;
+    double damaged_fraction;
+    double failed_fraction;
+    double max_temperature;          /* NaN when no element has a Johnson-Cook law */
+    int32_t clamped_points;          /* Damage.java:391-397 */
+    int32_t most_damaged_element;    /* :1778-1793 */
+} nf_audit;
+
+/* RigidWall.java:285-315 */
+typedef struct {
+    double plane;
+    double friction;
+    double impulse;
+    double energy_loss;
+    double friction_dissipation;
+    int32_t contact_count;
+    int32_t stuck_count;
+    int32_t present;
+    int32_t reserved;
+} nf_wall_info;
+
+/* Contact.java:366-404 */
+typedef struct {
+    double friction;
+    double energy;
+    double dissipation;
+    double max_penetration;
+    int32_t pair_count;
+    int32_t escaped_nodes;
+    int32_t segment_count;
+    int32_t present;
+} nf_contact_info;
+
+/* Measurements on the deformed body: TaylorImpactCase.java:272-288 (length, mushroom). */
+typedef struct {
+    double z_max;
+    double z_min;
+    double length;                   /* z_max - z_min */
+    double mushroom_diameter;        /* 2 max(r + ur) */
+} nf_measure;
+
+/* Fields readable with nf_read_field. Per-node doubles, per-point doubles (stride 4 for
+ * tensors, {rr, zz, tt, rz}), per-element doubles, byte flags and int32 lists. */
+typedef enum {
+    NF_FIELD_UR = 0, NF_FIELD_UZ, NF_FIELD_VR, NF_FIELD_VZ, NF_FIELD_FR, NF_FIELD_FZ,
+    NF_FIELD_MASS,
+    NF_FIELD_STRESS,                 /* 4 doubles per point */
+    NF_FIELD_BACK_STRESS,            /* 4 doubles per point */
+    NF_FIELD_PLASTIC_STRAIN,         /* per point */
+    NF_FIELD_PLASTIC_WORK,           /* per point, J/m^3 */
+    NF_FIELD_HOURGLASS_R,            /* per element */
+    NF_FIELD_HOURGLASS_Z,
+    NF_FIELD_HOURGLASS_STIFFNESS,
+    NF_FIELD_DAMAGE_STRENGTH,        /* per point; zero until onset */
+    NF_FIELD_DAMAGE_SOFTENING,
+    NF_FIELD_DAMAGE_WIDTH,
+    NF_FIELD_ERODED,                 /* uint8 per element */
+    NF_FIELD_ON_WALL,                /* uint8 per node */
+    NF_FIELD_WALL_STATE,             /* uint8 per node, last step: NF_WALL_* bits */
+    NF_FIELD_CONTACT_MASTER,         /* int32 per node: master segment or -1 */
+    NF_FIELD_CONTACT_STATE,          /* uint8 per node: NF_CONTACT_* of its own pair */
+    NF_FIELD_SURFACE_EDGES,          /* int32 pairs, current free surface */
+    NF_FIELD_SURFACE_NODES,          /* int32, ascending */
+    NF_FIELD_FIXED,                  /* uint8 per node: bit0 radial, bit1 axial */
+    NF_FIELD_COUNT
+} nf_field;
+
+enum { NF_WALL_HELD = 1, NF_WALL_STUCK = 2, NF_WALL_SLID = 4, NF_WALL_ARRIVED = 8 };
+enum { NF_CONTACT_PAIR = 1, NF_CONTACT_STICK = 2, NF_CONTACT_SLIP = 4 };
+
+/* ------------------------------------------------------------------ lifecycle */
+
+/* ExplicitSolver(QuadMesh, Materials, Formulation, Integration, Kinematics, thickness,
+ * cflSafety), ExplicitSolver.java:264-339 (per-element material unroll :284-300, node slots
+ * :347-366, lumped mass :1559-1597, initial CFL step :333-338). element_material may be
+ * NULL when material_count == 1 (Materials.uniform, core/Materials.java:36-39). */
+nf_status nf_create(const nf_mesh *mesh, const nf_material *materials, int32_t material_count,
+                    const int32_t *element_material, int32_t formulation, int32_t integration,
+                    int32_t kinematics, double thickness, double cfl_safety, nf_solver **out);
+/* ExplicitSolver.shutdown, ExplicitSolver.java:395-400 (also frees device memory). */
+nf_status nf_destroy(nf_solver *h);
+/* Message of the last failure on this handle, or of the calling thread when h is NULL. */
+const char *nf_last_error(const nf_solver *h);
+/* Sticky device-side status bits (NaN seen, wait timed out); 0 when healthy. */
+nf_status nf_status_word(nf_solver *h, uint32_t *word);
+
+/* ------------------------------------------------------------------ setup (ExplicitSolver) */
+
+nf_status nf_set_threads(nf_solver *h, int32_t n);                           /* :386-392, no-op */
+nf_status nf_fix_radial(nf_solver *h, int32_t node);                         /* :408-410 */
+nf_status nf_fix_axial(nf_solver *h, int32_t node);                          /* :413-415 */
+nf_status nf_fix_all_axial(nf_solver *h);                                    /* :423-425 */
+nf_status nf_set_pressure_ramp(nf_solver *h, double pascals, double ramp_seconds); /* :432-435 */
+nf_status nf_set_relaxation_damping(nf_solver *h, double fraction_of_critical,
+                                    double angular_frequency);              /* :450-455 */
+nf_status nf_set_hourglass_coefficient(nf_solver *h, double q);              /* :466-469 */
+/* setRigidWall(RigidWall.atZ(plane, friction)), :475-477 and RigidWall.java:110-136.
+ * friction = +inf is the welded limit. */
+nf_status nf_set_rigid_wall(nf_solver *h, double plane, double friction);
+nf_status nf_clear_rigid_wall(nf_solver *h);
+/* setContact(new Contact(mesh).withFriction(mu).withDamping(zeta).withStiffnessScale(s)),
+ * :487-489 and Contact.java:273-364. */
+nf_status nf_set_contact(nf_solver *h, double friction, double damping, double stiffness_scale);
+nf_status nf_clear_contact(nf_solver *h);
+nf_status nf_set_gravity(nf_solver *h, double accel_r, double accel_z);      /* :509-512 */
+nf_status nf_set_erosion(nf_solver *h, double damage_threshold);             /* :549-561 */
+nf_status nf_set_mass_scaling(nf_solver *h, double target_step);             /* :601-619 */
+/* setDamage(double[] fractureEnergy, double[] failureStrain), :729-791; one value per
+ * element each. */
+nf_status nf_set_damage(nf_solver *h, const double *fracture_energy, const double *failure_strain);
+nf_status nf_set_velocity(nf_solver *h, int32_t node, double vr, double vz);  /* :799-802 */
+nf_status nf_set_uniform_velocity(nf_solver *h, double vr, double vz);        /* :805-808 */
+/* Bulk form of setVelocity over every node, for callers that would loop :799-802. */
+nf_status nf_set_velocities(nf_solver *h, const double *vr, const double *vz);
+
+/* ------------------------------------------------------------------ run */
+
+nf_status nf_step(nf_solver *h, int64_t steps);     /* run(int) / step(), :936-991 */
+nf_status nf_advance(nf_solver *h);                 /* advance(), :1069-1075 */
+/* run until time() >= t_end, the loop of TaylorImpactCase.java:250-253; steps taken are
+ * returned in *taken when non-NULL. The check is made on the device, so no per-step host
+ * round trip is needed. */
+nf_status nf_run_until(nf_solver *h, double t_end, int64_t max_steps, int64_t *taken);
+/* Blocks until the handle's stream is idle. */
+nf_status nf_synchronize(nf_solver *h);
+
+/* ------------------------------------------------------------------ read-back */
+
+/* Element count and element size in bytes of a field, for sizing the destination. */
+nf_status nf_field_size(nf_solver *h, int32_t field, size_t *count, size_t *element_bytes);
+/* Copies a field device -> host (the reference's live getters, :842-932). */
+nf_status nf_read_field(nf_solver *h, int32_t field, void *dst, size_t bytes);
+/* Overwrites a state field host -> device (UR..VZ, STRESS, BACK_STRESS, PLASTIC_STRAIN,
+ * PLASTIC_WORK): the writes reference callers make through the live arrays. */
+nf_status nf_write_field(nf_solver *h, int32_t field, const void *src, size_t bytes);
+nf_status nf_get_state(nf_solver *h, nf_state *out);
+nf_status nf_audits(nf_solver *h, nf_audit *out);
+nf_status nf_wall_stats(nf_solver *h, nf_wall_info *out);
+nf_status nf_contact_stats(nf_solver *h, nf_contact_info *out);
+nf_status nf_measure_body(nf_solver *h, nf_measure *out);
+
+/* ------------------------------------------------------------------ material point */
+
+/* J2.update(sig, back, epsP, work, p, dRR, dZZ, dTT, dGamRZ, lambda, mu, flow, strainDt,
+ * damage), solver/J2.java:163-296 with the Johnson-Cook solve :332-375 and damage onset
+ * Damage.java:306-336, run once per point on the device. lambda/mu/flow come from the
+ * material as the solver derives them (ExplicitSolver.java:289-299). Arrays are host memory,
+ * updated in place; damage arrays may all be NULL for a material that cannot fail, else
+ * geometry has 5 doubles per point (area, uR, uZ, vR, vZ). dgamma receives J2.update's
+ * return value. strain holds {dRR, dZZ, dTT, dGamRZ} per point. */
+typedef struct {
+    const double *failure_strain;
+    const double *fracture_energy;
+    const double *youngs_modulus;
+    const double *geometry;
+    double *strength;
+    double *softening;
+    double *width;
+} nf_damage_points;
+
+nf_status nf_material_point_update(const nf_material *material, int32_t formulation,
+                                   int32_t count, double *sig, double *back, double *eps_p,
+                                   double *work, const double *strain, double strain_dt,
+                                   const nf_damage_points *damage, double *dgamma);
+
+#ifdef __cplusplus
+}
+#endif
+
+#endif /* NEOFIZ_H */

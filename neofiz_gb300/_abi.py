@@ -1,0 +1,167 @@
+"""ctypes description of the C ABI in include/neofiz.h.
+
+Every library that implements the ABI is bound through ``bind(lib, prefix)``, which declares
+argument and return types for each entry point and returns a namespace whose attributes are
+the entry points without their prefix (``api.create``, ``api.step`` ...).
+"""
+from __future__ import annotations
+
+import ctypes as C
+import types
+
+c_double_p = C.POINTER(C.c_double)
+c_int32_p = C.POINTER(C.c_int32)
+
+NF_OK, NF_EINVAL, NF_ESTATE, NF_EDEVICE, NF_ETIMEOUT, NF_ENOMEM = range(6)
+
+(FIELD_UR, FIELD_UZ, FIELD_VR, FIELD_VZ, FIELD_FR, FIELD_FZ, FIELD_MASS, FIELD_STRESS,
+ FIELD_BACK_STRESS, FIELD_PLASTIC_STRAIN, FIELD_PLASTIC_WORK, FIELD_HOURGLASS_R,
+ FIELD_HOURGLASS_Z, FIELD_HOURGLASS_STIFFNESS, FIELD_DAMAGE_STRENGTH, FIELD_DAMAGE_SOFTENING,
+ FIELD_DAMAGE_WIDTH, FIELD_ERODED, FIELD_ON_WALL, FIELD_WALL_STATE, FIELD_CONTACT_MASTER,
+ FIELD_CONTACT_STATE, FIELD_SURFACE_EDGES, FIELD_SURFACE_NODES, FIELD_FIXED) = range(25)
+
+WALL_HELD, WALL_STUCK, WALL_SLID, WALL_ARRIVED = 1, 2, 4, 8
+CONTACT_PAIR, CONTACT_STICK, CONTACT_SLIP = 1, 2, 4
+
+
+class Mesh(C.Structure):
+    _fields_ = [("node_count", C.c_int32), ("element_count", C.c_int32),
+                ("pressure_edge_count", C.c_int32),
+                ("r", c_double_p), ("z", c_double_p),
+                ("conn", c_int32_p), ("pressure_edges", c_int32_p)]
+
+
+class MaterialC(C.Structure):
+    _fields_ = [("youngs_modulus", C.c_double), ("poisson_ratio", C.c_double),
+                ("density", C.c_double), ("yield_stress", C.c_double),
+                ("isotropic_hardening", C.c_double), ("kinematic_hardening", C.c_double),
+                ("has_johnson_cook", C.c_int32), ("reserved", C.c_int32),
+                ("jc_a", C.c_double), ("jc_b", C.c_double), ("jc_n", C.c_double),
+                ("jc_c", C.c_double), ("jc_m", C.c_double),
+                ("jc_reference_strain_rate", C.c_double),
+                ("jc_room_temperature", C.c_double), ("jc_melt_temperature", C.c_double),
+                ("jc_specific_heat", C.c_double), ("jc_taylor_quinney", C.c_double)]
+
+
+class State(C.Structure):
+    _fields_ = [("time", C.c_double), ("timestep", C.c_double),
+                ("timestep_previous", C.c_double), ("reference_timestep", C.c_double),
+                ("mass_scale", C.c_double), ("min_edge_squared", C.c_double),
+                ("fastest_wave", C.c_double), ("eroded_energy", C.c_double),
+                ("bore_pressure", C.c_double), ("steps", C.c_int64),
+                ("eroded_elements", C.c_int32), ("inverted_elements", C.c_int32),
+                ("node_count", C.c_int32), ("element_count", C.c_int32),
+                ("points_per_element", C.c_int32), ("pressure_edge_count", C.c_int32)]
+
+
+class Audit(C.Structure):
+    _fields_ = [(n, C.c_double) for n in (
+        "kinetic_energy", "centred_kinetic_energy", "strain_energy", "plastic_dissipation",
+        "hourglass_energy", "fracture_dissipation", "axial_momentum", "radial_momentum",
+        "max_plastic_strain", "yielded_fraction", "max_damage", "damaged_fraction",
+        "failed_fraction", "max_temperature")] + [
+        ("clamped_points", C.c_int32), ("most_damaged_element", C.c_int32)]
+
+
+class WallInfo(C.Structure):
+    _fields_ = [("plane", C.c_double), ("friction", C.c_double), ("impulse", C.c_double),
+                ("energy_loss", C.c_double), ("friction_dissipation", C.c_double),
+                ("contact_count", C.c_int32), ("stuck_count", C.c_int32),
+                ("present", C.c_int32), ("reserved", C.c_int32)]
+
+
+class ContactInfo(C.Structure):
+    _fields_ = [("friction", C.c_double), ("energy", C.c_double),
+                ("dissipation", C.c_double), ("max_penetration", C.c_double),
+                ("pair_count", C.c_int32), ("escaped_nodes", C.c_int32),
+                ("segment_count", C.c_int32), ("present", C.c_int32)]
+
+
+class Measure(C.Structure):
+    _fields_ = [("z_max", C.c_double), ("z_min", C.c_double), ("length", C.c_double),
+                ("mushroom_diameter", C.c_double)]
+
+
+class DamagePoints(C.Structure):
+    _fields_ = [("failure_strain", c_double_p), ("fracture_energy", c_double_p),
+                ("youngs_modulus", c_double_p), ("geometry", c_double_p),
+                ("strength", c_double_p), ("softening", c_double_p), ("width", c_double_p)]
+
+
+_H = C.c_void_p
+_S = C.c_int
+_PROTOS = {
+    "create": (_S, [C.POINTER(Mesh), C.POINTER(MaterialC), C.c_int32, c_int32_p, C.c_int32,
+                    C.c_int32, C.c_int32, C.c_double, C.c_double, C.POINTER(C.c_void_p)]),
+    "destroy": (None, [_H]),
+    "last_error": (C.c_char_p, [_H]),
+    "status_word": (_S, [_H, C.POINTER(C.c_uint32)]),
+    "set_threads": (_S, [_H, C.c_int32]),
+    "fix_radial": (_S, [_H, C.c_int32]),
+    "fix_axial": (_S, [_H, C.c_int32]),
+    "fix_all_axial": (_S, [_H]),
+    "set_pressure_ramp": (_S, [_H, C.c_double, C.c_double]),
+    "set_relaxation_damping": (_S, [_H, C.c_double, C.c_double]),
+    "set_hourglass_coefficient": (_S, [_H, C.c_double]),
+    "set_rigid_wall": (_S, [_H, C.c_double, C.c_double]),
+    "clear_rigid_wall": (_S, [_H]),
+    "set_contact": (_S, [_H, C.c_double, C.c_double, C.c_double]),
+    "clear_contact": (_S, [_H]),
+    "set_gravity": (_S, [_H, C.c_double, C.c_double]),
+    "set_erosion": (_S, [_H, C.c_double]),
+    "set_mass_scaling": (_S, [_H, C.c_double]),
+    "set_damage": (_S, [_H, c_double_p, c_double_p]),
+    "set_velocity": (_S, [_H, C.c_int32, C.c_double, C.c_double]),
+    "set_uniform_velocity": (_S, [_H, C.c_double, C.c_double]),
+    "set_velocities": (_S, [_H, c_double_p, c_double_p]),
+    "step": (_S, [_H, C.c_int64]),
+    "advance": (_S, [_H]),
+    "run_until": (_S, [_H, C.c_double, C.c_int64, C.POINTER(C.c_int64)]),
+    "synchronize": (_S, [_H]),
+    "field_size": (_S, [_H, C.c_int32, C.POINTER(C.c_size_t), C.POINTER(C.c_size_t)]),
+    "read_field": (_S, [_H, C.c_int32, C.c_void_p, C.c_size_t]),
+    "write_field": (_S, [_H, C.c_int32, C.c_void_p, C.c_size_t]),
+    "get_state": (_S, [_H, C.POINTER(State)]),
+    "audits": (_S, [_H, C.POINTER(Audit)]),
+    "wall_stats": (_S, [_H, C.POINTER(WallInfo)]),
+    "contact_stats": (_S, [_H, C.POINTER(ContactInfo)]),
+    "measure_body": (_S, [_H, C.POINTER(Measure)]),
+    "material_point_update": (_S, [C.POINTER(MaterialC), C.c_int32, C.c_int32, c_double_p,
+                                   c_double_p, c_double_p, c_double_p, c_double_p, C.c_double,
+                                   C.POINTER(DamagePoints), c_double_p]),
+}
+
+ENTRY_POINTS = tuple("nf_" + name for name in _PROTOS)
+
+
+def bind(lib: C.CDLL, prefix: str) -> types.SimpleNamespace:
+    ns = types.SimpleNamespace()
+    for name, (res, args) in _PROTOS.items():
+        fn = getattr(lib, prefix + name)
+        fn.restype = res
+        fn.argtypes = args
+        setattr(ns, name, fn)
+    ns.lib = lib
+    ns.prefix = prefix
+    return ns
+
+
+def material_struct(m) -> MaterialC:
+    """Fills the C record from a neofiz_gb300.materials.Material."""
+    s = MaterialC()
+    s.youngs_modulus = m.youngsModulus
+    s.poisson_ratio = m.poissonRatio
+    s.density = m.density
+    s.yield_stress = m.yieldStress
+    s.isotropic_hardening = m.isotropicHardening
+    s.kinematic_hardening = m.kinematicHardening
+    jc = m.johnsonCook
+    s.has_johnson_cook = 1 if jc is not None else 0
+    if jc is not None:
+        s.jc_a, s.jc_b, s.jc_n, s.jc_c, s.jc_m = jc.a, jc.b, jc.n, jc.c, jc.m
+        s.jc_reference_strain_rate = jc.referenceStrainRate
+        s.jc_room_temperature = jc.roomTemperature
+        s.jc_melt_temperature = jc.meltTemperature
+        s.jc_specific_heat = jc.specificHeat
+        s.jc_taylor_quinney = jc.taylorQuinney
+    return s
