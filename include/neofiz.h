@@ -181,6 +181,9 @@ enum { NF_CONTACT_PAIR = 1, NF_CONTACT_STICK = 2, NF_CONTACT_SLIP = 4 };
 
 /* ------------------------------------------------------------------ lifecycle */
 
+/* Number of CUDA devices visible to the library (0 when none); no reference counterpart. */
+int nf_device_count(void);
+
 /* ExplicitSolver(QuadMesh, Materials, Formulation, Integration, Kinematics, thickness,
  * cflSafety), ExplicitSolver.java:264-339 (per-element material unroll :284-300, node slots
  * :347-366, lumped mass :1559-1597, initial CFL step :333-338). element_material may be

@@ -1,0 +1,554 @@
+// k_contact.cu -- penalty node-to-segment contact with a Coulomb cone
+// (src/main/java/org/neofiz/solver/Contact.java), and the free-surface rebuild it needs after
+// erosion (mesh/QuadMesh.java:188-226 via Contact.adopt, Contact.java:290-322).
+//
+// The reference's result depends on three orders, and each is reproduced exactly:
+//   * the surface is listed in element order and its nodes ascending (a stream compaction
+//     of per-edge and per-node flags, i.e. an ordered scan);
+//   * the search visits the nine cells in (dj, di) order and, within a cell, the segments in
+//     the order the counting sort filed them -- ascending segment, first endpoint before the
+//     second (Contact.java:530-545, :578-603). Buckets are filled with atomics and then
+//     sorted by (cell, 2 s + endpoint), which restores exactly that order;
+//   * every node's force receives its contact terms in slave order, normal before tangent
+//     (Contact.java:446-462, :717-754). Each pair's twelve terms are computed in parallel,
+//     each node then sorts its incident pairs and adds them in that order.
+// The running totals (spring energy, dissipation) are audits; they are reduced in a fixed
+// order per block, so they are deterministic but not summed in the reference's serial order.
+#include "nf_internal.h"
+
+namespace nf {
+
+constexpr int CB = 128;
+constexpr double MAX_DEPTH = 0.5;
+constexpr double STICK_RELAXATION = 0.5;
+constexpr double FACING = 0.25;
+
+__device__ __forceinline__ unsigned long long okey(double v) {     // order-preserving image
+    const unsigned long long b = (unsigned long long)__double_as_longlong(v);
+    return (b >> 63) ? ~b : (b | 0x8000000000000000ULL);
+}
+__device__ __forceinline__ double unokey(unsigned long long k) {
+    const unsigned long long b = (k >> 63) ? (k & 0x7fffffffffffffffULL) : ~k;
+    return __longlong_as_double((long long)b);
+}
+
+__device__ double block_sum_c(double v, double *sh) {
+    for (int o = 16; o > 0; o >>= 1) v += __shfl_down_sync(0xffffffffu, v, o);
+    const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
+    __syncthreads();
+    if (lane == 0) sh[warp] = v;
+    __syncthreads();
+    double t = 0.0;
+    if (threadIdx.x == 0) {
+        const int warps = (blockDim.x + 31) >> 5;
+        for (int w = 0; w < warps; w++) t += sh[w];
+    }
+    return t;
+}
+
+// ---------------------------------------------------------------------------- begin
+
+// Contact.begin, Contact.java:424-436: per-step totals, and whether the surface is stale.
+__global__ void k_contact_begin(Dev d) {
+    DevScalars *s = d.s;
+    s->rebuild = s->active && s->stale;
+    if (!s->active) return;
+    s->pairs = 0;
+    s->maxPenBits = 0ULL;
+    s->bbox[0] = ~0ULL;   // min r
+    s->bbox[1] = ~0ULL;   // min z
+    s->bbox[2] = 0ULL;    // max r
+    s->bbox[3] = 0ULL;    // max z
+    s->longestBits = 0ULL;
+}
+
+// ---------------------------------------------------------------------------- surface rebuild
+
+__global__ void k_surf_flags(Dev d) {
+    if (!d.s->rebuild) return;
+    const int q = blockIdx.x * blockDim.x + threadIdx.x;
+    if (q >= 4 * d.E) return;
+    const int e = q >> 2;
+    int flag = 0;
+    if (!d.dead[e]) {
+        const int g = d.edgeGroup[q];
+        int live = 0;
+        for (int m = d.groupStart[g]; m < d.groupStart[g + 1]; m++)
+            if (!d.dead[d.groupMember[m] >> 2]) live++;
+        flag = live == 1;
+    }
+    d.surfFlag[q] = flag;
+}
+
+__global__ void k_zero_int(int32_t *a, int n, const int *pred) {
+    if (pred && !*pred) return;
+    const int i = blockIdx.x * blockDim.x + threadIdx.x;
+    if (i < n) a[i] = 0;
+}
+
+__global__ void k_copy_int(const int32_t *src, int32_t *dst, int n, const int *pred) {
+    if (pred && !*pred) return;
+    const int i = blockIdx.x * blockDim.x + threadIdx.x;
+    if (i < n) dst[i] = src[i];
+}
+
+__global__ void k_surf_emit(Dev d) {
+    if (!d.s->rebuild) return;
+    const int q = blockIdx.x * blockDim.x + threadIdx.x;
+    if (q >= 4 * d.E || !d.surfFlag[q]) return;
+    const int e = q >> 2, k = q & 3;
+    const int4 c = d.conn[e];
+    const int nn[4] = {c.x, c.y, c.z, c.w};
+    const int a = nn[k], b = nn[(k + 1) & 3];
+    const int p = d.surfPos[q];
+    d.segA[p] = a;
+    d.segB[p] = b;
+    d.segOwner[p] = e;
+    d.nodeFlag[a] = 1;
+    d.nodeFlag[b] = 1;
+}
+
+__global__ void k_surf_nodes(Dev d) {
+    if (!d.s->rebuild) return;
+    const int n = blockIdx.x * blockDim.x + threadIdx.x;
+    if (n >= d.N) return;
+    if (d.nodeFlag[n]) {
+        const int slot = d.nodePos[n];
+        d.surfNodes[slot] = n;
+        d.slotOf[n] = slot;
+        d.lastMaster[slot] = -1;         // Contact.adopt, :319-321
+        d.master[slot] = -1;
+        d.dropped[slot] = 0;
+        d.segCount[slot] = 0;
+    } else {
+        d.slotOf[n] = -1;
+    }
+}
+
+__global__ void k_seg_count(Dev d) {
+    if (!d.s->rebuild) return;
+    const int s = blockIdx.x * blockDim.x + threadIdx.x;
+    if (s >= d.s->surfEdges) return;
+    atomicAdd(&d.segCount[d.slotOf[d.segA[s]]], 1);
+    atomicAdd(&d.segCount[d.slotOf[d.segB[s]]], 1);
+}
+
+__global__ void k_seg_fill(Dev d) {
+    if (!d.s->rebuild) return;
+    const int s = blockIdx.x * blockDim.x + threadIdx.x;
+    if (s >= d.s->surfEdges) return;
+    d.segOf[atomicAdd(&d.segCursor[d.slotOf[d.segA[s]]], 1)] = s;
+    d.segOf[atomicAdd(&d.segCursor[d.slotOf[d.segB[s]]], 1)] = s;
+}
+
+// Restores ascending segment order in each node's list (Contact.java:306-313), then retires
+// the rebuild.
+__global__ void k_seg_sort(Dev d) {
+    if (!d.s->rebuild) return;
+    const int i = blockIdx.x * blockDim.x + threadIdx.x;
+    if (i == 0) d.s->stale = 0;
+    if (i >= d.s->surfNodes) return;
+    const int lo = d.segStart[i], hi = d.segStart[i + 1];
+    for (int k = lo + 1; k < hi; k++) {
+        const int v = d.segOf[k];
+        int j = k - 1;
+        while (j >= lo && d.segOf[j] > v) {
+            d.segOf[j + 1] = d.segOf[j];
+            j--;
+        }
+        d.segOf[j + 1] = v;
+    }
+}
+
+// ---------------------------------------------------------------------------- geometry
+
+// Contact.geometry, Contact.java:467-500 (coordinates and the bounding box of the grid)
+__global__ void k_contact_nodes(Dev d) {
+    if (!d.s->active) return;
+    const int i = blockIdx.x * blockDim.x + threadIdx.x;
+    if (i >= d.s->surfNodes) return;
+    const int n = d.surfNodes[i];
+    const double2 x = d.X0[n], u = d.U[n];
+    const double cr = x.x + u.x, cz = x.y + u.y;
+    d.cr[n] = cr;
+    d.cz[n] = cz;
+    d.incCount[i] = 0;
+    d.pairNodes[i] = make_int4(-1, -1, -1, 0);
+    atomicMin(&d.s->bbox[0], okey(cr));
+    atomicMin(&d.s->bbox[1], okey(cz));
+    atomicMax(&d.s->bbox[2], okey(cr));
+    atomicMax(&d.s->bbox[3], okey(cz));
+}
+
+__global__ void k_contact_segs(Dev d) {
+    if (!d.s->active) return;
+    const int s = blockIdx.x * blockDim.x + threadIdx.x;
+    if (s >= d.s->surfEdges) return;
+    const int a = d.segA[s], b = d.segB[s];
+    const double dr = d.cr[b] - d.cr[a], dz = d.cz[b] - d.cz[a];
+    const double len = sqrt(dr * dr + dz * dz);
+    d.slen[s] = len;
+    if (len > 0.0) {
+        d.snr[s] = dz / len;
+        d.snz[s] = -dr / len;
+    } else {
+        d.snr[s] = 0.0;
+        d.snz[s] = 0.0;
+    }
+    atomicMax(&d.s->longestBits, (unsigned long long)__double_as_longlong(len));
+}
+
+__global__ void k_contact_pnorm(Dev d) {
+    if (!d.s->active) return;
+    const int i = blockIdx.x * blockDim.x + threadIdx.x;
+    if (i >= d.s->surfNodes) return;
+    double sr = 0.0, sz = 0.0;
+    for (int k = d.segStart[i]; k < d.segStart[i + 1]; k++) {
+        sr += d.snr[d.segOf[k]];
+        sz += d.snz[d.segOf[k]];
+    }
+    const double len = sqrt(sr * sr + sz * sz);
+    d.pnr[i] = len > 0.0 ? sr / len : 0.0;
+    d.pnz[i] = len > 0.0 ? sz / len : 0.0;
+}
+
+// Contact.grid, Contact.java:515-545 (the grid's extent and cell size)
+__global__ void k_grid_setup(Dev d) {
+    DevScalars *s = d.s;
+    if (!s->active) return;
+    if (s->surfNodes == 0) {
+        s->cols = s->rows = 1;
+        s->cells = 1;
+        s->hashed = 0;
+        return;
+    }
+    const double rlo = unokey(s->bbox[0]), zlo = unokey(s->bbox[1]);
+    const double rhi = unokey(s->bbox[2]), zhi = unokey(s->bbox[3]);
+    const double longest = __longlong_as_double((long long)s->longestBits);
+    const double cellSize = longest > 0.0 ? 1.5 * longest : 1.0;
+    s->cellSize = cellSize;
+    s->gridR0 = rlo;
+    s->gridZ0 = zlo;
+    const int a = jd2i((rhi - rlo) / cellSize) + 1;
+    const int b = jd2i((zhi - zlo) / cellSize) + 1;
+    s->cols = a > 1 ? a : 1;
+    s->rows = b > 1 ? b : 1;
+    s->cells = (long long)s->cols * (long long)s->rows;
+    s->hashed = s->cells > d.bucketCap;
+    if (s->hashed) atomicOr(&s->status, STATUS_GRID_HASHED);
+}
+
+__device__ __forceinline__ int iclamp(int v, int n) { return v < 0 ? 0 : v >= n ? n - 1 : v; }
+
+__device__ __forceinline__ long long cell_of(const DevScalars *s, double r, double z) {
+    const int i = iclamp(jd2i((r - s->gridR0) / s->cellSize), s->cols);
+    const int j = iclamp(jd2i((z - s->gridZ0) / s->cellSize), s->rows);
+    return (long long)j * s->cols + i;
+}
+
+__device__ __forceinline__ int bucket_of(const Dev &d, long long cell) {
+    return d.s->hashed ? (int)(cell % d.bucketCap) : (int)cell;
+}
+
+__global__ void k_bucket_count(Dev d) {
+    if (!d.s->active) return;
+    const int q = blockIdx.x * blockDim.x + threadIdx.x;
+    if (q >= 2 * d.s->surfEdges) return;
+    const int s = q >> 1;
+    const int node = (q & 1) ? d.segB[s] : d.segA[s];
+    const long long cell = cell_of(d.s, d.cr[node], d.cz[node]);
+    d.entryCell[q] = cell;
+    atomicAdd(&d.bucketCount[bucket_of(d, cell)], 1);
+}
+
+__global__ void k_bucket_fill(Dev d) {
+    if (!d.s->active) return;
+    const int q = blockIdx.x * blockDim.x + threadIdx.x;
+    if (q >= 2 * d.s->surfEdges) return;
+    const long long cell = d.entryCell[q];
+    const int pos = atomicAdd(&d.bucketCursor[bucket_of(d, cell)], 1);
+    d.bucketEntry[pos] = q;
+    d.bucketCell[pos] = cell;
+}
+
+// Sorts each bucket by (cell, entry): the counting sort's filing order.
+__global__ void k_bucket_sort(Dev d) {
+    if (!d.s->active) return;
+    const int b = blockIdx.x * blockDim.x + threadIdx.x;
+    if (b >= d.bucketCap) return;
+    const int lo = d.bucketStart[b], hi = d.bucketStart[b + 1];
+    for (int k = lo + 1; k < hi; k++) {
+        const int v = d.bucketEntry[k];
+        const long long c = d.bucketCell[k];
+        int j = k - 1;
+        while (j >= lo && (d.bucketCell[j] > c || (d.bucketCell[j] == c && d.bucketEntry[j] > v))) {
+            d.bucketEntry[j + 1] = d.bucketEntry[j];
+            d.bucketCell[j + 1] = d.bucketCell[j];
+            j--;
+        }
+        d.bucketEntry[j + 1] = v;
+        d.bucketCell[j + 1] = c;
+    }
+}
+
+// ---------------------------------------------------------------------------- search
+
+// Contact.excluded, Contact.java:620-639
+__device__ __forceinline__ bool excluded(const Dev &d, int i, int n, int s) {
+    const int a = d.segA[s], b = d.segB[s];
+    if (d.pnr[i] * d.snr[s] + d.pnz[i] * d.snz[s] > -FACING) return true;
+    if (a == n || b == n) return true;
+    for (int k = d.segStart[i]; k < d.segStart[i + 1]; k++) {
+        const int own = d.segOf[k];
+        const int p = d.segA[own], q = d.segB[own];
+        if (p == a || p == b || q == a || q == b) return true;
+    }
+    return false;
+}
+
+// Contact.depth, Contact.java:642-652
+__device__ __forceinline__ double depth_of(const Dev &d, int n, int s) {
+    const int a = d.segA[s], b = d.segB[s];
+    const double len = d.slen[s];
+    if (len <= 0.0) return 0.0;
+    const double tr = (d.cr[b] - d.cr[a]) / len, tz = (d.cz[b] - d.cz[a]) / len;
+    const double dr = d.cr[n] - d.cr[a], dz = d.cz[n] - d.cz[a];
+    const double along = dr * tr + dz * tz;
+    if (along < 0.0 || along > len) return 0.0;
+    const double gap = dr * d.snr[s] + dz * d.snz[s];
+    return gap < 0.0 ? -gap : 0.0;
+}
+
+// Contact.nearestPenetrated, Contact.java:570-606
+__global__ void __launch_bounds__(CB) k_contact_search(Dev d) {
+    const DevScalars *s = d.s;
+    if (!s->active) return;
+    const int i = blockIdx.x * blockDim.x + threadIdx.x;
+    if (i >= s->surfNodes) return;
+    const int n = d.surfNodes[i];
+    const double crn = d.cr[n], czn = d.cz[n];
+    const int ci = iclamp(jd2i((crn - s->gridR0) / s->cellSize), s->cols);
+    const int cj = iclamp(jd2i((czn - s->gridZ0) / s->cellSize), s->rows);
+    const int last = d.lastMaster[i];
+    int best = -1;
+    double deepest = 0.0;
+    bool fell = false;
+    for (int dj = -1; dj <= 1; dj++) {
+        const int j = cj + dj;
+        if (j < 0 || j >= s->rows) continue;
+        for (int di = -1; di <= 1; di++) {
+            const int ii = ci + di;
+            if (ii < 0 || ii >= s->cols) continue;
+            const long long cell = (long long)j * s->cols + ii;
+            const int bkt = bucket_of(d, cell);
+            for (int k = d.bucketStart[bkt]; k < d.bucketStart[bkt + 1]; k++) {
+                if (d.bucketCell[k] != cell) continue;
+                const int sg = d.bucketEntry[k] >> 1;
+                if (excluded(d, i, n, sg)) continue;
+                const double depth = depth_of(d, n, sg);
+                if (depth <= 0.0) continue;
+                if (depth > MAX_DEPTH * d.slen[sg]) {
+                    if (sg == last) fell = true;
+                    continue;
+                }
+                if (depth > deepest) {
+                    deepest = depth;
+                    best = sg;
+                }
+            }
+        }
+    }
+    d.dropped[i] = fell ? 1 : 0;
+    d.master[i] = best;
+}
+
+// ---------------------------------------------------------------------------- resolve
+
+// Contact.accumulate + resolve, Contact.java:446-462, :663-762: each slave's pair, computed
+// independently (resolve reads velocities and masses only). Writes the twelve force terms of
+// the pair as values to ADD (x - y is computed as x + (-y), which is the same IEEE result).
+__global__ void __launch_bounds__(CB) k_contact_resolve(Dev d) {
+    __shared__ double sh[CB / 32];
+    const DevScalars *sc = d.s;
+    if (!sc->active) return;
+    const int i = blockIdx.x * blockDim.x + threadIdx.x;
+    double energy = 0.0, diss = 0.0;
+    if (i < sc->surfNodes) {
+        const int n = d.surfNodes[i];
+        const int best = d.master[i];
+        if (best < 0) {
+            if (d.lastMaster[i] >= 0 && d.dropped[i]) atomicAdd(&d.s->escaped, 1);
+            d.lastMaster[i] = -1;
+        } else {
+            d.lastMaster[i] = best;
+            const int s = best;
+            const double dt = sc->dt;
+            const double reference = d.dt0;
+            const int a = d.segA[s], b = d.segB[s];
+            const double depth = depth_of(d, n, s);
+            const double len = d.slen[s];
+            const double tr = (d.cr[b] - d.cr[a]) / len;            // parameter, :655-661
+            const double tz = (d.cz[b] - d.cz[a]) / len;
+            const double t = ((d.cr[n] - d.cr[a]) * tr + (d.cz[n] - d.cz[a]) * tz) / len;
+            const double wa = 1.0 - t, wb = t;
+            const double ma = d.mass[a], mb = d.mass[b];
+            const double invMaster = 0.25 / ma + 0.25 / mb;
+            if (invMaster > 0.0) {
+                const double mMaster = 1.0 / invMaster;
+                const double mSlave = d.mass[n];
+                const double mStar = mSlave * mMaster / (mSlave + mMaster);
+                const double k = d.cScale * mStar / (reference * reference);
+                const double nR = d.snr[s], nZ = d.snz[s];
+                const double mTrue = 1.0 / (wa * wa / ma + wb * wb / mb);
+                const double mTangent = mSlave * mTrue / (mSlave + mTrue);
+                const double2 vn = d.V[n], va = d.V[a], vb = d.V[b];
+                const double closing = (vn.x - wa * va.x - wb * vb.x) * nR
+                                       + (vn.y - wa * va.y - wb * vb.y) * nZ;
+                const double damper = 2.0 * d.cDamping * mStar * sqrt(d.cScale) / reference;
+                const double normal = jmax(0.0, k * depth - damper * closing);
+                double *pv = d.pairVal + 12 * (size_t)i;
+                pv[0] = normal * nR;
+                pv[1] = normal * nZ;
+                pv[4] = -(wa * normal * nR);
+                pv[5] = -(wa * normal * nZ);
+                pv[8] = -(wb * normal * nR);
+                pv[9] = -(wb * normal * nZ);
+                atomicAdd(&d.s->pairs, 1);
+                energy = 0.5 * k * depth * depth;
+                atomicMax(&d.s->maxPenBits, (unsigned long long)__double_as_longlong(depth));
+                const double damperForce = normal - k * depth;
+                if (damperForce != 0.0) {
+                    const double closingAfter = closing + damperForce * dt / mTangent;
+                    diss -= damperForce * 0.5 * (closing + closingAfter) * dt;
+                }
+                uint8_t state = NF_CONTACT_PAIR;
+                if (d.cFriction > 0.0) {
+                    const double tR = -nZ, tZ = nR;
+                    const double slide = (vn.x - wa * va.x - wb * vb.x) * tR
+                                         + (vn.y - wa * va.y - wb * vb.y) * tZ;
+                    double tangent = -STICK_RELAXATION * mTangent * slide / dt;
+                    const double cone = d.cFriction * normal;
+                    bool slipped = false;
+                    if (tangent > cone) { tangent = cone; slipped = true; }
+                    else if (tangent < -cone) { tangent = -cone; slipped = true; }
+                    pv[2] = tangent * tR;
+                    pv[3] = tangent * tZ;
+                    pv[6] = -(wa * tangent * tR);
+                    pv[7] = -(wa * tangent * tZ);
+                    pv[10] = -(wb * tangent * tR);
+                    pv[11] = -(wb * tangent * tZ);
+                    const double after = slide + tangent * dt / mTangent;
+                    diss += -tangent * 0.5 * (slide + after) * dt;
+                    state |= slipped ? NF_CONTACT_SLIP : NF_CONTACT_STICK;
+                }
+                d.contactState[n] = state;
+                d.pairNodes[i] = make_int4(n, a, b, 1);
+            }
+        }
+    }
+    const double e1 = block_sum_c(energy, sh);
+    const double e2 = block_sum_c(diss, sh);
+    if (threadIdx.x == 0) {
+        d.partials[(PARTIAL_CONTACT + 0) * d.maxBlocks + blockIdx.x] = e1;
+        d.partials[(PARTIAL_CONTACT + 1) * d.maxBlocks + blockIdx.x] = e2;
+    }
+}
+
+__global__ void k_inc_count(Dev d) {
+    if (!d.s->active) return;
+    const int i = blockIdx.x * blockDim.x + threadIdx.x;
+    if (i >= d.s->surfNodes) return;
+    const int4 p = d.pairNodes[i];
+    if (!p.w) return;
+    atomicAdd(&d.incCount[d.slotOf[p.x]], 1);
+    atomicAdd(&d.incCount[d.slotOf[p.y]], 1);
+    atomicAdd(&d.incCount[d.slotOf[p.z]], 1);
+}
+
+__global__ void k_inc_fill(Dev d) {
+    if (!d.s->active) return;
+    const int i = blockIdx.x * blockDim.x + threadIdx.x;
+    if (i >= d.s->surfNodes) return;
+    const int4 p = d.pairNodes[i];
+    if (!p.w) return;
+    d.incEntry[atomicAdd(&d.incCursor[d.slotOf[p.x]], 1)] = (i << 2) | 0;
+    d.incEntry[atomicAdd(&d.incCursor[d.slotOf[p.y]], 1)] = (i << 2) | 1;
+    d.incEntry[atomicAdd(&d.incCursor[d.slotOf[p.z]], 1)] = (i << 2) | 2;
+}
+
+// Adds each node's contact terms in slave order, normal then tangent (Contact.java:717-754).
+__global__ void k_inc_apply(Dev d) {
+    if (!d.s->active) return;
+    const int j = blockIdx.x * blockDim.x + threadIdx.x;
+    if (j >= d.s->surfNodes) return;
+    const int lo = d.incStart[j], hi = d.incStart[j + 1];
+    if (lo == hi) return;
+    for (int k = lo + 1; k < hi; k++) {
+        const int v = d.incEntry[k];
+        int q = k - 1;
+        while (q >= lo && d.incEntry[q] > v) {
+            d.incEntry[q + 1] = d.incEntry[q];
+            q--;
+        }
+        d.incEntry[q + 1] = v;
+    }
+    const int node = d.surfNodes[j];
+    double2 f = d.F[node];
+    const bool friction = d.cFriction > 0.0;
+    for (int k = lo; k < hi; k++) {
+        const int ent = d.incEntry[k];
+        const double *pv = d.pairVal + 12 * (size_t)(ent >> 2) + 4 * (ent & 3);
+        f.x += pv[0];
+        f.y += pv[1];
+        if (friction) {
+            f.x += pv[2];
+            f.y += pv[3];
+        }
+    }
+    d.F[node] = f;
+}
+
+// ---------------------------------------------------------------------------- launch
+
+void launch_contact(Solver &S, bool) {
+    Dev &d = S.d;
+    const cudaStream_t st = S.stream;
+    const int *rebuild = &d.s->rebuild;
+    const int *active = &d.s->active;
+    const int gE4 = grid_for(4LL * d.E, CB), gN = grid_for(d.N, CB), gQ = grid_for(8LL * d.E, CB);
+    k_contact_begin<<<1, 1, 0, st>>>(d);
+    // free surface, only on the steps after an erosion (or the first)
+    k_surf_flags<<<gE4, CB, 0, st>>>(d);
+    scan_exclusive(d.surfFlag, d.surfPos, 4 * d.E, &d.s->surfEdges, d.scanTmp, st, rebuild);
+    k_zero_int<<<gN, CB, 0, st>>>(d.nodeFlag, d.N, rebuild);
+    k_surf_emit<<<gE4, CB, 0, st>>>(d);
+    scan_exclusive(d.nodeFlag, d.nodePos, d.N, &d.s->surfNodes, d.scanTmp, st, rebuild);
+    k_surf_nodes<<<gN, CB, 0, st>>>(d);
+    k_seg_count<<<gE4, CB, 0, st>>>(d);
+    scan_exclusive(d.segCount, d.segStart, d.N + 1, nullptr, d.scanTmp, st, rebuild);
+    k_copy_int<<<grid_for(d.N + 1, CB), CB, 0, st>>>(d.segStart, d.segCursor, d.N + 1, rebuild);
+    k_seg_fill<<<gE4, CB, 0, st>>>(d);
+    k_seg_sort<<<gN, CB, 0, st>>>(d);
+    // geometry and grid
+    k_contact_nodes<<<gN, CB, 0, st>>>(d);
+    k_contact_segs<<<gE4, CB, 0, st>>>(d);
+    k_contact_pnorm<<<gN, CB, 0, st>>>(d);
+    k_grid_setup<<<1, 1, 0, st>>>(d);
+    k_zero_int<<<grid_for(d.bucketCap + 1, CB), CB, 0, st>>>(d.bucketCount, d.bucketCap + 1, active);
+    k_bucket_count<<<gQ, CB, 0, st>>>(d);
+    scan_exclusive(d.bucketCount, d.bucketStart, d.bucketCap + 1, nullptr, d.scanTmp, st, active);
+    k_copy_int<<<grid_for(d.bucketCap + 1, CB), CB, 0, st>>>(d.bucketStart, d.bucketCursor,
+                                                             d.bucketCap + 1, active);
+    k_bucket_fill<<<gQ, CB, 0, st>>>(d);
+    k_bucket_sort<<<grid_for(d.bucketCap, CB), CB, 0, st>>>(d);
+    // search, resolve, ordered accumulation
+    k_contact_search<<<gN, CB, 0, st>>>(d);
+    k_contact_resolve<<<gN, CB, 0, st>>>(d);
+    k_inc_count<<<gN, CB, 0, st>>>(d);
+    scan_exclusive(d.incCount, d.incStart, d.N + 1, nullptr, d.scanTmp, st, active);
+    k_copy_int<<<grid_for(d.N + 1, CB), CB, 0, st>>>(d.incStart, d.incCursor, d.N + 1, active);
+    k_inc_fill<<<gN, CB, 0, st>>>(d);
+    k_inc_apply<<<gN, CB, 0, st>>>(d);
+}
+
+}  // namespace nf

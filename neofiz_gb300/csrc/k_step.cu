@@ -1,0 +1,962 @@
+// k_step.cu -- the kernels of one explicit central-difference timestep
+// (ExplicitSolver.step, src/main/java/org/neofiz/solver/ExplicitSolver.java:940-991):
+//
+//   k_begin            dtAvg, decay, gain; the run predicate                       :947-956
+//   k_nodal            velocity/position update, fixed DOFs, rigid wall            :998-1062
+//   k_erode            deletion of failed or inverted elements                      :663-691
+//   k_element_reduced  one-point quadrature + Flanagan-Belytschko hourglass        :1373-1504
+//   k_element_full     2x2 Gauss quadrature                                         :1219-1339
+//   k_pressure         follower pressure on the bore edges                          :1511-1556
+//   k_gather           per-node sum of its sources in CSR order, plus m g           :1147-1165
+//   (contact kernels, k_contact.cu)                                                :1099-1109
+//   k_end              running totals, adaptive CFL step                            :985-990
+//
+// Every kernel reads the solver's scalars (dt, time, ...) from device memory, so a sequence
+// of steps is a fixed sequence of launches with no host decision between them.
+#include "nf_internal.h"
+
+namespace nf {
+
+constexpr int BLOCK = 128;
+
+__device__ __forceinline__ unsigned long long dbits(double x) {
+    return (unsigned long long)__double_as_longlong(x);
+}
+__device__ __forceinline__ double bitsd(unsigned long long u) {
+    return __longlong_as_double((long long)u);
+}
+
+// Fixed-shape block sum: the same inputs in the same threads always add in the same order.
+__device__ double block_sum(double v, double *sh) {
+    for (int o = 16; o > 0; o >>= 1) v += __shfl_down_sync(0xffffffffu, v, o);
+    const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
+    __syncthreads();
+    if (lane == 0) sh[warp] = v;
+    __syncthreads();
+    double t = 0.0;
+    if (threadIdx.x == 0) {
+        const int warps = (blockDim.x + 31) >> 5;
+        for (int w = 0; w < warps; w++) t += sh[w];
+    }
+    return t;   // valid in thread 0
+}
+
+// ------------------------------------------------------------------------------------ begin
+
+__global__ void k_begin(Dev d, int initial) {
+    DevScalars *s = d.s;
+    const bool active = s->time < s->tEnd && s->stepsTaken < s->maxSteps;
+    s->active = active ? 1 : 0;
+    if (!active || initial) return;
+    const double dtAvg = 0.5 * (s->dtPrevious + s->dt);
+    const double half = 0.5 * d.damping * dtAvg;
+    s->decay = (1.0 - half) / (1.0 + half);
+    s->gain = dtAvg / (1.0 + half);
+    s->dtAvg = dtAvg;
+    if (d.hasWall) {                 // RigidWall.beginStep, RigidWall.java:153-156
+        s->wContact = 0;
+        s->wStuck = 0;
+    }
+}
+
+// ------------------------------------------------------------------------------------ nodal
+
+// nodalUpdate, ExplicitSolver.java:998-1062, with RigidWall.hold/crosses/arrive/slide
+// (RigidWall.java:163-259). Wall totals are reduced per block in a fixed order.
+__global__ void __launch_bounds__(BLOCK) k_nodal(Dev d) {
+    __shared__ double sh[BLOCK / 32];
+    const DevScalars *s = d.s;
+    if (!s->active) return;
+    const int i = blockIdx.x * blockDim.x + threadIdx.x;
+    const double decay = s->decay, gain = s->gain, dtAvg = s->dtAvg, dt = s->dt;
+    double impulse = 0.0, loss = 0.0, fric = 0.0;
+    if (i < d.N) {
+        uint8_t fl = d.flags[i];
+        const bool fixedR = fl & 1, fixedZ = fl & 2;
+        bool onWall = fl & 4;
+        double2 u = d.U[i], v = d.V[i];
+        const double2 f = d.F[i];
+        const double m = d.mass[i];
+        const double invM = 1.0 / m;
+        const bool resting = d.hasWall && onWall && f.y <= 0.0;
+        uint8_t ws = 0;
+        if (fixedR) {
+            v.x = 0.0;
+        } else if (resting && d.wallFriction > 0.0) {
+            // RigidWall.slide, RigidWall.java:236-259
+            const double normal = -f.y;
+            const double trial = -m * decay * v.x / gain - f.x;
+            const double limit = isinf(d.wallFriction) ? INFINITY : d.wallFriction * normal;
+            if (fabs(trial) <= limit) {
+                loss += 0.5 * m * v.x * v.x;
+                atomicAdd(&d.s->wStuck, 1);
+                ws |= NF_WALL_STUCK;
+                v.x = 0.0;
+            } else {
+                const double tangential = copysign(limit, trial);
+                const double slid = decay * v.x + gain * (f.x + tangential) / m;
+                fric += -tangential * slid * dt;
+                ws |= NF_WALL_SLID;
+                v.x = slid;
+            }
+            u.x += v.x * dt;
+        } else {
+            v.x = decay * v.x + gain * f.x * invM;
+            u.x += v.x * dt;
+        }
+        if (fixedZ) {
+            v.y = 0.0;
+        } else if (resting) {
+            impulse += -f.y * dtAvg;                         // RigidWall.hold :178-181
+            atomicAdd(&d.s->wContact, 1);
+            ws |= NF_WALL_HELD;
+        } else {
+            const double trial = decay * v.y + gain * f.y * invM;
+            const double zc = d.X0[i].y + u.y;
+            if (d.hasWall && zc + trial * dt < d.wallPlane) {
+                impulse += -m * trial;                       // RigidWall.arrive :205-209
+                loss += 0.5 * m * trial * trial;
+                atomicAdd(&d.s->wContact, 1);
+                u.y += d.wallPlane - zc;
+                v.y = 0.0;
+                onWall = true;
+                ws |= NF_WALL_ARRIVED;
+            } else {
+                v.y = trial;
+                u.y += v.y * dt;
+                if (d.hasWall) onWall = false;
+            }
+        }
+        d.U[i] = u;
+        d.V[i] = v;
+        if (d.hasWall) {
+            d.flags[i] = (uint8_t)((fl & 3) | (onWall ? 4 : 0));
+            d.wallState[i] = ws;
+        }
+        if (!(isfinite(u.x) && isfinite(u.y) && isfinite(v.x) && isfinite(v.y)))
+            atomicOr(&d.s->status, STATUS_NONFINITE);
+    }
+    if (d.hasWall) {
+        const double a = block_sum(impulse, sh);
+        const double b = block_sum(loss, sh);
+        const double c = block_sum(fric, sh);
+        if (threadIdx.x == 0) {
+            d.partials[(PARTIAL_WALL + 0) * d.maxBlocks + blockIdx.x] = a;
+            d.partials[(PARTIAL_WALL + 1) * d.maxBlocks + blockIdx.x] = b;
+            d.partials[(PARTIAL_WALL + 2) * d.maxBlocks + blockIdx.x] = c;
+        }
+    }
+    if (i == 0) {                                            // ExplicitSolver.java:973-974
+        d.s->time += dt;
+        d.s->steps += 1;
+    }
+}
+
+// ------------------------------------------------------------------------------------ geometry helpers
+
+// gaussVolume, ExplicitSolver.java:1939-1965 (reference configuration)
+__device__ double gauss_volume(const Dev &d, int e, int g) {
+    const int4 c = d.conn[e];
+    const double2 p0 = d.X0[c.x], p1 = d.X0[c.y], p2 = d.X0[c.z], p3 = d.X0[c.w];
+    const double r0 = p0.x, r1 = p1.x, r2 = p2.x, r3 = p3.x;
+    const double z0 = p0.y, z1 = p1.y, z2 = p2.y, z3 = p3.y;
+    const double G = 0.5773502691896258;
+    const double gx[4] = {-G, G, G, -G}, ge[4] = {-G, -G, G, G};
+    const double xi = d.ppe == 1 ? 0.0 : gx[g];
+    const double eta = d.ppe == 1 ? 0.0 : ge[g];
+    const double weight = d.ppe == 1 ? 4.0 : 1.0;
+    const double xm = 1.0 - xi, xp = 1.0 + xi, em = 1.0 - eta, ep = 1.0 + eta;
+    const double N0 = 0.25 * xm * em, N1 = 0.25 * xp * em;
+    const double N2 = 0.25 * xp * ep, N3 = 0.25 * xm * ep;
+    const double dN0x = -0.25 * em, dN1x = 0.25 * em, dN2x = 0.25 * ep, dN3x = -0.25 * ep;
+    const double dN0e = -0.25 * xm, dN1e = -0.25 * xp, dN2e = 0.25 * xp, dN3e = 0.25 * xm;
+    const double J00 = dN0x * r0 + dN1x * r1 + dN2x * r2 + dN3x * r3;
+    const double J01 = dN0x * z0 + dN1x * z1 + dN2x * z2 + dN3x * z3;
+    const double J10 = dN0e * r0 + dN1e * r1 + dN2e * r2 + dN3e * r3;
+    const double J11 = dN0e * z0 + dN1e * z1 + dN2e * z2 + dN3e * z3;
+    const double det = J00 * J11 - J01 * J10;
+    const double rg = N0 * r0 + N1 * r1 + N2 * r2 + N3 * r3;
+    return weight * (d.axi ? 2.0 * NF_PI * rg * det : d.thickness * det);
+}
+
+// pointStrainEnergy, ExplicitSolver.java:1666-1675
+__device__ double point_strain_energy(const Dev &d, int e, int g) {
+    const int p = e * d.ppe + g;
+    const double *sg = d.sig + 4 * (size_t)p;
+    const MatDev &m = d.mats[d.emat[e]];
+    const double press = (sg[0] + sg[1] + sg[2]) / 3.0;
+    const double a = sg[0] - press, bb = sg[1] - press, c = sg[2] - press;
+    const double dd = sg[3];
+    const double density = (a * a + bb * bb + c * c + 2.0 * dd * dd) / (4.0 * m.mu)
+                           + press * press / (2.0 * m.bulk);
+    return density * gauss_volume(d, e, g);
+}
+
+// ------------------------------------------------------------------------------------ erosion
+
+// erode, ExplicitSolver.java:663-691
+__global__ void __launch_bounds__(BLOCK) k_erode(Dev d) {
+    __shared__ double sh[BLOCK / 32];
+    if (!d.s->active) return;
+    const int e = blockIdx.x * blockDim.x + threadIdx.x;
+    double energy = 0.0;
+    if (e < d.E && !d.gone[e]) {
+        bool failed = false;
+        if (d.hasDamage) {                                  // elementDamage, :1764-1772
+            double sum = 0.0;
+            for (int g = 0; g < d.ppe; g++) {
+                const int p = e * d.ppe + g;
+                sum += damage_at(d.dStrength[p], d.dSoft[p], d.dFail[e], d.epsP[p]);
+            }
+            failed = sum / d.ppe >= d.erosionDamage;
+        }
+        const int4 c = d.conn[e];                            // currentArea, :681-691
+        const int nn[4] = {c.x, c.y, c.z, c.w};
+        double a = 0.0;
+        for (int k = 0; k < 4; k++) {
+            const int i = nn[k], j = nn[(k + 1) & 3];
+            const double2 xi = d.X0[i], xj = d.X0[j], ui = d.U[i], uj = d.U[j];
+            a += (xi.x + ui.x) * (xj.y + uj.y) - (xj.x + uj.x) * (xi.y + ui.y);
+        }
+        const bool inverted = 0.5 * a <= 0.0;
+        if (failed || inverted) {
+            d.gone[e] = 1;
+            atomicAdd(&d.s->erodedCount, 1);
+            if (inverted && !failed) atomicAdd(&d.s->invertedCount, 1);
+            for (int g = 0; g < d.ppe; g++) energy += point_strain_energy(d, e, g);
+            if (d.hasContact) {                              // Contact.forget, :329-332
+                d.dead[e] = 1;
+                d.s->stale = 1;
+            }
+        }
+    }
+    const double t = block_sum(energy, sh);
+    if (threadIdx.x == 0) d.partials[PARTIAL_ERODE * d.maxBlocks + blockIdx.x] = t;
+}
+
+// ------------------------------------------------------------------------------------ element kernels
+
+__device__ __forceinline__ void min_edge_commit(Dev &d, double minEdge) {
+    for (int o = 16; o > 0; o >>= 1) minEdge = jmin(minEdge, __shfl_down_sync(0xffffffffu, minEdge, o));
+    if ((threadIdx.x & 31) == 0) atomicMin(&d.s->minEdgeBits, dbits(minEdge));
+}
+
+// reducedIntegration, ExplicitSolver.java:1373-1504
+__global__ void __launch_bounds__(BLOCK) k_element_reduced(Dev d, int zeroStrain) {
+    if (!d.s->active) return;
+    const int e = blockIdx.x * blockDim.x + threadIdx.x;
+    double minEdge = DMAX;
+    if (e < d.E) {
+        double *ef = d.contribution + 8 * (size_t)e;
+        if (d.gone != nullptr && d.gone[e]) {
+            for (int k = 0; k < 8; k++) ef[k] = 0.0;
+        } else {
+            const double strainDt = zeroStrain ? 0.0 : d.s->dt;
+            const MatDev &fl = d.mats[d.emat[e]];
+            const double lambda = fl.lambda, mu = fl.mu;
+            const int4 c = d.conn[e];
+            const double mid = -0.5 * strainDt;
+            const double2 x0 = d.X0[c.x], x1 = d.X0[c.y], x2 = d.X0[c.z], x3 = d.X0[c.w];
+            const double2 u0 = d.U[c.x], u1 = d.U[c.y], u2 = d.U[c.z], u3 = d.U[c.w];
+            const double2 v0 = d.V[c.x], v1 = d.V[c.y], v2 = d.V[c.z], v3 = d.V[c.w];
+            double r0, r1, r2, r3, z0, z1, z2, z3;
+            if (d.finite) {                                  // cr/cz, :1176-1182
+                r0 = x0.x + u0.x + mid * v0.x; r1 = x1.x + u1.x + mid * v1.x;
+                r2 = x2.x + u2.x + mid * v2.x; r3 = x3.x + u3.x + mid * v3.x;
+                z0 = x0.y + u0.y + mid * v0.y; z1 = x1.y + u1.y + mid * v1.y;
+                z2 = x2.y + u2.y + mid * v2.y; z3 = x3.y + u3.y + mid * v3.y;
+            } else {
+                r0 = x0.x; r1 = x1.x; r2 = x2.x; r3 = x3.x;
+                z0 = x0.y; z1 = x1.y; z2 = x2.y; z3 = x3.y;
+            }
+            const double a0 = v0.x * strainDt, a1 = v1.x * strainDt;
+            const double a2 = v2.x * strainDt, a3 = v3.x * strainDt;
+            const double c0 = v0.y * strainDt, c1 = v1.y * strainDt;
+            const double c2 = v2.y * strainDt, c3 = v3.y * strainDt;
+
+            if (d.finite) minEdge = shortestEdge(minEdge, r0, r1, r2, r3, z0, z1, z2, z3);
+
+            const double J00 = 0.25 * (-r0 + r1 + r2 - r3);
+            const double J01 = 0.25 * (-z0 + z1 + z2 - z3);
+            const double J10 = 0.25 * (-r0 - r1 + r2 + r3);
+            const double J11 = 0.25 * (-z0 - z1 + z2 + z3);
+            const double det = J00 * J11 - J01 * J10;
+            const double inv = 1.0 / det;
+
+            const double d0r = 0.25 * (J01 - J11) * inv;
+            const double d1r = 0.25 * (J01 + J11) * inv;
+            const double d2r = -d0r;
+            const double d3r = -d1r;
+            const double d0z = 0.25 * (J10 - J00) * inv;
+            const double d1z = -0.25 * (J10 + J00) * inv;
+            const double d2z = -d0z;
+            const double d3z = -d1z;
+
+            const double dEpsR = d0r * a0 + d1r * a1 + d2r * a2 + d3r * a3;
+            const double dEpsZ = d0z * c0 + d1z * c1 + d2z * c2 + d3z * c3;
+            const double dRdZ = d0z * a0 + d1z * a1 + d2z * a2 + d3z * a3;
+            const double dZdR = d0r * c0 + d1r * c1 + d2r * c2 + d3r * c3;
+            const double dGamRZ = dRdZ + dZdR;
+
+            double rg = 0.0, dEpsT = 0.0;
+            if (d.axi) {
+                rg = 0.25 * (r0 + r1 + r2 + r3);
+                dEpsT = 0.25 * (a0 + a1 + a2 + a3) / rg;
+            }
+            double sg[4], bk[4];
+            {
+                const double2 *ps = reinterpret_cast<const double2 *>(d.sig + 4 * (size_t)e);
+                const double2 *pb = reinterpret_cast<const double2 *>(d.back + 4 * (size_t)e);
+                const double2 s01 = ps[0], s23 = ps[1], b01 = pb[0], b23 = pb[1];
+                sg[0] = s01.x; sg[1] = s01.y; sg[2] = s23.x; sg[3] = s23.y;
+                bk[0] = b01.x; bk[1] = b01.y; bk[2] = b23.x; bk[3] = b23.y;
+            }
+            if (d.finite) {
+                const double spinDt = 0.5 * (dZdR - dRdZ);
+                if (spinDt != 0.0) {
+                    const double cs = corot_cos(spinDt), sn = corot_sin(spinDt);
+                    corot_rotate(sg, cs, sn);
+                    corot_rotate(bk, cs, sn);
+                }
+            }
+            double epsP = d.epsP[e], work = d.wP[e];
+            if (d.hasDamage) {
+                DamageRef dr;
+                dr.failureStrain = d.dFail[e];
+                dr.strength = d.dStrength + e;
+                dr.softening = d.dSoft + e;
+                dr.width = d.dWidth + e;
+                dr.geometry = d.dGeom + 5 * (size_t)e;
+                dr.fractureEnergy = d.dGf[e];
+                dr.youngs = fl.youngs;
+                j2_update(sg, bk, epsP, work, dEpsR, dEpsZ, dEpsT, dGamRZ, lambda, mu, fl,
+                          strainDt, &dr, d.dStrength[e], d.dSoft[e]);
+            } else {
+                j2_update(sg, bk, epsP, work, dEpsR, dEpsZ, dEpsT, dGamRZ, lambda, mu, fl,
+                          strainDt, nullptr, 0.0, 0.0);
+            }
+            {
+                double2 *ps = reinterpret_cast<double2 *>(d.sig + 4 * (size_t)e);
+                double2 *pb = reinterpret_cast<double2 *>(d.back + 4 * (size_t)e);
+                ps[0] = make_double2(sg[0], sg[1]); ps[1] = make_double2(sg[2], sg[3]);
+                pb[0] = make_double2(bk[0], bk[1]); pb[1] = make_double2(bk[2], bk[3]);
+                d.epsP[e] = epsP;
+                d.wP[e] = work;
+            }
+            const double sR = sg[0], sZ = sg[1], sT = sg[2], sRZ = sg[3];
+            const double dV = 4.0 * (d.axi ? 2.0 * NF_PI * rg * det : d.thickness * det);
+
+            double g0r, g1r, g2r, g3r;
+            if (d.axi) {
+                const double hh = sT / rg * dV * 0.25;
+                g0r = -((d0r * sR + d0z * sRZ) * dV + hh);
+                g1r = -((d1r * sR + d1z * sRZ) * dV + hh);
+                g2r = -((d2r * sR + d2z * sRZ) * dV + hh);
+                g3r = -((d3r * sR + d3z * sRZ) * dV + hh);
+            } else {
+                g0r = -(d0r * sR + d0z * sRZ) * dV;
+                g1r = -(d1r * sR + d1z * sRZ) * dV;
+                g2r = -(d2r * sR + d2z * sRZ) * dV;
+                g3r = -(d3r * sR + d3z * sRZ) * dV;
+            }
+            double g0z = -(d0z * sZ + d0r * sRZ) * dV;
+            double g1z = -(d1z * sZ + d1r * sRZ) * dV;
+            double g2z = -(d2z * sZ + d2r * sRZ) * dV;
+            double g3z = -(d3z * sZ + d3r * sRZ) * dV;
+
+            const double qhg = d.hourglass;
+            if (qhg > 0.0) {
+                const double hr = r0 - r1 + r2 - r3;
+                const double hz = z0 - z1 + z2 - z3;
+                const double y0 = 1.0 - hr * d0r - hz * d0z;
+                const double y1 = -1.0 - hr * d1r - hz * d1z;
+                const double y2 = 1.0 - hr * d2r - hz * d2z;
+                const double y3 = -1.0 - hr * d3r - hz * d3z;
+                const double k = qhg * mu * dV
+                                 * (d0r * d0r + d1r * d1r + d2r * d2r + d3r * d3r
+                                    + d0z * d0z + d1z * d1z + d2z * d2z + d3z * d3z);
+                double2 hg = d.hg[e];
+                hg.x += k * (y0 * a0 + y1 * a1 + y2 * a2 + y3 * a3);
+                hg.y += k * (y0 * c0 + y1 * c1 + y2 * c2 + y3 * c3);
+                d.hg[e] = hg;
+                const double qr = hg.x, qz = hg.y;
+                g0r -= y0 * qr; g1r -= y1 * qr; g2r -= y2 * qr; g3r -= y3 * qr;
+                g0z -= y0 * qz; g1z -= y1 * qz; g2z -= y2 * qz; g3z -= y3 * qz;
+                d.hgK[e] = k;
+            }
+            double2 *ef2 = reinterpret_cast<double2 *>(ef);
+            ef2[0] = make_double2(g0r, g1r);
+            ef2[1] = make_double2(g2r, g3r);
+            ef2[2] = make_double2(g0z, g1z);
+            ef2[3] = make_double2(g2z, g3z);
+        }
+    }
+    min_edge_commit(d, minEdge);
+}
+
+// fullIntegration, ExplicitSolver.java:1219-1339
+__global__ void __launch_bounds__(BLOCK) k_element_full(Dev d, int zeroStrain) {
+    if (!d.s->active) return;
+    const int e = blockIdx.x * blockDim.x + threadIdx.x;
+    double minEdge = DMAX;
+    if (e < d.E) {
+        double *ef = d.contribution + 8 * (size_t)e;
+        if (d.gone != nullptr && d.gone[e]) {
+            for (int k = 0; k < 8; k++) ef[k] = 0.0;
+        } else {
+            const double strainDt = zeroStrain ? 0.0 : d.s->dt;
+            const MatDev &fl = d.mats[d.emat[e]];
+            const double lambda = fl.lambda, mu = fl.mu;
+            const int4 c = d.conn[e];
+            const double mid = -0.5 * strainDt;
+            const double2 x0 = d.X0[c.x], x1 = d.X0[c.y], x2 = d.X0[c.z], x3 = d.X0[c.w];
+            const double2 u0 = d.U[c.x], u1 = d.U[c.y], u2 = d.U[c.z], u3 = d.U[c.w];
+            const double2 v0 = d.V[c.x], v1 = d.V[c.y], v2 = d.V[c.z], v3 = d.V[c.w];
+            double r0, r1, r2, r3, z0, z1, z2, z3;
+            if (d.finite) {
+                r0 = x0.x + u0.x + mid * v0.x; r1 = x1.x + u1.x + mid * v1.x;
+                r2 = x2.x + u2.x + mid * v2.x; r3 = x3.x + u3.x + mid * v3.x;
+                z0 = x0.y + u0.y + mid * v0.y; z1 = x1.y + u1.y + mid * v1.y;
+                z2 = x2.y + u2.y + mid * v2.y; z3 = x3.y + u3.y + mid * v3.y;
+            } else {
+                r0 = x0.x; r1 = x1.x; r2 = x2.x; r3 = x3.x;
+                z0 = x0.y; z1 = x1.y; z2 = x2.y; z3 = x3.y;
+            }
+            const double a0 = v0.x * strainDt, a1 = v1.x * strainDt;
+            const double a2 = v2.x * strainDt, a3 = v3.x * strainDt;
+            const double c0 = v0.y * strainDt, c1 = v1.y * strainDt;
+            const double c2 = v2.y * strainDt, c3 = v3.y * strainDt;
+
+            if (d.finite) minEdge = shortestEdge(minEdge, r0, r1, r2, r3, z0, z1, z2, z3);
+
+            double g0r = 0, g1r = 0, g2r = 0, g3r = 0;
+            double g0z = 0, g1z = 0, g2z = 0, g3z = 0;
+            const double G = 0.5773502691896258;
+#pragma unroll 1
+            for (int g = 0; g < 4; g++) {
+                const double xi = (g == 0 || g == 3) ? -G : G;
+                const double eta = (g < 2) ? -G : G;
+                const double xm = 1.0 - xi, xp = 1.0 + xi;
+                const double em = 1.0 - eta, ep = 1.0 + eta;
+                const double N0 = 0.25 * xm * em, N1 = 0.25 * xp * em;
+                const double N2 = 0.25 * xp * ep, N3 = 0.25 * xm * ep;
+                const double dN0x = -0.25 * em, dN1x = 0.25 * em, dN2x = 0.25 * ep, dN3x = -0.25 * ep;
+                const double dN0e = -0.25 * xm, dN1e = -0.25 * xp, dN2e = 0.25 * xp, dN3e = 0.25 * xm;
+
+                const double J00 = dN0x * r0 + dN1x * r1 + dN2x * r2 + dN3x * r3;
+                const double J01 = dN0x * z0 + dN1x * z1 + dN2x * z2 + dN3x * z3;
+                const double J10 = dN0e * r0 + dN1e * r1 + dN2e * r2 + dN3e * r3;
+                const double J11 = dN0e * z0 + dN1e * z1 + dN2e * z2 + dN3e * z3;
+                const double det = J00 * J11 - J01 * J10;
+                const double inv = 1.0 / det;
+
+                const double d0r = (J11 * dN0x - J01 * dN0e) * inv;
+                const double d1r = (J11 * dN1x - J01 * dN1e) * inv;
+                const double d2r = (J11 * dN2x - J01 * dN2e) * inv;
+                const double d3r = (J11 * dN3x - J01 * dN3e) * inv;
+                const double d0z = (-J10 * dN0x + J00 * dN0e) * inv;
+                const double d1z = (-J10 * dN1x + J00 * dN1e) * inv;
+                const double d2z = (-J10 * dN2x + J00 * dN2e) * inv;
+                const double d3z = (-J10 * dN3x + J00 * dN3e) * inv;
+
+                const double dEpsR = d0r * a0 + d1r * a1 + d2r * a2 + d3r * a3;
+                const double dEpsZ = d0z * c0 + d1z * c1 + d2z * c2 + d3z * c3;
+                const double dRdZ = d0z * a0 + d1z * a1 + d2z * a2 + d3z * a3;
+                const double dZdR = d0r * c0 + d1r * c1 + d2r * c2 + d3r * c3;
+                const double dGamRZ = dRdZ + dZdR;
+
+                double rg = 0.0, dEpsT = 0.0;
+                if (d.axi) {
+                    rg = N0 * r0 + N1 * r1 + N2 * r2 + N3 * r3;
+                    dEpsT = (N0 * a0 + N1 * a1 + N2 * a2 + N3 * a3) / rg;
+                }
+                const int p = e * 4 + g;
+                double sg[4], bk[4];
+                {
+                    const double2 *ps = reinterpret_cast<const double2 *>(d.sig + 4 * (size_t)p);
+                    const double2 *pb = reinterpret_cast<const double2 *>(d.back + 4 * (size_t)p);
+                    const double2 s01 = ps[0], s23 = ps[1], b01 = pb[0], b23 = pb[1];
+                    sg[0] = s01.x; sg[1] = s01.y; sg[2] = s23.x; sg[3] = s23.y;
+                    bk[0] = b01.x; bk[1] = b01.y; bk[2] = b23.x; bk[3] = b23.y;
+                }
+                if (d.finite) {
+                    const double spinDt = 0.5 * (dZdR - dRdZ);
+                    if (spinDt != 0.0) {
+                        const double cs = corot_cos(spinDt), sn = corot_sin(spinDt);
+                        corot_rotate(sg, cs, sn);
+                        corot_rotate(bk, cs, sn);
+                    }
+                }
+                double epsP = d.epsP[p], work = d.wP[p];
+                if (d.hasDamage) {
+                    DamageRef dr;
+                    dr.failureStrain = d.dFail[e];
+                    dr.strength = d.dStrength + p;
+                    dr.softening = d.dSoft + p;
+                    dr.width = d.dWidth + p;
+                    dr.geometry = d.dGeom + 5 * (size_t)e;
+                    dr.fractureEnergy = d.dGf[e];
+                    dr.youngs = fl.youngs;
+                    j2_update(sg, bk, epsP, work, dEpsR, dEpsZ, dEpsT, dGamRZ, lambda, mu, fl,
+                              strainDt, &dr, d.dStrength[p], d.dSoft[p]);
+                } else {
+                    j2_update(sg, bk, epsP, work, dEpsR, dEpsZ, dEpsT, dGamRZ, lambda, mu, fl,
+                              strainDt, nullptr, 0.0, 0.0);
+                }
+                {
+                    double2 *ps = reinterpret_cast<double2 *>(d.sig + 4 * (size_t)p);
+                    double2 *pb = reinterpret_cast<double2 *>(d.back + 4 * (size_t)p);
+                    ps[0] = make_double2(sg[0], sg[1]); ps[1] = make_double2(sg[2], sg[3]);
+                    pb[0] = make_double2(bk[0], bk[1]); pb[1] = make_double2(bk[2], bk[3]);
+                    d.epsP[p] = epsP;
+                    d.wP[p] = work;
+                }
+                const double sR = sg[0], sZ = sg[1], sT = sg[2], sRZ = sg[3];
+                const double dV = d.axi ? 2.0 * NF_PI * rg * det : d.thickness * det;
+                if (d.axi) {
+                    const double hh = sT / rg * dV;
+                    g0r -= (d0r * sR + d0z * sRZ) * dV + N0 * hh;
+                    g1r -= (d1r * sR + d1z * sRZ) * dV + N1 * hh;
+                    g2r -= (d2r * sR + d2z * sRZ) * dV + N2 * hh;
+                    g3r -= (d3r * sR + d3z * sRZ) * dV + N3 * hh;
+                } else {
+                    g0r -= (d0r * sR + d0z * sRZ) * dV;
+                    g1r -= (d1r * sR + d1z * sRZ) * dV;
+                    g2r -= (d2r * sR + d2z * sRZ) * dV;
+                    g3r -= (d3r * sR + d3z * sRZ) * dV;
+                }
+                g0z -= (d0z * sZ + d0r * sRZ) * dV;
+                g1z -= (d1z * sZ + d1r * sRZ) * dV;
+                g2z -= (d2z * sZ + d2r * sRZ) * dV;
+                g3z -= (d3z * sZ + d3r * sRZ) * dV;
+            }
+            double2 *ef2 = reinterpret_cast<double2 *>(ef);
+            ef2[0] = make_double2(g0r, g1r);
+            ef2[1] = make_double2(g2r, g3r);
+            ef2[2] = make_double2(g0z, g1z);
+            ef2[3] = make_double2(g2z, g3z);
+        }
+    }
+    min_edge_commit(d, minEdge);
+}
+
+// ------------------------------------------------------------------------------------ pressure
+
+// applyPressure + pressureAt, ExplicitSolver.java:1203-1207, :1511-1556
+__global__ void k_pressure(Dev d) {
+    if (!d.s->active) return;
+    const int e = blockIdx.x * blockDim.x + threadIdx.x;
+    if (e >= d.K) return;
+    const double t = d.s->time;
+    double p = d.targetPressure;
+    if (d.rampDuration > 0.0) {
+        const double s = jmin(1.0, t / d.rampDuration);
+        p = d.targetPressure * s * s * (3.0 - 2.0 * s);
+    }
+    double *c = d.contribution + 8 * (size_t)(d.E + e);
+    const int2 ed = d.pedges[e];
+    const double2 xa = d.X0[ed.x], xb = d.X0[ed.y];
+    double ra, rb, za, zb;
+    if (d.finite) {
+        const double2 ua = d.U[ed.x], ub = d.U[ed.y], va = d.V[ed.x], vb = d.V[ed.y];
+        ra = xa.x + ua.x + 0.0 * va.x; rb = xb.x + ub.x + 0.0 * vb.x;
+        za = xa.y + ua.y + 0.0 * va.y; zb = xb.y + ub.y + 0.0 * vb.y;
+    } else {
+        ra = xa.x; rb = xb.x; za = xa.y; zb = xb.y;
+    }
+    const double tr = rb - ra;
+    const double tz = zb - za;
+    const double len = sqrt(tr * tr + tz * tz);
+    if (len == 0.0) {
+        c[0] = 0.0; c[1] = 0.0; c[4] = 0.0; c[5] = 0.0;
+        return;
+    }
+    const double nr = tz / len;
+    const double nz = -tr / len;
+    double wa, wb;
+    if (d.axi) {
+        const double circumference = 2.0 * NF_PI * len;
+        wa = circumference * (ra / 3.0 + rb / 6.0);
+        wb = circumference * (ra / 6.0 + rb / 3.0);
+    } else {
+        wa = d.thickness * len * 0.5;
+        wb = wa;
+    }
+    c[0] = p * nr * wa;
+    c[1] = p * nr * wb;
+    c[4] = p * nz * wa;
+    c[5] = p * nz * wb;
+}
+
+// ------------------------------------------------------------------------------------ gather
+
+// gather, ExplicitSolver.java:1147-1165: ascending source order, then gravity.
+__global__ void __launch_bounds__(BLOCK) k_gather(Dev d) {
+    if (!d.s->active) return;
+    const int n = blockIdx.x * blockDim.x + threadIdx.x;
+    if (n >= d.N) return;
+    double sr = 0.0, sz = 0.0;
+    const int end = d.nodeSlotStart[n + 1];
+    for (int k = d.nodeSlotStart[n]; k < end; k++) {
+        const int slot = d.nodeSlot[k];
+        sr += d.contribution[slot];
+        sz += d.contribution[slot + 4];
+    }
+    const double m = d.mass[n];
+    d.F[n] = make_double2(sr + m * d.gravR, sz + m * d.gravZ);
+    if (d.hasContact) d.contactState[n] = 0;
+}
+
+// ------------------------------------------------------------------------------------ end of step
+
+// Folds the block partials in block order, then the adaptive CFL step (:985-990).
+__global__ void k_end(Dev d, int nodeBlocks, int elemBlocks, int slotBlocks, int updateDt) {
+    DevScalars *s = d.s;
+    if (!s->active) return;
+    if (threadIdx.x != 0) return;
+    if (updateDt && d.hasWall) {
+        double a = 0.0, b = 0.0, c = 0.0;
+        for (int k = 0; k < nodeBlocks; k++) {
+            a += d.partials[(PARTIAL_WALL + 0) * d.maxBlocks + k];
+            b += d.partials[(PARTIAL_WALL + 1) * d.maxBlocks + k];
+            c += d.partials[(PARTIAL_WALL + 2) * d.maxBlocks + k];
+        }
+        s->wImpulse += a;
+        s->wEnergyLoss += b;
+        s->wFriction += c;
+    }
+    if (updateDt && d.hasErosion) {
+        double a = 0.0;
+        for (int k = 0; k < elemBlocks; k++) a += d.partials[PARTIAL_ERODE * d.maxBlocks + k];
+        s->erodedEnergy += a;
+    }
+    if (d.hasContact) {
+        double a = 0.0, b = 0.0;
+        for (int k = 0; k < slotBlocks; k++) {
+            a += d.partials[(PARTIAL_CONTACT + 0) * d.maxBlocks + k];
+            b += d.partials[(PARTIAL_CONTACT + 1) * d.maxBlocks + k];
+        }
+        s->cEnergy = a;
+        s->cDissipation += b;
+    }
+    const double minEdge = bitsd(s->minEdgeBits);
+    s->minEdgeSquared = minEdge;
+    s->minEdgeBits = dbits(DMAX);
+    if (updateDt) {
+        if (d.finite) {
+            s->dtPrevious = s->dt;
+            s->dt = d.cfl * sqrt(minEdge * d.massScale) / d.fastestWave;
+        }
+        s->stepsTaken += 1;
+    }
+}
+
+// advance(), ExplicitSolver.java:1069-1075: displacement from the current velocity, no
+// velocity update.
+__global__ void k_advance_nodes(Dev d) {
+    const int i = blockIdx.x * blockDim.x + threadIdx.x;
+    if (i >= d.N) return;
+    const uint8_t fl = d.flags[i];
+    const double dt = d.s->dt;
+    double2 u = d.U[i];
+    const double2 v = d.V[i];
+    if (!(fl & 1)) u.x += v.x * dt;
+    if (!(fl & 2)) u.y += v.y * dt;
+    d.U[i] = u;
+}
+
+__global__ void k_set_active(Dev d) {
+    d.s->active = 1;
+}
+
+// ------------------------------------------------------------------------------------ launch
+
+static void assemble(Solver &S, int zeroStrain) {
+    Dev &d = S.d;
+    const cudaStream_t st = S.stream;
+    if (d.E > 0) {
+        if (d.full) k_element_full<<<grid_for(d.E, BLOCK), BLOCK, 0, st>>>(d, zeroStrain);
+        else k_element_reduced<<<grid_for(d.E, BLOCK), BLOCK, 0, st>>>(d, zeroStrain);
+    }
+    if (d.K > 0) k_pressure<<<grid_for(d.K, BLOCK), BLOCK, 0, st>>>(d);
+    if (d.N > 0) k_gather<<<grid_for(d.N, BLOCK), BLOCK, 0, st>>>(d);
+    if (d.hasContact) launch_contact(S, true);
+}
+
+void launch_initial_assembly(Solver &S) {
+    Dev &d = S.d;
+    k_begin<<<1, 1, 0, S.stream>>>(d, 1);
+    assemble(S, 1);
+    k_end<<<1, 32, 0, S.stream>>>(d, grid_for(d.N, BLOCK), grid_for(d.E, BLOCK),
+                                  grid_for(d.N, BLOCK), 0);
+}
+
+void launch_step(Solver &S, bool) {
+    Dev &d = S.d;
+    const cudaStream_t st = S.stream;
+    k_begin<<<1, 1, 0, st>>>(d, 0);
+    if (d.N > 0) k_nodal<<<grid_for(d.N, BLOCK), BLOCK, 0, st>>>(d);
+    if (d.hasErosion && d.E > 0) k_erode<<<grid_for(d.E, BLOCK), BLOCK, 0, st>>>(d);
+    assemble(S, 0);
+    k_end<<<1, 32, 0, st>>>(d, grid_for(d.N, BLOCK), grid_for(d.E, BLOCK), grid_for(d.N, BLOCK), 1);
+}
+
+void launch_advance(Solver &S) {
+    Dev &d = S.d;
+    k_set_active<<<1, 1, 0, S.stream>>>(d);
+    if (d.N > 0) k_advance_nodes<<<grid_for(d.N, BLOCK), BLOCK, 0, S.stream>>>(d);
+    assemble(S, 0);
+    k_end<<<1, 32, 0, S.stream>>>(d, grid_for(d.N, BLOCK), grid_for(d.E, BLOCK),
+                                  grid_for(d.N, BLOCK), 0);
+}
+
+// ------------------------------------------------------------------------------------ audits
+
+enum {
+    A_KE, A_CKE, A_PZ, A_PR, A_SE, A_WP, A_FD, A_HG, A_COUNT
+};
+
+// Node audits (ExplicitSolver.java:875-886, :1610-1640), reduced per block.
+__global__ void __launch_bounds__(BLOCK) k_audit_nodes(Dev d, double *out) {
+    __shared__ double sh[BLOCK / 32];
+    const int i = blockIdx.x * blockDim.x + threadIdx.x;
+    double ke = 0, cke = 0, pz = 0, pr = 0;
+    if (i < d.N) {
+        const double hh = 0.5 * d.s->dt;
+        const double m = d.mass[i];
+        const double invM = 1.0 / m;
+        const uint8_t fl = d.flags[i];
+        const double2 v = d.V[i], f = d.F[i];
+        const bool held = d.hasWall && (fl & 4) && f.y <= 0.0;
+        const double cvr = (fl & 1) ? v.x : v.x + hh * f.x * invM;
+        const double cvz = ((fl & 2) || held) ? v.y : v.y + hh * f.y * invM;
+        cke = 0.5 * m * (cvr * cvr + cvz * cvz);
+        ke = m * (v.x * v.x + v.y * v.y);
+        pz = m * v.y;
+        pr = m * v.x;
+    }
+    const double a = block_sum(ke, sh), b = block_sum(cke, sh);
+    const double c = block_sum(pz, sh), e = block_sum(pr, sh);
+    if (threadIdx.x == 0) {
+        out[4 * blockIdx.x + 0] = a;
+        out[4 * blockIdx.x + 1] = b;
+        out[4 * blockIdx.x + 2] = c;
+        out[4 * blockIdx.x + 3] = e;
+    }
+}
+
+// Point audits (:1654-1860), reduced per block: SE, Wp V, fracture, hourglass, max eps,
+// yielded, max damage, begun, failed, clamped, max temperature (-1 marks no thermal model).
+__global__ void __launch_bounds__(BLOCK) k_audit_points(Dev d, double *out) {
+    __shared__ double sh[BLOCK / 32];
+    const int e = blockIdx.x * blockDim.x + threadIdx.x;
+    double se = 0, wp = 0, fd = 0, hg = 0, mx = 0, yielded = 0, md = 0, begun = 0, failed = 0,
+           clamped = 0, tmax = -INFINITY;
+    if (e < d.E) {
+        const MatDev &m = d.mats[d.emat[e]];
+        for (int g = 0; g < d.ppe; g++) {
+            const int p = e * d.ppe + g;
+            const double vol = gauss_volume(d, e, g);
+            if (!(d.gone != nullptr && d.gone[e])) se += point_strain_energy(d, e, g);
+            wp += d.wP[p] * vol;
+            const double ep = d.epsP[p];
+            if (ep > mx) mx = ep;
+            if (ep > 0.0) yielded += 1.0;
+            if (d.hasDamage) {
+                const double sf = d.dStrength[p], slope = d.dSoft[p];
+                if (sf > 0.0) {
+                    const double full = -sf / slope;
+                    double excess = ep - d.dFail[e];
+                    double diss = 0.0;
+                    if (excess > 0.0) {
+                        if (excess > full) excess = full;
+                        diss = excess * (sf + 0.5 * slope * excess);
+                    }
+                    fd += diss * vol;
+                    begun += 1.0;
+                }
+                const double dm = damage_at(sf, slope, d.dFail[e], ep);
+                if (dm > md) md = dm;
+                if (dm >= 1.0) failed += 1.0;
+                if (slope == -m.youngs) clamped += 1.0;
+            }
+            if (m.jc) {
+                const double t = m.room + m.tq * d.wP[p] / (m.density * m.cp);
+                tmax = jmax(tmax, t);
+            } else {
+                tmax = NAN;
+            }
+        }
+        if (!d.full && d.hourglass != 0.0) {
+            const double k = d.hgK[e];
+            const double2 q = d.hg[e];
+            if (k > 0.0) hg = 0.5 * (q.x * q.x + q.y * q.y) / k;
+        }
+    }
+    const double r0 = block_sum(se, sh), r1 = block_sum(wp, sh), r2 = block_sum(fd, sh);
+    const double r3 = block_sum(hg, sh), r4 = block_sum(yielded, sh), r5 = block_sum(begun, sh);
+    const double r6 = block_sum(failed, sh), r7 = block_sum(clamped, sh);
+    // maxima: exact, any order
+    __shared__ double smx[BLOCK], smd[BLOCK], stm[BLOCK];
+    smx[threadIdx.x] = mx; smd[threadIdx.x] = md; stm[threadIdx.x] = tmax;
+    __syncthreads();
+    if (threadIdx.x == 0) {
+        double a = 0.0, b = 0.0, c = -INFINITY;
+        for (int k = 0; k < blockDim.x; k++) {
+            if (smx[k] > a) a = smx[k];
+            if (smd[k] > b) b = smd[k];
+            c = jmax(c, stm[k]);
+        }
+        double *o = out + 12 * blockIdx.x;
+        o[0] = r0; o[1] = r1; o[2] = r2; o[3] = r3; o[4] = r4; o[5] = r5; o[6] = r6; o[7] = r7;
+        o[8] = a; o[9] = b; o[10] = c;
+        // most damaged element: first element (lowest index) holding this block's max damage
+        int worst = -1;
+        double wv = 0.0;
+        for (int k = 0; k < blockDim.x; k++) {
+            const int el = blockIdx.x * blockDim.x + k;
+            if (el >= d.E || !d.hasDamage) break;
+            for (int g = 0; g < d.ppe; g++) {
+                const int p = el * d.ppe + g;
+                const double dm = damage_at(d.dStrength[p], d.dSoft[p], d.dFail[el], d.epsP[p]);
+                if (dm > wv) { wv = dm; worst = el; }
+            }
+        }
+        o[11] = (double)worst;
+    }
+}
+
+void launch_audits(Solver &S, nf_audit *o) {
+    Dev &d = S.d;
+    const int nb = grid_for(d.N, BLOCK), eb = grid_for(d.E, BLOCK);
+    double *buf = nullptr;
+    cudaMalloc(&buf, sizeof(double) * (4 * (size_t)nb + 12 * (size_t)eb));
+    k_audit_nodes<<<nb, BLOCK, 0, S.stream>>>(d, buf);
+    k_audit_points<<<eb, BLOCK, 0, S.stream>>>(d, buf + 4 * (size_t)nb);
+    std::vector<double> h(4 * (size_t)nb + 12 * (size_t)eb);
+    cudaMemcpyAsync(h.data(), buf, sizeof(double) * h.size(), cudaMemcpyDeviceToHost, S.stream);
+    cudaStreamSynchronize(S.stream);
+    cudaFree(buf);
+    memset(o, 0, sizeof *o);
+    for (int b = 0; b < nb; b++) {
+        o->kinetic_energy += h[4 * b + 0];
+        o->centred_kinetic_energy += h[4 * b + 1];
+        o->axial_momentum += h[4 * b + 2];
+        o->radial_momentum += h[4 * b + 3];
+    }
+    o->kinetic_energy *= 0.5;
+    double yielded = 0, begun = 0, failed = 0, clamped = 0, tmax = -INFINITY;
+    double worstVal = 0.0;
+    int worst = -1;
+    const double *p = h.data() + 4 * (size_t)nb;
+    for (int b = 0; b < eb; b++) {
+        const double *q = p + 12 * (size_t)b;
+        o->strain_energy += q[0];
+        o->plastic_dissipation += q[1];
+        o->fracture_dissipation += q[2];
+        o->hourglass_energy += q[3];
+        yielded += q[4]; begun += q[5]; failed += q[6]; clamped += q[7];
+        if (q[8] > o->max_plastic_strain) o->max_plastic_strain = q[8];
+        if (q[9] > worstVal) { worstVal = q[9]; worst = (int)q[11]; }
+        if (q[9] > o->max_damage) o->max_damage = q[9];
+        if (std::isnan(q[10]) || std::isnan(tmax)) tmax = NAN;
+        else if (q[10] > tmax) tmax = q[10];
+    }
+    const double P = (double)d.E * d.ppe;
+    o->yielded_fraction = yielded / P;
+    o->damaged_fraction = d.hasDamage ? begun / P : 0.0;
+    o->failed_fraction = d.hasDamage ? failed / P : 0.0;
+    o->clamped_points = (int32_t)clamped;
+    o->max_temperature = tmax;
+    o->most_damaged_element = d.hasDamage ? worst : -1;
+    if (S.integration == NF_FULL || S.hourglass == 0.0) o->hourglass_energy = 0.0;
+}
+
+// Body measurements (TaylorImpactCase.java:272-288): exact extrema, any order.
+__global__ void k_measure(Dev d, unsigned long long *out) {
+    const int i = blockIdx.x * blockDim.x + threadIdx.x;
+    if (i >= d.N) return;
+    const double2 x = d.X0[i], u = d.U[i];
+    const double zc = x.y + u.y;
+    const double rc = x.x + u.x;
+    // order-preserving integer images of doubles
+    auto key = [](double v) -> unsigned long long {
+        const unsigned long long b = dbits(v);
+        return (b >> 63) ? ~b : (b | 0x8000000000000000ULL);
+    };
+    atomicMax(&out[0], key(zc));
+    atomicMin(&out[1], key(zc));
+    atomicMax(&out[2], key(rc));
+}
+
+static double unkey(unsigned long long k) {
+    const unsigned long long b = (k >> 63) ? (k & 0x7fffffffffffffffULL) : ~k;
+    double v;
+    memcpy(&v, &b, 8);
+    return v;
+}
+
+void launch_measure(Solver &S, nf_measure *o) {
+    Dev &d = S.d;
+    unsigned long long *buf = nullptr;
+    cudaMalloc(&buf, 3 * sizeof(unsigned long long));
+    unsigned long long init[3] = {0ULL, ~0ULL, 0ULL};
+    cudaMemcpyAsync(buf, init, sizeof init, cudaMemcpyHostToDevice, S.stream);
+    if (d.N > 0) k_measure<<<grid_for(d.N, BLOCK), BLOCK, 0, S.stream>>>(d, buf);
+    unsigned long long h[3];
+    cudaMemcpyAsync(h, buf, sizeof h, cudaMemcpyDeviceToHost, S.stream);
+    cudaStreamSynchronize(S.stream);
+    cudaFree(buf);
+    o->z_max = d.N ? unkey(h[0]) : -INFINITY;
+    o->z_min = d.N ? unkey(h[1]) : INFINITY;
+    o->length = o->z_max - o->z_min;
+    const double rmax = d.N ? unkey(h[2]) : 0.0;
+    o->mushroom_diameter = 2.0 * (rmax > 0.0 ? rmax : 0.0);
+}
+
+// ------------------------------------------------------------------------------------ material points
+
+__global__ void k_material_points(MatDev m, int count, double *sig, double *back, double *epsP,
+                                  double *work, const double *strain, double strainDt,
+                                  const double *fail, const double *gf, const double *youngs,
+                                  const double *geom, double *strength, double *soft,
+                                  double *width, double *dgamma) {
+    const int p = blockIdx.x * blockDim.x + threadIdx.x;
+    if (p >= count) return;
+    double sg[4] = {sig[4 * p], sig[4 * p + 1], sig[4 * p + 2], sig[4 * p + 3]};
+    double bk[4] = {back[4 * p], back[4 * p + 1], back[4 * p + 2], back[4 * p + 3]};
+    double ep = epsP[p], w = work[p];
+    double g;
+    if (fail != nullptr) {
+        DamageRef dr;
+        dr.failureStrain = fail[p];
+        dr.strength = strength + p;
+        dr.softening = soft + p;
+        dr.width = width + p;
+        dr.geometry = geom + 5 * (size_t)p;
+        dr.fractureEnergy = gf[p];
+        dr.youngs = youngs[p];
+        g = j2_update(sg, bk, ep, w, strain[4 * p], strain[4 * p + 1], strain[4 * p + 2],
+                      strain[4 * p + 3], m.lambda, m.mu, m, strainDt, &dr, strength[p], soft[p]);
+    } else {
+        g = j2_update(sg, bk, ep, w, strain[4 * p], strain[4 * p + 1], strain[4 * p + 2],
+                      strain[4 * p + 3], m.lambda, m.mu, m, strainDt, nullptr, 0.0, 0.0);
+    }
+    for (int k = 0; k < 4; k++) { sig[4 * p + k] = sg[k]; back[4 * p + k] = bk[k]; }
+    epsP[p] = ep;
+    work[p] = w;
+    dgamma[p] = g;
+}
+
+void launch_material_points(const MatDev &m, int count, double *sig, double *back, double *epsP,
+                            double *work, const double *strain, double strainDt,
+                            const double *fail, const double *gf, const double *youngs,
+                            const double *geom, double *strength, double *soft, double *width,
+                            double *dgamma, cudaStream_t stream) {
+    if (count <= 0) return;
+    k_material_points<<<grid_for(count, BLOCK), BLOCK, 0, stream>>>(
+        m, count, sig, back, epsP, work, strain, strainDt, fail, gf, youngs, geom, strength,
+        soft, width, dgamma);
+}
+
+}  // namespace nf

@@ -1,0 +1,171 @@
+// nf_internal.h -- device-side layout of one solver handle and the launchers that advance it.
+//
+// Layout in HBM (structure of arrays, everything resident across steps):
+//   nodes     X0 (r,z), U (ur,uz), V (vr,vz), F (fr,fz) as double2; mass double; flags uint8
+//             (bit0 fixed radial, bit1 fixed axial, bit2 on wall)
+//   elements  conn int4; material index int32; hourglass force double2 (hgR,hgZ); hourglass
+//             stiffness double; eroded uint8
+//   points    stress and back stress double[4] per point ({rr, zz, tt, rz}); plastic strain,
+//             plastic work double per point; damage strength/softening/width per point;
+//             failure strain, fracture energy, reference geometry[5] per element
+//   sources   contribution double[8] per element and per pressure edge (four radial, then
+//             four axial), gathered per node through the CSR nodeSlotStart/nodeSlot in the
+//             reference's serial order (ExplicitSolver.java:139-170, :347-366)
+//   scalars   one DevScalars record: dt, time, step count and every running total, so a step
+//             never needs the host.
+#pragma once
+
+#include <cuda_runtime.h>
+#include <cstdint>
+#include <string>
+#include <vector>
+#include <cstring>
+#include <cmath>
+
+#include "../../include/neofiz.h"
+#include "nf_device.cuh"
+
+namespace nf {
+
+// Status-word bits (nf_status_word).
+enum : uint32_t {
+    STATUS_NONFINITE = 1u,       // a nodal velocity or displacement stopped being finite
+    STATUS_GRID_HASHED = 2u,     // informational: the contact grid outgrew direct indexing
+    STATUS_BUCKET_OVERFLOW = 4u, // a contact bucket exceeded the sort bound
+};
+
+struct DevScalars {
+    double dt, dtPrevious, time;
+    double decay, gain, dtAvg;
+    unsigned long long minEdgeBits;          // Double bits of the running min edge^2
+    long long steps;
+    long long stepsTaken;                    // steps taken by the current nf_step/nf_run_until
+    long long maxSteps;                      // bound of the current call
+    double tEnd;                             // time bound of the current call
+    double minEdgeSquared;                   // from the last assembly
+    int active;                              // the run predicate: time < tEnd && taken < max
+    int pad0;
+    // rigid wall (RigidWall.java:103-107)
+    double wImpulse, wEnergyLoss, wFriction;
+    int wContact, wStuck;
+    // erosion (ExplicitSolver.java:228-234)
+    int erodedCount, invertedCount;
+    double erodedEnergy;
+    // contact (Contact.java:236-250)
+    int stale, surfEdges, surfNodes, pairs, escaped, rebuild;
+    double cEnergy, cDissipation;
+    unsigned long long maxPenBits;
+    unsigned long long bbox[4];              // order-preserving bits of rlo, zlo, -rhi, -zhi
+    unsigned long long longestBits;
+    double cellSize, gridR0, gridZ0;
+    int cols, rows;
+    long long cells;
+    int hashed, pad2;
+    uint32_t status;
+    int pad3;
+};
+
+struct Dev {
+    // sizes and switches
+    int N, E, K, ppe;
+    int axi, finite, full, hasWall, hasDamage, hasErosion, hasContact;
+    double thickness, cfl, fastestWave, massScale, damping, hourglass;
+    double gravR, gravZ, targetPressure, rampDuration, erosionDamage;
+    double wallPlane, wallFriction;
+    double cFriction, cScale, cDamping, dt0;
+    int nmat;
+    // nodes
+    double2 *X0, *U, *V, *F;
+    double *mass;
+    uint8_t *flags, *wallState, *contactState;
+    // elements / points
+    int4 *conn;
+    int32_t *emat;
+    MatDev *mats;
+    double *sig, *back, *epsP, *wP;
+    double2 *hg;
+    double *hgK;
+    uint8_t *gone, *dead;
+    double *dFail, *dGf, *dGeom, *dStrength, *dSoft, *dWidth;
+    // sources
+    double *contribution;
+    int32_t *nodeSlotStart, *nodeSlot;
+    int2 *pedges;
+    // partial sums (deterministic reductions)
+    double *partials;                        // [PARTIAL_SLOTS * maxBlocks]
+    int maxBlocks;
+    // surface / contact
+    int32_t *edgeGroup, *groupStart, *groupMember;   // element-edge -> group of equal edges
+    int32_t *surfFlag, *surfPos;             // [4E]
+    int32_t *nodeFlag, *nodePos;             // [N]
+    int32_t *segA, *segB, *segOwner;         // [4E] current surface edges
+    int32_t *surfNodes, *slotOf;             // [N]
+    int32_t *segCount, *segStart, *segOf, *segCursor;   // per surface node
+    double *cr, *cz;                         // [N]
+    double *snr, *snz, *slen;                // [4E]
+    double *pnr, *pnz;                       // [N]
+    int32_t *lastMaster, *master;            // [N]
+    uint8_t *dropped;                        // [N]
+    int32_t *bucketCount, *bucketStart, *bucketCursor;   // [bucketCap + 1]
+    int32_t *bucketEntry;                    // [8E] entries (2 s + end)
+    long long *bucketCell;                   // [8E] cell of each filed entry, by position
+    long long *entryCell;                    // [8E] cell of each entry, by entry
+    int bucketCap;
+    // pair records, per surface slot
+    int4 *pairNodes;                         // (n, a, b, valid)
+    double *pairVal;                         // [12 per slot]: role-major (n,a,b) x (normal r,z, tangent r,z)
+    double *pairEnergy, *pairDiss;           // per slot
+    int32_t *incCount, *incStart, *incCursor, *incEntry;   // per surface slot, entries (i<<2 | role)
+    // scan workspace
+    int32_t *scanTmp;
+    int scanTmpSize;
+    DevScalars *s;
+};
+
+enum { PARTIAL_WALL = 0, PARTIAL_ERODE = 3, PARTIAL_CONTACT = 4, PARTIAL_SLOTS = 6 };
+
+struct Solver {
+    Dev d{};
+    cudaStream_t stream = nullptr;
+    int device = 0;
+    long long hostSteps = 0;     // mirror of the device step count (steps are deterministic)
+    bool hasWall = false;
+    std::string err;
+    // host copies needed by reads and set-up
+    int N = 0, E = 0, K = 0, ppe = 1;
+    int formulation = 0, integration = 0, kinematics = 0;
+    double *hostScratch = nullptr;
+    size_t hostScratchBytes = 0;
+    std::vector<nf_material> materials;
+    std::vector<int32_t> emat;
+    std::vector<double> hostR, hostZ;
+    std::vector<int32_t> hostConn;
+    double massScale = 1.0;
+    double hourglass = 0.05;
+    bool contactSet = false, damageSet = false, erosionSet = false;
+    cudaGraphExec_t graph = nullptr;
+    int graphSteps = 0;
+    unsigned long long graphKey = 0;
+};
+
+// Launchers (k_step.cu)
+void launch_initial_assembly(Solver &S);
+void launch_step(Solver &S, bool predicated);
+void launch_advance(Solver &S);
+void launch_audits(Solver &S, nf_audit *out);
+void launch_measure(Solver &S, nf_measure *out);
+void launch_material_points(const MatDev &m, int count, double *sig, double *back, double *epsP,
+                            double *work, const double *strain, double strainDt,
+                            const double *fail, const double *gf, const double *youngs,
+                            const double *geom, double *strength, double *soft, double *width,
+                            double *dgamma, cudaStream_t stream);
+// Launchers (k_contact.cu)
+void launch_contact(Solver &S, bool predicated);
+// Launchers (k_scan.cu)
+void scan_exclusive(const int32_t *in, int32_t *out, int n, int32_t *totalOut, int32_t *tmp,
+                    cudaStream_t stream, const int *pred);
+size_t scan_tmp_ints(int n);
+
+int grid_for(long long n, int block);
+
+}  // namespace nf

@@ -1,0 +1,173 @@
+"""The workloads the solver is measured and checked on, built through the reference API.
+
+Each builder takes the solver class to instantiate (so the same scene can be run on the GPU
+and through the CPU oracle) and returns ``(solver, mesh, info)``.
+
+* ``taylor_rod``   -- the axisymmetric Taylor impact: TaylorImpactCase.run
+                     (validate/TaylorImpactCase.java:214-331), and the 10 x 60 rod used as the
+                     plain FP64 parity case;
+* ``perforation``  -- the plane-strain multi-body scene: a steel slug through a stacked wall of
+                     copper blocks on a rigid floor, the template of Smash.main (Smash.java:82-150)
+                     at the sizes of the 200k-quad perforation benchmark;
+* ``two_blocks``   -- Bench.build (Bench.java:142-169): two copper bodies, optional damage,
+                     floor and contact;
+* ``tube``         -- the pressurised thin wall of DefectBurst.fire / BurstCase.run
+                     (QuadMesh.cylinderWall, smoothstep pressure ramp, relaxation damping).
+"""
+from __future__ import annotations
+
+import math
+
+import numpy as np
+
+from .defects import DefectField, Weibull
+from .materials import Formulation, Integration, JohnsonCook, Kinematics, Material, Materials
+from .mesh import Outline, QuadMesh
+from .solver import Contact, RigidWall
+
+MM = 1.0e-3
+
+# The 10 x 60 rod's steel: E 200 GPa, nu 0.29, rho 7850, Johnson-Cook (350 MPa, 275 MPa,
+# 0.36, 0.022, m 1.0, 1/s, 293 K, 1793 K, 477 J/kgK, 0.9).
+ROD_JC = JohnsonCook(350.0e6, 275.0e6, 0.36, 0.022, 1.0, 1.0, 293.0, 1793.0, 477.0, 0.9)
+# Kinematic fraction 0.3 of the Johnson-Cook secant modulus at 0.6 plastic strain (the fit
+# strain the reference's rate-independent surrogate uses, TaylorImpactCase.java:147-152).
+ROD_KINEMATIC_FRACTION = 0.3
+ROD_FIT_STRAIN = 0.6
+
+
+def rod_material() -> Material:
+    secant = ROD_JC.b * ROD_FIT_STRAIN ** ROD_JC.n / ROD_FIT_STRAIN
+    base = Material("rod steel", 200.0e9, 0.29, 7850.0)
+    return base.withKinematicHardening(ROD_KINEMATIC_FRACTION * secant).withJohnsonCook(ROD_JC)
+
+
+def taylor_rod(cls, nr=10, nz=60, radius=3.8e-3, length=25.0e-3, speed=200.0, friction=0.09,
+               cfl=0.6, hourglass=0.10, integration=Integration.REDUCED, material=None):
+    """The axisymmetric rod on a rigid Coulomb anvil (TaylorImpactCase.java:214-258)."""
+    mesh = QuadMesh.solidCylinder(radius, length, nr, nz)
+    mat = material if material is not None else rod_material()
+    s = cls(mesh, mat, Formulation.AXISYMMETRIC, integration, Kinematics.FINITE_STRAIN, 1.0, cfl)
+    s.setHourglassCoefficient(hourglass)
+    for n in QuadMesh.axisNodes(nr, nz):
+        s.fixRadial(n)
+    wall = RigidWall.atZ(0.0, friction)
+    s.setRigidWall(wall)
+    s.setUniformVelocity(0.0, -speed)
+    return s, mesh, {"wall": wall, "length": length}
+
+
+def taylor_reference(cls, nr, integration=Integration.REDUCED, friction=0.0, jc=True):
+    """TaylorImpactCase.referenceAt: 4340 steel, 37.97 x 7.595 mm, 181 m/s, square cells."""
+    L, D = 37.97e-3, 7.595e-3
+    R = 0.5 * D
+    h = R / nr
+    nz = max(1, int(math.floor(L / h + 0.5)))
+    if jc:
+        mat = Material.STEEL_4340.withJohnsonCook(JohnsonCook.STEEL_4340)
+    else:
+        jc4340 = JohnsonCook.STEEL_4340
+        secant = jc4340.b * 0.6 ** jc4340.n / 0.6
+        mat = Material.STEEL_4340.yielding(jc4340.a, secant)
+    mesh = QuadMesh.solidCylinder(R, L, nr, nz)
+    s = cls(mesh, mat, Formulation.AXISYMMETRIC, integration, Kinematics.FINITE_STRAIN, 1.0, 0.5)
+    for n in QuadMesh.axisNodes(nr, nz):
+        s.fixRadial(n)
+    wall = RigidWall.atZ(0.0, friction)
+    s.setRigidWall(wall)
+    s.setUniformVelocity(0.0, -181.0)
+    return s, mesh, {"wall": wall, "length": L}
+
+
+SLUG = None
+
+
+def perforation_materials():
+    """Slug: 4340 elastic constants (205 GPa, 0.29), rho 7850, J2 800 MPa with 1 GPa linear
+    hardening. Blocks: OFHC copper (117 GPa, 0.34, 8960) with the copper Johnson-Cook law."""
+    slug = Material.STEEL_4340.yielding(800.0e6, 1.0e9)
+    copper = Material.COPPER_OFHC.withJohnsonCook(JohnsonCook.COPPER_OFHC)
+    return slug, copper
+
+
+def perforation(cls, cell=0.114 * MM, blocks=12, speed=700.0, contact_friction=0.2,
+                floor_friction=0.2, gravity=-9.81, fracture_energy=20.0e3, weibull_modulus=10.0,
+                seed=20240611, slug_scale=0.6, copper_scale=0.9, correlation=2.0 * MM,
+                erosion=1.0, depth=20.0 * MM, cfl=0.5, damage=True):
+    """A 10 x 20 mm steel slug at 700 m/s into a column of copper blocks 20 x 10 mm resting on
+    a rigid floor (the Smash.main template, Smash.java:86-132). Failure strains come from a
+    Weibull defect field of modulus 10 with a fixed seed, sampled at element centroids so the
+    field does not depend on the mesh."""
+    bodies = []
+    for j in range(blocks):
+        bodies.append(Outline.rectangle(0.0, j * 10.0 * MM, 20.0 * MM, (j + 1) * 10.0 * MM))
+    midz = 0.5 * blocks * 10.0 * MM
+    slug = Outline.rectangle(-16.0 * MM, midz - 10.0 * MM, -6.0 * MM, midz + 10.0 * MM)
+    bodies.append(slug)
+    mesh = Outline.assemble(cell, *bodies)
+    rc, zc = mesh.centroidRadii(), mesh.centroidZs()
+    isSlug = rc < 0.0
+    steel, copper = perforation_materials()
+    mats = Materials.of(*[steel if b else copper for b in isSlug])
+    s = cls(mesh, mats, Formulation.PLANE_STRAIN, Integration.REDUCED, Kinematics.FINITE_STRAIN,
+            depth, cfl)
+    if gravity:
+        s.setGravity(0.0, gravity)
+    wall = RigidWall.atZ(0.0, floor_friction)
+    s.setRigidWall(wall)
+    c = Contact(mesh).withFriction(contact_friction)
+    s.setContact(c)
+    vr = np.where(mesh.r < 0.0, speed, 0.0)
+    s.setVelocities(vr, np.zeros(mesh.nodeCount))
+    if damage:
+        eps = np.empty(mesh.elementCount)
+        V0 = correlation ** 2 * depth
+        for flag, scale in ((True, slug_scale), (False, copper_scale)):
+            field = DefectField(Weibull(scale, weibull_modulus), V0, correlation,
+                                seed + (1 if flag else 0))
+            sel = isSlug == flag
+            eps[sel] = field.failureStrainForVolume(rc[sel], zc[sel], V0)
+        s.setDamage(np.full(mesh.elementCount, fracture_energy), eps)
+        if erosion:
+            s.setErosion(erosion)
+    return s, mesh, {"wall": wall, "contact": c, "slug": isSlug}
+
+
+def two_blocks(cls, side=10, speed=120.0, damage=True, floor=True, contact=True, cell=MM):
+    """Bench.build, Bench.java:142-169."""
+    half = side * cell / 2.0
+    mesh = Outline.assemble(cell, Outline.rectangle(0.0, 0.0, side * cell, half),
+                            Outline.rectangle(0.0, half, side * cell, side * cell))
+    copper = Material.COPPER_OFHC.withJohnsonCook(JohnsonCook.COPPER_OFHC)
+    s = cls(mesh, copper, Formulation.PLANE_STRAIN, Integration.REDUCED, Kinematics.FINITE_STRAIN,
+            20.0 * MM, 0.5)
+    if damage:
+        s.setDamage(np.full(mesh.elementCount, 100.0e3), np.full(mesh.elementCount, 0.8))
+        s.setErosion(1.0)
+    if floor:
+        s.setRigidWall(RigidWall.atZ(0.0, 0.3))
+    if contact:
+        s.setContact(Contact(mesh).withFriction(0.3))
+    vz = np.where(mesh.z > half, -speed, 0.0)
+    s.setVelocities(np.zeros(mesh.nodeCount), vz)
+    return s, mesh, {}
+
+
+def tube(cls, inner=19.6e-3, outer=20.4e-3, height=4.0e-3, nr=4, nz=20, pressure=60.0e6,
+         ramp=20.0e-6, integration=Integration.FULL, kinematics=Kinematics.FINITE_STRAIN,
+         damage=True, seed=7):
+    """A pressurised thin wall with a smoothstep ramp and relaxation damping
+    (DefectBurst.fire, DefectBurst.java:385-411)."""
+    mesh = QuadMesh.cylinderWall(inner, outer, height, nr, nz)
+    copper = Material.COPPER_OFHC.withJohnsonCook(JohnsonCook.COPPER_OFHC.quasiStatic())
+    s = cls(mesh, copper, Formulation.AXISYMMETRIC, integration, kinematics, 1.0, 0.5)
+    for n in QuadMesh.axialEndNodes(nr, nz):
+        s.fixAxial(n)
+    s.setPressureRamp(pressure, ramp)
+    wave = copper.barWaveSpeed()
+    s.setRelaxationDamping(0.05, wave / (0.5 * (inner + outer)))
+    if damage:
+        field = DefectField(Weibull(0.35, 10.0), 1.0e-9, 1.0e-3, seed)
+        eps = field.sampleOnto(mesh)
+        s.setDamage(np.full(mesh.elementCount, 60.0e3), eps)
+    return s, mesh, {}
