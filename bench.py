@@ -1,0 +1,342 @@
+#!/usr/bin/env python3
+"""Element-cycles/s of the plain FP64 explicit timestep on GB300.
+
+Workload: the plane-strain multi-body perforation -- a 10 x 20 mm steel slug (J2, 800 MPa,
+1 GPa linear hardening) at 700 m/s into a column of twelve 20 x 10 mm OFHC copper blocks
+(Johnson-Cook) on a rigid floor under gravity, ~200k quads at 0.114 mm, penalty contact with
+Coulomb friction 0.2, Weibull (m = 10) failure strains with fracture-energy softening
+(G_f = 20 kJ/m^2) and erosion at full damage. One "step" is one central-difference timestep
+of the whole scene. Inputs are synthetic (the scene is generated); the state (~60 MB) fits
+in L2, so a 256 MB buffer is written between timed steps to flush it.
+
+  python bench.py [--gpus N] [--steps K] [--warmup W] [--impl ours|reference]
+
+--impl reference times the reference algorithm on the host cores: the C restatement of the
+Java path (oracle/refcpu.c) with its assembly, gather and contact search split over every
+host thread exactly as the reference's Parallel pool splits them.
+"""
+import argparse
+import json
+import os
+import statistics
+import subprocess
+import sys
+import threading
+import time
+
+HERE = os.path.dirname(os.path.abspath(__file__))
+sys.path.insert(0, HERE)
+
+CELL = 0.114e-3
+GAP = 0.5e-3
+L2_FLUSH_BYTES = 256 << 20
+
+
+def parse():
+    p = argparse.ArgumentParser()
+    p.add_argument("--gpus", type=int, default=1)
+    p.add_argument("--steps", type=int, default=400)
+    p.add_argument("--warmup", type=int, default=20)
+    p.add_argument("--impl", default="ours", choices=["ours", "reference"])
+    p.add_argument("--cell", type=float, default=CELL)
+    p.add_argument("--no-cpu-baseline", action="store_true")
+    p.add_argument("--no-e2e", action="store_true")
+    return p.parse_args()
+
+
+def dist_setup():
+    world = int(os.environ.get("WORLD_SIZE", "1"))
+    rank = int(os.environ.get("RANK", "0"))
+    local = int(os.environ.get("LOCAL_RANK", "0"))
+    if world > 1:
+        import torch
+        import torch.distributed as dist
+        os.environ.setdefault("MASTER_ADDR", "127.0.0.1")
+        backend = "nccl" if torch.cuda.is_available() else "gloo"
+        if backend == "nccl":
+            torch.cuda.set_device(local)
+        dist.init_process_group(backend)
+    return world, rank, local
+
+
+def barrier(world):
+    if world > 1:
+        import torch.distributed as dist
+        dist.barrier()
+
+
+def max_over_ranks(x, world):
+    if world == 1:
+        return x
+    import torch
+    import torch.distributed as dist
+    dev = "cuda" if dist.get_backend() == "nccl" else "cpu"
+    t = torch.tensor([x], dtype=torch.float64, device=dev)
+    dist.all_reduce(t, op=dist.ReduceOp.MAX)
+    return float(t.item())
+
+
+class Clocks:
+    """nvidia-smi samples during the timed region."""
+
+    Q = ("clocks.sm,clocks.max.sm,power.draw,clocks_event_reasons.active,"
+         "clocks_event_reasons.hw_slowdown,clocks_event_reasons.hw_thermal_slowdown,"
+         "clocks_event_reasons.sw_thermal_slowdown,clocks_event_reasons.sw_power_cap")
+
+    def __init__(self, index):
+        self.index = index
+        self.proc = None
+
+    def start(self):
+        try:
+            self.proc = subprocess.Popen(
+                ["nvidia-smi", "-i", str(self.index), f"--query-gpu={self.Q}",
+                 "--format=csv,noheader,nounits", "-lms", "200"],
+                stdout=subprocess.PIPE, stderr=subprocess.DEVNULL, text=True)
+        except OSError:
+            self.proc = None
+
+    def stop(self):
+        if self.proc is None:
+            return {"sm_mhz": None, "sm_max_mhz": None, "reasons": ["nvidia-smi unavailable"]}
+        self.proc.terminate()
+        out, _ = self.proc.communicate(timeout=10)
+        sm, smax, reasons = [], None, set()
+        names = ["hw_slowdown", "hw_thermal_slowdown", "sw_thermal_slowdown", "sw_power_cap"]
+        for line in out.strip().splitlines():
+            f = [x.strip() for x in line.split(",")]
+            if len(f) < 8:
+                continue
+            try:
+                sm.append(float(f[0]))
+                smax = float(f[1])
+            except ValueError:
+                continue
+            for n, v in zip(names, f[4:8]):
+                if v.lower() == "active":
+                    reasons.add(n)
+        return {"sm_mhz": statistics.median(sm) if sm else None, "sm_max_mhz": smax,
+                "reasons": sorted(reasons), "samples": len(sm)}
+
+
+def measured_peaks():
+    try:
+        with open(os.path.join(HERE, "MEASURED_PEAKS.json")) as f:
+            return json.load(f), "measured"
+    except OSError:
+        return {"hbm_gbs": 6800.0, "bf16_tflops": 1900.0}, "fallback"
+
+
+def live_element_steps(elements, eroded0, eroded1, steps):
+    return steps * (elements - 0.5 * (eroded0 + eroded1))
+
+
+# Algorithmic bytes of the element kernel per element (reduced, FP64, finite strain, damage):
+# connectivity 16 R; stress 32 + back stress 32 + plastic strain 8 + plastic work 8 +
+# hourglass force 16, each read and written (2 x 96); damage strength, softening and failure
+# strain 24 R. Per node: reference coordinates 16 + displacement 16 + velocity 16 R.
+ELEMENT_BYTES = 16 + 2 * 96 + 24
+NODE_BYTES = 48
+
+
+def run_ours(args, world, rank, local):
+    import torch
+    torch.cuda.set_device(local)
+    from neofiz_gb300 import build as nb
+    nb.build()
+    from neofiz_gb300 import ExplicitSolver, scenes
+
+    g, mesh, info = scenes.perforation(ExplicitSolver, cell=args.cell, gap=GAP)
+    E, N = mesh.elementCount, mesh.nodeCount
+    stream = torch.cuda.Stream()
+    g.setStream(stream.cuda_stream)
+    flush = torch.empty(L2_FLUSH_BYTES, dtype=torch.uint8, device="cuda")
+    g.run(args.warmup)
+    g.synchronize()
+    torch.cuda.synchronize()
+    eroded0 = g.erodedElements()
+    launches0 = g.launchCount()
+    clocks = Clocks(local)
+    barrier(world)
+    torch.cuda.synchronize()
+    clocks.start()
+    time.sleep(0.3)
+    evs = []
+    for _ in range(args.steps):
+        with torch.cuda.stream(stream):
+            flush.zero_()
+        a = torch.cuda.Event(enable_timing=True)
+        b = torch.cuda.Event(enable_timing=True)
+        a.record(stream)
+        g.run(1)
+        b.record(stream)
+        evs.append((a, b))
+    torch.cuda.synchronize()
+    g.synchronize()
+    clk = clocks.stop()
+    barrier(world)
+    ms = sum(a.elapsed_time(b) for a, b in evs)
+    launches = g.launchCount() - launches0
+    eroded1 = g.erodedElements()
+    ms_max = max_over_ranks(ms, world)
+    work = live_element_steps(E, eroded0, eroded1, args.steps)
+    value = world * work / (ms_max * 1e-3)
+    status = g.statusWord()
+
+    # Roofline of the dominant kernel: the same kind of steps with every kernel group
+    # bracketed by events on the solver's stream.
+    prof_steps = min(args.steps, 100)
+    g.profile(True)
+    for _ in range(prof_steps):
+        with torch.cuda.stream(stream):
+            flush.zero_()
+        g.run(1)
+    groups, covered = g.profileRead()
+    g.profile(False)
+    per_step = {k: v / max(covered, 1) for k, v in groups.items()}
+    top = max(per_step, key=per_step.get)
+    elem_ms = per_step["element"]
+    live = E - g.erodedElements()
+    elem_bytes = ELEMENT_BYTES * live + NODE_BYTES * N
+    peaks, peak_kind = measured_peaks()
+    achieved = elem_bytes / (elem_ms * 1e-3) / 1e9 if elem_ms > 0 else None
+
+    e2e = None
+    if not args.no_e2e:
+        e2e = run_e2e(args, torch)
+
+    cpu = None
+    if rank == 0 and world == 1 and not args.no_cpu_baseline:
+        cpu = cpu_baseline(args)
+
+    if rank == 0:
+        line = {
+            "metric": "element-cycles/s, plain FP64 explicit timestep (live elements x steps / s)",
+            "value": value,
+            "unit": "element-cycles/s",
+            "n_gpus": world,
+            "steps": args.steps,
+            "warmup": args.warmup,
+            "ms_per_step": ms_max / args.steps,
+            "higher_is_better": True,
+            "scaling": "weak",
+            "vs_baseline": None,
+            "dtype": "f64",
+            "data": "synthetic (generated scene; no dataset)",
+            "config": {
+                "workload": "plane-strain perforation: 10x20 mm steel slug at 700 m/s into 12 "
+                            "copper blocks 20x10 mm on a rigid floor, gravity, penalty contact "
+                            "mu 0.2, Weibull m=10 damage, erosion",
+                "elements": E, "nodes": N, "cell_mm": args.cell * 1e3,
+                "parallelism": f"replicas x{world}" if world > 1 else "single scene",
+                "l2": f"flushed between timed steps ({L2_FLUSH_BYTES >> 20} MB write)",
+                "eroded_during_timing": eroded1 - eroded0,
+            },
+            "roofline": {
+                "bound": "hbm", "kernel": "k_element_reduced",
+                "achieved": achieved, "peak": peaks.get("hbm_gbs"), "unit": "GB/s",
+                "frac": (achieved / peaks["hbm_gbs"]) if achieved else None,
+                "peak_source": peak_kind,
+                "bytes_per_launch": elem_bytes, "launch_ms": elem_ms,
+                "traffic": None,
+                "note": "FP64 arithmetic, not HBM, bounds this kernel on GB300",
+                "group_ms_per_step": per_step, "top_group": top,
+            },
+            "cpu_baseline": cpu,
+            "e2e": e2e,
+            "clocks": clk,
+            "gpu_launches": launches,
+            "status_word": status,
+        }
+        print(json.dumps(line))
+
+
+def run_e2e(args, torch):
+    """The same metric through the public API from host buffers: the scene's host inputs (mesh,
+    materials, velocities, failure strains) are generated first; the timed region then creates
+    the solver from them (every upload), sets it up, runs the steps, and reads the nodal
+    displacement and velocity fields back every 50 steps (a sampled frame) and at the end."""
+    from neofiz_gb300 import ExplicitSolver, scenes
+    steps = args.steps
+    inputs = scenes.perforation_inputs(cell=args.cell, gap=GAP)
+    mesh = inputs["mesh"]
+    E, N = mesh.elementCount, mesh.nodeCount
+    h2d = (mesh.r.nbytes + mesh.z.nbytes + mesh.conn.nbytes + 4 * E
+           + inputs["vr"].nbytes + inputs["vz"].nbytes
+           + inputs["failure_strain"].nbytes + inputs["fracture_energy"].nbytes)
+    torch.cuda.synchronize()
+    t0 = time.perf_counter()
+    g, _, _ = scenes.perforation_build(ExplicitSolver, inputs)
+    d2h = 0
+    frames = 0
+    for k in range(0, steps, 50):
+        g.run(min(50, steps - k))
+        for f in (g.radialDisplacement(), g.axialDisplacement(), g.velocityR(), g.velocityZ()):
+            d2h += f.nbytes
+        frames += 1
+    g.synchronize()
+    elapsed = time.perf_counter() - t0
+    eroded = g.erodedElements()
+    work = live_element_steps(E, 0, eroded, steps)
+    return {"value": work / elapsed, "unit": "element-cycles/s",
+            "h2d_bytes_per_step": h2d / steps, "d2h_bytes_per_step": d2h / steps,
+            "seconds": elapsed, "frames": frames,
+            "note": "create + uploads + set-up + steps + frame read-backs, host wall clock"}
+
+
+def cpu_baseline(args, budget_s=12.0):
+    """The reference algorithm on this host's cores (oracle, threaded as the reference's
+    Parallel pool), on the same scene; a bounded sample of steps."""
+    from neofiz_gb300 import scenes
+    from oracle.oracle import OracleSolver
+    cores = os.cpu_count() or 1
+    s, mesh, _ = scenes.perforation(OracleSolver, cell=args.cell, gap=GAP)
+    s.setThreads(cores)
+    s.run(2)
+    done, t = 0, 0.0
+    eroded0 = s.erodedElements()
+    while t < budget_s and done < 2000:
+        t0 = time.perf_counter()
+        s.run(5)
+        t += time.perf_counter() - t0
+        done += 5
+    work = live_element_steps(mesh.elementCount, eroded0, s.erodedElements(), done)
+    return {"value": work / t, "unit": "element-cycles/s", "cores": cores, "kind": "port",
+            "sample": f"{done} steps of the {mesh.elementCount}-quad perforation from t=0, "
+                      f"{t:.1f} s, {cores} threads"}
+
+
+def run_reference(args, world, rank):
+    if rank != 0:
+        return
+    cpu = cpu_baseline(args, budget_s=max(10.0, 2.0 * args.steps / 100.0))
+    line = {
+        "impl": "reference",
+        "metric": "element-cycles/s, plain FP64 explicit timestep (live elements x steps / s)",
+        "value": cpu["value"], "unit": "element-cycles/s", "n_gpus": world,
+        "steps": args.steps, "warmup": args.warmup, "higher_is_better": True,
+        "scaling": "weak", "vs_baseline": None, "dtype": "f64",
+        "data": "synthetic (generated scene; no dataset)",
+        "config": {"workload": "plane-strain perforation, ~200k quads (as --impl ours)",
+                   "cell_mm": args.cell * 1e3},
+        "cpu_baseline": cpu,
+        "e2e": {"value": cpu["value"], "unit": "element-cycles/s", "h2d_bytes_per_step": 0,
+                "d2h_bytes_per_step": 0},
+    }
+    print(json.dumps(line))
+
+
+def main():
+    args = parse()
+    world, rank, local = dist_setup()
+    if args.impl == "reference":
+        run_reference(args, world, rank)
+    else:
+        run_ours(args, world, rank, local)
+    if world > 1:
+        import torch.distributed as dist
+        dist.destroy_process_group()
+
+
+if __name__ == "__main__":
+    main()

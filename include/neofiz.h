@@ -235,8 +235,27 @@ nf_status nf_advance(nf_solver *h);                 /* advance(), :1069-1075 */
  * returned in *taken when non-NULL. The check is made on the device, so no per-step host
  * round trip is needed. */
 nf_status nf_run_until(nf_solver *h, double t_end, int64_t max_steps, int64_t *taken);
-/* Blocks until the handle's stream is idle. */
+/* Blocks until the handle's stream is idle. nf_step and nf_advance only enqueue work; reads,
+ * audits and nf_synchronize wait for it. */
 nf_status nf_synchronize(nf_solver *h);
+/* Runs the handle's kernels on a caller-owned cudaStream_t (passed as void*), or on its own
+ * stream again when stream is NULL. No reference counterpart: lets a host application order
+ * the solver with its own device work. */
+nf_status nf_set_stream(nf_solver *h, void *stream);
+
+/* ------------------------------------------------------------------ instrumentation */
+
+/* Kernel groups of one step, for nf_profile_read. No reference counterpart. */
+enum { NF_GROUP_NODAL = 0, NF_GROUP_ERODE, NF_GROUP_ELEMENT, NF_GROUP_PRESSURE, NF_GROUP_GATHER,
+       NF_GROUP_CONTACT, NF_GROUP_END, NF_GROUP_COUNT };
+/* When enabled, steps run without graph replay and every kernel group is bracketed by CUDA
+ * events on the handle's stream. */
+nf_status nf_profile(nf_solver *h, int32_t enable);
+/* Accumulated device milliseconds per group since profiling was enabled, and the number of
+ * steps they cover; resets the accumulation. ms must hold NF_GROUP_COUNT doubles. */
+nf_status nf_profile_read(nf_solver *h, double *ms, int64_t *steps);
+/* Kernel launches issued so far by this handle (a replayed graph counts its kernels). */
+nf_status nf_launch_count(nf_solver *h, int64_t *launches);
 
 /* ------------------------------------------------------------------ read-back */
 

@@ -20,6 +20,10 @@ NF_OK, NF_EINVAL, NF_ESTATE, NF_EDEVICE, NF_ETIMEOUT, NF_ENOMEM = range(6)
  FIELD_DAMAGE_WIDTH, FIELD_ERODED, FIELD_ON_WALL, FIELD_WALL_STATE, FIELD_CONTACT_MASTER,
  FIELD_CONTACT_STATE, FIELD_SURFACE_EDGES, FIELD_SURFACE_NODES, FIELD_FIXED) = range(25)
 
+(GROUP_NODAL, GROUP_ERODE, GROUP_ELEMENT, GROUP_PRESSURE, GROUP_GATHER, GROUP_CONTACT,
+ GROUP_END) = range(7)
+GROUP_NAMES = ("nodal", "erode", "element", "pressure", "gather", "contact", "end")
+
 WALL_HELD, WALL_STUCK, WALL_SLID, WALL_ARRIVED = 1, 2, 4, 8
 CONTACT_PAIR, CONTACT_STICK, CONTACT_SLIP = 1, 2, 4
 
@@ -118,6 +122,10 @@ _PROTOS = {
     "advance": (_S, [_H]),
     "run_until": (_S, [_H, C.c_double, C.c_int64, C.POINTER(C.c_int64)]),
     "synchronize": (_S, [_H]),
+    "set_stream": (_S, [_H, C.c_void_p]),
+    "profile": (_S, [_H, C.c_int32]),
+    "profile_read": (_S, [_H, C.POINTER(C.c_double), C.POINTER(C.c_int64)]),
+    "launch_count": (_S, [_H, C.POINTER(C.c_int64)]),
     "field_size": (_S, [_H, C.c_int32, C.POINTER(C.c_size_t), C.POINTER(C.c_size_t)]),
     "read_field": (_S, [_H, C.c_int32, C.c_void_p, C.c_size_t]),
     "write_field": (_S, [_H, C.c_int32, C.c_void_p, C.c_size_t]),

@@ -224,6 +224,7 @@ nf_status nf_create(const nf_mesh *mesh, const nf_material *materials, int32_t m
     Dev &d = S->d;
     CK(nullptr, cudaGetDevice(&S->device));
     CK(nullptr, cudaStreamCreateWithFlags(&S->stream, cudaStreamNonBlocking));
+    S->ownStream = S->stream;
     S->N = N; S->E = E; S->K = K;
     S->formulation = formulation; S->integration = integration; S->kinematics = kinematics;
     S->ppe = integration == NF_FULL ? 4 : 1;
@@ -413,7 +414,12 @@ nf_status nf_destroy(nf_solver *h) {
     Solver *S = reinterpret_cast<Solver *>(h);
     if (!S) return NF_OK;
     if (S->stream) cudaStreamSynchronize(S->stream);
-    if (S->graph) cudaGraphExecDestroy(S->graph);
+    if (S->graph1) cudaGraphExecDestroy(S->graph1);
+    if (S->graph16) cudaGraphExecDestroy(S->graph16);
+    for (auto &r : S->recs) {
+        cudaEventDestroy(r.a);
+        cudaEventDestroy(r.b);
+    }
     Dev &d = S->d;
     void *ptrs[] = {d.X0, d.U, d.V, d.F, d.mass, d.flags, d.wallState, d.contactState, d.conn,
                     d.emat, d.mats, d.sig, d.back, d.epsP, d.wP, d.hg, d.hgK, d.gone, d.dead,
@@ -428,7 +434,7 @@ nf_status nf_destroy(nf_solver *h) {
                     d.scanTmp, d.s};
     for (void *p : ptrs)
         if (p) cudaFree(p);
-    if (S->stream) cudaStreamDestroy(S->stream);
+    if (S->ownStream) cudaStreamDestroy(S->ownStream);
     delete S;
     return NF_OK;
 }
@@ -690,34 +696,99 @@ nf_status nf_set_velocities(nf_solver *h, const double *vr, const double *vz) {
     return sync_check(S);
 }
 
-// run(int), ExplicitSolver.java:936-938
+// Captures `steps` whole steps into an executable graph (kernel nodes only).
+static nf_status capture_steps(Solver &S, int steps, cudaGraphExec_t *out, int *kernels) {
+    cudaGraph_t g = nullptr;
+    CK(&S, cudaStreamBeginCapture(S.stream, cudaStreamCaptureModeThreadLocal));
+    int n = 0;
+    for (int k = 0; k < steps; k++) n += launch_step(S, true);
+    cudaError_t e = cudaStreamEndCapture(S.stream, &g);
+    if (e != cudaSuccess) return fail(&S, NF_EDEVICE, "graph capture: %s", cudaGetErrorString(e));
+    e = cudaGraphInstantiate(out, g, 0);
+    cudaGraphDestroy(g);
+    if (e != cudaSuccess) return fail(&S, NF_EDEVICE, "graph instantiate: %s", cudaGetErrorString(e));
+    *kernels = n;
+    return NF_OK;
+}
+
+// Graphs are captured for the current configuration (the Dev record the kernels receive by
+// value); any setter that changes it invalidates them.
+static nf_status ensure_graphs(Solver &S) {
+    if (S.graphValid && memcmp(&S.graphDev, &S.d, sizeof(Dev)) == 0) return NF_OK;
+    if (S.graph1) cudaGraphExecDestroy(S.graph1);
+    if (S.graph16) cudaGraphExecDestroy(S.graph16);
+    S.graph1 = S.graph16 = nullptr;
+    S.graphValid = false;
+    nf_status st = capture_steps(S, 1, &S.graph1, &S.graphKernels1);
+    if (st) return st;
+    st = capture_steps(S, 16, &S.graph16, &S.graphKernels16);
+    if (st) return st;
+    memcpy(&S.graphDev, &S.d, sizeof(Dev));
+    S.graphValid = true;
+    return NF_OK;
+}
+
+static nf_status enqueue_steps(Solver &S, int64_t steps) {
+    if (S.profiling) {
+        for (int64_t k = 0; k < steps; k++) S.launches += launch_step(S, true);
+        S.profSteps += steps;
+        return NF_OK;
+    }
+    nf_status st = ensure_graphs(S);
+    if (st) return st;
+    while (steps >= 16) {
+        CK(&S, cudaGraphLaunch(S.graph16, S.stream));
+        S.launches += S.graphKernels16;
+        steps -= 16;
+    }
+    for (; steps > 0; steps--) {
+        CK(&S, cudaGraphLaunch(S.graph1, S.stream));
+        S.launches += S.graphKernels1;
+    }
+    return NF_OK;
+}
+
+// run(int), ExplicitSolver.java:936-938. Enqueues the steps and returns; reads wait for them.
 nf_status nf_step(nf_solver *h, int64_t steps) {
     Solver &S = *reinterpret_cast<Solver *>(h);
     if (steps <= 0) return NF_OK;
-    k_set_run<<<1, 1, 0, S.stream>>>(S.d.s, INFINITY, steps);
-    if (S.hostSteps == 0) launch_initial_assembly(S);
-    for (int64_t k = 0; k < steps; k++) launch_step(S, true);
+    if (!S.unbounded) {
+        k_set_run<<<1, 1, 0, S.stream>>>(S.d.s, INFINITY, (long long)9.0e18);
+        S.launches++;
+        S.unbounded = true;
+    }
+    if (S.hostSteps == 0) {
+        S.launches += launch_initial_assembly(S);
+        S.profSteps += 0;
+    }
+    nf_status st = enqueue_steps(S, steps);
+    if (st) return st;
     S.hostSteps += steps;
-    return sync_check(S);
+    CK(&S, cudaGetLastError());
+    return NF_OK;
 }
 
 nf_status nf_advance(nf_solver *h) {
     Solver &S = *reinterpret_cast<Solver *>(h);
-    launch_advance(S);
+    S.launches += launch_advance(S);
     return sync_check(S);
 }
 
+// The loop of TaylorImpactCase.java:250-253: steps while time < t_end. The predicate is
+// evaluated on the device; chunks of sixteen predicated steps are replayed between checks.
 nf_status nf_run_until(nf_solver *h, double t_end, int64_t max_steps, int64_t *taken) {
     Solver &S = *reinterpret_cast<Solver *>(h);
     if (taken) *taken = 0;
     if (max_steps <= 0) return NF_OK;
     k_set_run<<<1, 1, 0, S.stream>>>(S.d.s, t_end, max_steps);
-    if (S.hostSteps == 0) launch_initial_assembly(S);
-    const int chunk = 32;
+    S.launches++;
+    S.unbounded = false;
+    if (S.hostSteps == 0) S.launches += launch_initial_assembly(S);
     DevScalars s{};
     for (;;) {
-        for (int k = 0; k < chunk; k++) launch_step(S, true);
-        nf_status st = read_scalars(S, &s);
+        nf_status st = enqueue_steps(S, 16);
+        if (st) return st;
+        st = read_scalars(S, &s);
         if (st) return st;
         if (!s.active || s.stepsTaken >= max_steps || !(s.time < t_end)) break;
     }
@@ -728,6 +799,46 @@ nf_status nf_run_until(nf_solver *h, double t_end, int64_t max_steps, int64_t *t
 
 nf_status nf_synchronize(nf_solver *h) {
     return sync_check(*reinterpret_cast<Solver *>(h));
+}
+
+nf_status nf_set_stream(nf_solver *h, void *stream) {
+    Solver &S = *reinterpret_cast<Solver *>(h);
+    nf_status st = sync_check(S);
+    if (st) return st;
+    S.stream = stream ? reinterpret_cast<cudaStream_t>(stream) : S.ownStream;
+    return NF_OK;
+}
+
+nf_status nf_profile(nf_solver *h, int32_t enable) {
+    Solver &S = *reinterpret_cast<Solver *>(h);
+    S.profiling = enable != 0;
+    return NF_OK;
+}
+
+nf_status nf_profile_read(nf_solver *h, double *ms, int64_t *steps) {
+    Solver &S = *reinterpret_cast<Solver *>(h);
+    nf_status st = sync_check(S);
+    if (st) return st;
+    for (auto &r : S.recs) {
+        float t = 0.0f;
+        CK(&S, cudaEventElapsedTime(&t, r.a, r.b));
+        S.profMs[r.group] += t;
+        cudaEventDestroy(r.a);
+        cudaEventDestroy(r.b);
+    }
+    S.recs.clear();
+    for (int g = 0; g < NF_GROUP_COUNT; g++) {
+        ms[g] = S.profMs[g];
+        S.profMs[g] = 0.0;
+    }
+    if (steps) *steps = S.profSteps;
+    S.profSteps = 0;
+    return NF_OK;
+}
+
+nf_status nf_launch_count(nf_solver *h, int64_t *launches) {
+    *launches = reinterpret_cast<Solver *>(h)->launches;
+    return NF_OK;
 }
 
 nf_status nf_field_size(nf_solver *h, int32_t field, size_t *count, size_t *bytes) {

@@ -166,36 +166,53 @@ __global__ void k_seg_sort(Dev d) {
 __global__ void k_contact_nodes(Dev d) {
     if (!d.s->active) return;
     const int i = blockIdx.x * blockDim.x + threadIdx.x;
-    if (i >= d.s->surfNodes) return;
-    const int n = d.surfNodes[i];
-    const double2 x = d.X0[n], u = d.U[n];
-    const double cr = x.x + u.x, cz = x.y + u.y;
-    d.cr[n] = cr;
-    d.cz[n] = cz;
-    d.incCount[i] = 0;
-    d.pairNodes[i] = make_int4(-1, -1, -1, 0);
-    atomicMin(&d.s->bbox[0], okey(cr));
-    atomicMin(&d.s->bbox[1], okey(cz));
-    atomicMax(&d.s->bbox[2], okey(cr));
-    atomicMax(&d.s->bbox[3], okey(cz));
+    unsigned long long kr0 = ~0ULL, kz0 = ~0ULL, kr1 = 0ULL, kz1 = 0ULL;
+    if (i < d.s->surfNodes) {
+        const int n = d.surfNodes[i];
+        const double2 x = d.X0[n], u = d.U[n];
+        const double cr = x.x + u.x, cz = x.y + u.y;
+        d.cr[n] = cr;
+        d.cz[n] = cz;
+        d.incCount[i] = 0;
+        d.pairNodes[i] = make_int4(-1, -1, -1, 0);
+        kr0 = kr1 = okey(cr);
+        kz0 = kz1 = okey(cz);
+    }
+    // extrema are exact in any order: reduce in the warp, one atomic per warp
+    for (int o = 16; o > 0; o >>= 1) {
+        kr0 = min(kr0, __shfl_down_sync(0xffffffffu, kr0, o));
+        kz0 = min(kz0, __shfl_down_sync(0xffffffffu, kz0, o));
+        kr1 = max(kr1, __shfl_down_sync(0xffffffffu, kr1, o));
+        kz1 = max(kz1, __shfl_down_sync(0xffffffffu, kz1, o));
+    }
+    if ((threadIdx.x & 31) == 0 && kr1 != 0ULL) {
+        atomicMin(&d.s->bbox[0], kr0);
+        atomicMin(&d.s->bbox[1], kz0);
+        atomicMax(&d.s->bbox[2], kr1);
+        atomicMax(&d.s->bbox[3], kz1);
+    }
 }
 
 __global__ void k_contact_segs(Dev d) {
     if (!d.s->active) return;
     const int s = blockIdx.x * blockDim.x + threadIdx.x;
-    if (s >= d.s->surfEdges) return;
-    const int a = d.segA[s], b = d.segB[s];
-    const double dr = d.cr[b] - d.cr[a], dz = d.cz[b] - d.cz[a];
-    const double len = sqrt(dr * dr + dz * dz);
-    d.slen[s] = len;
-    if (len > 0.0) {
-        d.snr[s] = dz / len;
-        d.snz[s] = -dr / len;
-    } else {
-        d.snr[s] = 0.0;
-        d.snz[s] = 0.0;
+    unsigned long long lb = 0ULL;
+    if (s < d.s->surfEdges) {
+        const int a = d.segA[s], b = d.segB[s];
+        const double dr = d.cr[b] - d.cr[a], dz = d.cz[b] - d.cz[a];
+        const double len = sqrt(dr * dr + dz * dz);
+        d.slen[s] = len;
+        if (len > 0.0) {
+            d.snr[s] = dz / len;
+            d.snz[s] = -dr / len;
+        } else {
+            d.snr[s] = 0.0;
+            d.snz[s] = 0.0;
+        }
+        lb = (unsigned long long)__double_as_longlong(len);
     }
-    atomicMax(&d.s->longestBits, (unsigned long long)__double_as_longlong(len));
+    for (int o = 16; o > 0; o >>= 1) lb = max(lb, __shfl_down_sync(0xffffffffu, lb, o));
+    if ((threadIdx.x & 31) == 0 && lb != 0ULL) atomicMax(&d.s->longestBits, lb);
 }
 
 __global__ void k_contact_pnorm(Dev d) {
@@ -275,7 +292,7 @@ __global__ void k_bucket_fill(Dev d) {
 __global__ void k_bucket_sort(Dev d) {
     if (!d.s->active) return;
     const int b = blockIdx.x * blockDim.x + threadIdx.x;
-    if (b >= d.bucketCap) return;
+    if (b >= d.bucketCap || (long long)b >= d.s->cells) return;
     const int lo = d.bucketStart[b], hi = d.bucketStart[b + 1];
     for (int k = lo + 1; k < hi; k++) {
         const int v = d.bucketEntry[k];
@@ -320,7 +337,7 @@ __device__ __forceinline__ double depth_of(const Dev &d, int n, int s) {
 }
 
 // Contact.nearestPenetrated, Contact.java:570-606
-__global__ void __launch_bounds__(CB) k_contact_search(Dev d) {
+__global__ void __launch_bounds__(32) k_contact_search(Dev d) {
     const DevScalars *s = d.s;
     if (!s->active) return;
     const int i = blockIdx.x * blockDim.x + threadIdx.x;
@@ -510,45 +527,71 @@ __global__ void k_inc_apply(Dev d) {
 
 // ---------------------------------------------------------------------------- launch
 
-void launch_contact(Solver &S, bool) {
+int launch_contact(Solver &S, bool) {
     Dev &d = S.d;
     const cudaStream_t st = S.stream;
     const int *rebuild = &d.s->rebuild;
     const int *active = &d.s->active;
     const int gE4 = grid_for(4LL * d.E, CB), gN = grid_for(d.N, CB), gQ = grid_for(8LL * d.E, CB);
+    int n = 0;
     k_contact_begin<<<1, 1, 0, st>>>(d);
+    n++;
     // free surface, only on the steps after an erosion (or the first)
     k_surf_flags<<<gE4, CB, 0, st>>>(d);
-    scan_exclusive(d.surfFlag, d.surfPos, 4 * d.E, &d.s->surfEdges, d.scanTmp, st, rebuild);
+    n++;
+    n += scan_exclusive(d.surfFlag, d.surfPos, 4 * d.E, &d.s->surfEdges, d.scanTmp, st, rebuild);
     k_zero_int<<<gN, CB, 0, st>>>(d.nodeFlag, d.N, rebuild);
+    n++;
     k_surf_emit<<<gE4, CB, 0, st>>>(d);
-    scan_exclusive(d.nodeFlag, d.nodePos, d.N, &d.s->surfNodes, d.scanTmp, st, rebuild);
+    n++;
+    n += scan_exclusive(d.nodeFlag, d.nodePos, d.N, &d.s->surfNodes, d.scanTmp, st, rebuild);
     k_surf_nodes<<<gN, CB, 0, st>>>(d);
+    n++;
     k_seg_count<<<gE4, CB, 0, st>>>(d);
-    scan_exclusive(d.segCount, d.segStart, d.N + 1, nullptr, d.scanTmp, st, rebuild);
+    n++;
+    n += scan_exclusive(d.segCount, d.segStart, d.N + 1, nullptr, d.scanTmp, st, rebuild);
     k_copy_int<<<grid_for(d.N + 1, CB), CB, 0, st>>>(d.segStart, d.segCursor, d.N + 1, rebuild);
+    n++;
     k_seg_fill<<<gE4, CB, 0, st>>>(d);
+    n++;
     k_seg_sort<<<gN, CB, 0, st>>>(d);
+    n++;
     // geometry and grid
     k_contact_nodes<<<gN, CB, 0, st>>>(d);
+    n++;
     k_contact_segs<<<gE4, CB, 0, st>>>(d);
+    n++;
     k_contact_pnorm<<<gN, CB, 0, st>>>(d);
+    n++;
     k_grid_setup<<<1, 1, 0, st>>>(d);
+    n++;
     k_zero_int<<<grid_for(d.bucketCap + 1, CB), CB, 0, st>>>(d.bucketCount, d.bucketCap + 1, active);
+    n++;
     k_bucket_count<<<gQ, CB, 0, st>>>(d);
-    scan_exclusive(d.bucketCount, d.bucketStart, d.bucketCap + 1, nullptr, d.scanTmp, st, active);
+    n++;
+    n += scan_exclusive(d.bucketCount, d.bucketStart, d.bucketCap + 1, nullptr, d.scanTmp, st, active);
     k_copy_int<<<grid_for(d.bucketCap + 1, CB), CB, 0, st>>>(d.bucketStart, d.bucketCursor,
                                                              d.bucketCap + 1, active);
+    n++;
     k_bucket_fill<<<gQ, CB, 0, st>>>(d);
+    n++;
     k_bucket_sort<<<grid_for(d.bucketCap, CB), CB, 0, st>>>(d);
+    n++;
     // search, resolve, ordered accumulation
-    k_contact_search<<<gN, CB, 0, st>>>(d);
+    k_contact_search<<<grid_for(d.N, 32), 32, 0, st>>>(d);
+    n++;
     k_contact_resolve<<<gN, CB, 0, st>>>(d);
+    n++;
     k_inc_count<<<gN, CB, 0, st>>>(d);
-    scan_exclusive(d.incCount, d.incStart, d.N + 1, nullptr, d.scanTmp, st, active);
+    n++;
+    n += scan_exclusive(d.incCount, d.incStart, d.N + 1, nullptr, d.scanTmp, st, active);
     k_copy_int<<<grid_for(d.N + 1, CB), CB, 0, st>>>(d.incStart, d.incCursor, d.N + 1, active);
+    n++;
     k_inc_fill<<<gN, CB, 0, st>>>(d);
+    n++;
     k_inc_apply<<<gN, CB, 0, st>>>(d);
+    n++;
+    return n;
 }
 
 }  // namespace nf

@@ -93,22 +93,30 @@ size_t scan_tmp_ints(int n) {
 // in and out may alias.
 // When pred is non-null every kernel of the scan does nothing unless *pred is non-zero, so
 // the scan can sit in a fixed launch sequence and only run on the steps that need it.
-void scan_exclusive(const int32_t *in, int32_t *out, int n, int32_t *totalOut, int32_t *tmp,
-                    cudaStream_t stream, const int *pred) {
+int scan_exclusive(const int32_t *in, int32_t *out, int n, int32_t *totalOut, int32_t *tmp,
+                   cudaStream_t stream, const int *pred) {
     if (n <= 0) {
-        if (totalOut) k_scan_zero_total<<<1, 1, 0, stream>>>(totalOut, pred);
-        return;
+        if (totalOut) {
+            k_scan_zero_total<<<1, 1, 0, stream>>>(totalOut, pred);
+            return 1;
+        }
+        return 0;
     }
     const int tiles = (n + SCAN_TILE - 1) / SCAN_TILE;
     int32_t *tileSums = tmp;
     int32_t *tileOffsets = tmp + tiles + 1;
+    int launched = 1;
     k_scan_tiles<<<tiles, SCAN_BLOCK, 0, stream>>>(in, out, n, tileSums, pred);
     if (tiles > 1) {
-        scan_exclusive(tileSums, tileOffsets, tiles, totalOut, tmp + 2 * tiles + 2, stream, pred);
+        launched += scan_exclusive(tileSums, tileOffsets, tiles, totalOut, tmp + 2 * tiles + 2,
+                                   stream, pred);
         k_scan_add<<<tiles, SCAN_BLOCK, 0, stream>>>(out, n, tileOffsets, pred);
+        launched++;
     } else if (totalOut) {
         k_scan_copy_total<<<1, 1, 0, stream>>>(tileSums, totalOut, pred);
+        launched++;
     }
+    return launched;
 }
 
 }  // namespace nf

@@ -609,35 +609,41 @@ __global__ void __launch_bounds__(BLOCK) k_gather(Dev d) {
 
 // ------------------------------------------------------------------------------------ end of step
 
-// Folds the block partials in block order, then the adaptive CFL step (:985-990).
-__global__ void k_end(Dev d, int nodeBlocks, int elemBlocks, int slotBlocks, int updateDt) {
+// Deterministic sum of n partials by one block: thread t adds partials t, t + B, t + 2B, ...
+// in that order, then the block's fixed tree adds the threads. Same inputs, same result.
+__device__ double fold(const double *p, int n, double *sh) {
+    double v = 0.0;
+    for (int k = threadIdx.x; k < n; k += blockDim.x) v += p[k];
+    return block_sum(v, sh);      // valid in thread 0
+}
+
+// Folds the block partials, then the adaptive CFL step (:985-990).
+__global__ void __launch_bounds__(256) k_end(Dev d, int nodeBlocks, int elemBlocks,
+                                            int slotBlocks, int updateDt) {
+    __shared__ double sh[256 / 32];
     DevScalars *s = d.s;
     if (!s->active) return;
+    double w0 = 0.0, w1 = 0.0, w2 = 0.0, er = 0.0, c0 = 0.0, c1 = 0.0;
+    if (updateDt && d.hasWall) {
+        w0 = fold(d.partials + (PARTIAL_WALL + 0) * d.maxBlocks, nodeBlocks, sh);
+        w1 = fold(d.partials + (PARTIAL_WALL + 1) * d.maxBlocks, nodeBlocks, sh);
+        w2 = fold(d.partials + (PARTIAL_WALL + 2) * d.maxBlocks, nodeBlocks, sh);
+    }
+    if (updateDt && d.hasErosion) er = fold(d.partials + PARTIAL_ERODE * d.maxBlocks, elemBlocks, sh);
+    if (d.hasContact) {
+        c0 = fold(d.partials + (PARTIAL_CONTACT + 0) * d.maxBlocks, slotBlocks, sh);
+        c1 = fold(d.partials + (PARTIAL_CONTACT + 1) * d.maxBlocks, slotBlocks, sh);
+    }
     if (threadIdx.x != 0) return;
     if (updateDt && d.hasWall) {
-        double a = 0.0, b = 0.0, c = 0.0;
-        for (int k = 0; k < nodeBlocks; k++) {
-            a += d.partials[(PARTIAL_WALL + 0) * d.maxBlocks + k];
-            b += d.partials[(PARTIAL_WALL + 1) * d.maxBlocks + k];
-            c += d.partials[(PARTIAL_WALL + 2) * d.maxBlocks + k];
-        }
-        s->wImpulse += a;
-        s->wEnergyLoss += b;
-        s->wFriction += c;
+        s->wImpulse += w0;
+        s->wEnergyLoss += w1;
+        s->wFriction += w2;
     }
-    if (updateDt && d.hasErosion) {
-        double a = 0.0;
-        for (int k = 0; k < elemBlocks; k++) a += d.partials[PARTIAL_ERODE * d.maxBlocks + k];
-        s->erodedEnergy += a;
-    }
+    if (updateDt && d.hasErosion) s->erodedEnergy += er;
     if (d.hasContact) {
-        double a = 0.0, b = 0.0;
-        for (int k = 0; k < slotBlocks; k++) {
-            a += d.partials[(PARTIAL_CONTACT + 0) * d.maxBlocks + k];
-            b += d.partials[(PARTIAL_CONTACT + 1) * d.maxBlocks + k];
-        }
-        s->cEnergy = a;
-        s->cDissipation += b;
+        s->cEnergy = c0;
+        s->cDissipation += c1;
     }
     const double minEdge = bitsd(s->minEdgeBits);
     s->minEdgeSquared = minEdge;
@@ -671,43 +677,98 @@ __global__ void k_set_active(Dev d) {
 
 // ------------------------------------------------------------------------------------ launch
 
-static void assemble(Solver &S, int zeroStrain) {
+static int assemble(Solver &S, int zeroStrain) {
     Dev &d = S.d;
     const cudaStream_t st = S.stream;
+    int n = 0;
+    S.mark(NF_GROUP_ELEMENT, true);
     if (d.E > 0) {
         if (d.full) k_element_full<<<grid_for(d.E, BLOCK), BLOCK, 0, st>>>(d, zeroStrain);
         else k_element_reduced<<<grid_for(d.E, BLOCK), BLOCK, 0, st>>>(d, zeroStrain);
+        n++;
     }
-    if (d.K > 0) k_pressure<<<grid_for(d.K, BLOCK), BLOCK, 0, st>>>(d);
-    if (d.N > 0) k_gather<<<grid_for(d.N, BLOCK), BLOCK, 0, st>>>(d);
-    if (d.hasContact) launch_contact(S, true);
+    S.mark(NF_GROUP_ELEMENT, false);
+    if (d.K > 0) {
+        S.mark(NF_GROUP_PRESSURE, true);
+        k_pressure<<<grid_for(d.K, BLOCK), BLOCK, 0, st>>>(d);
+        n++;
+        S.mark(NF_GROUP_PRESSURE, false);
+    }
+    S.mark(NF_GROUP_GATHER, true);
+    if (d.N > 0) {
+        k_gather<<<grid_for(d.N, BLOCK), BLOCK, 0, st>>>(d);
+        n++;
+    }
+    S.mark(NF_GROUP_GATHER, false);
+    if (d.hasContact) {
+        S.mark(NF_GROUP_CONTACT, true);
+        n += launch_contact(S, true);
+        S.mark(NF_GROUP_CONTACT, false);
+    }
+    return n;
 }
 
-void launch_initial_assembly(Solver &S) {
+int launch_initial_assembly(Solver &S) {
     Dev &d = S.d;
     k_begin<<<1, 1, 0, S.stream>>>(d, 1);
-    assemble(S, 1);
-    k_end<<<1, 32, 0, S.stream>>>(d, grid_for(d.N, BLOCK), grid_for(d.E, BLOCK),
+    int n = 1 + assemble(S, 1);
+    k_end<<<1, 256, 0, S.stream>>>(d, grid_for(d.N, BLOCK), grid_for(d.E, BLOCK),
                                   grid_for(d.N, BLOCK), 0);
+    return n + 1;
 }
 
-void launch_step(Solver &S, bool) {
+int launch_step(Solver &S, bool) {
     Dev &d = S.d;
     const cudaStream_t st = S.stream;
+    int n = 0;
+    S.mark(NF_GROUP_NODAL, true);
     k_begin<<<1, 1, 0, st>>>(d, 0);
-    if (d.N > 0) k_nodal<<<grid_for(d.N, BLOCK), BLOCK, 0, st>>>(d);
-    if (d.hasErosion && d.E > 0) k_erode<<<grid_for(d.E, BLOCK), BLOCK, 0, st>>>(d);
-    assemble(S, 0);
-    k_end<<<1, 32, 0, st>>>(d, grid_for(d.N, BLOCK), grid_for(d.E, BLOCK), grid_for(d.N, BLOCK), 1);
+    n++;
+    if (d.N > 0) {
+        k_nodal<<<grid_for(d.N, BLOCK), BLOCK, 0, st>>>(d);
+        n++;
+    }
+    S.mark(NF_GROUP_NODAL, false);
+    if (d.hasErosion && d.E > 0) {
+        S.mark(NF_GROUP_ERODE, true);
+        k_erode<<<grid_for(d.E, BLOCK), BLOCK, 0, st>>>(d);
+        n++;
+        S.mark(NF_GROUP_ERODE, false);
+    }
+    n += assemble(S, 0);
+    S.mark(NF_GROUP_END, true);
+    k_end<<<1, 256, 0, st>>>(d, grid_for(d.N, BLOCK), grid_for(d.E, BLOCK), grid_for(d.N, BLOCK), 1);
+    n++;
+    S.mark(NF_GROUP_END, false);
+    return n;
 }
 
-void launch_advance(Solver &S) {
+int launch_advance(Solver &S) {
     Dev &d = S.d;
     k_set_active<<<1, 1, 0, S.stream>>>(d);
-    if (d.N > 0) k_advance_nodes<<<grid_for(d.N, BLOCK), BLOCK, 0, S.stream>>>(d);
-    assemble(S, 0);
-    k_end<<<1, 32, 0, S.stream>>>(d, grid_for(d.N, BLOCK), grid_for(d.E, BLOCK),
+    int n = 1;
+    if (d.N > 0) {
+        k_advance_nodes<<<grid_for(d.N, BLOCK), BLOCK, 0, S.stream>>>(d);
+        n++;
+    }
+    n += assemble(S, 0);
+    k_end<<<1, 256, 0, S.stream>>>(d, grid_for(d.N, BLOCK), grid_for(d.E, BLOCK),
                                   grid_for(d.N, BLOCK), 0);
+    return n + 1;
+}
+
+// Event bracketing of kernel groups while profiling (nf_profile).
+void Solver::mark(int group, bool begin) {
+    if (!profiling) return;
+    if (begin) {
+        Rec r{group, nullptr, nullptr};
+        cudaEventCreate(&r.a);
+        cudaEventCreate(&r.b);
+        cudaEventRecord(r.a, stream);
+        recs.push_back(r);
+    } else {
+        cudaEventRecord(recs.back().b, stream);
+    }
 }
 
 // ------------------------------------------------------------------------------------ audits

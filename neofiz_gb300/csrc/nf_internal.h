@@ -143,15 +143,28 @@ struct Solver {
     double massScale = 1.0;
     double hourglass = 0.05;
     bool contactSet = false, damageSet = false, erosionSet = false;
-    cudaGraphExec_t graph = nullptr;
-    int graphSteps = 0;
-    unsigned long long graphKey = 0;
+    // launch bookkeeping
+    cudaStream_t ownStream = nullptr;
+    long long launches = 0;
+    bool unbounded = false;      // nf_step mode: no time or step bound on the device
+    // graph replay of whole steps: one- and sixteen-step graphs captured for a given Dev
+    cudaGraphExec_t graph1 = nullptr, graph16 = nullptr;
+    int graphKernels1 = 0, graphKernels16 = 0;
+    Dev graphDev{};
+    bool graphValid = false;
+    // per-group event profiling
+    bool profiling = false;
+    struct Rec { int group; cudaEvent_t a, b; };
+    std::vector<Rec> recs;
+    double profMs[NF_GROUP_COUNT] = {0};
+    long long profSteps = 0;
+    void mark(int group, bool begin);
 };
 
-// Launchers (k_step.cu)
-void launch_initial_assembly(Solver &S);
-void launch_step(Solver &S, bool predicated);
-void launch_advance(Solver &S);
+// Launchers (k_step.cu). Each returns the number of kernels it enqueued.
+int launch_initial_assembly(Solver &S);
+int launch_step(Solver &S, bool predicated);
+int launch_advance(Solver &S);
 void launch_audits(Solver &S, nf_audit *out);
 void launch_measure(Solver &S, nf_measure *out);
 void launch_material_points(const MatDev &m, int count, double *sig, double *back, double *epsP,
@@ -160,9 +173,9 @@ void launch_material_points(const MatDev &m, int count, double *sig, double *bac
                             const double *geom, double *strength, double *soft, double *width,
                             double *dgamma, cudaStream_t stream);
 // Launchers (k_contact.cu)
-void launch_contact(Solver &S, bool predicated);
+int launch_contact(Solver &S, bool predicated);
 // Launchers (k_scan.cu)
-void scan_exclusive(const int32_t *in, int32_t *out, int n, int32_t *totalOut, int32_t *tmp,
+int scan_exclusive(const int32_t *in, int32_t *out, int n, int32_t *totalOut, int32_t *tmp,
                     cudaStream_t stream, const int *pred);
 size_t scan_tmp_ints(int n);
 

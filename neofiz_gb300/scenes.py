@@ -79,9 +79,6 @@ def taylor_reference(cls, nr, integration=Integration.REDUCED, friction=0.0, jc=
     return s, mesh, {"wall": wall, "length": L}
 
 
-SLUG = None
-
-
 def perforation_materials():
     """Slug: 4340 elastic constants (205 GPa, 0.29), rho 7850, J2 800 MPa with 1 GPa linear
     hardening. Blocks: OFHC copper (117 GPa, 0.34, 8960) with the copper Johnson-Cook law."""
@@ -90,35 +87,24 @@ def perforation_materials():
     return slug, copper
 
 
-def perforation(cls, cell=0.114 * MM, blocks=12, speed=700.0, contact_friction=0.2,
-                floor_friction=0.2, gravity=-9.81, fracture_energy=20.0e3, weibull_modulus=10.0,
-                seed=20240611, slug_scale=0.6, copper_scale=0.9, correlation=2.0 * MM,
-                erosion=1.0, depth=20.0 * MM, cfl=0.5, damage=True):
-    """A 10 x 20 mm steel slug at 700 m/s into a column of copper blocks 20 x 10 mm resting on
-    a rigid floor (the Smash.main template, Smash.java:86-132). Failure strains come from a
-    Weibull defect field of modulus 10 with a fixed seed, sampled at element centroids so the
-    field does not depend on the mesh."""
+def perforation_inputs(cell=0.114 * MM, blocks=12, speed=700.0, weibull_modulus=10.0,
+                       seed=20240611, slug_scale=0.6, copper_scale=0.9, correlation=2.0 * MM,
+                       fracture_energy=20.0e3, depth=20.0 * MM, gap=6.0 * MM, damage=True):
+    """Host-side inputs of the perforation scene: the assembled lattice mesh, the per-element
+    materials, the initial velocities and the per-element damage data."""
     bodies = []
     for j in range(blocks):
         bodies.append(Outline.rectangle(0.0, j * 10.0 * MM, 20.0 * MM, (j + 1) * 10.0 * MM))
     midz = 0.5 * blocks * 10.0 * MM
-    slug = Outline.rectangle(-16.0 * MM, midz - 10.0 * MM, -6.0 * MM, midz + 10.0 * MM)
+    slug = Outline.rectangle(-10.0 * MM - gap, midz - 10.0 * MM, -gap, midz + 10.0 * MM)
     bodies.append(slug)
     mesh = Outline.assemble(cell, *bodies)
     rc, zc = mesh.centroidRadii(), mesh.centroidZs()
     isSlug = rc < 0.0
     steel, copper = perforation_materials()
     mats = Materials.of(*[steel if b else copper for b in isSlug])
-    s = cls(mesh, mats, Formulation.PLANE_STRAIN, Integration.REDUCED, Kinematics.FINITE_STRAIN,
-            depth, cfl)
-    if gravity:
-        s.setGravity(0.0, gravity)
-    wall = RigidWall.atZ(0.0, floor_friction)
-    s.setRigidWall(wall)
-    c = Contact(mesh).withFriction(contact_friction)
-    s.setContact(c)
     vr = np.where(mesh.r < 0.0, speed, 0.0)
-    s.setVelocities(vr, np.zeros(mesh.nodeCount))
+    eps = gf = None
     if damage:
         eps = np.empty(mesh.elementCount)
         V0 = correlation ** 2 * depth
@@ -127,10 +113,47 @@ def perforation(cls, cell=0.114 * MM, blocks=12, speed=700.0, contact_friction=0
                                 seed + (1 if flag else 0))
             sel = isSlug == flag
             eps[sel] = field.failureStrainForVolume(rc[sel], zc[sel], V0)
-        s.setDamage(np.full(mesh.elementCount, fracture_energy), eps)
+        gf = np.full(mesh.elementCount, fracture_energy)
+    return {"mesh": mesh, "materials": mats, "vr": vr, "vz": np.zeros(mesh.nodeCount),
+            "failure_strain": eps, "fracture_energy": gf, "slug": isSlug, "depth": depth}
+
+
+def perforation_build(cls, inputs, contact_friction=0.2, floor_friction=0.2, gravity=-9.81,
+                      erosion=1.0, cfl=0.5):
+    """The solver calls that set the perforation scene up (Smash.java:108-132)."""
+    mesh = inputs["mesh"]
+    s = cls(mesh, inputs["materials"], Formulation.PLANE_STRAIN, Integration.REDUCED,
+            Kinematics.FINITE_STRAIN, inputs["depth"], cfl)
+    if gravity:
+        s.setGravity(0.0, gravity)
+    wall = RigidWall.atZ(0.0, floor_friction)
+    s.setRigidWall(wall)
+    c = Contact(mesh).withFriction(contact_friction)
+    s.setContact(c)
+    s.setVelocities(inputs["vr"], inputs["vz"])
+    if inputs["failure_strain"] is not None:
+        s.setDamage(inputs["fracture_energy"], inputs["failure_strain"])
         if erosion:
             s.setErosion(erosion)
-    return s, mesh, {"wall": wall, "contact": c, "slug": isSlug}
+    return s, mesh, {"wall": wall, "contact": c, "slug": inputs["slug"]}
+
+
+def perforation(cls, cell=0.114 * MM, blocks=12, speed=700.0, contact_friction=0.2,
+                floor_friction=0.2, gravity=-9.81, fracture_energy=20.0e3, weibull_modulus=10.0,
+                seed=20240611, slug_scale=0.6, copper_scale=0.9, correlation=2.0 * MM,
+                erosion=1.0, depth=20.0 * MM, cfl=0.5, damage=True, gap=6.0 * MM):
+    """A 10 x 20 mm steel slug at 700 m/s into a column of copper blocks 20 x 10 mm resting on
+    a rigid floor (the Smash.main template, Smash.java:86-132). Failure strains come from a
+    Weibull defect field of modulus 10 with a fixed seed, sampled at element centroids so the
+    field does not depend on the mesh."""
+    inputs = perforation_inputs(cell=cell, blocks=blocks, speed=speed,
+                                weibull_modulus=weibull_modulus, seed=seed, slug_scale=slug_scale,
+                                copper_scale=copper_scale, correlation=correlation,
+                                fracture_energy=fracture_energy, depth=depth, gap=gap,
+                                damage=damage)
+    return perforation_build(cls, inputs, contact_friction=contact_friction,
+                             floor_friction=floor_friction, gravity=gravity, erosion=erosion,
+                             cfl=cfl)
 
 
 def two_blocks(cls, side=10, speed=120.0, damage=True, floor=True, contact=True, cell=MM):

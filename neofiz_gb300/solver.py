@@ -336,6 +336,25 @@ class ExplicitSolver:
     def synchronize(self):
         self._call(self._api.synchronize)
 
+    def setStream(self, stream_handle: int) -> None:
+        """Runs this solver's kernels on a caller-owned cudaStream_t (0: its own)."""
+        self._call(self._api.set_stream, C.c_void_p(stream_handle or None))
+
+    def profile(self, enable: bool) -> None:
+        self._call(self._api.profile, 1 if enable else 0)
+
+    def profileRead(self):
+        """(milliseconds per kernel group, steps covered) since profiling was enabled."""
+        ms = (C.c_double * 7)()
+        steps = C.c_int64()
+        self._call(self._api.profile_read, ms, C.byref(steps))
+        return dict(zip(_abi.GROUP_NAMES, list(ms))), steps.value
+
+    def launchCount(self) -> int:
+        n = C.c_int64()
+        self._call(self._api.launch_count, C.byref(n))
+        return n.value
+
     # ------------------------------------------------------------------ setup (:386-808)
     def setThreads(self, n: int) -> None:
         if n < 1:

@@ -2009,3 +2009,14 @@ API double nfo_math(int which, double x, double y) {
         default: return NAN;
     }
 }
+
+/* Device-only entry points of the ABI: no-ops on the CPU. */
+API nf_status nfo_set_stream(nfo_solver *h, void *stream) { (void)h; (void)stream; return NF_OK; }
+API nf_status nfo_profile(nfo_solver *h, int32_t enable) { (void)h; (void)enable; return NF_OK; }
+API nf_status nfo_profile_read(nfo_solver *h, double *ms, int64_t *steps) {
+    (void)h;
+    for (int g = 0; g < NF_GROUP_COUNT; g++) ms[g] = 0.0;
+    if (steps) *steps = 0;
+    return NF_OK;
+}
+API nf_status nfo_launch_count(nfo_solver *h, int64_t *launches) { (void)h; *launches = 0; return NF_OK; }
