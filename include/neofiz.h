@@ -296,6 +296,19 @@ nf_status nf_material_point_update(const nf_material *material, int32_t formulat
                                    double *work, const double *strain, double strain_dt,
                                    const nf_damage_points *damage, double *dgamma);
 
+/* No counterpart in the reference. The same update as nf_material_point_update for callers
+ * that cannot allocate device memory -- cudaMalloc/cudaFree synchronise the whole device, and
+ * a process whose GPU memory is owned by its own pool allocator has none to spare. It stages
+ * through a fixed device array of 8192 points held by the library (1.77 MB on each GPU that
+ * loads it), so it calls no allocator; count > 8192 is rejected with NF_EINVAL. The array's
+ * address is looked up on the first call on each device (make that call before any stream
+ * capture); calls share the array, so calls that overlap on the GPU race. */
+nf_status nf_material_point_update_static(const nf_material *material, int32_t formulation,
+                                          int32_t count, double *sig, double *back,
+                                          double *eps_p, double *work, const double *strain,
+                                          double strain_dt, const nf_damage_points *damage,
+                                          double *dgamma);
+
 #ifdef __cplusplus
 }
 #endif

@@ -1128,3 +1128,10 @@ nf_status nf_material_point_update(const nf_material *material, int32_t formulat
 }
 
 }  // extern "C"
+
+// Helpers shared with the allocation-free entry point (noalloc.cu).
+namespace nf {
+const char *validate_material(const nf_material &m) { return material_invalid(m); }
+MatDev material_constants(const nf_material &m, int formulation) { return mat_dev(m, formulation); }
+void set_thread_error(const char *message) { g_err = message; }
+}  // namespace nf

@@ -40,9 +40,12 @@ def test_library_exports_every_declared_symbol(library):
     assert r.returncode == 0, f"missing exports: {r.stdout} {r.stderr}"
 
 
+DEVICE_ONLY = {"nf_device_count", "nf_material_point_update_static"}
+
+
 def test_abi_binding_covers_the_header():
     from neofiz_gb300 import _abi
-    declared = set(declared_symbols()) - {"nf_device_count"}
+    declared = set(declared_symbols()) - DEVICE_ONLY
     assert declared == set(_abi.ENTRY_POINTS)
 
 
@@ -50,7 +53,7 @@ def test_oracle_exports_the_same_surface():
     from oracle import oracle
     lib = ctypes.CDLL(oracle.build())
     for name in declared_symbols():
-        if name == "nf_device_count":
+        if name in DEVICE_ONLY:
             continue
         assert hasattr(lib, "nfo_" + name[3:]), name
 
