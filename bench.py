@@ -41,6 +41,9 @@ def parse():
     p.add_argument("--cell", type=float, default=CELL)
     p.add_argument("--no-cpu-baseline", action="store_true")
     p.add_argument("--no-e2e", action="store_true")
+    p.add_argument("--no-mixed", action="store_true")
+    p.add_argument("--mixed-cell", type=float, default=0.051e-3)
+    p.add_argument("--mixed-steps", type=int, default=600)
     return p.parse_args()
 
 
@@ -209,6 +212,10 @@ def run_ours(args, world, rank, local):
     if rank == 0 and world == 1 and not args.no_cpu_baseline:
         cpu = cpu_baseline(args)
 
+    mixed = None
+    if not args.no_mixed:
+        mixed = run_mixed(args, torch)
+
     if rank == 0:
         line = {
             "metric": "element-cycles/s, plain FP64 explicit timestep (live elements x steps / s)",
@@ -244,6 +251,7 @@ def run_ours(args, world, rank, local):
             },
             "cpu_baseline": cpu,
             "e2e": e2e,
+            "mixed": mixed,
             "clocks": clk,
             "gpu_launches": launches,
             "status_word": status,
@@ -282,6 +290,78 @@ def run_e2e(args, torch):
             "h2d_bytes_per_step": h2d / steps, "d2h_bytes_per_step": d2h / steps,
             "seconds": elapsed, "frames": frames,
             "note": "create + uploads + set-up + steps + frame read-backs, host wall clock"}
+
+
+def _slug_velocity(g, mesh, slug):
+    import numpy as np
+    from neofiz_gb300 import _abi
+    vr = g.velocityR()
+    m = g.readField(_abi.FIELD_MASS)
+    nodes = np.unique(mesh.conn.reshape(-1, 4)[slug].reshape(-1))
+    return float(np.sum(m[nodes] * vr[nodes]) / np.sum(m[nodes]))
+
+
+def _balance(g, info, k0):
+    a = g._auditC()
+    w, c = info["wall"], info["contact"]
+    return (a.centred_kinetic_energy + a.strain_energy + a.plastic_dissipation
+            + a.hourglass_energy + g.erodedEnergy() + w.energyLoss() + w.frictionDissipation()
+            + c.dissipation() + c.energy()) / k0
+
+
+def run_mixed(args, torch):
+    """The mixed-precision form on the 1M-quad perforation (FP32 element arithmetic and
+    state, FP64 kinematics and audits): element-cycles/s over the last steps of a run from
+    t = 0, and its errors against the FP64 path run from the same inputs for the same steps."""
+    from neofiz_gb300 import ExplicitSolver, _abi, scenes
+    inputs = scenes.perforation_inputs(cell=args.mixed_cell, gap=GAP)
+    mesh = inputs["mesh"]
+    E = mesh.elementCount
+    steps = args.mixed_steps
+    timed = max(50, steps // 4)
+    flush = torch.empty(L2_FLUSH_BYTES, dtype=torch.uint8, device="cuda")
+    out = {}
+    for prec in (_abi.PRECISION_FP64, _abi.PRECISION_MIXED):
+        g, _, info = scenes.perforation_build(ExplicitSolver, inputs)
+        stream = torch.cuda.Stream()
+        g.setStream(stream.cuda_stream)
+        g.setPrecision(prec)
+        k0 = g.kineticEnergy()
+        g.run(steps - timed)
+        g.synchronize()
+        e0 = g.erodedElements()
+        ms = 0.0
+        for _ in range(timed):
+            with torch.cuda.stream(stream):
+                flush.zero_()
+            a = torch.cuda.Event(enable_timing=True)
+            b = torch.cuda.Event(enable_timing=True)
+            a.record(stream)
+            g.run(1)
+            b.record(stream)
+            stream.synchronize()
+            ms += a.elapsed_time(b)
+        e1 = g.erodedElements()
+        out[prec] = {"rate": live_element_steps(E, e0, e1, timed) / (ms * 1e-3),
+                     "ms_per_step": ms / timed, "slug_velocity": _slug_velocity(g, mesh, info["slug"]),
+                     "eroded": e1, "balance": _balance(g, info, k0),
+                     "status": g.statusWord()}
+        del g
+    f64, mp = out[_abi.PRECISION_FP64], out[_abi.PRECISION_MIXED]
+    return {
+        "workload": f"the perforation at {args.mixed_cell * 1e3:.3f} mm cells, {E} quads, "
+                    f"{steps} steps from t=0 (last {timed} timed, L2 flushed)",
+        "value": mp["rate"], "unit": "element-cycles/s", "ms_per_step": mp["ms_per_step"],
+        "fp64_same_scene": f64["rate"], "fp64_ms_per_step": f64["ms_per_step"],
+        "speedup_vs_fp64": mp["rate"] / f64["rate"],
+        "errors_vs_fp64": {
+            "slug_residual_velocity_rel": abs(mp["slug_velocity"] - f64["slug_velocity"])
+                                          / abs(f64["slug_velocity"]),
+            "eroded_count": [mp["eroded"], f64["eroded"]],
+            "energy_balance": [mp["balance"], f64["balance"]],
+        },
+        "status_words": [f64["status"], mp["status"]],
+    }
 
 
 def cpu_baseline(args, budget_s=12.0):

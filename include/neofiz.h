@@ -243,6 +243,14 @@ nf_status nf_synchronize(nf_solver *h);
  * the solver with its own device work. */
 nf_status nf_set_stream(nf_solver *h, void *stream);
 
+/* Arithmetic of the element kernels. NF_PRECISION_FP64 (the default) is the reference's
+ * arithmetic, bit for bit. NF_PRECISION_MIXED runs the element constitutive, hourglass and
+ * force arithmetic and keeps the element state in FP32, while nodal kinematics, the force
+ * gather, contact and all audits stay FP64. Switching converts the current state. No
+ * reference counterpart. */
+enum { NF_PRECISION_FP64 = 0, NF_PRECISION_MIXED = 1 };
+nf_status nf_set_precision(nf_solver *h, int32_t precision);
+
 /* ------------------------------------------------------------------ instrumentation */
 
 /* Kernel groups of one step, for nf_profile_read. No reference counterpart. */

@@ -24,6 +24,8 @@ NF_OK, NF_EINVAL, NF_ESTATE, NF_EDEVICE, NF_ETIMEOUT, NF_ENOMEM = range(6)
  GROUP_END) = range(7)
 GROUP_NAMES = ("nodal", "erode", "element", "pressure", "gather", "contact", "end")
 
+PRECISION_FP64, PRECISION_MIXED = 0, 1
+
 WALL_HELD, WALL_STUCK, WALL_SLID, WALL_ARRIVED = 1, 2, 4, 8
 CONTACT_PAIR, CONTACT_STICK, CONTACT_SLIP = 1, 2, 4
 
@@ -123,6 +125,7 @@ _PROTOS = {
     "run_until": (_S, [_H, C.c_double, C.c_int64, C.POINTER(C.c_int64)]),
     "synchronize": (_S, [_H]),
     "set_stream": (_S, [_H, C.c_void_p]),
+    "set_precision": (_S, [_H, C.c_int32]),
     "profile": (_S, [_H, C.c_int32]),
     "profile_read": (_S, [_H, C.POINTER(C.c_double), C.POINTER(C.c_int64)]),
     "launch_count": (_S, [_H, C.POINTER(C.c_int64)]),

@@ -166,6 +166,28 @@ nf_status read_scalars(Solver &S, DevScalars *out) {
     return sync_check(S);
 }
 
+nf_status ensure_mixed_damage(Solver &S) {
+    Dev &d = S.d;
+    if (d.dStrF) return NF_OK;
+    const size_t P = (size_t)S.E * S.ppe;
+    cudaError_t e_ = cudaSuccess;
+    if (e_ == cudaSuccess) e_ = dalloc(S, &d.dStrF, P);
+    if (e_ == cudaSuccess) e_ = dalloc(S, &d.dSoftF, P);
+    if (e_ == cudaSuccess) e_ = dalloc(S, &d.dWidthF, P);
+    if (e_ == cudaSuccess) e_ = dalloc(S, &d.dFailF, S.E);
+    if (e_ == cudaSuccess) e_ = dalloc(S, &d.dGfF, S.E);
+    if (e_ == cudaSuccess) e_ = dalloc(S, &d.dGeomF, 5 * (size_t)S.E);
+    if (e_ != cudaSuccess)
+        return fail(&S, NF_ENOMEM, "mixed-precision damage allocation failed: %s", cudaGetErrorString(e_));
+    return NF_OK;
+}
+
+// In mixed precision the FP64 element arrays are a staging copy: brought up to date before
+// anything reads them (audits, field reads).
+void mixed_to_double(Solver &S) {
+    if (S.d.mixed) launch_convert_state(S, false, 3);
+}
+
 }  // namespace
 
 extern "C" {
@@ -431,7 +453,9 @@ nf_status nf_destroy(nf_solver *h) {
                     d.master, d.dropped, d.bucketCount, d.bucketStart, d.bucketCursor,
                     d.bucketEntry, d.bucketCell, d.entryCell, d.pairNodes, d.pairVal,
                     d.pairEnergy, d.pairDiss, d.incCount, d.incStart, d.incCursor, d.incEntry,
-                    d.scanTmp, d.s};
+                    d.scanTmp, d.s, d.matsF, d.sigF, d.backF, d.epsPF, d.wPF, d.hgKF,
+                    d.contribF, d.hgF, d.dStrF, d.dSoftF, d.dWidthF, d.dFailF, d.dGfF, d.dGeomF,
+                    d.pMid, d.pCur, d.vdt, d.gaussVol};
     for (void *p : ptrs)
         if (p) cudaFree(p);
     if (S->ownStream) cudaStreamDestroy(S->ownStream);
@@ -674,6 +698,11 @@ nf_status nf_set_damage(nf_solver *h, const double *gf, const double *eps) {
     CK(&S, upload(S, d.dGeom, geom.data(), geom.size()));
     d.hasDamage = 1;
     S.damageSet = true;
+    if (d.mixed) {
+        nf_status st = ensure_mixed_damage(S);
+        if (st) return st;
+        launch_convert_state(S, true, 2);
+    }
     return sync_check(S);
 }
 
@@ -836,6 +865,54 @@ nf_status nf_profile_read(nf_solver *h, double *ms, int64_t *steps) {
     return NF_OK;
 }
 
+nf_status nf_set_precision(nf_solver *h, int32_t precision) {
+    Solver &S = *reinterpret_cast<Solver *>(h);
+    if (precision != NF_PRECISION_FP64 && precision != NF_PRECISION_MIXED)
+        return fail(&S, NF_EINVAL, "unknown precision %d", precision);
+    nf_status st = sync_check(S);
+    if (st) return st;
+    Dev &d = S.d;
+    if (precision == NF_PRECISION_MIXED && !d.mixed) {
+        const size_t P = (size_t)S.E * S.ppe;
+        if (!d.sigF) {
+            cudaError_t e_ = cudaSuccess;
+#define A(ptr, n) if (e_ == cudaSuccess) e_ = dalloc(S, &(ptr), (n))
+            A(d.matsF, S.materials.size());
+            A(d.sigF, 4 * P); A(d.backF, 4 * P); A(d.epsPF, P); A(d.wPF, P);
+            A(d.hgF, S.E); A(d.hgKF, S.E); A(d.contribF, 8 * ((size_t)S.E + S.K));
+            A(d.pMid, S.N); A(d.pCur, S.N); A(d.vdt, S.N); A(d.gaussVol, P);
+#undef A
+            if (e_ != cudaSuccess)
+                return fail(&S, NF_ENOMEM, "mixed-precision allocation failed: %s", cudaGetErrorString(e_));
+            std::vector<MatF> mf(S.materials.size());
+            for (size_t m = 0; m < S.materials.size(); m++) {
+                const MatDev a = mat_dev(S.materials[m], S.formulation);
+                MatF &o = mf[m];
+                o.lambda = (float)a.lambda; o.mu = (float)a.mu; o.bulk = (float)a.bulk;
+                o.density = (float)a.density; o.youngs = (float)a.youngs;
+                o.sy0 = (float)a.sy0; o.hIso = (float)a.hIso; o.hKin = (float)a.hKin;
+                o.a = (float)a.a; o.b = (float)a.b; o.n = (float)a.n; o.c = (float)a.c;
+                o.m = (float)a.m; o.refRate = (float)a.refRate; o.room = (float)a.room;
+                o.melt = (float)a.melt; o.cp = (float)a.cp; o.tq = (float)a.tq;
+                o.thermalCoefficient = (float)a.thermalCoefficient;
+                o.jc = a.jc;
+            }
+            CK(&S, upload(S, d.matsF, mf.data(), mf.size()));
+            launch_point_volumes(S, d.gaussVol);
+        }
+        if (S.damageSet) {
+            st = ensure_mixed_damage(S);
+            if (st) return st;
+        }
+        launch_convert_state(S, true, 3);
+        d.mixed = 1;
+    } else if (precision == NF_PRECISION_FP64 && d.mixed) {
+        launch_convert_state(S, false, 3);
+        d.mixed = 0;
+    }
+    return sync_check(S);
+}
+
 nf_status nf_launch_count(nf_solver *h, int64_t *launches) {
     *launches = reinterpret_cast<Solver *>(h)->launches;
     return NF_OK;
@@ -881,6 +958,7 @@ nf_status nf_read_field(nf_solver *h, int32_t field, void *dst, size_t nbytes) {
         return fail(&S, NF_EINVAL, "field %d holds %zu bytes, caller passed %zu", field, count * eb, nbytes);
     if (count == 0) return NF_OK;
     Dev &d = S.d;
+    mixed_to_double(S);
     st = sync_check(S);
     if (st) return st;
     auto pair = [&](const double2 *src, int comp) -> nf_status {
@@ -965,8 +1043,18 @@ nf_status nf_write_field(nf_solver *h, int32_t field, const void *src, size_t nb
     if (st) return st;
     if (nbytes != count * eb)
         return fail(&S, NF_EINVAL, "field %d holds %zu bytes, caller passed %zu", field, count * eb, nbytes);
+    mixed_to_double(S);
     st = sync_check(S);
     if (st) return st;
+    struct Refloat {
+        Solver &S;
+        ~Refloat() {
+            if (S.d.mixed) {
+                launch_convert_state(S, true, 1);
+                cudaStreamSynchronize(S.stream);
+            }
+        }
+    } refloat{S};
     auto pair = [&](double2 *dstp, int comp) -> nf_status {
         std::vector<double2> tmp(count);
         CK(&S, cudaMemcpy(tmp.data(), dstp, sizeof(double2) * count, cudaMemcpyDeviceToHost));
@@ -1020,6 +1108,7 @@ nf_status nf_get_state(nf_solver *h, nf_state *o) {
 
 nf_status nf_audits(nf_solver *h, nf_audit *o) {
     Solver &S = *reinterpret_cast<Solver *>(h);
+    mixed_to_double(S);
     nf_status st = sync_check(S);
     if (st) return st;
     launch_audits(S, o);

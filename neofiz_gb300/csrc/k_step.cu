@@ -192,6 +192,18 @@ __device__ double point_strain_energy(const Dev &d, int e, int g) {
     return density * gauss_volume(d, e, g);
 }
 
+__global__ void k_point_volumes(Dev d, double *out) {
+    const int p = blockIdx.x * blockDim.x + threadIdx.x;
+    if (p >= d.E * d.ppe) return;
+    out[p] = gauss_volume(d, p / d.ppe, p % d.ppe);
+}
+
+int launch_point_volumes(Solver &S, double *out) {
+    const int P = S.d.E * S.d.ppe;
+    if (P > 0) k_point_volumes<<<grid_for(P, BLOCK), BLOCK, 0, S.stream>>>(S.d, out);
+    return 1;
+}
+
 // ------------------------------------------------------------------------------------ erosion
 
 // erode, ExplicitSolver.java:663-691
@@ -333,7 +345,7 @@ __global__ void __launch_bounds__(BLOCK) k_element_reduced(Dev d, int zeroStrain
                           strainDt, &dr, d.dStrength[e], d.dSoft[e]);
             } else {
                 j2_update(sg, bk, epsP, work, dEpsR, dEpsZ, dEpsT, dGamRZ, lambda, mu, fl,
-                          strainDt, nullptr, 0.0, 0.0);
+                          strainDt, (const DamageRef *)nullptr, 0.0, 0.0);
             }
             {
                 double2 *ps = reinterpret_cast<double2 *>(d.sig + 4 * (size_t)e);
@@ -501,7 +513,7 @@ __global__ void __launch_bounds__(BLOCK) k_element_full(Dev d, int zeroStrain) {
                               strainDt, &dr, d.dStrength[p], d.dSoft[p]);
                 } else {
                     j2_update(sg, bk, epsP, work, dEpsR, dEpsZ, dEpsT, dGamRZ, lambda, mu, fl,
-                              strainDt, nullptr, 0.0, 0.0);
+                              strainDt, (const DamageRef *)nullptr, 0.0, 0.0);
                 }
                 {
                     double2 *ps = reinterpret_cast<double2 *>(d.sig + 4 * (size_t)p);
@@ -677,12 +689,15 @@ __global__ void k_set_active(Dev d) {
 
 // ------------------------------------------------------------------------------------ launch
 
-static int assemble(Solver &S, int zeroStrain) {
+static int assemble(Solver &S, int zeroStrain, bool prepared = false) {
     Dev &d = S.d;
     const cudaStream_t st = S.stream;
     int n = 0;
     S.mark(NF_GROUP_ELEMENT, true);
-    if (d.E > 0) {
+    if (d.mixed) {
+        if (!prepared) n += launch_prepare_mixed(S, zeroStrain);
+        n += launch_element_mixed(S, zeroStrain);
+    } else if (d.E > 0) {
         if (d.full) k_element_full<<<grid_for(d.E, BLOCK), BLOCK, 0, st>>>(d, zeroStrain);
         else k_element_reduced<<<grid_for(d.E, BLOCK), BLOCK, 0, st>>>(d, zeroStrain);
         n++;
@@ -690,14 +705,20 @@ static int assemble(Solver &S, int zeroStrain) {
     S.mark(NF_GROUP_ELEMENT, false);
     if (d.K > 0) {
         S.mark(NF_GROUP_PRESSURE, true);
-        k_pressure<<<grid_for(d.K, BLOCK), BLOCK, 0, st>>>(d);
-        n++;
+        if (d.mixed) n += launch_pressure_mixed(S);
+        else {
+            k_pressure<<<grid_for(d.K, BLOCK), BLOCK, 0, st>>>(d);
+            n++;
+        }
         S.mark(NF_GROUP_PRESSURE, false);
     }
     S.mark(NF_GROUP_GATHER, true);
     if (d.N > 0) {
-        k_gather<<<grid_for(d.N, BLOCK), BLOCK, 0, st>>>(d);
-        n++;
+        if (d.mixed) n += launch_gather_mixed(S);
+        else {
+            k_gather<<<grid_for(d.N, BLOCK), BLOCK, 0, st>>>(d);
+            n++;
+        }
     }
     S.mark(NF_GROUP_GATHER, false);
     if (d.hasContact) {
@@ -729,13 +750,23 @@ int launch_step(Solver &S, bool) {
         n++;
     }
     S.mark(NF_GROUP_NODAL, false);
+    bool prepared = false;
+    if (d.mixed) {
+        S.mark(NF_GROUP_ELEMENT, true);
+        n += launch_prepare_mixed(S, 0);
+        S.mark(NF_GROUP_ELEMENT, false);
+        prepared = true;
+    }
     if (d.hasErosion && d.E > 0) {
         S.mark(NF_GROUP_ERODE, true);
-        k_erode<<<grid_for(d.E, BLOCK), BLOCK, 0, st>>>(d);
-        n++;
+        if (d.mixed) n += launch_erode_mixed(S);
+        else {
+            k_erode<<<grid_for(d.E, BLOCK), BLOCK, 0, st>>>(d);
+            n++;
+        }
         S.mark(NF_GROUP_ERODE, false);
     }
-    n += assemble(S, 0);
+    n += assemble(S, 0, prepared);
     S.mark(NF_GROUP_END, true);
     k_end<<<1, 256, 0, st>>>(d, grid_for(d.N, BLOCK), grid_for(d.E, BLOCK), grid_for(d.N, BLOCK), 1);
     n++;
@@ -1001,7 +1032,7 @@ __global__ void k_material_points(MatDev m, int count, double *sig, double *back
                       strain[4 * p + 3], m.lambda, m.mu, m, strainDt, &dr, strength[p], soft[p]);
     } else {
         g = j2_update(sg, bk, ep, w, strain[4 * p], strain[4 * p + 1], strain[4 * p + 2],
-                      strain[4 * p + 3], m.lambda, m.mu, m, strainDt, nullptr, 0.0, 0.0);
+                      strain[4 * p + 3], m.lambda, m.mu, m, strainDt, (const DamageRef *)nullptr, 0.0, 0.0);
     }
     for (int k = 0; k < 4; k++) { sig[4 * p + k] = sg[k]; back[4 * p + k] = bk[k]; }
     epsP[p] = ep;

@@ -1,6 +1,12 @@
 // nf_device.cuh -- per-point constitutive arithmetic of the Neofiz timestep, as device
-// functions. Each expression keeps the reference's evaluation order (Java is strict
-// left-to-right IEEE double); the library is compiled with --fmad=false so nothing is fused.
+// functions templated on the real type.
+//
+// The double instantiation is the plain path: each expression keeps the reference's
+// evaluation order (Java is strict left-to-right IEEE double), the library is compiled with
+// --fmad=false so nothing is fused, and the transcendentals are the deterministic ones of
+// nf_math.h, so it is bit-identical to the CPU restatement. The float instantiation is the
+// mixed-precision path's element arithmetic: the same algorithm in FP32 with CUDA's float
+// math functions and a Johnson-Cook solve tolerance that FP32 can reach.
 //
 // Reference (src/main/java/org/neofiz/): solver/J2.java:163-296 (update), :332-375 (solve);
 // core/JohnsonCook.java:138-209; solver/Damage.java:306-347; solver/Corotational.java:59-98.
@@ -19,33 +25,66 @@ constexpr double ISOTROPIC = 1.0e-9;
 constexpr double DMAX = 1.7976931348623157e308;        // Double.MAX_VALUE
 
 // Per-material constants, unrolled once at set-up (ExplicitSolver.java:284-300, J2.Flow.of).
-struct MatDev {
-    double lambda, mu, bulk, density, youngs;
-    double sy0, hIso, hKin;
-    double a, b, n, c, m, refRate, room, melt, cp, tq, thermalCoefficient;
+template <typename T>
+struct MatT {
+    T lambda, mu, bulk, density, youngs;
+    T sy0, hIso, hKin;
+    T a, b, n, c, m, refRate, room, melt, cp, tq, thermalCoefficient;
     int jc;
     int pad;
+};
+using MatDev = MatT<double>;
+using MatF = MatT<float>;
+
+// Elementary functions per real type.
+template <typename T> struct Fn;
+template <> struct Fn<double> {
+    static __device__ __forceinline__ double pow(double a, double b) { return nf_pow(a, b); }
+    static __device__ __forceinline__ double log(double a) { return nf_log(a); }
+    static __device__ __forceinline__ double sqrt(double a) { return ::sqrt(a); }
+    static __device__ __forceinline__ double hypot(double a, double b) { return nf_hypot(a, b); }
+    static __device__ __forceinline__ double atan2(double a, double b) { return nf_atan2(a, b); }
+    static __device__ __forceinline__ double sin(double a) { return nf_sin(a); }
+    static __device__ __forceinline__ double cos(double a) { return nf_cos(a); }
+    static __device__ __forceinline__ double abs(double a) { return ::fabs(a); }
+    static constexpr double tolerance = SOLVE_TOLERANCE;
+};
+template <> struct Fn<float> {
+    static __device__ __forceinline__ float pow(float a, float b) { return ::powf(a, b); }
+    static __device__ __forceinline__ float log(float a) { return ::logf(a); }
+    static __device__ __forceinline__ float sqrt(float a) { return ::sqrtf(a); }
+    static __device__ __forceinline__ float hypot(float a, float b) { return ::hypotf(a, b); }
+    static __device__ __forceinline__ float atan2(float a, float b) { return ::atan2f(a, b); }
+    static __device__ __forceinline__ float sin(float a) { return ::sinf(a); }
+    static __device__ __forceinline__ float cos(float a) { return ::cosf(a); }
+    static __device__ __forceinline__ float abs(float a) { return ::fabsf(a); }
+    // 1e-10 A is below FP32 resolution of the residual; 1e-5 A is a few ulp of it.
+    static constexpr float tolerance = 1.0e-5f;
 };
 
 // Damage state of one point (Damage.java:166-200), accessed through pointers so the
 // element kernel can leave the rarely-touched geometry in global memory.
-struct DamageRef {
-    double failureStrain;
-    double *strength, *softening, *width;
-    const double *geometry;      // 5 doubles: area, uR, uZ, vR, vZ (reference configuration)
-    double fractureEnergy, youngs;
+template <typename T>
+struct DamageRefT {
+    T failureStrain;
+    T *strength, *softening, *width;
+    const T *geometry;           // 5 values: area, uR, uZ, vR, vZ (reference configuration)
+    T fractureEnergy, youngs;
 };
+using DamageRef = DamageRefT<double>;
 
-__device__ __forceinline__ double jmin(double a, double b) {      // Math.min
+template <typename T>
+__device__ __forceinline__ T jmin(T a, T b) {                      // Math.min
     if (a != a) return a;
     if (b != b) return b;
-    if (a == 0.0 && b == 0.0) return signbit(a) ? a : b;
+    if (a == T(0) && b == T(0)) return signbit(a) ? a : b;
     return a <= b ? a : b;
 }
-__device__ __forceinline__ double jmax(double a, double b) {      // Math.max
+template <typename T>
+__device__ __forceinline__ T jmax(T a, T b) {                      // Math.max
     if (a != a) return a;
     if (b != b) return b;
-    if (a == 0.0 && b == 0.0) return signbit(a) ? b : a;
+    if (a == T(0) && b == T(0)) return signbit(a) ? b : a;
     return a >= b ? a : b;
 }
 __device__ __forceinline__ int jd2i(double x) {                    // Java (int) cast
@@ -56,109 +95,114 @@ __device__ __forceinline__ int jd2i(double x) {                    // Java (int)
 }
 
 // JohnsonCook.java:138-209
-__device__ __forceinline__ double jc_strainTerm(const MatDev &f, double eps) {
-    return eps <= 0.0 ? f.a : f.a + f.b * nf_pow(eps, f.n);
+template <typename T>
+__device__ __forceinline__ T jc_strainTerm(const MatT<T> &f, T eps) {
+    return eps <= T(0) ? f.a : f.a + f.b * Fn<T>::pow(eps, f.n);
 }
-__device__ __forceinline__ double jc_rateTerm(const MatDev &f, double rate) {
-    if (rate <= f.refRate) return 1.0;
-    return 1.0 + f.c * nf_log(rate / f.refRate);
+template <typename T>
+__device__ __forceinline__ T jc_rateTerm(const MatT<T> &f, T rate) {
+    if (rate <= f.refRate) return T(1);
+    return T(1) + f.c * Fn<T>::log(rate / f.refRate);
 }
-__device__ __forceinline__ double jc_thermalTerm(const MatDev &f, double temperature) {
-    const double homologous = (temperature - f.room) / (f.melt - f.room);
-    if (homologous <= 0.0) return 1.0;
-    if (homologous >= 1.0) return 0.0;
-    return 1.0 - nf_pow(homologous, f.m);
+template <typename T>
+__device__ __forceinline__ T jc_thermalTerm(const MatT<T> &f, T temperature) {
+    const T homologous = (temperature - f.room) / (f.melt - f.room);
+    if (homologous <= T(0)) return T(1);
+    if (homologous >= T(1)) return T(0);
+    return T(1) - Fn<T>::pow(homologous, f.m);
 }
-__device__ __forceinline__ double jc_quasiStatic(const MatDev &f, double eps, double temperature) {
+template <typename T>
+__device__ __forceinline__ T jc_quasiStatic(const MatT<T> &f, T eps, T temperature) {
     return jc_strainTerm(f, eps) * jc_thermalTerm(f, temperature);
 }
 
 // J2.solve, J2.java:332-375
-static __device__ __noinline__ double j2_solve(double norm, double stiffness, double plasticStrain,
-                                        double temperature, double dt, const MatDev &jc) {
-    const double thermal = jc_thermalTerm(jc, temperature);
-    const double tolerance = SOLVE_TOLERANCE * jc.a;
-    double lo = 0.0;
-    double hi = norm / stiffness;
-    double dGamma = hi;
+template <typename T>
+static __device__ __noinline__ T j2_solve(T norm, T stiffness, T plasticStrain, T temperature,
+                                          T dt, const MatT<T> &jc) {
+    const T thermal = jc_thermalTerm(jc, temperature);
+    const T tolerance = Fn<T>::tolerance * jc.a;
+    T lo = T(0);
+    T hi = norm / stiffness;
+    T dGamma = hi;
     for (int iteration = 0; iteration < SOLVE_ITERATIONS; iteration++) {
-        const double dEps = SQRT_2_3 * dGamma;
-        const double eps = plasticStrain + dEps;
-        const double rate = dt > 0.0 ? dEps / dt : 0.0;
-        const double strain = jc_strainTerm(jc, eps);
-        const double rateFactor = jc_rateTerm(jc, rate);
-        const double g = norm - stiffness * dGamma - SQRT_2_3 * strain * rateFactor * thermal;
-        if (g > 0.0) lo = dGamma; else hi = dGamma;
-        if (fabs(g) <= tolerance) return dGamma;
-        double slope = -stiffness
-                       - TWO_THIRDS * (jc.n * (strain - jc.a) / eps) * rateFactor * thermal;
+        const T dEps = T(SQRT_2_3) * dGamma;
+        const T eps = plasticStrain + dEps;
+        const T rate = dt > T(0) ? dEps / dt : T(0);
+        const T strain = jc_strainTerm(jc, eps);
+        const T rateFactor = jc_rateTerm(jc, rate);
+        const T g = norm - stiffness * dGamma - T(SQRT_2_3) * strain * rateFactor * thermal;
+        if (g > T(0)) lo = dGamma; else hi = dGamma;
+        if (Fn<T>::abs(g) <= tolerance) return dGamma;
+        T slope = -stiffness
+                  - T(TWO_THIRDS) * (jc.n * (strain - jc.a) / eps) * rateFactor * thermal;
         if (!(rate <= jc.refRate)) {
-            slope -= SQRT_2_3 * strain * jc.c * thermal / dGamma;
+            slope -= T(SQRT_2_3) * strain * jc.c * thermal / dGamma;
         }
-        double next = dGamma - g / slope;
-        if (!(next > lo && next < hi)) next = 0.5 * (lo + hi);
+        T next = dGamma - g / slope;
+        if (!(next > lo && next < hi)) next = T(0.5) * (lo + hi);
         dGamma = next;
     }
     return dGamma;
 }
 
 // Damage.begin, Damage.java:306-336
-static __device__ __noinline__ void damage_begin(const DamageRef &d, double flowStress,
-                                          double nRR, double nZZ, double nRZ) {
-    const double area = d.geometry[0];
-    const double diff = nRR - nZZ;
-    const double cross = 2.0 * nRZ;
-    const double anisotropy = nf_hypot(diff, cross);
-    double h;
-    if (anisotropy < ISOTROPIC) {
-        h = sqrt(area);
+template <typename T>
+static __device__ __noinline__ void damage_begin(const DamageRefT<T> &d, T flowStress, T nRR,
+                                                 T nZZ, T nRZ) {
+    const T area = d.geometry[0];
+    const T diff = nRR - nZZ;
+    const T cross = T(2) * nRZ;
+    const T anisotropy = Fn<T>::hypot(diff, cross);
+    T h;
+    if (anisotropy < T(ISOTROPIC)) {
+        h = Fn<T>::sqrt(area);
     } else {
-        const double phi = 0.5 * nf_atan2(cross, diff);
-        const double tR = -nf_sin(phi), tZ = nf_cos(phi);
-        const double line = fabs(d.geometry[1] * tR + d.geometry[2] * tZ)
-                            + fabs(d.geometry[3] * tR + d.geometry[4] * tZ);
+        const T phi = T(0.5) * Fn<T>::atan2(cross, diff);
+        const T tR = -Fn<T>::sin(phi), tZ = Fn<T>::cos(phi);
+        const T line = Fn<T>::abs(d.geometry[1] * tR + d.geometry[2] * tZ)
+                       + Fn<T>::abs(d.geometry[3] * tR + d.geometry[4] * tZ);
         h = area / line;
     }
     *d.width = h;
     *d.strength = flowStress;
-    const double slope = -flowStress * flowStress * h / (2.0 * d.fractureEnergy);
-    const double floor_ = -d.youngs;
+    const T slope = -flowStress * flowStress * h / (T(2) * d.fractureEnergy);
+    const T floor_ = -d.youngs;
     *d.softening = slope < floor_ ? floor_ : slope;
 }
 
-// J2.update, J2.java:163-296. s[4] and b[4] are the point's stress and back stress
+// J2.update, J2.java:163-296. s[4] and bk[4] are the point's stress and back stress
 // ({rr, zz, tt, rz}); damage is null for a material that cannot fail, in which case
 // dStrength/dSoft are ignored. Returns the plastic multiplier.
-__device__ __forceinline__ double j2_update(double *s, double *bk, double &epsP, double &work,
-                                            double dRR, double dZZ, double dTT, double dGamRZ,
-                                            double lambda, double mu, const MatDev &flow,
-                                            double strainDt, const DamageRef *damage,
-                                            double dStrength, double dSoft) {
-    const double lt = lambda * (dRR + dZZ + dTT);
-    const double tRR = s[0] + lt + 2.0 * mu * dRR;
-    const double tZZ = s[1] + lt + 2.0 * mu * dZZ;
-    const double tTT = s[2] + lt + 2.0 * mu * dTT;
-    const double tRZ = s[3] + mu * dGamRZ;
+template <typename T>
+__device__ __forceinline__ T j2_update(T *s, T *bk, T &epsP, T &work, T dRR, T dZZ, T dTT,
+                                       T dGamRZ, T lambda, T mu, const MatT<T> &flow, T strainDt,
+                                       const DamageRefT<T> *damage, T dStrength, T dSoft) {
+    const T lt = lambda * (dRR + dZZ + dTT);
+    const T tRR = s[0] + lt + T(2) * mu * dRR;
+    const T tZZ = s[1] + lt + T(2) * mu * dZZ;
+    const T tTT = s[2] + lt + T(2) * mu * dTT;
+    const T tRZ = s[3] + mu * dGamRZ;
 
-    const double p = (tRR + tZZ + tTT) / 3.0;
-    const double xRR = tRR - p - bk[0];
-    const double xZZ = tZZ - p - bk[1];
-    const double xTT = tTT - p - bk[2];
-    const double xRZ = tRZ - bk[3];
-    const double norm = sqrt(xRR * xRR + xZZ * xZZ + xTT * xTT + 2.0 * xRZ * xRZ);
+    const T p = (tRR + tZZ + tTT) / T(3);
+    const T xRR = tRR - p - bk[0];
+    const T xZZ = tZZ - p - bk[1];
+    const T xTT = tTT - p - bk[2];
+    const T xRZ = tRZ - bk[3];
+    const T norm = Fn<T>::sqrt(xRR * xRR + xZZ * xZZ + xTT * xTT + T(2) * xRZ * xRZ);
 
     const bool jc = flow.jc != 0;
-    const double temperature = !jc ? 0.0 : flow.room + flow.thermalCoefficient * work;
+    const T temperature = !jc ? T(0) : flow.room + flow.thermalCoefficient * work;
 
-    const bool softening = damage != nullptr && dStrength > 0.0;
-    double hardening = 0.0;
-    double flowStress;
+    const bool softening = damage != nullptr && dStrength > T(0);
+    T hardening = T(0);
+    T flowStress;
     if (softening) {
         flowStress = dStrength + dSoft * (epsP - damage->failureStrain);
-        if (flowStress > 0.0) {
+        if (flowStress > T(0)) {
             hardening = dSoft;
         } else {
-            flowStress = 0.0;
+            flowStress = T(0);
         }
     } else if (!jc) {
         flowStress = flow.sy0 + flow.hIso * epsP;
@@ -166,45 +210,45 @@ __device__ __forceinline__ double j2_update(double *s, double *bk, double &epsP,
     } else {
         flowStress = jc_quasiStatic(flow, epsP, temperature);
     }
-    const double radius = SQRT_2_3 * flowStress;
+    const T radius = T(SQRT_2_3) * flowStress;
 
     if (!(norm > radius)) {
         s[0] = tRR;
         s[1] = tZZ;
         s[2] = tTT;
         s[3] = tRZ;
-        return 0.0;
+        return T(0);
     }
 
-    const double stiffness = 2.0 * mu + TWO_THIRDS * flow.hKin;
-    double dGamma;
+    const T stiffness = T(2) * mu + T(TWO_THIRDS) * flow.hKin;
+    T dGamma;
     if (!jc || softening) {
-        dGamma = (norm - radius) / (stiffness + TWO_THIRDS * hardening);
-        if (softening && flowStress + hardening * SQRT_2_3 * dGamma < 0.0) {
+        dGamma = (norm - radius) / (stiffness + T(TWO_THIRDS) * hardening);
+        if (softening && flowStress + hardening * T(SQRT_2_3) * dGamma < T(0)) {
             dGamma = norm / stiffness;
         }
     } else {
         dGamma = j2_solve(norm, stiffness, epsP, temperature, strainDt, flow);
     }
-    const double inv = 1.0 / norm;
-    const double nRR = xRR * inv, nZZ = xZZ * inv, nTT = xTT * inv, nRZ = xRZ * inv;
+    const T inv = T(1) / norm;
+    const T nRR = xRR * inv, nZZ = xZZ * inv, nTT = xTT * inv, nRZ = xRZ * inv;
 
-    const double pull = 2.0 * mu * dGamma;
+    const T pull = T(2) * mu * dGamma;
     s[0] = tRR - pull * nRR;
     s[1] = tZZ - pull * nZZ;
     s[2] = tTT - pull * nTT;
     s[3] = tRZ - pull * nRZ;
 
-    const double alphaDotN = bk[0] * nRR + bk[1] * nZZ + bk[2] * nTT + 2.0 * bk[3] * nRZ;
+    const T alphaDotN = bk[0] * nRR + bk[1] * nZZ + bk[2] * nTT + T(2) * bk[3] * nRZ;
     work += dGamma * (norm - pull + alphaDotN);
 
-    const double shift = TWO_THIRDS * flow.hKin * dGamma;
+    const T shift = T(TWO_THIRDS) * flow.hKin * dGamma;
     bk[0] += shift * nRR;
     bk[1] += shift * nZZ;
     bk[2] += shift * nTT;
     bk[3] += shift * nRZ;
 
-    epsP += SQRT_2_3 * dGamma;
+    epsP += T(SQRT_2_3) * dGamma;
 
     if (damage != nullptr && !softening && epsP >= damage->failureStrain) {
         damage_begin(*damage,
@@ -215,39 +259,43 @@ __device__ __forceinline__ double j2_update(double *s, double *bk, double &epsP,
 }
 
 // Corotational.java:59-98
-__device__ __forceinline__ void corot_rotate(double *t, double c, double sn) {
-    const double rr = t[0], zz = t[1], rz = t[3];
-    const double cc = c * c, ss = sn * sn, cs = c * sn;
-    t[0] = cc * rr - 2.0 * cs * rz + ss * zz;
-    t[1] = ss * rr + 2.0 * cs * rz + cc * zz;
+template <typename T>
+__device__ __forceinline__ void corot_rotate(T *t, T c, T sn) {
+    const T rr = t[0], zz = t[1], rz = t[3];
+    const T cc = c * c, ss = sn * sn, cs = c * sn;
+    t[0] = cc * rr - T(2) * cs * rz + ss * zz;
+    t[1] = ss * rr + T(2) * cs * rz + cc * zz;
     t[3] = cs * (rr - zz) + (cc - ss) * rz;
 }
-__device__ __forceinline__ double corot_cos(double spinDt) {
-    const double h = 0.5 * spinDt;
-    return (1.0 - h * h) / (1.0 + h * h);
+template <typename T>
+__device__ __forceinline__ T corot_cos(T spinDt) {
+    const T h = T(0.5) * spinDt;
+    return (T(1) - h * h) / (T(1) + h * h);
 }
-__device__ __forceinline__ double corot_sin(double spinDt) {
-    const double h = 0.5 * spinDt;
-    return 2.0 * h / (1.0 + h * h);
+template <typename T>
+__device__ __forceinline__ T corot_sin(T spinDt) {
+    const T h = T(0.5) * spinDt;
+    return T(2) * h / (T(1) + h * h);
 }
 
-__device__ __forceinline__ double sq2(double a, double b) { return a * a + b * b; }
+template <typename T>
+__device__ __forceinline__ T sq2(T a, T b) { return a * a + b * b; }
 
 // shortestEdge, ExplicitSolver.java:1191-1197
-__device__ __forceinline__ double shortestEdge(double running, double r0, double r1, double r2,
-                                               double r3, double z0, double z1, double z2,
-                                               double z3) {
+template <typename T>
+__device__ __forceinline__ T shortestEdge(T running, T r0, T r1, T r2, T r3, T z0, T z1, T z2,
+                                          T z3) {
     return jmin(running, jmin(jmin(sq2(r1 - r0, z1 - z0), sq2(r2 - r1, z2 - z1)),
                               jmin(sq2(r3 - r2, z3 - z2), sq2(r0 - r3, z0 - z3))));
 }
 
 // Damage.at, Damage.java:342-347
-__device__ __forceinline__ double damage_at(double strength, double softening,
-                                            double failureStrain, double plasticStrain) {
-    const double sf = strength;
-    if (sf <= 0.0) return 0.0;
-    const double v = -softening * (plasticStrain - failureStrain) / sf;
-    return v <= 0.0 ? 0.0 : (v >= 1.0 ? 1.0 : v);
+template <typename T>
+__device__ __forceinline__ T damage_at(T strength, T softening, T failureStrain, T plasticStrain) {
+    const T sf = strength;
+    if (sf <= T(0)) return T(0);
+    const T v = -softening * (plasticStrain - failureStrain) / sf;
+    return v <= T(0) ? T(0) : (v >= T(1) ? T(1) : v);
 }
 
 }  // namespace nf

@@ -116,6 +116,15 @@ struct Dev {
     double *pairVal;                         // [12 per slot]: role-major (n,a,b) x (normal r,z, tangent r,z)
     double *pairEnergy, *pairDiss;           // per slot
     int32_t *incCount, *incStart, *incCursor, *incEntry;   // per surface slot, entries (i<<2 | role)
+    // mixed precision: FP32 element state, float contributions, per-node float positions
+    int mixed;
+    MatF *matsF;
+    float *sigF, *backF, *epsPF, *wPF, *hgKF, *contribF;
+    float2 *hgF;
+    float *dStrF, *dSoftF, *dWidthF, *dFailF, *dGfF, *dGeomF;
+    float4 *pMid, *pCur;
+    float2 *vdt;
+    double *gaussVol;                        // reference volume of each point
     // scan workspace
     int32_t *scanTmp;
     int scanTmpSize;
@@ -172,6 +181,14 @@ void launch_material_points(const MatDev &m, int count, double *sig, double *bac
                             const double *fail, const double *gf, const double *youngs,
                             const double *geom, double *strength, double *soft, double *width,
                             double *dgamma, cudaStream_t stream);
+// Launchers (k_mixed.cu)
+int launch_prepare_mixed(Solver &S, int zeroStrain);
+int launch_erode_mixed(Solver &S);
+int launch_element_mixed(Solver &S, int zeroStrain);
+int launch_pressure_mixed(Solver &S);
+int launch_gather_mixed(Solver &S);
+void launch_convert_state(Solver &S, bool toFloat, int what);
+int launch_point_volumes(Solver &S, double *out);
 // Launchers (k_contact.cu)
 int launch_contact(Solver &S, bool predicated);
 // Launchers (k_scan.cu)

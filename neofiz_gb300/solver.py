@@ -340,6 +340,11 @@ class ExplicitSolver:
         """Runs this solver's kernels on a caller-owned cudaStream_t (0: its own)."""
         self._call(self._api.set_stream, C.c_void_p(stream_handle or None))
 
+    def setPrecision(self, precision: int) -> None:
+        """PRECISION_FP64 (the reference's arithmetic) or PRECISION_MIXED (FP32 element
+        arithmetic and state, FP64 kinematics and audits)."""
+        self._call(self._api.set_precision, int(precision))
+
     def profile(self, enable: bool) -> None:
         self._call(self._api.profile, 1 if enable else 0)
 

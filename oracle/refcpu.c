@@ -2012,6 +2012,8 @@ API double nfo_math(int which, double x, double y) {
 
 /* Device-only entry points of the ABI: no-ops on the CPU. */
 API nf_status nfo_set_stream(nfo_solver *h, void *stream) { (void)h; (void)stream; return NF_OK; }
+/* The oracle is the FP64 algorithm; a precision request leaves it unchanged. */
+API nf_status nfo_set_precision(nfo_solver *h, int32_t precision) { (void)h; (void)precision; return NF_OK; }
 API nf_status nfo_profile(nfo_solver *h, int32_t enable) { (void)h; (void)enable; return NF_OK; }
 API nf_status nfo_profile_read(nfo_solver *h, double *ms, int64_t *steps) {
     (void)h;
