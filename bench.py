@@ -42,6 +42,8 @@ def parse():
     p.add_argument("--no-cpu-baseline", action="store_true")
     p.add_argument("--no-e2e", action="store_true")
     p.add_argument("--no-mixed", action="store_true")
+    p.add_argument("--precision", default="fp64", choices=["fp64", "mixed"],
+                   help="arithmetic of the headline leg (default: the reference's FP64)")
     p.add_argument("--mixed-cell", type=float, default=0.051e-3)
     p.add_argument("--mixed-steps", type=int, default=600)
     return p.parse_args()
@@ -151,6 +153,9 @@ def run_ours(args, world, rank, local):
 
     g, mesh, info = scenes.perforation(ExplicitSolver, cell=args.cell, gap=GAP)
     E, N = mesh.elementCount, mesh.nodeCount
+    if args.precision == "mixed":
+        from neofiz_gb300 import _abi
+        g.setPrecision(_abi.PRECISION_MIXED)
     stream = torch.cuda.Stream()
     g.setStream(stream.cuda_stream)
     flush = torch.empty(L2_FLUSH_BYTES, dtype=torch.uint8, device="cuda")
@@ -228,7 +233,7 @@ def run_ours(args, world, rank, local):
             "higher_is_better": True,
             "scaling": "weak",
             "vs_baseline": None,
-            "dtype": "f64",
+            "dtype": "f64" if args.precision == "fp64" else "f32 element arithmetic, f64 kinematics",
             "data": "synthetic (generated scene; no dataset)",
             "config": {
                 "workload": "plane-strain perforation: 10x20 mm steel slug at 700 m/s into 12 "

@@ -145,9 +145,12 @@ __global__ void k_uniform_velocity(double2 *V, int n, double vr, double vz) {
     const int i = blockIdx.x * blockDim.x + threadIdx.x;
     if (i < n) V[i] = make_double2(vr, vz);
 }
-__global__ void k_scale_mass(double *mass, int n, double factor) {
+__global__ void k_scale_mass(double *mass, double *invMass, int n, double factor) {
     const int i = blockIdx.x * blockDim.x + threadIdx.x;
-    if (i < n) mass[i] *= factor;
+    if (i < n) {
+        mass[i] *= factor;
+        invMass[i] = 1.0 / mass[i];
+    }
 }
 __global__ void k_set_run(DevScalars *s, double tEnd, long long maxSteps) {
     s->tEnd = tEnd;
@@ -247,6 +250,11 @@ nf_status nf_create(const nf_mesh *mesh, const nf_material *materials, int32_t m
     CK(nullptr, cudaGetDevice(&S->device));
     CK(nullptr, cudaStreamCreateWithFlags(&S->stream, cudaStreamNonBlocking));
     S->ownStream = S->stream;
+    {
+        int sms = 0;
+        cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, S->device);
+        S->d.sms = sms > 0 ? sms : 1;
+    }
     S->N = N; S->E = E; S->K = K;
     S->formulation = formulation; S->integration = integration; S->kinematics = kinematics;
     S->ppe = integration == NF_FULL ? 4 : 1;
@@ -386,12 +394,14 @@ nf_status nf_create(const nf_mesh *mesh, const nf_material *materials, int32_t m
     std::vector<int2> pe(K);
     for (int k = 0; k < K; k++)
         pe[k] = make_int2(mesh->pressure_edges[2 * k], mesh->pressure_edges[2 * k + 1]);
-    d.maxBlocks = grid_for(std::max(std::max(N, E), 1), 128) + 1;
+    // partial-sum slots: the per-item grids (nodes, elements) and the fixed contact grid
+    d.maxBlocks = std::max(grid_for(std::max(std::max(N, E), 1), 128),
+                           std::max(contact_partial_blocks(), 8 * d.sms)) + 1;
     d.bucketCap = std::max(1 << 14, 2 * N);
     const size_t scanInts = scan_tmp_ints(std::max(std::max(4 * E, N + 1), d.bucketCap + 1)) + 16;
     cudaError_t e_ = cudaSuccess;
 #define A(ptr, n) if (e_ == cudaSuccess) e_ = dalloc(*S, &(ptr), (n))
-    A(d.X0, N); A(d.U, N); A(d.V, N); A(d.F, N); A(d.mass, N);
+    A(d.X0, N); A(d.U, N); A(d.V, N); A(d.F, N); A(d.mass, N); A(d.invMass, N);
     A(d.flags, N); A(d.wallState, N); A(d.contactState, N);
     A(d.conn, E); A(d.emat, E); A(d.mats, material_count);
     A(d.sig, 4 * P); A(d.back, 4 * P); A(d.epsP, P); A(d.wP, P);
@@ -410,6 +420,9 @@ nf_status nf_create(const nf_mesh *mesh, const nf_material *materials, int32_t m
     }
     upload(*S, d.X0, X0.data(), N);
     upload(*S, d.mass, mass.data(), N);
+    std::vector<double> invMass(N);
+    for (int i = 0; i < N; i++) invMass[i] = 1.0 / mass[i];     // nodalUpdate's 1/m, once
+    upload(*S, d.invMass, invMass.data(), N);
     upload(*S, d.conn, conn4.data(), E);
     upload(*S, d.emat, S->emat.data(), E);
     upload(*S, d.mats, mats.data(), material_count);
@@ -443,7 +456,7 @@ nf_status nf_destroy(nf_solver *h) {
         cudaEventDestroy(r.b);
     }
     Dev &d = S->d;
-    void *ptrs[] = {d.X0, d.U, d.V, d.F, d.mass, d.flags, d.wallState, d.contactState, d.conn,
+    void *ptrs[] = {d.X0, d.U, d.V, d.F, d.mass, d.invMass, d.flags, d.wallState, d.contactState, d.conn,
                     d.emat, d.mats, d.sig, d.back, d.epsP, d.wP, d.hg, d.hgK, d.gone, d.dead,
                     d.dFail, d.dGf, d.dGeom, d.dStrength, d.dSoft, d.dWidth, d.contribution,
                     d.nodeSlotStart, d.nodeSlot, d.pedges, d.partials, d.edgeGroup, d.groupStart,
@@ -633,7 +646,7 @@ nf_status nf_set_mass_scaling(nf_solver *h, double target) {
                     "the step is already %.17g s, longer than the target %.17g; mass scaling adds "
                     "mass and cannot shorten a step", s.dt, target);
     const double factor = (target / s.dt) * (target / s.dt);
-    if (S.N > 0) k_scale_mass<<<grid_for(S.N, 256), 256, 0, S.stream>>>(S.d.mass, S.N, factor);
+    if (S.N > 0) k_scale_mass<<<grid_for(S.N, 256), 256, 0, S.stream>>>(S.d.mass, S.d.invMass, S.N, factor);
     S.d.massScale *= factor;
     s.dt = target;
     s.dtPrevious = s.dt;

@@ -54,9 +54,9 @@ __device__ __forceinline__ float diff_hl(float4 a, float4 b, int comp) {
 __global__ void __launch_bounds__(MB) k_erode_mixed(Dev d) {
     __shared__ double sh[MB / 32];
     if (!d.s->active) return;
-    const int e = blockIdx.x * blockDim.x + threadIdx.x;
     double energy = 0.0;
-    if (e < d.E && !d.gone[e]) {
+    for (int e = blockIdx.x * blockDim.x + threadIdx.x; e < d.E; e += gridDim.x * blockDim.x) {
+        if (d.gone[e]) continue;
         bool failed = false;
         if (d.hasDamage) {
             float sum = 0.0f;
@@ -450,7 +450,7 @@ int launch_prepare_mixed(Solver &S, int zeroStrain) {
     return 1;
 }
 int launch_erode_mixed(Solver &S) {
-    k_erode_mixed<<<grid_for(S.d.E, MB), MB, 0, S.stream>>>(S.d);
+    k_erode_mixed<<<element_grid(S), MB, 0, S.stream>>>(S.d);
     return 1;
 }
 int launch_element_mixed(Solver &S, int zeroStrain) {

@@ -15,9 +15,14 @@ int grid_for(long long n, int block) {
     return (int)(g < 1 ? 1 : g);
 }
 
-__global__ void k_scan_tiles(const int32_t *in, int32_t *out, int n, int32_t *tileSums,
-                             const int *pred) {
+__global__ void k_scan_tiles(const int32_t *in, int32_t *out, int nMax, int32_t *tileSums,
+                             const int *pred, const int *nDev) {
     if (pred && !*pred) return;
+    const int n = nDev ? min(*nDev, nMax) : nMax;
+    if (blockIdx.x * SCAN_TILE >= n) {          // a tile past the live length contributes 0
+        if (threadIdx.x == 0) tileSums[blockIdx.x] = 0;
+        return;
+    }
     __shared__ int32_t warpSums[SCAN_BLOCK / 32];
     const int base = blockIdx.x * SCAN_TILE + threadIdx.x * SCAN_ITEMS;
     int32_t v[SCAN_ITEMS];
@@ -58,8 +63,10 @@ __global__ void k_scan_tiles(const int32_t *in, int32_t *out, int n, int32_t *ti
     if (threadIdx.x == SCAN_BLOCK - 1) tileSums[blockIdx.x] = run;
 }
 
-__global__ void k_scan_add(int32_t *out, int n, const int32_t *tileOffsets, const int *pred) {
+__global__ void k_scan_add(int32_t *out, int nMax, const int32_t *tileOffsets, const int *pred,
+                           const int *nDev) {
     if (pred && !*pred) return;
+    const int n = nDev ? min(*nDev, nMax) : nMax;
     const int tile = blockIdx.x;
     const int32_t add = tileOffsets[tile];
     const int base = tile * SCAN_TILE;
@@ -93,8 +100,9 @@ size_t scan_tmp_ints(int n) {
 // in and out may alias.
 // When pred is non-null every kernel of the scan does nothing unless *pred is non-zero, so
 // the scan can sit in a fixed launch sequence and only run on the steps that need it.
+// nDev, when given, is a device-side live length (at most n): only that prefix is scanned.
 int scan_exclusive(const int32_t *in, int32_t *out, int n, int32_t *totalOut, int32_t *tmp,
-                   cudaStream_t stream, const int *pred) {
+                   cudaStream_t stream, const int *pred, const int *nDev) {
     if (n <= 0) {
         if (totalOut) {
             k_scan_zero_total<<<1, 1, 0, stream>>>(totalOut, pred);
@@ -106,11 +114,11 @@ int scan_exclusive(const int32_t *in, int32_t *out, int n, int32_t *totalOut, in
     int32_t *tileSums = tmp;
     int32_t *tileOffsets = tmp + tiles + 1;
     int launched = 1;
-    k_scan_tiles<<<tiles, SCAN_BLOCK, 0, stream>>>(in, out, n, tileSums, pred);
+    k_scan_tiles<<<tiles, SCAN_BLOCK, 0, stream>>>(in, out, n, tileSums, pred, nDev);
     if (tiles > 1) {
         launched += scan_exclusive(tileSums, tileOffsets, tiles, totalOut, tmp + 2 * tiles + 2,
-                                   stream, pred);
-        k_scan_add<<<tiles, SCAN_BLOCK, 0, stream>>>(out, n, tileOffsets, pred);
+                                   stream, pred, nullptr);
+        k_scan_add<<<tiles, SCAN_BLOCK, 0, stream>>>(out, n, tileOffsets, pred, nDev);
         launched++;
     } else if (totalOut) {
         k_scan_copy_total<<<1, 1, 0, stream>>>(tileSums, totalOut, pred);

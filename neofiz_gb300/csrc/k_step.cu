@@ -62,22 +62,24 @@ __global__ void k_begin(Dev d, int initial) {
 // ------------------------------------------------------------------------------------ nodal
 
 // nodalUpdate, ExplicitSolver.java:998-1062, with RigidWall.hold/crosses/arrive/slide
-// (RigidWall.java:163-259). Wall totals are reduced per block in a fixed order.
+// (RigidWall.java:163-259). A fixed grid strides over the nodes; each thread adds its nodes'
+// wall terms in node order and the block adds its threads in a fixed tree, so the totals are
+// deterministic. 1/m comes from the invMass array (the same division, done once). In the
+// mixed form the kernel also writes the FP32 geometry the element kernel reads.
 __global__ void __launch_bounds__(BLOCK) k_nodal(Dev d) {
     __shared__ double sh[BLOCK / 32];
     const DevScalars *s = d.s;
     if (!s->active) return;
-    const int i = blockIdx.x * blockDim.x + threadIdx.x;
     const double decay = s->decay, gain = s->gain, dtAvg = s->dtAvg, dt = s->dt;
     double impulse = 0.0, loss = 0.0, fric = 0.0;
-    if (i < d.N) {
+    for (int i = blockIdx.x * blockDim.x + threadIdx.x; i < d.N; i += gridDim.x * blockDim.x) {
         uint8_t fl = d.flags[i];
         const bool fixedR = fl & 1, fixedZ = fl & 2;
         bool onWall = fl & 4;
         double2 u = d.U[i], v = d.V[i];
         const double2 f = d.F[i];
         const double m = d.mass[i];
-        const double invM = 1.0 / m;
+        const double invM = d.invMass[i];
         const bool resting = d.hasWall && onWall && f.y <= 0.0;
         uint8_t ws = 0;
         if (fixedR) {
@@ -104,6 +106,7 @@ __global__ void __launch_bounds__(BLOCK) k_nodal(Dev d) {
             v.x = decay * v.x + gain * f.x * invM;
             u.x += v.x * dt;
         }
+        const double2 x0 = d.X0[i];
         if (fixedZ) {
             v.y = 0.0;
         } else if (resting) {
@@ -112,7 +115,7 @@ __global__ void __launch_bounds__(BLOCK) k_nodal(Dev d) {
             ws |= NF_WALL_HELD;
         } else {
             const double trial = decay * v.y + gain * f.y * invM;
-            const double zc = d.X0[i].y + u.y;
+            const double zc = x0.y + u.y;
             if (d.hasWall && zc + trial * dt < d.wallPlane) {
                 impulse += -m * trial;                       // RigidWall.arrive :205-209
                 loss += 0.5 * m * trial * trial;
@@ -135,6 +138,24 @@ __global__ void __launch_bounds__(BLOCK) k_nodal(Dev d) {
         }
         if (!(isfinite(u.x) && isfinite(u.y) && isfinite(v.x) && isfinite(v.y)))
             atomicOr(&d.s->status, STATUS_NONFINITE);
+        if (d.mixed) {
+            // the geometry of the coming assembly: mid-step and current positions as float
+            // pairs, and v dt (see k_prepare_mixed)
+            const double mid = -0.5 * dt;
+            double pr, pz;
+            if (d.finite) {
+                pr = x0.x + u.x + mid * v.x;
+                pz = x0.y + u.y + mid * v.y;
+            } else {
+                pr = x0.x;
+                pz = x0.y;
+            }
+            const double cr = x0.x + u.x, cz = x0.y + u.y;
+            const float prh = (float)pr, pzh = (float)pz, crh = (float)cr, czh = (float)cz;
+            d.pMid[i] = make_float4(prh, (float)(pr - (double)prh), pzh, (float)(pz - (double)pzh));
+            d.pCur[i] = make_float4(crh, (float)(cr - (double)crh), czh, (float)(cz - (double)czh));
+            d.vdt[i] = make_float2((float)(v.x * dt), (float)(v.y * dt));
+        }
     }
     if (d.hasWall) {
         const double a = block_sum(impulse, sh);
@@ -146,7 +167,7 @@ __global__ void __launch_bounds__(BLOCK) k_nodal(Dev d) {
             d.partials[(PARTIAL_WALL + 2) * d.maxBlocks + blockIdx.x] = c;
         }
     }
-    if (i == 0) {                                            // ExplicitSolver.java:973-974
+    if (blockIdx.x == 0 && threadIdx.x == 0) {               // ExplicitSolver.java:973-974
         d.s->time += dt;
         d.s->steps += 1;
     }
@@ -210,9 +231,9 @@ int launch_point_volumes(Solver &S, double *out) {
 __global__ void __launch_bounds__(BLOCK) k_erode(Dev d) {
     __shared__ double sh[BLOCK / 32];
     if (!d.s->active) return;
-    const int e = blockIdx.x * blockDim.x + threadIdx.x;
     double energy = 0.0;
-    if (e < d.E && !d.gone[e]) {
+    for (int e = blockIdx.x * blockDim.x + threadIdx.x; e < d.E; e += gridDim.x * blockDim.x) {
+        if (d.gone[e]) continue;
         bool failed = false;
         if (d.hasDamage) {                                  // elementDamage, :1764-1772
             double sum = 0.0;
@@ -733,8 +754,7 @@ int launch_initial_assembly(Solver &S) {
     Dev &d = S.d;
     k_begin<<<1, 1, 0, S.stream>>>(d, 1);
     int n = 1 + assemble(S, 1);
-    k_end<<<1, 256, 0, S.stream>>>(d, grid_for(d.N, BLOCK), grid_for(d.E, BLOCK),
-                                  grid_for(d.N, BLOCK), 0);
+    k_end<<<1, 256, 0, S.stream>>>(d, nodal_grid(S), element_grid(S), contact_partial_blocks(), 0);
     return n + 1;
 }
 
@@ -746,29 +766,22 @@ int launch_step(Solver &S, bool) {
     k_begin<<<1, 1, 0, st>>>(d, 0);
     n++;
     if (d.N > 0) {
-        k_nodal<<<grid_for(d.N, BLOCK), BLOCK, 0, st>>>(d);
+        k_nodal<<<nodal_grid(S), BLOCK, 0, st>>>(d);    // in the mixed form it also prepares
         n++;
     }
     S.mark(NF_GROUP_NODAL, false);
-    bool prepared = false;
-    if (d.mixed) {
-        S.mark(NF_GROUP_ELEMENT, true);
-        n += launch_prepare_mixed(S, 0);
-        S.mark(NF_GROUP_ELEMENT, false);
-        prepared = true;
-    }
     if (d.hasErosion && d.E > 0) {
         S.mark(NF_GROUP_ERODE, true);
         if (d.mixed) n += launch_erode_mixed(S);
         else {
-            k_erode<<<grid_for(d.E, BLOCK), BLOCK, 0, st>>>(d);
+            k_erode<<<element_grid(S), BLOCK, 0, st>>>(d);
             n++;
         }
         S.mark(NF_GROUP_ERODE, false);
     }
-    n += assemble(S, 0, prepared);
+    n += assemble(S, 0, d.N > 0 && d.mixed);
     S.mark(NF_GROUP_END, true);
-    k_end<<<1, 256, 0, st>>>(d, grid_for(d.N, BLOCK), grid_for(d.E, BLOCK), grid_for(d.N, BLOCK), 1);
+    k_end<<<1, 256, 0, st>>>(d, nodal_grid(S), element_grid(S), contact_partial_blocks(), 1);
     n++;
     S.mark(NF_GROUP_END, false);
     return n;
@@ -783,8 +796,7 @@ int launch_advance(Solver &S) {
         n++;
     }
     n += assemble(S, 0);
-    k_end<<<1, 256, 0, S.stream>>>(d, grid_for(d.N, BLOCK), grid_for(d.E, BLOCK),
-                                  grid_for(d.N, BLOCK), 0);
+    k_end<<<1, 256, 0, S.stream>>>(d, nodal_grid(S), element_grid(S), contact_partial_blocks(), 0);
     return n + 1;
 }
 

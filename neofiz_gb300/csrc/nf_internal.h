@@ -61,6 +61,7 @@ struct DevScalars {
     int cols, rows;
     long long cells;
     int hashed, pad2;
+    int slotScanN, bucketScanN;              // live lengths of the per-step scans
     uint32_t status;
     int pad3;
 };
@@ -74,9 +75,10 @@ struct Dev {
     double wallPlane, wallFriction;
     double cFriction, cScale, cDamping, dt0;
     int nmat;
+    int sms;                                 // multiprocessors on the device
     // nodes
     double2 *X0, *U, *V, *F;
-    double *mass;
+    double *mass, *invMass;
     uint8_t *flags, *wallState, *contactState;
     // elements / points
     int4 *conn;
@@ -193,9 +195,20 @@ int launch_point_volumes(Solver &S, double *out);
 int launch_contact(Solver &S, bool predicated);
 // Launchers (k_scan.cu)
 int scan_exclusive(const int32_t *in, int32_t *out, int n, int32_t *totalOut, int32_t *tmp,
-                    cudaStream_t stream, const int *pred);
+                   cudaStream_t stream, const int *pred, const int *nDev);
+int contact_partial_blocks();
 size_t scan_tmp_ints(int n);
 
 int grid_for(long long n, int block);
+// Fixed grids of the node and element kernels that reduce per block: a few blocks per SM,
+// striding over the items, so the number of partial sums stays small.
+inline int nodal_grid(const Solver &S) {
+    const int g = grid_for(S.d.N, 128), cap = 8 * S.d.sms;
+    return g < cap ? g : cap;
+}
+inline int element_grid(const Solver &S) {
+    const int g = grid_for(S.d.E, 128), cap = 8 * S.d.sms;
+    return g < cap ? g : cap;
+}
 
 }  // namespace nf
