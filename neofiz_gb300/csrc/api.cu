@@ -254,6 +254,7 @@ nf_status nf_create(const nf_mesh *mesh, const nf_material *materials, int32_t m
         int sms = 0;
         cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, S->device);
         S->d.sms = sms > 0 ? sms : 1;
+        S->d.coopBlocks = contact_coop_blocks(S->d.sms);
     }
     S->N = N; S->E = E; S->K = K;
     S->formulation = formulation; S->integration = integration; S->kinematics = kinematics;
@@ -396,7 +397,7 @@ nf_status nf_create(const nf_mesh *mesh, const nf_material *materials, int32_t m
         pe[k] = make_int2(mesh->pressure_edges[2 * k], mesh->pressure_edges[2 * k + 1]);
     // partial-sum slots: the per-item grids (nodes, elements) and the fixed contact grid
     d.maxBlocks = std::max(grid_for(std::max(std::max(N, E), 1), 128),
-                           std::max(contact_partial_blocks(), 8 * d.sms)) + 1;
+                           std::max(d.coopBlocks, 8 * d.sms)) + 1;
     d.bucketCap = std::max(1 << 14, 2 * N);
     const size_t scanInts = scan_tmp_ints(std::max(std::max(4 * E, N + 1), d.bucketCap + 1)) + 16;
     cudaError_t e_ = cudaSuccess;
@@ -468,7 +469,7 @@ nf_status nf_destroy(nf_solver *h) {
                     d.pairEnergy, d.pairDiss, d.incCount, d.incStart, d.incCursor, d.incEntry,
                     d.scanTmp, d.s, d.matsF, d.sigF, d.backF, d.epsPF, d.wPF, d.hgKF,
                     d.contribF, d.hgF, d.dStrF, d.dSoftF, d.dWidthF, d.dFailF, d.dGfF, d.dGeomF,
-                    d.pMid, d.pCur, d.vdt, d.gaussVol};
+                    d.pMid, d.pCur, d.vdt, d.gaussVol, d.coopSums, d.incSlots, d.bucketA, d.bucketN, d.slaveXY};
     for (void *p : ptrs)
         if (p) cudaFree(p);
     if (S->ownStream) cudaStreamDestroy(S->ownStream);
@@ -579,10 +580,13 @@ nf_status nf_set_contact(nf_solver *h, double friction, double damping, double s
         A(d.lastMaster, N); A(d.master, N); A(d.dropped, N);
         A(d.bucketCount, d.bucketCap + 1); A(d.bucketStart, d.bucketCap + 1);
         A(d.bucketCursor, d.bucketCap + 1);
-        A(d.bucketEntry, 8LL * E); A(d.bucketCell, 8LL * E); A(d.entryCell, 8LL * E);
+        A(d.bucketEntry, 8LL * E); A(d.bucketA, 8LL * E); A(d.bucketN, 8LL * E);
+        A(d.slaveXY, N); A(d.bucketCell, 8LL * E); A(d.entryCell, 8LL * E);
         A(d.pairNodes, N); A(d.pairVal, 12LL * N); A(d.pairEnergy, N); A(d.pairDiss, N);
         A(d.incCount, N + 1); A(d.incStart, N + 1); A(d.incCursor, N + 1); A(d.incEntry, 3LL * N);
+        A(d.incSlots, (size_t)NF_INC_CAP * N);
         A(d.scanTmp, (size_t)d.scanTmpSize);
+        A(d.coopSums, (size_t)d.coopBlocks);
 #undef A
         if (e_ != cudaSuccess)
             return fail(&S, NF_ENOMEM, "contact allocation failed: %s", cudaGetErrorString(e_));
@@ -776,8 +780,17 @@ static nf_status enqueue_steps(Solver &S, int64_t steps) {
         S.profSteps += steps;
         return NF_OK;
     }
-    nf_status st = ensure_graphs(S);
-    if (st) return st;
+    if (!S.noGraphs && ensure_graphs(S) != NF_OK) {
+        // a stream that cannot capture (a cooperative kernel node the runtime refuses): the
+        // same launches, enqueued one step at a time
+        (void)cudaGetLastError();
+        S.noGraphs = true;
+        S.err.clear();
+    }
+    if (S.noGraphs) {
+        for (int64_t k = 0; k < steps; k++) S.launches += launch_step(S, true);
+        return NF_OK;
+    }
     while (steps >= 16) {
         CK(&S, cudaGraphLaunch(S.graph16, S.stream));
         S.launches += S.graphKernels16;

@@ -2,30 +2,43 @@
 // (src/main/java/org/neofiz/solver/Contact.java), and the free-surface rebuild it needs after
 // erosion (mesh/QuadMesh.java:188-226 via Contact.adopt, Contact.java:290-322).
 //
+// One cooperative, persistent kernel per step runs the whole contact pass as phases separated
+// by grid-wide barriers: the surface rebuild (only on steps after an erosion), geometry, the
+// counting-sort grid, the search, the pair forces and their ordered accumulation. It replaces
+// some thirty launches of small kernels, whose launch gaps dominated the pass.
+//
 // The reference's result depends on three orders, and each is reproduced exactly:
-//   * the surface is listed in element order and its nodes ascending (a stream compaction
-//     of per-edge and per-node flags, i.e. an ordered scan);
+//   * the surface is listed in element order and its nodes ascending (ordered compactions,
+//     i.e. exclusive scans of per-edge and per-node flags);
 //   * the search visits the nine cells in (dj, di) order and, within a cell, the segments in
 //     the order the counting sort filed them -- ascending segment, first endpoint before the
-//     second (Contact.java:530-545, :578-603). Buckets are filled with atomics and then
-//     sorted by (cell, 2 s + endpoint), which restores exactly that order;
+//     second (Contact.java:530-545, :578-603). Buckets are filled with atomics in any order;
+//     each candidate carries its visit key (cell in the nine, 2 s + endpoint) instead, and
+//     ties in depth go to the smallest key, the candidate the serial loop keeps;
 //   * every node's force receives its contact terms in slave order, normal before tangent
-//     (Contact.java:446-462, :717-754). Each pair's twelve terms are computed in parallel,
-//     each node then sorts its incident pairs and adds them in that order.
+//     (Contact.java:446-462, :717-754). Each pair's twelve terms are computed in parallel and
+//     filed in fixed per-node lists; each node then sorts its list and adds in that order.
 // The running totals (spring energy, dissipation) are audits; they are reduced in a fixed
-// order per block, so they are deterministic but not summed in the reference's serial order.
+// order per block over a fixed grid, so they are deterministic but not summed in the
+// reference's serial order.
+//
+// The grid barrier is a counter and a generation word in device memory. The launch is
+// cooperative, so every block is resident and the barrier cannot deadlock; its wait is bounded
+// all the same: a block that waits longer than a second sets STATUS_TIMEOUT and an abort word
+// that releases the others, and the kernel returns.
 #include "nf_internal.h"
 
 namespace nf {
 
-constexpr int CB = 128;
-constexpr int STEP_GRID = 256;       // blocks of the per-step kernels (grid-stride over counts)
-constexpr int REBUILD_GRID = 1024;   // blocks of the surface-rebuild kernels
-constexpr int SEARCH_GRID = 512;     // blocks of 4 warps, one warp per slave at a time
-constexpr int RESOLVE_BLOCKS = 256;  // fixed, so the partial sums have a fixed order
+constexpr int CB = 256;                  // threads per block
+constexpr int CB_WARPS = CB / 32;
+constexpr int MAX_COOP_BLOCKS_PER_SM = 4;
 constexpr double MAX_DEPTH = 0.5;
 constexpr double STICK_RELAXATION = 0.5;
 constexpr double FACING = 0.25;
+constexpr int INC_CAP = NF_INC_CAP;      // incident terms a surface node's fixed list holds
+constexpr unsigned long long WAIT_LIMIT_NS = 1000000000ULL;   // one second
+constexpr long long WAIT_LIMIT_SPINS = 1LL << 27;             // a bound independent of the timer
 
 __device__ __forceinline__ unsigned long long okey(double v) {     // order-preserving image
     const unsigned long long b = (unsigned long long)__double_as_longlong(v);
@@ -36,6 +49,18 @@ __device__ __forceinline__ double unokey(unsigned long long k) {
     return __longlong_as_double((long long)b);
 }
 
+__device__ __forceinline__ unsigned long long global_ns() {
+    unsigned long long t;
+    asm volatile("mov.u64 %0, %%globaltimer;" : "=l"(t));
+    return t;
+}
+
+template <typename T>
+__device__ __forceinline__ T vload(const T *p) { return *(const volatile T *)p; }
+
+// ---------------------------------------------------------------------------- block helpers
+
+// Fixed-order block sum; the result is valid in thread 0. Leaves sh free for reuse.
 __device__ double block_sum_c(double v, double *sh) {
     for (int o = 16; o > 0; o >>= 1) v += __shfl_down_sync(0xffffffffu, v, o);
     const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
@@ -43,292 +68,185 @@ __device__ double block_sum_c(double v, double *sh) {
     if (lane == 0) sh[warp] = v;
     __syncthreads();
     double t = 0.0;
-    if (threadIdx.x == 0) {
-        const int warps = (blockDim.x + 31) >> 5;
-        for (int w = 0; w < warps; w++) t += sh[w];
-    }
+    if (threadIdx.x == 0)
+        for (int w = 0; w < CB_WARPS; w++) t += sh[w];
+    __syncthreads();
     return t;
 }
 
-// ---------------------------------------------------------------------------- begin
-
-#define GRID_STRIDE(i, count) \
-    for (int i = blockIdx.x * blockDim.x + threadIdx.x; i < (count); i += gridDim.x * blockDim.x)
-
-// Contact.begin, Contact.java:424-436: per-step totals, and whether the surface is stale.
-__global__ void k_contact_begin(Dev d) {
-    DevScalars *s = d.s;
-    s->rebuild = s->active && s->stale;
-    if (!s->active) return;
-    s->pairs = 0;
-    s->maxPenBits = 0ULL;
-    s->bbox[0] = ~0ULL;   // min r
-    s->bbox[1] = ~0ULL;   // min z
-    s->bbox[2] = 0ULL;    // max r
-    s->bbox[3] = 0ULL;    // max z
-    s->longestBits = 0ULL;
-}
-
-// ---------------------------------------------------------------------------- surface rebuild
-
-__global__ void k_surf_flags(Dev d) {
-    if (!d.s->rebuild) return;
-    GRID_STRIDE(q, 4 * d.E) {
-        const int e = q >> 2;
-        int flag = 0;
-        if (!d.dead[e]) {
-            const int g = d.edgeGroup[q];
-            int live = 0;
-            for (int m = d.groupStart[g]; m < d.groupStart[g + 1]; m++)
-                if (!d.dead[d.groupMember[m] >> 2]) live++;
-            flag = live == 1;
+// Inclusive scan of one int per thread over the block; *total (in every thread) gets the sum.
+__device__ int block_scan_incl(int v, int *sh, int *total) {
+    const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
+    int x = v;
+    for (int o = 1; o < 32; o <<= 1) {
+        const int t = __shfl_up_sync(0xffffffffu, x, o);
+        if (lane >= o) x += t;
+    }
+    __syncthreads();
+    if (lane == 31) sh[warp] = x;
+    __syncthreads();
+    if (warp == 0) {
+        int w = lane < CB_WARPS ? sh[lane] : 0;
+        for (int o = 1; o < 32; o <<= 1) {
+            const int t = __shfl_up_sync(0xffffffffu, w, o);
+            if (lane >= o) w += t;
         }
-        d.surfFlag[q] = flag;
+        if (lane < CB_WARPS) sh[lane] = w;
     }
+    __syncthreads();
+    const int r = x + (warp > 0 ? sh[warp - 1] : 0);
+    *total = sh[CB_WARPS - 1];
+    __syncthreads();
+    return r;
 }
 
-// a[0 .. n) = 0, with n = min(*nDev, nMax) when nDev is given
-__global__ void k_zero_int(int32_t *a, int nMax, const int *pred, const int *nDev) {
-    if (pred && !*pred) return;
-    const int n = nDev ? min(*nDev, nMax) : nMax;
-    GRID_STRIDE(i, n) a[i] = 0;
+// ---------------------------------------------------------------------------- grid barrier
+
+__device__ __forceinline__ unsigned int ld_acquire(const unsigned int *p) {
+    unsigned int v;
+    asm volatile("ld.acquire.gpu.global.u32 %0, [%1];" : "=r"(v) : "l"(p) : "memory");
+    return v;
+}
+__device__ __forceinline__ unsigned int ld_relaxed(const unsigned int *p) {
+    unsigned int v;
+    asm volatile("ld.relaxed.gpu.global.u32 %0, [%1];" : "=r"(v) : "l"(p) : "memory");
+    return v;
+}
+__device__ __forceinline__ unsigned int atom_add_acq_rel(unsigned int *p, unsigned int v) {
+    unsigned int old;
+    asm volatile("atom.acq_rel.gpu.global.add.u32 %0, [%1], %2;" : "=r"(old) : "l"(p), "r"(v) : "memory");
+    return old;
+}
+__device__ __forceinline__ void st_relaxed(unsigned int *p, unsigned int v) {
+    asm volatile("st.relaxed.gpu.global.u32 [%0], %1;" :: "l"(p), "r"(v) : "memory");
+}
+__device__ __forceinline__ void st_release(unsigned int *p, unsigned int v) {
+    asm volatile("st.release.gpu.global.u32 [%0], %1;" :: "l"(p), "r"(v) : "memory");
 }
 
-__global__ void k_copy_int(const int32_t *src, int32_t *dst, int nMax, const int *pred,
-                           const int *nDev) {
-    if (pred && !*pred) return;
-    const int n = nDev ? min(*nDev, nMax) : nMax;
-    GRID_STRIDE(i, n) dst[i] = src[i];
-}
-
-__global__ void k_surf_emit(Dev d) {
-    if (!d.s->rebuild) return;
-    GRID_STRIDE(q, 4 * d.E) {
-        if (!d.surfFlag[q]) continue;
-        const int e = q >> 2, k = q & 3;
-        const int4 c = d.conn[e];
-        const int nn[4] = {c.x, c.y, c.z, c.w};
-        const int a = nn[k], b = nn[(k + 1) & 3];
-        const int p = d.surfPos[q];
-        d.segA[p] = a;
-        d.segB[p] = b;
-        d.segOwner[p] = e;
-        d.nodeFlag[a] = 1;
-        d.nodeFlag[b] = 1;
-    }
-}
-
-__global__ void k_surf_nodes(Dev d) {
-    if (!d.s->rebuild) return;
-    GRID_STRIDE(n, d.N) {
-        if (d.nodeFlag[n]) {
-            const int slot = d.nodePos[n];
-            d.surfNodes[slot] = n;
-            d.slotOf[n] = slot;
-            d.lastMaster[slot] = -1;         // Contact.adopt, :319-321
-            d.master[slot] = -1;
-            d.dropped[slot] = 0;
-            d.segCount[slot] = 0;
+// Sense-reversal barrier over all blocks of the cooperative grid. After the block's own
+// barrier, thread 0 arrives on the counter with an acquire-release add (publishing what the
+// block wrote, which the block barrier ordered before it) and waits with acquire loads for the
+// generation to move; the last arriver resets the counter and moves the generation with a
+// release store. Returns false when the wait ran out or another block gave up; the caller then
+// leaves the kernel.
+__device__ bool grid_sync(DevScalars *s) {
+    __shared__ int ok;
+    __syncthreads();
+    if (threadIdx.x == 0) {
+        const unsigned int g = ld_relaxed(&s->barGen);
+        const unsigned int arrived = atom_add_acq_rel(&s->barCount, 1u);
+        int good = 1;
+        if (arrived == gridDim.x - 1) {
+            st_relaxed(&s->barCount, 0u);
+            st_release(&s->barGen, g + 1u);
         } else {
-            d.slotOf[n] = -1;
-        }
-    }
-    if (blockIdx.x == 0 && threadIdx.x == 0) d.s->slotScanN = 0;   // set by k_seg_scan_n
-}
-
-__global__ void k_seg_scan_n(Dev d) {
-    if (!d.s->rebuild) return;
-    d.s->slotScanN = d.s->surfNodes + 1;
-    d.segCount[d.s->surfNodes] = 0;
-}
-
-__global__ void k_seg_count(Dev d) {
-    if (!d.s->rebuild) return;
-    GRID_STRIDE(s, d.s->surfEdges) {
-        atomicAdd(&d.segCount[d.slotOf[d.segA[s]]], 1);
-        atomicAdd(&d.segCount[d.slotOf[d.segB[s]]], 1);
-    }
-}
-
-__global__ void k_seg_fill(Dev d) {
-    if (!d.s->rebuild) return;
-    GRID_STRIDE(s, d.s->surfEdges) {
-        d.segOf[atomicAdd(&d.segCursor[d.slotOf[d.segA[s]]], 1)] = s;
-        d.segOf[atomicAdd(&d.segCursor[d.slotOf[d.segB[s]]], 1)] = s;
-    }
-}
-
-// Restores ascending segment order in each node's list (Contact.java:306-313), then retires
-// the rebuild.
-__global__ void k_seg_sort(Dev d) {
-    if (!d.s->rebuild) return;
-    if (blockIdx.x == 0 && threadIdx.x == 0) d.s->stale = 0;
-    GRID_STRIDE(i, d.s->surfNodes) {
-        const int lo = d.segStart[i], hi = d.segStart[i + 1];
-        for (int k = lo + 1; k < hi; k++) {
-            const int v = d.segOf[k];
-            int j = k - 1;
-            while (j >= lo && d.segOf[j] > v) {
-                d.segOf[j + 1] = d.segOf[j];
-                j--;
+            const unsigned long long t0 = global_ns();
+            long long spins = 0;
+            while (ld_acquire(&s->barGen) == g) {
+                if (ld_relaxed(&s->barAbort)) {
+                    good = 0;
+                    break;
+                }
+                if (++spins > WAIT_LIMIT_SPINS || global_ns() - t0 > WAIT_LIMIT_NS) {
+                    atomicOr(&s->status, STATUS_TIMEOUT);
+                    atomicExch(&s->barAbort, 1u);
+                    good = 0;
+                    break;
+                }
+                __nanosleep(20);
             }
-            d.segOf[j + 1] = v;
         }
+        ok = good;
     }
+    __syncthreads();
+    return ok != 0;
 }
 
-// ---------------------------------------------------------------------------- geometry
-
-// Contact.geometry, Contact.java:467-500 (coordinates and the bounding box of the grid)
-__global__ void k_contact_nodes(Dev d) {
-    if (!d.s->active) return;
-    unsigned long long kr0 = ~0ULL, kz0 = ~0ULL, kr1 = 0ULL, kz1 = 0ULL;
-    GRID_STRIDE(i, d.s->surfNodes) {
-        const int n = d.surfNodes[i];
-        const double2 x = d.X0[n], u = d.U[n];
-        const double cr = x.x + u.x, cz = x.y + u.y;
-        d.cr[n] = cr;
-        d.cz[n] = cz;
-        d.incCount[i] = 0;
-        d.pairNodes[i] = make_int4(-1, -1, -1, 0);
-        const unsigned long long kr = okey(cr), kz = okey(cz);
-        kr0 = min(kr0, kr); kr1 = max(kr1, kr);
-        kz0 = min(kz0, kz); kz1 = max(kz1, kz);
-    }
-    // extrema are exact in any order: reduce in the warp, one atomic per warp
-    for (int o = 16; o > 0; o >>= 1) {
-        kr0 = min(kr0, __shfl_down_sync(0xffffffffu, kr0, o));
-        kz0 = min(kz0, __shfl_down_sync(0xffffffffu, kz0, o));
-        kr1 = max(kr1, __shfl_down_sync(0xffffffffu, kr1, o));
-        kz1 = max(kz1, __shfl_down_sync(0xffffffffu, kz1, o));
-    }
-    if ((threadIdx.x & 31) == 0 && kr1 != 0ULL) {
-        atomicMin(&d.s->bbox[0], kr0);
-        atomicMin(&d.s->bbox[1], kz0);
-        atomicMax(&d.s->bbox[2], kr1);
-        atomicMax(&d.s->bbox[3], kz1);
-    }
-}
-
-__global__ void k_contact_segs(Dev d) {
-    if (!d.s->active) return;
-    unsigned long long lb = 0ULL;
-    GRID_STRIDE(s, d.s->surfEdges) {
-        const int a = d.segA[s], b = d.segB[s];
-        const double dr = d.cr[b] - d.cr[a], dz = d.cz[b] - d.cz[a];
-        const double len = sqrt(dr * dr + dz * dz);
-        d.slen[s] = len;
-        if (len > 0.0) {
-            d.snr[s] = dz / len;
-            d.snz[s] = -dr / len;
-        } else {
-            d.snr[s] = 0.0;
-            d.snz[s] = 0.0;
+// Exclusive scan of in[0, n) into out (and into out2 when given: the cursor copy the atomic
+// fills advance); zeroes in[] behind it when zeroIn; *total gets the sum when given. The
+// block sums go through d.coopSums. Ends with a barrier; returns false when one ran out.
+__device__ bool grid_scan(const Dev &d, int32_t *in, int32_t *out, int32_t *out2, int n,
+                          int32_t *total, bool zeroIn) {
+    __shared__ int sh[CB_WARPS];
+    const int G = gridDim.x;
+    const int chunk = (n + G - 1) / G;
+    const int lo = min(n, (int)blockIdx.x * chunk), hi = min(n, lo + chunk);
+    int local = 0;
+    for (int i = lo + threadIdx.x; i < hi; i += CB) local += in[i];
+    int bsum;
+    block_scan_incl(local, sh, &bsum);
+    if (threadIdx.x == 0) d.coopSums[blockIdx.x] = bsum;
+    if (!grid_sync(d.s)) return false;
+    // this block's offset: the sum over the earlier blocks' chunks
+    int pre = 0;
+    for (int j = threadIdx.x; j < (int)blockIdx.x; j += CB) pre += vload(&d.coopSums[j]);
+    int carry;
+    block_scan_incl(pre, sh, &carry);
+    if (total && threadIdx.x == 0 && (int)blockIdx.x == G - 1) *total = carry + bsum;
+    for (int base = lo; base < hi; base += CB) {
+        const int i = base + threadIdx.x;
+        const int v = i < hi ? in[i] : 0;
+        int tileTotal;
+        const int incl = block_scan_incl(v, sh, &tileTotal);
+        if (i < hi) {
+            out[i] = carry + incl - v;
+            if (out2) out2[i] = carry + incl - v;
+            if (zeroIn) in[i] = 0;
         }
-        lb = max(lb, (unsigned long long)__double_as_longlong(len));
+        carry += tileTotal;
     }
-    for (int o = 16; o > 0; o >>= 1) lb = max(lb, __shfl_down_sync(0xffffffffu, lb, o));
-    if ((threadIdx.x & 31) == 0 && lb != 0ULL) atomicMax(&d.s->longestBits, lb);
+    return grid_sync(d.s);
 }
 
-__global__ void k_contact_pnorm(Dev d) {
-    if (!d.s->active) return;
-    GRID_STRIDE(i, d.s->surfNodes) {
-        double sr = 0.0, sz = 0.0;
-        for (int k = d.segStart[i]; k < d.segStart[i + 1]; k++) {
-            sr += d.snr[d.segOf[k]];
-            sz += d.snz[d.segOf[k]];
-        }
-        const double len = sqrt(sr * sr + sz * sz);
-        d.pnr[i] = len > 0.0 ? sr / len : 0.0;
-        d.pnz[i] = len > 0.0 ? sz / len : 0.0;
-    }
-}
+// ---------------------------------------------------------------------------- contact geometry
 
-// Contact.grid, Contact.java:515-545 (the grid's extent and cell size)
-__global__ void k_grid_setup(Dev d) {
+// The search grid of one step (Contact.grid, Contact.java:515-545), derived from the bounding
+// box by every block for itself, so no pass over the grid waits on a single thread.
+struct Grid {
+    double cellSize, r0, z0;
+    int cols, rows, hashed, bucketN;
+    long long cells;
+};
+
+__device__ void grid_from_box(const Dev &d, int nodes, Grid &g) {
     DevScalars *s = d.s;
-    if (!s->active) return;
-    s->slotScanN = s->surfNodes + 1;
-    d.incCount[s->surfNodes] = 0;
-    if (s->surfNodes == 0) {
-        s->cols = s->rows = 1;
-        s->cells = 1;
-        s->hashed = 0;
-        s->bucketScanN = 2;
+    if (nodes == 0) {
+        g.cellSize = 1.0;
+        g.r0 = g.z0 = 0.0;
+        g.cols = g.rows = 1;
+        g.cells = 1;
+        g.hashed = 0;
+        g.bucketN = 2;
         return;
     }
-    const double rlo = unokey(s->bbox[0]), zlo = unokey(s->bbox[1]);
-    const double rhi = unokey(s->bbox[2]), zhi = unokey(s->bbox[3]);
-    const double longest = __longlong_as_double((long long)s->longestBits);
+    const double rlo = unokey(vload(&s->bbox[0])), zlo = unokey(vload(&s->bbox[1]));
+    const double rhi = unokey(vload(&s->bbox[2])), zhi = unokey(vload(&s->bbox[3]));
+    const double longest = __longlong_as_double((long long)vload(&s->longestBits));
     const double cellSize = longest > 0.0 ? 1.5 * longest : 1.0;
-    s->cellSize = cellSize;
-    s->gridR0 = rlo;
-    s->gridZ0 = zlo;
+    g.cellSize = cellSize;
+    g.r0 = rlo;
+    g.z0 = zlo;
     const int a = jd2i((rhi - rlo) / cellSize) + 1;
     const int b = jd2i((zhi - zlo) / cellSize) + 1;
-    s->cols = a > 1 ? a : 1;
-    s->rows = b > 1 ? b : 1;
-    s->cells = (long long)s->cols * (long long)s->rows;
-    s->hashed = s->cells > d.bucketCap;
-    s->bucketScanN = (int)((s->hashed ? (long long)d.bucketCap : s->cells) + 1);
-    if (s->hashed) atomicOr(&s->status, STATUS_GRID_HASHED);
+    g.cols = a > 1 ? a : 1;
+    g.rows = b > 1 ? b : 1;
+    g.cells = (long long)g.cols * (long long)g.rows;
+    g.hashed = g.cells > d.bucketCap;
+    g.bucketN = (int)((g.hashed ? (long long)d.bucketCap : g.cells) + 1);
 }
 
 __device__ __forceinline__ int iclamp(int v, int n) { return v < 0 ? 0 : v >= n ? n - 1 : v; }
 
-__device__ __forceinline__ long long cell_of(const DevScalars *s, double r, double z) {
-    const int i = iclamp(jd2i((r - s->gridR0) / s->cellSize), s->cols);
-    const int j = iclamp(jd2i((z - s->gridZ0) / s->cellSize), s->rows);
-    return (long long)j * s->cols + i;
+__device__ __forceinline__ long long cell_of(const Grid &g, double r, double z) {
+    const int i = iclamp(jd2i((r - g.r0) / g.cellSize), g.cols);
+    const int j = iclamp(jd2i((z - g.z0) / g.cellSize), g.rows);
+    return (long long)j * g.cols + i;
 }
 
-__device__ __forceinline__ int bucket_of(const Dev &d, long long cell) {
-    return d.s->hashed ? (int)(cell % d.bucketCap) : (int)cell;
+__device__ __forceinline__ int bucket_of(const Dev &d, const Grid &g, long long cell) {
+    return g.hashed ? (int)(cell % d.bucketCap) : (int)cell;
 }
-
-__global__ void k_bucket_count(Dev d) {
-    if (!d.s->active) return;
-    GRID_STRIDE(q, 2 * d.s->surfEdges) {
-        const int s = q >> 1;
-        const int node = (q & 1) ? d.segB[s] : d.segA[s];
-        const long long cell = cell_of(d.s, d.cr[node], d.cz[node]);
-        d.entryCell[q] = cell;
-        atomicAdd(&d.bucketCount[bucket_of(d, cell)], 1);
-    }
-}
-
-__global__ void k_bucket_fill(Dev d) {
-    if (!d.s->active) return;
-    GRID_STRIDE(q, 2 * d.s->surfEdges) {
-        const long long cell = d.entryCell[q];
-        const int pos = atomicAdd(&d.bucketCursor[bucket_of(d, cell)], 1);
-        d.bucketEntry[pos] = q;
-        d.bucketCell[pos] = cell;
-    }
-}
-
-// Sorts each bucket by (cell, entry): the counting sort's filing order.
-__global__ void k_bucket_sort(Dev d) {
-    if (!d.s->active) return;
-    GRID_STRIDE(b, d.s->bucketScanN - 1) {
-        const int lo = d.bucketStart[b], hi = d.bucketStart[b + 1];
-        for (int k = lo + 1; k < hi; k++) {
-            const int v = d.bucketEntry[k];
-            const long long c = d.bucketCell[k];
-            int j = k - 1;
-            while (j >= lo && (d.bucketCell[j] > c || (d.bucketCell[j] == c && d.bucketEntry[j] > v))) {
-                d.bucketEntry[j + 1] = d.bucketEntry[j];
-                d.bucketCell[j + 1] = d.bucketCell[j];
-                j--;
-            }
-            d.bucketEntry[j + 1] = v;
-            d.bucketCell[j + 1] = c;
-        }
-    }
-}
-
-// ---------------------------------------------------------------------------- search
 
 // Contact.excluded, Contact.java:620-639
 __device__ __forceinline__ bool excluded(const Dev &d, int i, int n, int s) {
@@ -356,212 +274,445 @@ __device__ __forceinline__ double depth_of(const Dev &d, int n, int s) {
     return gap < 0.0 ? -gap : 0.0;
 }
 
-// Contact.nearestPenetrated, Contact.java:570-606, one warp per slave. The reference visits
-// the nine cells in (dj, di) order and each cell's bucket in order, keeping the first
-// candidate of greatest depth. Here the nine bucket ranges are concatenated in that order,
-// the lanes take the candidates round-robin, each lane keeps its first deepest (strictly
-// greater replaces), and the warp reduction takes the greatest depth with the smallest
-// position in the visit sequence: the same segment the serial loop keeps.
-__global__ void __launch_bounds__(CB) k_contact_search(Dev d) {
-    const DevScalars *s = d.s;
-    if (!s->active) return;
-    const int lane = threadIdx.x & 31;
-    const int warpsTotal = gridDim.x * (blockDim.x >> 5);
-    const int count = s->surfNodes;
-    for (int i = blockIdx.x * (blockDim.x >> 5) + (threadIdx.x >> 5); i < count; i += warpsTotal) {
-        const int n = d.surfNodes[i];
-        const double crn = d.cr[n], czn = d.cz[n];
-        const int ci = iclamp(jd2i((crn - s->gridR0) / s->cellSize), s->cols);
-        const int cj = iclamp(jd2i((czn - s->gridZ0) / s->cellSize), s->rows);
-        const int last = d.lastMaster[i];
-        // lanes 0..8 describe the nine cells in visit order
-        int lo = 0, len = 0;
-        long long myCell = -1;
-        if (lane < 9) {
-            const int j = cj + lane / 3 - 1, ii = ci + lane % 3 - 1;
-            if (j >= 0 && j < s->rows && ii >= 0 && ii < s->cols) {
-                myCell = (long long)j * s->cols + ii;
-                const int bkt = bucket_of(d, myCell);
-                lo = d.bucketStart[bkt];
-                len = d.bucketStart[bkt + 1] - lo;
-            }
-        }
-        int off = len;                                   // inclusive scan over the nine
-        for (int o = 1; o < 16; o <<= 1) {
-            const int t = __shfl_up_sync(0xffffffffu, off, o);
-            if (lane >= o) off += t;
-        }
-        const int total = __shfl_sync(0xffffffffu, off, 8);
-        off -= len;                                      // exclusive
-        double best = 0.0;
-        int bestPos = 0x7fffffff, bestSeg = -1;
-        bool fell = false;
-        for (int base = 0; base < total; base += 32) {
-            const int t = base + lane;
-            // which of the nine ranges holds position t
-            int c = 0;
-#pragma unroll
-            for (int q = 1; q < 9; q++) {
-                const int oq = __shfl_sync(0xffffffffu, off, q);
-                if (t >= oq) c = q;
-            }
-            const int oc = __shfl_sync(0xffffffffu, off, c);
-            const int lc = __shfl_sync(0xffffffffu, lo, c);
-            const long long cc = __shfl_sync(0xffffffffu, myCell, c);
-            if (t >= total) continue;
-            const int k = lc + (t - oc);
-            if (d.bucketCell[k] != cc) continue;
-            const int sg = d.bucketEntry[k] >> 1;
-            if (excluded(d, i, n, sg)) continue;
-            const double depth = depth_of(d, n, sg);
-            if (depth <= 0.0) continue;
-            if (depth > MAX_DEPTH * d.slen[sg]) {
-                if (sg == last) fell = true;
-                continue;
-            }
-            if (depth > best) {
-                best = depth;
-                bestPos = t;
-                bestSeg = sg;
-            }
-        }
-        for (int o = 16; o > 0; o >>= 1) {
-            const double ob = __shfl_down_sync(0xffffffffu, best, o);
-            const int op = __shfl_down_sync(0xffffffffu, bestPos, o);
-            const int os = __shfl_down_sync(0xffffffffu, bestSeg, o);
-            if (ob > best || (ob == best && op < bestPos)) {
-                best = ob;
-                bestPos = op;
-                bestSeg = os;
-            }
-        }
-        const bool anyFell = __any_sync(0xffffffffu, fell);
-        if (lane == 0) {
-            d.dropped[i] = anyFell ? 1 : 0;
-            d.master[i] = best > 0.0 ? bestSeg : -1;
-        }
-    }
+// Files one incident term (pair i, role r as i << 2 | r) in node slot j's fixed list; a list
+// that overflows switches the step to the general path (a scan over the counts).
+__device__ __forceinline__ void inc_push(const Dev &d, int j, int entry) {
+    const int pos = atomicAdd(&d.incCount[j], 1);
+    if (pos < INC_CAP) d.incSlots[(size_t)j * INC_CAP + pos] = entry;
+    else d.s->incOverflow = 1;
 }
 
-// ---------------------------------------------------------------------------- resolve
+// Contact.accumulate + resolve, Contact.java:446-462, :663-762, for slave i (node n) and its
+// master segment s: writes the pair's twelve force terms as values to ADD (x - y is computed
+// as x + (-y), the same IEEE result) and files them at the pair's three nodes. Adds the
+// pair's spring energy and dissipation.
+__device__ void resolve_pair(const Dev &d, int i, int n, int s, double &energy, double &diss) {
+    const double dt = d.s->dt;
+    const double reference = d.dt0;
+    const int a = d.segA[s], b = d.segB[s];
+    const double depth = depth_of(d, n, s);
+    const double len = d.slen[s];
+    const double tr = (d.cr[b] - d.cr[a]) / len;            // parameter, :655-661
+    const double tz = (d.cz[b] - d.cz[a]) / len;
+    const double t = ((d.cr[n] - d.cr[a]) * tr + (d.cz[n] - d.cz[a]) * tz) / len;
+    const double wa = 1.0 - t, wb = t;
+    const double ma = d.mass[a], mb = d.mass[b];
+    const double invMaster = 0.25 / ma + 0.25 / mb;
+    if (!(invMaster > 0.0)) return;
+    const double mMaster = 1.0 / invMaster;
+    const double mSlave = d.mass[n];
+    const double mStar = mSlave * mMaster / (mSlave + mMaster);
+    const double k = d.cScale * mStar / (reference * reference);
+    const double nR = d.snr[s], nZ = d.snz[s];
+    const double mTrue = 1.0 / (wa * wa / ma + wb * wb / mb);
+    const double mTangent = mSlave * mTrue / (mSlave + mTrue);
+    const double2 vn = d.V[n], va = d.V[a], vb = d.V[b];
+    const double closing = (vn.x - wa * va.x - wb * vb.x) * nR
+                           + (vn.y - wa * va.y - wb * vb.y) * nZ;
+    const double damper = 2.0 * d.cDamping * mStar * sqrt(d.cScale) / reference;
+    const double normal = jmax(0.0, k * depth - damper * closing);
+    double *pv = d.pairVal + 12 * (size_t)i;
+    pv[0] = normal * nR;
+    pv[1] = normal * nZ;
+    pv[4] = -(wa * normal * nR);
+    pv[5] = -(wa * normal * nZ);
+    pv[8] = -(wb * normal * nR);
+    pv[9] = -(wb * normal * nZ);
+    atomicAdd(&d.s->pairs, 1);
+    energy += 0.5 * k * depth * depth;
+    atomicMax(&d.s->maxPenBits, (unsigned long long)__double_as_longlong(depth));
+    double dthis = 0.0;
+    const double damperForce = normal - k * depth;
+    if (damperForce != 0.0) {
+        const double closingAfter = closing + damperForce * dt / mTangent;
+        dthis -= damperForce * 0.5 * (closing + closingAfter) * dt;
+    }
+    uint8_t state = NF_CONTACT_PAIR;
+    if (d.cFriction > 0.0) {
+        const double tR = -nZ, tZ = nR;
+        const double slide = (vn.x - wa * va.x - wb * vb.x) * tR
+                             + (vn.y - wa * va.y - wb * vb.y) * tZ;
+        double tangent = -STICK_RELAXATION * mTangent * slide / dt;
+        const double cone = d.cFriction * normal;
+        bool slipped = false;
+        if (tangent > cone) { tangent = cone; slipped = true; }
+        else if (tangent < -cone) { tangent = -cone; slipped = true; }
+        pv[2] = tangent * tR;
+        pv[3] = tangent * tZ;
+        pv[6] = -(wa * tangent * tR);
+        pv[7] = -(wa * tangent * tZ);
+        pv[10] = -(wb * tangent * tR);
+        pv[11] = -(wb * tangent * tZ);
+        const double after = slide + tangent * dt / mTangent;
+        dthis += -tangent * 0.5 * (slide + after) * dt;
+        state |= slipped ? NF_CONTACT_SLIP : NF_CONTACT_STICK;
+    }
+    diss += dthis;
+    d.contactState[n] = state;
+    d.pairNodes[i] = make_int4(n, a, b, 1);
+    inc_push(d, i, (i << 2) | 0);              // the slave's slot is i
+    inc_push(d, d.slotOf[a], (i << 2) | 1);
+    inc_push(d, d.slotOf[b], (i << 2) | 2);
+}
 
-// Contact.accumulate + resolve, Contact.java:446-462, :663-762: each slave's pair, computed
-// independently (resolve reads velocities and masses only). Writes the twelve force terms of
-// the pair as values to ADD (x - y is computed as x + (-y), which is the same IEEE result).
-__global__ void __launch_bounds__(CB) k_contact_resolve(Dev d) {
-    __shared__ double sh[CB / 32];
-    const DevScalars *sc = d.s;
-    if (!sc->active) return;
-    double energy = 0.0, diss = 0.0;
-    GRID_STRIDE(i, sc->surfNodes) {
-        const int n = d.surfNodes[i];
-        const int best = d.master[i];
-        if (best < 0) {
-            if (d.lastMaster[i] >= 0 && d.dropped[i]) atomicAdd(&d.s->escaped, 1);
-            d.lastMaster[i] = -1;
+// Contact.nearestPenetrated, Contact.java:570-606, then the pair, for slave i, by one whole
+// warp. The reference visits the nine cells in (dj, di) order and each cell's entries in the
+// order its counting sort filed them, ascending entry (2 s + endpoint), and keeps the first
+// candidate of greatest depth. Here the nine bucket ranges are concatenated, the lanes take
+// the candidates round-robin, and each candidate carries its visit key (cell in the nine,
+// entry): the warp keeps the greatest depth with the smallest key, which is the candidate the
+// serial loop keeps, so the buckets need no order. A candidate's depth is zero unless its gap
+// is negative; that test is exact and reads only what the fill staged beside the entry, so it
+// runs first, before the exclusions and the divisions.
+__device__ void search_slave(const Dev &d, const Grid &g, int i, double &energy, double &diss) {
+    const int lane = threadIdx.x & 31;
+    const double2 xn = d.slaveXY[i];
+    const int n = d.surfNodes[i];
+    const int last = d.lastMaster[i];
+    const int ci = iclamp(jd2i((xn.x - g.r0) / g.cellSize), g.cols);
+    const int cj = iclamp(jd2i((xn.y - g.z0) / g.cellSize), g.rows);
+    int lo = 0, len = 0;                      // lanes 0..8: the nine cells in visit order
+    long long myCell = -1;
+    if (lane < 9) {
+        const int j = cj + lane / 3 - 1, ii = ci + lane % 3 - 1;
+        if (j >= 0 && j < g.rows && ii >= 0 && ii < g.cols) {
+            myCell = (long long)j * g.cols + ii;
+            const int bkt = bucket_of(d, g, myCell);
+            lo = d.bucketStart[bkt];
+            len = d.bucketStart[bkt + 1] - lo;
+        }
+    }
+    int off = len;                            // inclusive scan over the nine
+    for (int o = 1; o < 16; o <<= 1) {
+        const int t = __shfl_up_sync(0xffffffffu, off, o);
+        if (lane >= o) off += t;
+    }
+    const int total = __shfl_sync(0xffffffffu, off, 8);
+    off -= len;                               // exclusive
+    double best = 0.0;
+    unsigned long long bestKey = ~0ULL;
+    int bestSeg = -1;
+    bool fell = false;
+    for (int base = 0; base < total; base += 32) {
+        const int t = base + lane;
+        int c = 0;                            // which of the nine ranges holds position t
+#pragma unroll
+        for (int q = 1; q < 9; q++) {
+            const int oq = __shfl_sync(0xffffffffu, off, q);
+            if (t >= oq) c = q;
+        }
+        const int oc = __shfl_sync(0xffffffffu, off, c);
+        const int lc = __shfl_sync(0xffffffffu, lo, c);
+        const long long cc = __shfl_sync(0xffffffffu, myCell, c);
+        if (t >= total) continue;
+        const int k = lc + (t - oc);
+        const long long kc = d.bucketCell[k];
+        const int entry = d.bucketEntry[k];
+        const double2 pa = d.bucketA[k], nrm = d.bucketN[k];
+        if (kc != cc) continue;
+        const double gap = (xn.x - pa.x) * nrm.x + (xn.y - pa.y) * nrm.y;
+        if (!(gap < 0.0)) continue;           // depth_of would return zero
+        const int sg = entry >> 1;
+        if (excluded(d, i, n, sg)) continue;
+        const double depth = depth_of(d, n, sg);
+        if (depth <= 0.0) continue;
+        if (depth > MAX_DEPTH * d.slen[sg]) {
+            if (sg == last) fell = true;
             continue;
         }
-        d.lastMaster[i] = best;
-        const int s = best;
-        const double dt = sc->dt;
-        const double reference = d.dt0;
-        const int a = d.segA[s], b = d.segB[s];
-        const double depth = depth_of(d, n, s);
-        const double len = d.slen[s];
-        const double tr = (d.cr[b] - d.cr[a]) / len;            // parameter, :655-661
-        const double tz = (d.cz[b] - d.cz[a]) / len;
-        const double t = ((d.cr[n] - d.cr[a]) * tr + (d.cz[n] - d.cz[a]) * tz) / len;
-        const double wa = 1.0 - t, wb = t;
-        const double ma = d.mass[a], mb = d.mass[b];
-        const double invMaster = 0.25 / ma + 0.25 / mb;
-        if (!(invMaster > 0.0)) continue;
-        const double mMaster = 1.0 / invMaster;
-        const double mSlave = d.mass[n];
-        const double mStar = mSlave * mMaster / (mSlave + mMaster);
-        const double k = d.cScale * mStar / (reference * reference);
-        const double nR = d.snr[s], nZ = d.snz[s];
-        const double mTrue = 1.0 / (wa * wa / ma + wb * wb / mb);
-        const double mTangent = mSlave * mTrue / (mSlave + mTrue);
-        const double2 vn = d.V[n], va = d.V[a], vb = d.V[b];
-        const double closing = (vn.x - wa * va.x - wb * vb.x) * nR
-                               + (vn.y - wa * va.y - wb * vb.y) * nZ;
-        const double damper = 2.0 * d.cDamping * mStar * sqrt(d.cScale) / reference;
-        const double normal = jmax(0.0, k * depth - damper * closing);
-        double *pv = d.pairVal + 12 * (size_t)i;
-        pv[0] = normal * nR;
-        pv[1] = normal * nZ;
-        pv[4] = -(wa * normal * nR);
-        pv[5] = -(wa * normal * nZ);
-        pv[8] = -(wb * normal * nR);
-        pv[9] = -(wb * normal * nZ);
-        atomicAdd(&d.s->pairs, 1);
-        energy += 0.5 * k * depth * depth;
-        atomicMax(&d.s->maxPenBits, (unsigned long long)__double_as_longlong(depth));
-        double dthis = 0.0;
-        const double damperForce = normal - k * depth;
-        if (damperForce != 0.0) {
-            const double closingAfter = closing + damperForce * dt / mTangent;
-            dthis -= damperForce * 0.5 * (closing + closingAfter) * dt;
+        const unsigned long long key = ((unsigned long long)c << 32) | (unsigned int)entry;
+        if (depth > best || (depth == best && key < bestKey)) {
+            best = depth;
+            bestKey = key;
+            bestSeg = sg;
         }
-        uint8_t state = NF_CONTACT_PAIR;
-        if (d.cFriction > 0.0) {
-            const double tR = -nZ, tZ = nR;
-            const double slide = (vn.x - wa * va.x - wb * vb.x) * tR
-                                 + (vn.y - wa * va.y - wb * vb.y) * tZ;
-            double tangent = -STICK_RELAXATION * mTangent * slide / dt;
-            const double cone = d.cFriction * normal;
-            bool slipped = false;
-            if (tangent > cone) { tangent = cone; slipped = true; }
-            else if (tangent < -cone) { tangent = -cone; slipped = true; }
-            pv[2] = tangent * tR;
-            pv[3] = tangent * tZ;
-            pv[6] = -(wa * tangent * tR);
-            pv[7] = -(wa * tangent * tZ);
-            pv[10] = -(wb * tangent * tR);
-            pv[11] = -(wb * tangent * tZ);
-            const double after = slide + tangent * dt / mTangent;
-            dthis += -tangent * 0.5 * (slide + after) * dt;
-            state |= slipped ? NF_CONTACT_SLIP : NF_CONTACT_STICK;
-        }
-        diss += dthis;
-        d.contactState[n] = state;
-        d.pairNodes[i] = make_int4(n, a, b, 1);
     }
-    const double e1 = block_sum_c(energy, sh);
-    const double e2 = block_sum_c(diss, sh);
+    for (int o = 16; o > 0; o >>= 1) {
+        const double ob = __shfl_down_sync(0xffffffffu, best, o);
+        const unsigned long long ok = __shfl_down_sync(0xffffffffu, bestKey, o);
+        const int os = __shfl_down_sync(0xffffffffu, bestSeg, o);
+        if (ob > best || (ob == best && ok < bestKey)) {
+            best = ob;
+            bestKey = ok;
+            bestSeg = os;
+        }
+    }
+    const bool anyFell = __any_sync(0xffffffffu, fell);
+    if (lane != 0) return;
+    d.master[i] = best > 0.0 ? bestSeg : -1;
+    if (!(best > 0.0)) {                      // no pair: Contact.java:446-452
+        if (last >= 0 && anyFell) atomicAdd(&d.s->escaped, 1);
+        d.lastMaster[i] = -1;
+        return;
+    }
+    d.lastMaster[i] = bestSeg;
+    resolve_pair(d, i, n, bestSeg, energy, diss);
+}
+
+// ---------------------------------------------------------------------------- the pass
+
+// Items are dealt to warps across the blocks first (warp w of block b takes the 32 items from
+// (w G + b) 32 on), so that a short list still spreads over every SM.
+#define FOR_GRID(i, count)                                                                    \
+    for (int i = ((threadIdx.x >> 5) * gridDim.x + blockIdx.x) * 32 + (threadIdx.x & 31);     \
+         i < (count); i += gridDim.x * CB)
+#define SYNC() do { if (!grid_sync(s)) return; } while (0)
+
+// The per-step totals this pass accumulates into (Contact.begin, Contact.java:424-436) are
+// reset by the step's first kernel (contact_step_reset), so the pass needs no opening barrier.
+__global__ void __launch_bounds__(CB, 2) k_contact_pass(Dev d) {
+    __shared__ double shd[CB_WARPS];
+    __shared__ Grid grid;
+    DevScalars *s = d.s;
+    if (!vload(&s->active)) return;
+    const int gt = blockIdx.x * CB + threadIdx.x;
+
+    if (vload(&s->stale)) {
+        // Contact.adopt, Contact.java:290-322: the free surface (QuadMesh.surface over the live
+        // elements), edges in element order, nodes ascending
+        FOR_GRID(q, 4 * d.E) {
+            const int e = q >> 2;
+            int flag = 0;
+            if (!d.dead[e]) {
+                const int g = d.edgeGroup[q];
+                int live = 0;
+                for (int m = d.groupStart[g]; m < d.groupStart[g + 1]; m++)
+                    if (!d.dead[d.groupMember[m] >> 2]) live++;
+                flag = live == 1;
+            }
+            d.surfFlag[q] = flag;
+        }
+        FOR_GRID(n, d.N) d.nodeFlag[n] = 0;
+        SYNC();
+        if (!grid_scan(d, d.surfFlag, d.surfPos, nullptr, 4 * d.E, &s->surfEdges, false)) return;
+        FOR_GRID(q, 4 * d.E) {
+            if (!d.surfFlag[q]) continue;
+            const int e = q >> 2, k = q & 3;
+            const int4 c = d.conn[e];
+            const int nn[4] = {c.x, c.y, c.z, c.w};
+            const int a = nn[k], b = nn[(k + 1) & 3];
+            const int p = d.surfPos[q];
+            d.segA[p] = a;
+            d.segB[p] = b;
+            d.segOwner[p] = e;
+            d.nodeFlag[a] = 1;
+            d.nodeFlag[b] = 1;
+        }
+        SYNC();
+        if (!grid_scan(d, d.nodeFlag, d.nodePos, nullptr, d.N, &s->surfNodes, false)) return;
+        FOR_GRID(n, d.N) {
+            if (d.nodeFlag[n]) {
+                const int slot = d.nodePos[n];
+                d.surfNodes[slot] = n;
+                d.slotOf[n] = slot;
+                d.lastMaster[slot] = -1;             // :319-321
+                d.master[slot] = -1;
+                d.dropped[slot] = 0;
+                d.segCount[slot] = 0;
+            } else {
+                d.slotOf[n] = -1;
+            }
+        }
+        if (gt == 0) d.segCount[vload(&s->surfNodes)] = 0;
+        SYNC();
+        const int edges = vload(&s->surfEdges), nodes = vload(&s->surfNodes);
+        FOR_GRID(e, edges) {
+            atomicAdd(&d.segCount[d.slotOf[d.segA[e]]], 1);
+            atomicAdd(&d.segCount[d.slotOf[d.segB[e]]], 1);
+        }
+        SYNC();
+        if (!grid_scan(d, d.segCount, d.segStart, d.segCursor, nodes + 1, nullptr, false)) return;
+        FOR_GRID(e, edges) {
+            d.segOf[atomicAdd(&d.segCursor[d.slotOf[d.segA[e]]], 1)] = e;
+            d.segOf[atomicAdd(&d.segCursor[d.slotOf[d.segB[e]]], 1)] = e;
+        }
+        SYNC();
+        FOR_GRID(i, nodes) {                         // ascending order per node, :306-313
+            const int lo = d.segStart[i], hi = d.segStart[i + 1];
+            for (int k = lo + 1; k < hi; k++) {
+                const int v = d.segOf[k];
+                int j = k - 1;
+                while (j >= lo && d.segOf[j] > v) {
+                    d.segOf[j + 1] = d.segOf[j];
+                    j--;
+                }
+                d.segOf[j + 1] = v;
+            }
+        }
+        if (gt == 0) s->stale = 0;
+        SYNC();
+    }
+    const int nodes = vload(&s->surfNodes), edges = vload(&s->surfEdges);
+
+    // Contact.geometry, Contact.java:467-500: current coordinates, the bounding box, segment
+    // lengths and normals (from X0 + U directly, the same sums the coordinates hold)
+    {
+        unsigned long long kr0 = ~0ULL, kz0 = ~0ULL, kr1 = 0ULL, kz1 = 0ULL, lb = 0ULL;
+        FOR_GRID(i, nodes) {
+            const int n = d.surfNodes[i];
+            const double2 x = d.X0[n], u = d.U[n];
+            const double cr = x.x + u.x, cz = x.y + u.y;
+            d.cr[n] = cr;
+            d.cz[n] = cz;
+            d.slaveXY[i] = make_double2(cr, cz);
+            d.incCount[i] = 0;
+            d.pairNodes[i] = make_int4(-1, -1, -1, 0);
+            const unsigned long long kr = okey(cr), kz = okey(cz);
+            kr0 = min(kr0, kr); kr1 = max(kr1, kr);
+            kz0 = min(kz0, kz); kz1 = max(kz1, kz);
+        }
+        if (gt == 0) d.incCount[nodes] = 0;
+        FOR_GRID(e, edges) {
+            const int a = d.segA[e], b = d.segB[e];
+            const double2 xa = d.X0[a], ua = d.U[a], xb = d.X0[b], ub = d.U[b];
+            const double dr = (xb.x + ub.x) - (xa.x + ua.x);
+            const double dz = (xb.y + ub.y) - (xa.y + ua.y);
+            const double len = sqrt(dr * dr + dz * dz);
+            d.slen[e] = len;
+            if (len > 0.0) {
+                d.snr[e] = dz / len;
+                d.snz[e] = -dr / len;
+            } else {
+                d.snr[e] = 0.0;
+                d.snz[e] = 0.0;
+            }
+            lb = max(lb, (unsigned long long)__double_as_longlong(len));
+        }
+        // extrema are exact in any order: reduce in the warp, one atomic per warp
+        for (int o = 16; o > 0; o >>= 1) {
+            kr0 = min(kr0, __shfl_down_sync(0xffffffffu, kr0, o));
+            kz0 = min(kz0, __shfl_down_sync(0xffffffffu, kz0, o));
+            kr1 = max(kr1, __shfl_down_sync(0xffffffffu, kr1, o));
+            kz1 = max(kz1, __shfl_down_sync(0xffffffffu, kz1, o));
+            lb = max(lb, __shfl_down_sync(0xffffffffu, lb, o));
+        }
+        if ((threadIdx.x & 31) == 0) {
+            if (kr1 != 0ULL) {
+                atomicMin(&s->bbox[0], kr0);
+                atomicMin(&s->bbox[1], kz0);
+                atomicMax(&s->bbox[2], kr1);
+                atomicMax(&s->bbox[3], kz1);
+            }
+            if (lb != 0ULL) atomicMax(&s->longestBits, lb);
+        }
+    }
+    SYNC();
+
+    // the grid, in every block; node normals; the counting sort's counts (:530-545).
+    // bucketCount is all zero on entry and is left all zero.
     if (threadIdx.x == 0) {
-        d.partials[(PARTIAL_CONTACT + 0) * d.maxBlocks + blockIdx.x] = e1;
-        d.partials[(PARTIAL_CONTACT + 1) * d.maxBlocks + blockIdx.x] = e2;
+        grid_from_box(d, nodes, grid);
+        if (blockIdx.x == 0) {
+            s->cellSize = grid.cellSize;
+            s->gridR0 = grid.r0;
+            s->gridZ0 = grid.z0;
+            s->cols = grid.cols;
+            s->rows = grid.rows;
+            s->cells = grid.cells;
+            s->hashed = grid.hashed;
+            s->bucketScanN = grid.bucketN;
+            if (grid.hashed) atomicOr(&s->status, STATUS_GRID_HASHED);
+        }
     }
-}
-
-__global__ void k_inc_count(Dev d) {
-    if (!d.s->active) return;
-    GRID_STRIDE(i, d.s->surfNodes) {
-        const int4 p = d.pairNodes[i];
-        if (!p.w) continue;
-        atomicAdd(&d.incCount[d.slotOf[p.x]], 1);
-        atomicAdd(&d.incCount[d.slotOf[p.y]], 1);
-        atomicAdd(&d.incCount[d.slotOf[p.z]], 1);
+    __syncthreads();
+    const Grid g = grid;
+    FOR_GRID(i, nodes) {
+        double sr = 0.0, sz = 0.0;
+        for (int k = d.segStart[i]; k < d.segStart[i + 1]; k++) {
+            sr += d.snr[d.segOf[k]];
+            sz += d.snz[d.segOf[k]];
+        }
+        const double len = sqrt(sr * sr + sz * sz);
+        d.pnr[i] = len > 0.0 ? sr / len : 0.0;
+        d.pnz[i] = len > 0.0 ? sz / len : 0.0;
     }
-}
+    FOR_GRID(q, 2 * edges) {
+        const int e = q >> 1;
+        const int node = (q & 1) ? d.segB[e] : d.segA[e];
+        const long long cell = cell_of(g, d.cr[node], d.cz[node]);
+        d.entryCell[q] = cell;
+        atomicAdd(&d.bucketCount[bucket_of(d, g, cell)], 1);
+    }
+    SYNC();
+    if (!grid_scan(d, d.bucketCount, d.bucketStart, d.bucketCursor, g.bucketN, nullptr, true))
+        return;
+    // file the entries; stage beside each what the search's gap test reads
+    FOR_GRID(q, 2 * edges) {
+        const long long cell = d.entryCell[q];
+        const int e = q >> 1;
+        const int a = d.segA[e];
+        const int pos = atomicAdd(&d.bucketCursor[bucket_of(d, g, cell)], 1);
+        d.bucketEntry[pos] = q;
+        d.bucketCell[pos] = cell;
+        d.bucketA[pos] = make_double2(d.cr[a], d.cz[a]);
+        d.bucketN[pos] = make_double2(d.snr[e], d.snz[e]);
+    }
+    SYNC();
 
-__global__ void k_inc_fill(Dev d) {
-    if (!d.s->active) return;
-    GRID_STRIDE(i, d.s->surfNodes) {
+    // the search and the pair forces: one warp per slave; the totals as per-block partials,
+    // folded in a fixed order at the step's end
+    {
+        double energy = 0.0, diss = 0.0;
+        const int warpsTotal = gridDim.x * CB_WARPS;
+        for (int i = (threadIdx.x >> 5) * gridDim.x + blockIdx.x; i < nodes; i += warpsTotal)
+            search_slave(d, g, i, energy, diss);
+        const double e1 = block_sum_c(energy, shd);
+        const double e2 = block_sum_c(diss, shd);
+        if (threadIdx.x == 0) {
+            d.partials[(PARTIAL_CONTACT + 0) * d.maxBlocks + blockIdx.x] = e1;
+            d.partials[(PARTIAL_CONTACT + 1) * d.maxBlocks + blockIdx.x] = e2;
+        }
+    }
+    SYNC();
+    const bool friction = d.cFriction > 0.0;
+    if (!vload(&s->incOverflow)) {
+        // each node adds its terms in slave order, normal then tangent (:717-754): the fixed
+        // list, sorted in registers by an odd-even transposition network
+        FOR_GRID(j, nodes) {
+            const int c = d.incCount[j];
+            if (c == 0) continue;
+            int e[INC_CAP];
+#pragma unroll
+            for (int k = 0; k < INC_CAP; k++)
+                e[k] = k < c ? d.incSlots[(size_t)j * INC_CAP + k] : 0x7fffffff;
+#pragma unroll
+            for (int r = 0; r < INC_CAP; r++) {
+#pragma unroll
+                for (int k = r & 1; k + 1 < INC_CAP; k += 2) {
+                    const int x = min(e[k], e[k + 1]), y = max(e[k], e[k + 1]);
+                    e[k] = x;
+                    e[k + 1] = y;
+                }
+            }
+            const int node = d.surfNodes[j];
+            double2 f = d.F[node];
+#pragma unroll
+            for (int k = 0; k < INC_CAP; k++) {
+                if (k < c) {
+                    const double *pv = d.pairVal + 12 * (size_t)(e[k] >> 2) + 4 * (e[k] & 3);
+                    f.x += pv[0];
+                    f.y += pv[1];
+                    if (friction) {
+                        f.x += pv[2];
+                        f.y += pv[3];
+                    }
+                }
+            }
+            d.F[node] = f;
+        }
+        return;
+    }
+    // the general path: incidence lists by a scan over the counts
+    if (!grid_scan(d, d.incCount, d.incStart, d.incCursor, nodes + 1, nullptr, false)) return;
+    FOR_GRID(i, nodes) {
         const int4 p = d.pairNodes[i];
         if (!p.w) continue;
         d.incEntry[atomicAdd(&d.incCursor[d.slotOf[p.x]], 1)] = (i << 2) | 0;
         d.incEntry[atomicAdd(&d.incCursor[d.slotOf[p.y]], 1)] = (i << 2) | 1;
         d.incEntry[atomicAdd(&d.incCursor[d.slotOf[p.z]], 1)] = (i << 2) | 2;
     }
-}
-
-// Adds each node's contact terms in slave order, normal then tangent (Contact.java:717-754).
-__global__ void k_inc_apply(Dev d) {
-    if (!d.s->active) return;
-    const bool friction = d.cFriction > 0.0;
-    GRID_STRIDE(j, d.s->surfNodes) {
+    SYNC();
+    FOR_GRID(j, nodes) {
         const int lo = d.incStart[j], hi = d.incStart[j + 1];
         if (lo == hi) continue;
         for (int k = lo + 1; k < hi; k++) {
@@ -589,58 +740,37 @@ __global__ void k_inc_apply(Dev d) {
     }
 }
 
+#undef SYNC
+#undef FOR_GRID
+
 // ---------------------------------------------------------------------------- launch
 
-int contact_partial_blocks() { return RESOLVE_BLOCKS; }
+// Blocks of the cooperative pass: as many as can be resident at once, at most four per SM.
+// Fixed per device, so the partial sums have a fixed order. Needs the device current.
+int contact_coop_blocks(int sms) {
+    int perSm = 0;
+    if (cudaOccupancyMaxActiveBlocksPerMultiprocessor(&perSm, k_contact_pass, CB, 0) != cudaSuccess ||
+        perSm < 1)
+        perSm = 1;
+    if (perSm > MAX_COOP_BLOCKS_PER_SM) perSm = MAX_COOP_BLOCKS_PER_SM;
+    return perSm * sms;
+}
 
 int launch_contact(Solver &S, bool) {
     Dev &d = S.d;
-    const cudaStream_t st = S.stream;
-    const int *rebuild = &d.s->rebuild;
-    const int *active = &d.s->active;
-    const int *slotN = &d.s->slotScanN;
-    const int *bucketN = &d.s->bucketScanN;
-    const int rg = REBUILD_GRID, sg = STEP_GRID;
-    int n = 0;
-#define L(kernel, grid, ...) do { kernel<<<(grid), CB, 0, st>>>(__VA_ARGS__); n++; } while (0)
-    L(k_contact_begin, 1, d);
-    // free surface, only on the steps after an erosion (or the first)
-    L(k_surf_flags, rg, d);
-    n += scan_exclusive(d.surfFlag, d.surfPos, 4 * d.E, &d.s->surfEdges, d.scanTmp, st, rebuild,
-                        nullptr);
-    L(k_zero_int, rg, d.nodeFlag, d.N, rebuild, nullptr);
-    L(k_surf_emit, rg, d);
-    n += scan_exclusive(d.nodeFlag, d.nodePos, d.N, &d.s->surfNodes, d.scanTmp, st, rebuild,
-                        nullptr);
-    L(k_surf_nodes, rg, d);
-    L(k_seg_scan_n, 1, d);
-    L(k_seg_count, rg, d);
-    n += scan_exclusive(d.segCount, d.segStart, d.N + 1, nullptr, d.scanTmp, st, rebuild, slotN);
-    L(k_copy_int, rg, d.segStart, d.segCursor, d.N + 1, rebuild, slotN);
-    L(k_seg_fill, rg, d);
-    L(k_seg_sort, rg, d);
-    // geometry and grid
-    L(k_contact_nodes, sg, d);
-    L(k_contact_segs, sg, d);
-    L(k_contact_pnorm, sg, d);
-    L(k_grid_setup, 1, d);
-    L(k_zero_int, sg, d.bucketCount, d.bucketCap + 1, active, bucketN);
-    L(k_bucket_count, sg, d);
-    n += scan_exclusive(d.bucketCount, d.bucketStart, d.bucketCap + 1, nullptr, d.scanTmp, st,
-                        active, bucketN);
-    L(k_copy_int, sg, d.bucketStart, d.bucketCursor, d.bucketCap + 1, active, bucketN);
-    L(k_bucket_fill, sg, d);
-    L(k_bucket_sort, sg, d);
-    // search, resolve, ordered accumulation
-    L(k_contact_search, SEARCH_GRID, d);
-    L(k_contact_resolve, RESOLVE_BLOCKS, d);
-    L(k_inc_count, sg, d);
-    n += scan_exclusive(d.incCount, d.incStart, d.N + 1, nullptr, d.scanTmp, st, active, slotN);
-    L(k_copy_int, sg, d.incStart, d.incCursor, d.N + 1, active, slotN);
-    L(k_inc_fill, sg, d);
-    L(k_inc_apply, sg, d);
-#undef L
-    return n;
+    void *args[] = {&d};
+    cudaLaunchAttribute attr[1];
+    attr[0].id = cudaLaunchAttributeCooperative;
+    attr[0].val.cooperative = 1;
+    cudaLaunchConfig_t cfg = {};
+    cfg.gridDim = dim3((unsigned)d.coopBlocks);
+    cfg.blockDim = dim3(CB);
+    cfg.dynamicSmemBytes = 0;
+    cfg.stream = S.stream;
+    cfg.attrs = attr;
+    cfg.numAttrs = 1;
+    cudaLaunchKernelExC(&cfg, (const void *)k_contact_pass, args);
+    return 1;
 }
 
 }  // namespace nf

@@ -47,6 +47,7 @@ __global__ void k_begin(Dev d, int initial) {
     DevScalars *s = d.s;
     const bool active = s->time < s->tEnd && s->stepsTaken < s->maxSteps;
     s->active = active ? 1 : 0;
+    contact_step_reset(s);
     if (!active || initial) return;
     const double dtAvg = 0.5 * (s->dtPrevious + s->dt);
     const double half = 0.5 * d.damping * dtAvg;
@@ -706,6 +707,7 @@ __global__ void k_advance_nodes(Dev d) {
 
 __global__ void k_set_active(Dev d) {
     d.s->active = 1;
+    contact_step_reset(d.s);
 }
 
 // ------------------------------------------------------------------------------------ launch
@@ -754,7 +756,7 @@ int launch_initial_assembly(Solver &S) {
     Dev &d = S.d;
     k_begin<<<1, 1, 0, S.stream>>>(d, 1);
     int n = 1 + assemble(S, 1);
-    k_end<<<1, 256, 0, S.stream>>>(d, nodal_grid(S), element_grid(S), contact_partial_blocks(), 0);
+    k_end<<<1, 256, 0, S.stream>>>(d, nodal_grid(S), element_grid(S), d.coopBlocks, 0);
     return n + 1;
 }
 
@@ -781,7 +783,7 @@ int launch_step(Solver &S, bool) {
     }
     n += assemble(S, 0, d.N > 0 && d.mixed);
     S.mark(NF_GROUP_END, true);
-    k_end<<<1, 256, 0, st>>>(d, nodal_grid(S), element_grid(S), contact_partial_blocks(), 1);
+    k_end<<<1, 256, 0, st>>>(d, nodal_grid(S), element_grid(S), d.coopBlocks, 1);
     n++;
     S.mark(NF_GROUP_END, false);
     return n;
@@ -796,7 +798,7 @@ int launch_advance(Solver &S) {
         n++;
     }
     n += assemble(S, 0);
-    k_end<<<1, 256, 0, S.stream>>>(d, nodal_grid(S), element_grid(S), contact_partial_blocks(), 0);
+    k_end<<<1, 256, 0, S.stream>>>(d, nodal_grid(S), element_grid(S), d.coopBlocks, 0);
     return n + 1;
 }
 

@@ -32,6 +32,7 @@ enum : uint32_t {
     STATUS_NONFINITE = 1u,       // a nodal velocity or displacement stopped being finite
     STATUS_GRID_HASHED = 2u,     // informational: the contact grid outgrew direct indexing
     STATUS_BUCKET_OVERFLOW = 4u, // a contact bucket exceeded the sort bound
+    STATUS_TIMEOUT = 8u,         // a grid barrier of the contact pass waited past its limit
 };
 
 struct DevScalars {
@@ -63,7 +64,8 @@ struct DevScalars {
     int hashed, pad2;
     int slotScanN, bucketScanN;              // live lengths of the per-step scans
     uint32_t status;
-    int pad3;
+    uint32_t barCount, barGen, barAbort;     // grid barrier of the cooperative contact pass
+    int incOverflow;                         // a node's incident terms outgrew its fixed list
 };
 
 struct Dev {
@@ -110,14 +112,17 @@ struct Dev {
     uint8_t *dropped;                        // [N]
     int32_t *bucketCount, *bucketStart, *bucketCursor;   // [bucketCap + 1]
     int32_t *bucketEntry;                    // [8E] entries (2 s + end)
+    double2 *bucketA, *bucketN;              // [8E] by position: the segment's first node, normal
     long long *bucketCell;                   // [8E] cell of each filed entry, by position
     long long *entryCell;                    // [8E] cell of each entry, by entry
     int bucketCap;
     // pair records, per surface slot
     int4 *pairNodes;                         // (n, a, b, valid)
+    double2 *slaveXY;                        // [N] current coordinates by surface slot
     double *pairVal;                         // [12 per slot]: role-major (n,a,b) x (normal r,z, tangent r,z)
     double *pairEnergy, *pairDiss;           // per slot
     int32_t *incCount, *incStart, *incCursor, *incEntry;   // per surface slot, entries (i<<2 | role)
+    int32_t *incSlots;                       // [NF_INC_CAP per surface slot] fixed lists
     // mixed precision: FP32 element state, float contributions, per-node float positions
     int mixed;
     MatF *matsF;
@@ -127,11 +132,30 @@ struct Dev {
     float4 *pMid, *pCur;
     float2 *vdt;
     double *gaussVol;                        // reference volume of each point
-    // scan workspace
+    // scan workspace; the cooperative contact pass's grid and its per-block scan sums
     int32_t *scanTmp;
     int scanTmpSize;
+    int coopBlocks;
+    int32_t *coopSums;
     DevScalars *s;
 };
+
+constexpr int NF_INC_CAP = 8;
+
+// Contact.begin, Contact.java:424-436: the per-step totals and extrema the contact pass
+// accumulates into; run by the step's first kernel, before the pass.
+__device__ inline void contact_step_reset(DevScalars *s) {
+    s->pairs = 0;
+    s->maxPenBits = 0ULL;
+    s->bbox[0] = ~0ULL;   // min r
+    s->bbox[1] = ~0ULL;   // min z
+    s->bbox[2] = 0ULL;    // max r
+    s->bbox[3] = 0ULL;    // max z
+    s->longestBits = 0ULL;
+    s->incOverflow = 0;
+    s->barCount = 0;      // a fresh grid barrier
+    s->barAbort = 0;
+}
 
 enum { PARTIAL_WALL = 0, PARTIAL_ERODE = 3, PARTIAL_CONTACT = 4, PARTIAL_SLOTS = 6 };
 
@@ -163,6 +187,7 @@ struct Solver {
     int graphKernels1 = 0, graphKernels16 = 0;
     Dev graphDev{};
     bool graphValid = false;
+    bool noGraphs = false;       // capture failed once: steps are enqueued directly
     // per-group event profiling
     bool profiling = false;
     struct Rec { int group; cudaEvent_t a, b; };
@@ -196,7 +221,7 @@ int launch_contact(Solver &S, bool predicated);
 // Launchers (k_scan.cu)
 int scan_exclusive(const int32_t *in, int32_t *out, int n, int32_t *totalOut, int32_t *tmp,
                    cudaStream_t stream, const int *pred, const int *nDev);
-int contact_partial_blocks();
+int contact_coop_blocks(int sms);
 size_t scan_tmp_ints(int n);
 
 int grid_for(long long n, int block);
