@@ -317,6 +317,84 @@ nf_status nf_material_point_update_static(const nf_material *material, int32_t f
                                           double strain_dt, const nf_damage_points *damage,
                                           double *dgamma);
 
+/* ------------------------------------------------------------------ batched scenes */
+
+/* Many independent scenes of one formulation, stepped together on one GPU. The reference runs
+ * such sweeps one ExplicitSolver per host thread (Sweep.over, app/Sweep.java:82-105, over the
+ * Taylor case TaylorImpactCase.run :214-258). Each instance is the sequence
+ *   new ExplicitSolver(mesh, material, formulation, REDUCED, kinematics, thickness, cfl)
+ *   setHourglassCoefficient(q); fixRadial/fixAxial(fixed nodes);
+ *   setRigidWall(RigidWall.atZ(plane, friction)) unless plane is NaN;
+ *   setUniformVelocity(vr, vz); then step while time < t_end,
+ * and its trajectory is bit-identical to that scene run alone through nf_create/nf_step in the
+ * same precision (NF_PRECISION_FP64 or NF_PRECISION_MIXED). Only reduced integration is
+ * batched. Instances may differ in mesh, material, wall, velocity, hourglass and t_end. */
+typedef struct nf_batch nf_batch;
+
+typedef struct {
+    int32_t instance_count;
+    const int32_t *node_offset;      /* [count + 1]: instance k owns nodes [k] .. [k + 1) */
+    const int32_t *element_offset;   /* [count + 1]: and elements [k] .. [k + 1) */
+    const double *r;                 /* [total nodes] reference coordinates */
+    const double *z;
+    const int32_t *conn;             /* [4 * total elements], node numbers local to the
+                                        instance, CCW */
+    const uint8_t *fixed;            /* [total nodes] bit 0 radial, bit 1 axial, or NULL */
+} nf_batch_mesh;
+
+typedef struct {
+    nf_material material;
+    double velocity_r, velocity_z;   /* setUniformVelocity */
+    double wall_plane;               /* RigidWall.atZ(plane, friction); NaN for no wall */
+    double wall_friction;
+    double hourglass;                /* setHourglassCoefficient */
+    double t_end;                    /* the run: step while time < t_end */
+} nf_batch_instance;
+
+/* A launch shape of the batched step; any valid shape gives the same trajectories. */
+typedef struct {
+    int32_t threads;                 /* threads per block: 128 or 256 */
+    int32_t stage_nodes;             /* mixed form: node geometry staged in shared memory */
+    int32_t blocks_per_sm;           /* resident blocks per SM (1 .. occupancy limit) */
+    int32_t chunk_steps;             /* steps an instance takes per launch */
+} nf_batch_config;
+
+/* Per-instance progress. */
+typedef struct {
+    double time;
+    double timestep;
+    int64_t steps;
+    uint32_t status;                 /* device status bits of the instance */
+    int32_t done;
+} nf_batch_progress;
+
+nf_status nf_batch_create(const nf_batch_mesh *mesh, const nf_batch_instance *instances,
+                          int32_t formulation, int32_t kinematics, double thickness,
+                          double cfl_safety, int32_t precision, nf_batch **out);
+nf_status nf_batch_destroy(nf_batch *b);
+const char *nf_batch_last_error(const nf_batch *b);
+/* Autotuner: times every valid shape on trial_steps steps of the whole batch (state saved and
+ * restored, so the trajectory is untouched), keeps the fastest and returns it. */
+nf_status nf_batch_tune(nf_batch *b, int32_t trial_steps, nf_batch_config *chosen);
+nf_status nf_batch_set_config(nf_batch *b, const nf_batch_config *config);
+nf_status nf_batch_get_config(nf_batch *b, nf_batch_config *config);
+/* Steps every instance until its time reaches t_end, or max_steps more steps. The chunked
+ * launches are replayed as a CUDA graph; returns when all instances are done. */
+nf_status nf_batch_run(nf_batch *b, int64_t max_steps);
+/* Device time of the last nf_batch_run, milliseconds. */
+nf_status nf_batch_elapsed(nf_batch *b, double *ms);
+nf_status nf_batch_launch_count(nf_batch *b, int64_t *launches);
+/* Fields over all instances, concatenated: node fields (NF_FIELD_UR .. NF_FIELD_MASS,
+ * NF_FIELD_WALL_STATE, NF_FIELD_FIXED), element fields (NF_FIELD_STRESS,
+ * NF_FIELD_BACK_STRESS, NF_FIELD_PLASTIC_STRAIN, NF_FIELD_PLASTIC_WORK, NF_FIELD_HOURGLASS_*)
+ * as doubles (the mixed form's FP32 state widened). */
+nf_status nf_batch_field_size(nf_batch *b, int32_t field, size_t *count, size_t *bytes);
+nf_status nf_batch_read(nf_batch *b, int32_t field, void *dst, size_t bytes);
+/* [instance_count] each. */
+nf_status nf_batch_state(nf_batch *b, nf_batch_progress *out);
+nf_status nf_batch_measure(nf_batch *b, nf_measure *out);
+nf_status nf_batch_wall_stats(nf_batch *b, nf_wall_info *out);
+
 #ifdef __cplusplus
 }
 #endif

@@ -94,6 +94,28 @@ class DamagePoints(C.Structure):
                 ("strength", c_double_p), ("softening", c_double_p), ("width", c_double_p)]
 
 
+class BatchMesh(C.Structure):
+    _fields_ = [("instance_count", C.c_int32), ("node_offset", c_int32_p),
+                ("element_offset", c_int32_p), ("r", c_double_p), ("z", c_double_p),
+                ("conn", c_int32_p), ("fixed", C.POINTER(C.c_uint8))]
+
+
+class BatchInstance(C.Structure):
+    _fields_ = [("material", MaterialC), ("velocity_r", C.c_double), ("velocity_z", C.c_double),
+                ("wall_plane", C.c_double), ("wall_friction", C.c_double),
+                ("hourglass", C.c_double), ("t_end", C.c_double)]
+
+
+class BatchConfig(C.Structure):
+    _fields_ = [("threads", C.c_int32), ("stage_nodes", C.c_int32),
+                ("blocks_per_sm", C.c_int32), ("chunk_steps", C.c_int32)]
+
+
+class BatchProgress(C.Structure):
+    _fields_ = [("time", C.c_double), ("timestep", C.c_double), ("steps", C.c_int64),
+                ("status", C.c_uint32), ("done", C.c_int32)]
+
+
 _H = C.c_void_p
 _S = C.c_int
 _PROTOS = {
@@ -140,6 +162,21 @@ _PROTOS = {
     "material_point_update": (_S, [C.POINTER(MaterialC), C.c_int32, C.c_int32, c_double_p,
                                    c_double_p, c_double_p, c_double_p, c_double_p, C.c_double,
                                    C.POINTER(DamagePoints), c_double_p]),
+    "batch_create": (_S, [C.POINTER(BatchMesh), C.POINTER(BatchInstance), C.c_int32, C.c_int32,
+                          C.c_double, C.c_double, C.c_int32, C.POINTER(C.c_void_p)]),
+    "batch_destroy": (_S, [_H]),
+    "batch_last_error": (C.c_char_p, [_H]),
+    "batch_tune": (_S, [_H, C.c_int32, C.POINTER(BatchConfig)]),
+    "batch_set_config": (_S, [_H, C.POINTER(BatchConfig)]),
+    "batch_get_config": (_S, [_H, C.POINTER(BatchConfig)]),
+    "batch_run": (_S, [_H, C.c_int64]),
+    "batch_elapsed": (_S, [_H, C.POINTER(C.c_double)]),
+    "batch_launch_count": (_S, [_H, C.POINTER(C.c_int64)]),
+    "batch_field_size": (_S, [_H, C.c_int32, C.POINTER(C.c_size_t), C.POINTER(C.c_size_t)]),
+    "batch_read": (_S, [_H, C.c_int32, C.c_void_p, C.c_size_t]),
+    "batch_state": (_S, [_H, C.POINTER(BatchProgress)]),
+    "batch_measure": (_S, [_H, C.POINTER(Measure)]),
+    "batch_wall_stats": (_S, [_H, C.POINTER(WallInfo)]),
 }
 
 ENTRY_POINTS = tuple("nf_" + name for name in _PROTOS)

@@ -185,6 +185,86 @@ nf_status ensure_mixed_damage(Solver &S) {
     return NF_OK;
 }
 
+// lumpMass, ExplicitSolver.java:1559-1597: 2x2 Gauss lumping, in the reference's order.
+// emat may be NULL (every element material 0).
+void lumped_mass(const double *r, const double *z, const int32_t *conn, int E,
+                 const nf_material *materials, const int32_t *emat, bool axi, double thickness,
+                 double *mass) {
+    const double G = 0.5773502691896258;
+    const double gx[4] = {-G, G, G, -G}, ge[4] = {-G, -G, G, G};
+    for (int e = 0; e < E; e++) {
+        const double rho = materials[emat ? emat[e] : 0].density;
+        const int b = e * 4;
+        const int n0 = conn[b], n1 = conn[b + 1], n2 = conn[b + 2], n3 = conn[b + 3];
+        const double r0 = r[n0], r1 = r[n1], r2 = r[n2], r3 = r[n3];
+        const double z0 = z[n0], z1 = z[n1], z2 = z[n2], z3 = z[n3];
+        for (int g = 0; g < 4; g++) {
+            const double xi = gx[g], eta = ge[g];
+            const double xm = 1.0 - xi, xp = 1.0 + xi;
+            const double em = 1.0 - eta, ep = 1.0 + eta;
+            const double N0 = 0.25 * xm * em, N1 = 0.25 * xp * em;
+            const double N2 = 0.25 * xp * ep, N3 = 0.25 * xm * ep;
+            const double dN0x = -0.25 * em, dN1x = 0.25 * em, dN2x = 0.25 * ep, dN3x = -0.25 * ep;
+            const double dN0e = -0.25 * xm, dN1e = -0.25 * xp, dN2e = 0.25 * xp, dN3e = 0.25 * xm;
+            const double J00 = dN0x * r0 + dN1x * r1 + dN2x * r2 + dN3x * r3;
+            const double J01 = dN0x * z0 + dN1x * z1 + dN2x * z2 + dN3x * z3;
+            const double J10 = dN0e * r0 + dN1e * r1 + dN2e * r2 + dN3e * r3;
+            const double J11 = dN0e * z0 + dN1e * z1 + dN2e * z2 + dN3e * z3;
+            const double det = J00 * J11 - J01 * J10;
+            const double rg = N0 * r0 + N1 * r1 + N2 * r2 + N3 * r3;
+            const double dV = axi ? 2.0 * NF_PI * rg * det : thickness * det;
+            mass[n0] += rho * N0 * dV;
+            mass[n1] += rho * N1 * dV;
+            mass[n2] += rho * N2 * dV;
+            mass[n3] += rho * N3 * dV;
+        }
+    }
+}
+
+// buildNodeSlots, ExplicitSolver.java:347-366: per node its sources (element 8 e + corner,
+// then pressure-edge slots) in ascending order. slotStart has N + 1 entries, zeroed.
+void node_slots(const int32_t *conn, int N, int E, const int32_t *pedges, int K,
+                int32_t *slotStart, int32_t *slots) {
+    for (long long k = 0; k < 4LL * E; k++) slotStart[conn[k] + 1]++;
+    for (long long k = 0; k < 2LL * K; k++) slotStart[pedges[k] + 1]++;
+    for (int i = 0; i < N; i++) slotStart[i + 1] += slotStart[i];
+    std::vector<int32_t> cursor(slotStart, slotStart + N + 1);
+    for (int e = 0; e < E; e++)
+        for (int c = 0; c < 4; c++) slots[cursor[conn[e * 4 + c]]++] = e * 8 + c;
+    for (int k = 0; k < 2 * K; k += 2) {
+        const int slot = (E + k / 2) * 8;
+        slots[cursor[pedges[k]]++] = slot;
+        slots[cursor[pedges[k + 1]]++] = slot + 1;
+    }
+}
+
+// QuadMesh.minimumEdgeLength: the shortest element edge of the reference configuration.
+double min_edge_length(const double *r, const double *z, const int32_t *conn, int E) {
+    double edge = DBL_MAX;
+    for (int e = 0; e < E; e++)
+        for (int k = 0; k < 4; k++) {
+            const int i = conn[e * 4 + k], j = conn[e * 4 + (k + 1) % 4];
+            const double dr = r[j] - r[i], dz = z[j] - z[i];
+            const double len = sqrt(dr * dr + dz * dz);
+            if (len < edge) edge = len;
+        }
+    return edge;
+}
+
+// The FP32 copy of a material's constants (the mixed form).
+MatF mat_float(const MatDev &a) {
+    MatF o{};
+    o.lambda = (float)a.lambda; o.mu = (float)a.mu; o.bulk = (float)a.bulk;
+    o.density = (float)a.density; o.youngs = (float)a.youngs;
+    o.sy0 = (float)a.sy0; o.hIso = (float)a.hIso; o.hKin = (float)a.hKin;
+    o.a = (float)a.a; o.b = (float)a.b; o.n = (float)a.n; o.c = (float)a.c;
+    o.m = (float)a.m; o.refRate = (float)a.refRate; o.room = (float)a.room;
+    o.melt = (float)a.melt; o.cp = (float)a.cp; o.tq = (float)a.tq;
+    o.thermalCoefficient = (float)a.thermalCoefficient;
+    o.jc = a.jc;
+    return o;
+}
+
 // In mixed precision the FP64 element arrays are a staging copy: brought up to date before
 // anything reads them (audits, field reads).
 void mixed_to_double(Solver &S) {
@@ -294,65 +374,15 @@ nf_status nf_create(const nf_mesh *mesh, const nf_material *materials, int32_t m
 
     // lumped mass, ExplicitSolver.java:1559-1597
     std::vector<double> mass(N, 0.0);
-    {
-        const double G = 0.5773502691896258;
-        const double gx[4] = {-G, G, G, -G}, ge[4] = {-G, -G, G, G};
-        const double *r = mesh->r, *z = mesh->z;
-        const int32_t *conn = mesh->conn;
-        for (int e = 0; e < E; e++) {
-            const double rho = materials[S->emat[e]].density;
-            const int b = e * 4;
-            const int n0 = conn[b], n1 = conn[b + 1], n2 = conn[b + 2], n3 = conn[b + 3];
-            const double r0 = r[n0], r1 = r[n1], r2 = r[n2], r3 = r[n3];
-            const double z0 = z[n0], z1 = z[n1], z2 = z[n2], z3 = z[n3];
-            for (int g = 0; g < 4; g++) {
-                const double xi = gx[g], eta = ge[g];
-                const double xm = 1.0 - xi, xp = 1.0 + xi;
-                const double em = 1.0 - eta, ep = 1.0 + eta;
-                const double N0 = 0.25 * xm * em, N1 = 0.25 * xp * em;
-                const double N2 = 0.25 * xp * ep, N3 = 0.25 * xm * ep;
-                const double dN0x = -0.25 * em, dN1x = 0.25 * em, dN2x = 0.25 * ep, dN3x = -0.25 * ep;
-                const double dN0e = -0.25 * xm, dN1e = -0.25 * xp, dN2e = 0.25 * xp, dN3e = 0.25 * xm;
-                const double J00 = dN0x * r0 + dN1x * r1 + dN2x * r2 + dN3x * r3;
-                const double J01 = dN0x * z0 + dN1x * z1 + dN2x * z2 + dN3x * z3;
-                const double J10 = dN0e * r0 + dN1e * r1 + dN2e * r2 + dN3e * r3;
-                const double J11 = dN0e * z0 + dN1e * z1 + dN2e * z2 + dN3e * z3;
-                const double det = J00 * J11 - J01 * J10;
-                const double rg = N0 * r0 + N1 * r1 + N2 * r2 + N3 * r3;
-                const double dV = d.axi ? 2.0 * NF_PI * rg * det : thickness * det;
-                mass[n0] += rho * N0 * dV;
-                mass[n1] += rho * N1 * dV;
-                mass[n2] += rho * N2 * dV;
-                mass[n3] += rho * N3 * dV;
-            }
-        }
-    }
+    lumped_mass(mesh->r, mesh->z, mesh->conn, E, materials, S->emat.data(), d.axi != 0, thickness,
+                mass.data());
 
     // node slots, ExplicitSolver.java:347-366
     std::vector<int32_t> slotStart(N + 1, 0), slots(4LL * E + 2LL * K);
-    for (long long k = 0; k < 4LL * E; k++) slotStart[mesh->conn[k] + 1]++;
-    for (long long k = 0; k < 2LL * K; k++) slotStart[mesh->pressure_edges[k] + 1]++;
-    for (int i = 0; i < N; i++) slotStart[i + 1] += slotStart[i];
-    {
-        std::vector<int32_t> cursor(slotStart);
-        for (int e = 0; e < E; e++)
-            for (int c = 0; c < 4; c++) slots[cursor[mesh->conn[e * 4 + c]]++] = e * 8 + c;
-        for (int k = 0; k < 2 * K; k += 2) {
-            const int slot = (E + k / 2) * 8;
-            slots[cursor[mesh->pressure_edges[k]]++] = slot;
-            slots[cursor[mesh->pressure_edges[k + 1]]++] = slot + 1;
-        }
-    }
+    node_slots(mesh->conn, N, E, mesh->pressure_edges, K, slotStart.data(), slots.data());
 
     // initial step, QuadMesh.minimumEdgeLength + ExplicitSolver.java:333-338
-    double edge = DBL_MAX;
-    for (int e = 0; e < E; e++)
-        for (int k = 0; k < 4; k++) {
-            const int i = mesh->conn[e * 4 + k], j = mesh->conn[e * 4 + (k + 1) % 4];
-            const double dr = mesh->r[j] - mesh->r[i], dz = mesh->z[j] - mesh->z[i];
-            const double len = sqrt(dr * dr + dz * dz);
-            if (len < edge) edge = len;
-        }
+    const double edge = min_edge_length(mesh->r, mesh->z, mesh->conn, E);
     DevScalars s0{};
     s0.minEdgeSquared = edge * edge;
     s0.dt = cfl_safety * edge / d.fastestWave;
@@ -911,18 +941,8 @@ nf_status nf_set_precision(nf_solver *h, int32_t precision) {
             if (e_ != cudaSuccess)
                 return fail(&S, NF_ENOMEM, "mixed-precision allocation failed: %s", cudaGetErrorString(e_));
             std::vector<MatF> mf(S.materials.size());
-            for (size_t m = 0; m < S.materials.size(); m++) {
-                const MatDev a = mat_dev(S.materials[m], S.formulation);
-                MatF &o = mf[m];
-                o.lambda = (float)a.lambda; o.mu = (float)a.mu; o.bulk = (float)a.bulk;
-                o.density = (float)a.density; o.youngs = (float)a.youngs;
-                o.sy0 = (float)a.sy0; o.hIso = (float)a.hIso; o.hKin = (float)a.hKin;
-                o.a = (float)a.a; o.b = (float)a.b; o.n = (float)a.n; o.c = (float)a.c;
-                o.m = (float)a.m; o.refRate = (float)a.refRate; o.room = (float)a.room;
-                o.melt = (float)a.melt; o.cp = (float)a.cp; o.tq = (float)a.tq;
-                o.thermalCoefficient = (float)a.thermalCoefficient;
-                o.jc = a.jc;
-            }
+            for (size_t m = 0; m < S.materials.size(); m++)
+                mf[m] = mat_float(mat_dev(S.materials[m], S.formulation));
             CK(&S, upload(S, d.matsF, mf.data(), mf.size()));
             launch_point_volumes(S, d.gaussVol);
         }
@@ -1249,4 +1269,22 @@ namespace nf {
 const char *validate_material(const nf_material &m) { return material_invalid(m); }
 MatDev material_constants(const nf_material &m, int formulation) { return mat_dev(m, formulation); }
 void set_thread_error(const char *message) { g_err = message; }
+// Set-up helpers shared with the batched handle (api_batch.cu).
+double material_wave(const nf_material &m) { return mat_wave(m); }
+MatF material_constants_f32(const MatDev &m) { return mat_float(m); }
+double element_signed_area(const double *r, const double *z, const int32_t *conn, int e) {
+    return signed_area(r, z, conn, e);
+}
+void setup_lumped_mass(const double *r, const double *z, const int32_t *conn, int E,
+                       const nf_material *materials, const int32_t *emat, bool axi,
+                       double thickness, double *mass) {
+    lumped_mass(r, z, conn, E, materials, emat, axi, thickness, mass);
+}
+void setup_node_slots(const int32_t *conn, int N, int E, const int32_t *pedges, int K,
+                      int32_t *slotStart, int32_t *slots) {
+    node_slots(conn, N, E, pedges, K, slotStart, slots);
+}
+double setup_min_edge(const double *r, const double *z, const int32_t *conn, int E) {
+    return min_edge_length(r, z, conn, E);
+}
 }  // namespace nf

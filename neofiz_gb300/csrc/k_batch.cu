@@ -1,0 +1,323 @@
+// k_batch.cu -- many independent scenes (a parameter sweep: the reference runs one solver per
+// thread through Sweep.over, src/main/java/org/neofiz/app/Sweep.java:82-105) stepped by one
+// persistent kernel.
+//
+// One block owns one instance at a time and runs its whole step with block barriers between
+// the phases: nodal update, element assembly with the block's exact minimum edge, the
+// per-node gather, the next CFL step. Blocks take instances from a queue (most expensive
+// first), each for a chunk of steps, so uneven meshes and uneven step counts balance. Every
+// phase calls the same per-node and per-element bodies as the single-scene kernels
+// (nf_bodies.cuh), in the same order per node and per element, so an instance's trajectory is
+// bit-identical to the same scene run alone in the same precision. The audit totals (wall
+// impulse, energy loss, friction work) are summed per block in a fixed order: deterministic
+// for a given launch shape, but not in the single-scene kernels' association.
+//
+// Launch shape: block size (128, 256), whether the mixed form stages each instance's float
+// node geometry in shared memory, blocks per SM and the chunk length are chosen by the
+// autotuner (api_batch.cu); none of them changes the trajectory.
+#include "nf_bodies.cuh"
+
+namespace nf {
+
+constexpr int MEASURE_BLOCK = 256;
+
+__device__ __forceinline__ unsigned long long bbits(double x) {
+    return (unsigned long long)__double_as_longlong(x);
+}
+__device__ __forceinline__ double bdouble(unsigned long long u) {
+    return __longlong_as_double((long long)u);
+}
+
+// Exact block minimum of the per-thread shortest squared edges, returned to every thread. The
+// warps combine with jmin and the warps' results by the integer order of their bits, as the
+// single-scene kernels do with shuffles and atomicMin.
+template <int T>
+__device__ double block_min_edge(double v, double *sh) {
+    for (int o = 16; o > 0; o >>= 1) v = jmin(v, __shfl_down_sync(0xffffffffu, v, o));
+    const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
+    if (lane == 0) sh[warp] = v;
+    __syncthreads();
+    if (threadIdx.x == 0) {
+        unsigned long long m = bbits(sh[0]);
+        for (int w = 1; w < T / 32; w++) m = min(m, bbits(sh[w]));
+        sh[T / 32] = bdouble(m);
+    }
+    __syncthreads();
+    return sh[T / 32];
+}
+
+template <int T>
+__device__ double block_min_edge_f(float v, double *sh) {
+    for (int o = 16; o > 0; o >>= 1) v = fminf(v, __shfl_down_sync(0xffffffffu, v, o));
+    return block_min_edge<T>((double)v, sh);
+}
+
+// Fixed-tree block sum; valid in thread 0.
+template <int T>
+__device__ double block_total(double v, double *sh) {
+    for (int o = 16; o > 0; o >>= 1) v += __shfl_down_sync(0xffffffffu, v, o);
+    const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
+    __syncthreads();
+    if (lane == 0) sh[warp] = v;
+    __syncthreads();
+    double t = 0.0;
+    if (threadIdx.x == 0)
+        for (int w = 0; w < T / 32; w++) t += sh[w];
+    __syncthreads();
+    return t;
+}
+
+// Up to `chunk` steps of instance k by the whole block: ExplicitSolver.step, :940-991, with the
+// loop condition of TaylorImpactCase.java:250-253 (step while time < t_end).
+template <bool MIXED, bool STAGE, int T>
+__device__ void run_instance(const Dev &d, const BatchDev &b, int k, int chunk, float4 *sPMid,
+                             float2 *sVdt, double *shMin, int (*wallCount)[2]) {
+    const BatchInst in = b.inst[k];
+    BatchScalars *scp = b.sc + k;
+    if (scp->done) return;
+    const int tid = threadIdx.x;
+    double dt = scp->dt, dtPrev = scp->dtPrevious, time = scp->time;
+    double minEdge = scp->minEdgeSquared;
+    long long steps = scp->steps;
+    const long long limit = scp->stepLimit;
+    double impulse = 0.0, loss = 0.0, fric = 0.0;
+    if (tid == 0) {
+        wallCount[0][0] = wallCount[0][1] = 0;
+        wallCount[1][0] = wallCount[1][1] = 0;
+    }
+    __syncthreads();
+    float4 *pMid = STAGE ? sPMid : d.pMid;
+    float2 *vdt = STAGE ? sVdt : d.vdt;
+    const int base = STAGE ? in.n0 : 0;
+    const MixedGeo geo = MIXED ? MixedGeo{pMid, nullptr, vdt, -base}
+                               : MixedGeo{nullptr, nullptr, nullptr, 0};
+    int taken = 0;
+    for (; taken < chunk; taken++) {
+        if (!(time < in.tEnd) || steps >= limit) break;
+        // RigidWall.beginStep: this step's counts go to buffer `par`; the other is cleared for
+        // the next step (its last users passed this step's first barrier already)
+        const int par = taken & 1;
+        if (tid == 0) {
+            wallCount[par ^ 1][0] = 0;
+            wallCount[par ^ 1][1] = 0;
+        }
+        const double dtAvg = 0.5 * (dtPrev + dt);                   // :947-956
+        const double half = 0.5 * in.damping * dtAvg;
+        const NodalCoef co{(1.0 - half) / (1.0 + half), dtAvg / (1.0 + half), dtAvg, dt};
+        const WallRef w{in.hasWall, in.wallPlane, in.wallFriction, &wallCount[par][0],
+                        &wallCount[par][1]};
+        for (int i = in.n0 + tid; i < in.n1; i += T)
+            nodal_node(d, i, co, w, geo, &scp->status, impulse, loss, fric);
+        __syncthreads();
+        time += dt;                                                   // :973-974
+        steps += 1;
+        double me;
+        if (MIXED) {
+            float m = 3.4028235e38f;
+            const float sdt = (float)dt, qhg = (float)in.hourglass;
+            for (int e = in.e0 + tid; e < in.e1; e += T)
+                element_reduced_f32(d, e, sdt, qhg, pMid, vdt, base, m);
+            me = block_min_edge_f<T>(m, shMin);
+        } else {
+            double m = DMAX;
+            for (int e = in.e0 + tid; e < in.e1; e += T) element_reduced(d, e, dt, in.hourglass, m);
+            me = block_min_edge<T>(m, shMin);
+        }
+        // the gather keeps the nodal loop's node-to-thread map, so the next nodal update reads
+        // only forces its own thread wrote
+        for (int i = in.n0 + tid; i < in.n1; i += T)
+            d.F[i] = MIXED ? gather_node_f32(d, i) : gather_node(d, i);
+        minEdge = me;                                                 // :985-990
+        if (d.finite) {
+            dtPrev = dt;
+            dt = in.cfl * sqrt(me * in.massScale) / in.wave;
+        }
+    }
+    const double ti = block_total<T>(impulse, shMin);
+    const double tl = block_total<T>(loss, shMin);
+    const double tf = block_total<T>(fric, shMin);
+    if (tid == 0) {
+        scp->dt = dt;
+        scp->dtPrevious = dtPrev;
+        scp->time = time;
+        scp->steps = steps;
+        scp->minEdgeSquared = minEdge;
+        if (taken > 0) {
+            scp->wContact = wallCount[(taken - 1) & 1][0];
+            scp->wStuck = wallCount[(taken - 1) & 1][1];
+        }
+        scp->wImpulse += ti;
+        scp->wEnergyLoss += tl;
+        scp->wFriction += tf;
+        if (!(time < in.tEnd) || steps >= limit) {
+            scp->done = 1;
+            atomicSub(b.remaining, 1);
+        }
+    }
+    __syncthreads();
+}
+
+template <bool MIXED, bool STAGE, int T>
+__global__ void __launch_bounds__(T) k_batch_steps(Dev d, BatchDev b, int chunk) {
+    extern __shared__ __align__(16) unsigned char dyn[];
+    __shared__ double shMin[T / 32 + 1];
+    __shared__ int wallCount[2][2];
+    __shared__ int next;
+    float4 *sPMid = reinterpret_cast<float4 *>(dyn);
+    float2 *sVdt = reinterpret_cast<float2 *>(dyn + sizeof(float4) * (size_t)b.maxNodes);
+    for (;;) {
+        if (threadIdx.x == 0) next = atomicAdd(b.queue, 1);
+        __syncthreads();
+        const int q = next;
+        __syncthreads();
+        if (q >= b.count) return;
+        run_instance<MIXED, STAGE, T>(d, b, b.order[q], chunk, sPMid, sVdt, shMin, wallCount);
+    }
+}
+
+// The first assembly of every instance (zero strain increment), in the batch's precision, as
+// the single-scene path runs it before its first step; records the shortest edge.
+template <bool MIXED>
+__global__ void __launch_bounds__(256) k_batch_initial(Dev d, BatchDev b) {
+    __shared__ double shMin[256 / 32 + 1];
+    const BatchInst in = b.inst[blockIdx.x];
+    double me;
+    if (MIXED) {
+        for (int i = in.n0 + threadIdx.x; i < in.n1; i += 256)
+            prepare_node(d, i, 0.0, MixedGeo{d.pMid, nullptr, d.vdt, 0});
+        __syncthreads();
+        float m = 3.4028235e38f;
+        for (int e = in.e0 + threadIdx.x; e < in.e1; e += 256)
+            element_reduced_f32(d, e, 0.0f, (float)in.hourglass, d.pMid, d.vdt, 0, m);
+        me = block_min_edge_f<256>(m, shMin);
+    } else {
+        double m = DMAX;
+        for (int e = in.e0 + threadIdx.x; e < in.e1; e += 256)
+            element_reduced(d, e, 0.0, in.hourglass, m);
+        me = block_min_edge<256>(m, shMin);
+    }
+    for (int i = in.n0 + threadIdx.x; i < in.n1; i += 256)
+        d.F[i] = MIXED ? gather_node_f32(d, i) : gather_node(d, i);
+    if (threadIdx.x == 0) b.sc[blockIdx.x].minEdgeSquared = me;
+}
+
+// Arms a run: every instance may take maxSteps more steps; counts the instances left to run.
+__global__ void k_batch_arm(BatchDev b, long long maxSteps) {
+    const int k = blockIdx.x * blockDim.x + threadIdx.x;
+    if (k == 0) *b.queue = 0;
+    if (k >= b.count) return;
+    BatchScalars &s = b.sc[k];
+    s.stepLimit = s.steps + maxSteps;
+    const bool done = !(s.time < b.inst[k].tEnd) || maxSteps <= 0;
+    s.done = done ? 1 : 0;
+    if (!done) atomicAdd(b.remaining, 1);
+}
+
+// TaylorImpactCase.java:272-288 per instance: max z, min z, max r of the current
+// configuration, as order-preserving integer images (exact in any order).
+__device__ __forceinline__ unsigned long long okey_b(double v) {
+    const unsigned long long u = bbits(v);
+    return (u >> 63) ? ~u : (u | 0x8000000000000000ULL);
+}
+
+__global__ void __launch_bounds__(MEASURE_BLOCK) k_batch_measure(Dev d, BatchDev b) {
+    __shared__ unsigned long long sh[3][MEASURE_BLOCK / 32];
+    const BatchInst in = b.inst[blockIdx.x];
+    unsigned long long zmax = 0ULL, zmin = ~0ULL, rmax = 0ULL;
+    for (int i = in.n0 + threadIdx.x; i < in.n1; i += MEASURE_BLOCK) {
+        const double2 x = d.X0[i], u = d.U[i];
+        const unsigned long long kz = okey_b(x.y + u.y), kr = okey_b(x.x + u.x);
+        zmax = max(zmax, kz);
+        zmin = min(zmin, kz);
+        rmax = max(rmax, kr);
+    }
+    for (int o = 16; o > 0; o >>= 1) {
+        zmax = max(zmax, __shfl_down_sync(0xffffffffu, zmax, o));
+        zmin = min(zmin, __shfl_down_sync(0xffffffffu, zmin, o));
+        rmax = max(rmax, __shfl_down_sync(0xffffffffu, rmax, o));
+    }
+    const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
+    if (lane == 0) {
+        sh[0][warp] = zmax;
+        sh[1][warp] = zmin;
+        sh[2][warp] = rmax;
+    }
+    __syncthreads();
+    if (threadIdx.x == 0) {
+        for (int w = 1; w < MEASURE_BLOCK / 32; w++) {
+            zmax = max(zmax, sh[0][w]);
+            zmin = min(zmin, sh[1][w]);
+            rmax = max(rmax, sh[2][w]);
+        }
+        b.measure[3 * blockIdx.x + 0] = zmax;
+        b.measure[3 * blockIdx.x + 1] = zmin;
+        b.measure[3 * blockIdx.x + 2] = rmax;
+    }
+}
+
+// ------------------------------------------------------------------------------------ launch
+
+template <bool MIXED, bool STAGE, int T>
+static const void *steps_kernel() {
+    return (const void *)k_batch_steps<MIXED, STAGE, T>;
+}
+
+static const void *select_kernel(bool mixed, const BatchShape &s) {
+    if (mixed) {
+        if (s.stage) return s.threads == 128 ? steps_kernel<true, true, 128>() : steps_kernel<true, true, 256>();
+        return s.threads == 128 ? steps_kernel<true, false, 128>() : steps_kernel<true, false, 256>();
+    }
+    return s.threads == 128 ? steps_kernel<false, false, 128>() : steps_kernel<false, false, 256>();
+}
+
+size_t batch_shared_bytes(bool mixed, const BatchShape &s, int maxNodes) {
+    return mixed && s.stage ? (sizeof(float4) + sizeof(float2)) * (size_t)maxNodes : 0;
+}
+
+// Resident blocks per SM of a shape (0 when it cannot launch, e.g. too much shared memory).
+int batch_max_blocks_per_sm(bool mixed, const BatchShape &s, int maxNodes) {
+    const void *k = select_kernel(mixed, s);
+    const size_t smem = batch_shared_bytes(mixed, s, maxNodes);
+    if (smem > 48 * 1024 &&
+        cudaFuncSetAttribute(k, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem) != cudaSuccess) {
+        (void)cudaGetLastError();
+        return 0;
+    }
+    int n = 0;
+    if (cudaOccupancyMaxActiveBlocksPerMultiprocessor(&n, k, s.threads, smem) != cudaSuccess) {
+        (void)cudaGetLastError();
+        return 0;
+    }
+    return n;
+}
+
+cudaError_t launch_batch_steps(const Dev &d, const BatchDev &b, bool mixed, const BatchShape &s,
+                               int sms, cudaStream_t st) {
+    const void *k = select_kernel(mixed, s);
+    const size_t smem = batch_shared_bytes(mixed, s, b.maxNodes);
+    int blocks = sms * s.blocksPerSm;
+    if (blocks > b.count) blocks = b.count;
+    if (blocks < 1) blocks = 1;
+    Dev dd = d;
+    BatchDev bb = b;
+    int chunk = s.chunk;
+    void *args[] = {&dd, &bb, &chunk};
+    return cudaLaunchKernel(k, dim3(blocks), dim3(s.threads), args, smem, st);
+}
+
+void launch_batch_initial(const Dev &d, const BatchDev &b, bool mixed, cudaStream_t st) {
+    if (b.count <= 0) return;
+    if (mixed) k_batch_initial<true><<<b.count, 256, 0, st>>>(d, b);
+    else k_batch_initial<false><<<b.count, 256, 0, st>>>(d, b);
+}
+
+void launch_batch_arm(const BatchDev &b, long long maxSteps, cudaStream_t st) {
+    cudaMemsetAsync(b.remaining, 0, sizeof(int32_t), st);
+    k_batch_arm<<<grid_for(b.count > 0 ? b.count : 1, 256), 256, 0, st>>>(b, maxSteps);
+}
+
+void launch_batch_measure(const Dev &d, const BatchDev &b, cudaStream_t st) {
+    if (b.count > 0) k_batch_measure<<<b.count, MEASURE_BLOCK, 0, st>>>(d, b);
+}
+
+}  // namespace nf

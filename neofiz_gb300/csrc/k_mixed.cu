@@ -11,7 +11,7 @@
 // (ExplicitSolver.java:1373-1504) and fullIntegration (:1219-1339) in float on those
 // relative coordinates (B and strains are translation invariant; the axisymmetric radius is
 // formed from the hi parts).
-#include "nf_internal.h"
+#include "nf_bodies.cuh"
 
 namespace nf {
 
@@ -27,27 +27,7 @@ __global__ void k_prepare_mixed(Dev d, int zeroStrain) {
     if (!d.s->active) return;
     const int i = blockIdx.x * blockDim.x + threadIdx.x;
     if (i >= d.N) return;
-    const double sdt = zeroStrain ? 0.0 : d.s->dt;
-    const double mid = -0.5 * sdt;
-    const double2 x = d.X0[i], u = d.U[i], v = d.V[i];
-    double pr, pz;
-    if (d.finite) {
-        pr = x.x + u.x + mid * v.x;
-        pz = x.y + u.y + mid * v.y;
-    } else {
-        pr = x.x;
-        pz = x.y;
-    }
-    const double cr = x.x + u.x, cz = x.y + u.y;
-    const float prh = (float)pr, pzh = (float)pz, crh = (float)cr, czh = (float)cz;
-    d.pMid[i] = make_float4(prh, (float)(pr - (double)prh), pzh, (float)(pz - (double)pzh));
-    d.pCur[i] = make_float4(crh, (float)(cr - (double)crh), czh, (float)(cz - (double)czh));
-    d.vdt[i] = make_float2((float)(v.x * sdt), (float)(v.y * sdt));
-}
-
-__device__ __forceinline__ float diff_hl(float4 a, float4 b, int comp) {
-    // (a - b) for component comp (0: r, 1: z) of two hi/lo pairs
-    return comp == 0 ? (a.x - b.x) + (a.y - b.y) : (a.z - b.z) + (a.w - b.w);
+    prepare_node(d, i, zeroStrain ? 0.0 : d.s->dt, MixedGeo{d.pMid, d.pCur, d.vdt, 0});
 }
 
 // Element damage (mean over points) and signed current area, FP32 (:663-691).
@@ -112,137 +92,14 @@ __device__ __forceinline__ void min_edge_commit_f(Dev &d, float minEdge) {
     if ((threadIdx.x & 31) == 0) atomicMin(&d.s->minEdgeBits, dbits_m((double)minEdge));
 }
 
-// One point's update in FP32; shared by the reduced and full kernels.
-__device__ __forceinline__ void point_update_mixed(const Dev &d, int e, int p, const MatF &fl,
-                                                   float dEpsR, float dEpsZ, float dEpsT,
-                                                   float dGamRZ, float spinDt, float strainDt,
-                                                   float *sg) {
-    float bk[4];
-    {
-        const float4 s = reinterpret_cast<const float4 *>(d.sigF)[p];
-        const float4 b = reinterpret_cast<const float4 *>(d.backF)[p];
-        sg[0] = s.x; sg[1] = s.y; sg[2] = s.z; sg[3] = s.w;
-        bk[0] = b.x; bk[1] = b.y; bk[2] = b.z; bk[3] = b.w;
-    }
-    if (d.finite && spinDt != 0.0f) {
-        const float cs = corot_cos(spinDt), sn = corot_sin(spinDt);
-        corot_rotate(sg, cs, sn);
-        corot_rotate(bk, cs, sn);
-    }
-    float epsP = d.epsPF[p], work = d.wPF[p];
-    if (d.hasDamage) {
-        DamageRefT<float> dr;
-        dr.failureStrain = d.dFailF[e];
-        dr.strength = d.dStrF + p;
-        dr.softening = d.dSoftF + p;
-        dr.width = d.dWidthF + p;
-        dr.geometry = d.dGeomF + 5 * (size_t)e;
-        dr.fractureEnergy = d.dGfF[e];
-        dr.youngs = fl.youngs;
-        j2_update(sg, bk, epsP, work, dEpsR, dEpsZ, dEpsT, dGamRZ, fl.lambda, fl.mu, fl,
-                  strainDt, &dr, d.dStrF[p], d.dSoftF[p]);
-    } else {
-        j2_update(sg, bk, epsP, work, dEpsR, dEpsZ, dEpsT, dGamRZ, fl.lambda, fl.mu, fl,
-                  strainDt, (const DamageRefT<float> *)nullptr, 0.0f, 0.0f);
-    }
-    reinterpret_cast<float4 *>(d.sigF)[p] = make_float4(sg[0], sg[1], sg[2], sg[3]);
-    reinterpret_cast<float4 *>(d.backF)[p] = make_float4(bk[0], bk[1], bk[2], bk[3]);
-    d.epsPF[p] = epsP;
-    d.wPF[p] = work;
-}
-
 // reducedIntegration (ExplicitSolver.java:1373-1504) in FP32.
 __global__ void __launch_bounds__(MB) k_element_reduced_mixed(Dev d, int zeroStrain) {
     if (!d.s->active) return;
     const int e = blockIdx.x * blockDim.x + threadIdx.x;
     float minEdge = 3.4028235e38f;
     if (e < d.E) {
-        float4 *ef = reinterpret_cast<float4 *>(d.contribF + 8 * (size_t)e);
-        if (d.gone != nullptr && d.gone[e]) {
-            ef[0] = make_float4(0.f, 0.f, 0.f, 0.f);
-            ef[1] = make_float4(0.f, 0.f, 0.f, 0.f);
-        } else {
-            const float strainDt = zeroStrain ? 0.0f : (float)d.s->dt;
-            const MatF &fl = d.matsF[d.emat[e]];
-            const float mu = fl.mu;
-            const int4 c = d.conn[e];
-            const float4 p0 = d.pMid[c.x], p1 = d.pMid[c.y], p2 = d.pMid[c.z], p3 = d.pMid[c.w];
-            const float2 w0 = d.vdt[c.x], w1 = d.vdt[c.y], w2 = d.vdt[c.z], w3 = d.vdt[c.w];
-            const float r0 = 0.0f, z0 = 0.0f;
-            const float r1 = diff_hl(p1, p0, 0), r2 = diff_hl(p2, p0, 0), r3 = diff_hl(p3, p0, 0);
-            const float z1 = diff_hl(p1, p0, 1), z2 = diff_hl(p2, p0, 1), z3 = diff_hl(p3, p0, 1);
-            const float a0 = w0.x, a1 = w1.x, a2 = w2.x, a3 = w3.x;
-            const float c0 = w0.y, c1 = w1.y, c2 = w2.y, c3 = w3.y;
-            if (d.finite) minEdge = shortestEdge(minEdge, r0, r1, r2, r3, z0, z1, z2, z3);
-
-            const float J00 = 0.25f * (-r0 + r1 + r2 - r3);
-            const float J01 = 0.25f * (-z0 + z1 + z2 - z3);
-            const float J10 = 0.25f * (-r0 - r1 + r2 + r3);
-            const float J11 = 0.25f * (-z0 - z1 + z2 + z3);
-            const float det = J00 * J11 - J01 * J10;
-            const float inv = 1.0f / det;
-            const float d0r = 0.25f * (J01 - J11) * inv;
-            const float d1r = 0.25f * (J01 + J11) * inv;
-            const float d2r = -d0r, d3r = -d1r;
-            const float d0z = 0.25f * (J10 - J00) * inv;
-            const float d1z = -0.25f * (J10 + J00) * inv;
-            const float d2z = -d0z, d3z = -d1z;
-
-            const float dEpsR = d0r * a0 + d1r * a1 + d2r * a2 + d3r * a3;
-            const float dEpsZ = d0z * c0 + d1z * c1 + d2z * c2 + d3z * c3;
-            const float dRdZ = d0z * a0 + d1z * a1 + d2z * a2 + d3z * a3;
-            const float dZdR = d0r * c0 + d1r * c1 + d2r * c2 + d3r * c3;
-            const float dGamRZ = dRdZ + dZdR;
-            float rg = 0.0f, dEpsT = 0.0f;
-            if (d.axi) {
-                rg = 0.25f * (p0.x + p1.x + p2.x + p3.x);
-                dEpsT = 0.25f * (a0 + a1 + a2 + a3) / rg;
-            }
-            float sg[4];
-            point_update_mixed(d, e, e, fl, dEpsR, dEpsZ, dEpsT, dGamRZ,
-                               0.5f * (dZdR - dRdZ), strainDt, sg);
-            const float sR = sg[0], sZ = sg[1], sT = sg[2], sRZ = sg[3];
-            const float dV = 4.0f * (d.axi ? 2.0f * 3.14159265358979f * rg * det
-                                           : (float)d.thickness * det);
-            float g0r, g1r, g2r, g3r;
-            if (d.axi) {
-                const float hh = sT / rg * dV * 0.25f;
-                g0r = -((d0r * sR + d0z * sRZ) * dV + hh);
-                g1r = -((d1r * sR + d1z * sRZ) * dV + hh);
-                g2r = -((d2r * sR + d2z * sRZ) * dV + hh);
-                g3r = -((d3r * sR + d3z * sRZ) * dV + hh);
-            } else {
-                g0r = -(d0r * sR + d0z * sRZ) * dV;
-                g1r = -(d1r * sR + d1z * sRZ) * dV;
-                g2r = -(d2r * sR + d2z * sRZ) * dV;
-                g3r = -(d3r * sR + d3z * sRZ) * dV;
-            }
-            float g0z = -(d0z * sZ + d0r * sRZ) * dV;
-            float g1z = -(d1z * sZ + d1r * sRZ) * dV;
-            float g2z = -(d2z * sZ + d2r * sRZ) * dV;
-            float g3z = -(d3z * sZ + d3r * sRZ) * dV;
-            const float qhg = (float)d.hourglass;
-            if (qhg > 0.0f) {
-                const float hr = r0 - r1 + r2 - r3;
-                const float hz = z0 - z1 + z2 - z3;
-                const float y0 = 1.0f - hr * d0r - hz * d0z;
-                const float y1 = -1.0f - hr * d1r - hz * d1z;
-                const float y2 = 1.0f - hr * d2r - hz * d2z;
-                const float y3 = -1.0f - hr * d3r - hz * d3z;
-                const float k = qhg * mu * dV
-                                * (d0r * d0r + d1r * d1r + d2r * d2r + d3r * d3r
-                                   + d0z * d0z + d1z * d1z + d2z * d2z + d3z * d3z);
-                float2 hg = d.hgF[e];
-                hg.x += k * (y0 * a0 + y1 * a1 + y2 * a2 + y3 * a3);
-                hg.y += k * (y0 * c0 + y1 * c1 + y2 * c2 + y3 * c3);
-                d.hgF[e] = hg;
-                g0r -= y0 * hg.x; g1r -= y1 * hg.x; g2r -= y2 * hg.x; g3r -= y3 * hg.x;
-                g0z -= y0 * hg.y; g1z -= y1 * hg.y; g2z -= y2 * hg.y; g3z -= y3 * hg.y;
-                d.hgKF[e] = k;
-            }
-            ef[0] = make_float4(g0r, g1r, g2r, g3r);
-            ef[1] = make_float4(g0z, g1z, g2z, g3z);
-        }
+        element_reduced_f32(d, e, zeroStrain ? 0.0f : (float)d.s->dt, (float)d.hourglass, d.pMid,
+                            d.vdt, 0, minEdge);
     }
     min_edge_commit_f(d, minEdge);
 }
@@ -381,15 +238,7 @@ __global__ void __launch_bounds__(MB) k_gather_mixed(Dev d) {
     if (!d.s->active) return;
     const int n = blockIdx.x * blockDim.x + threadIdx.x;
     if (n >= d.N) return;
-    double sr = 0.0, sz = 0.0;
-    const int end = d.nodeSlotStart[n + 1];
-    for (int k = d.nodeSlotStart[n]; k < end; k++) {
-        const int slot = d.nodeSlot[k];
-        sr += (double)d.contribF[slot];
-        sz += (double)d.contribF[slot + 4];
-    }
-    const double m = d.mass[n];
-    d.F[n] = make_double2(sr + m * d.gravR, sz + m * d.gravZ);
+    d.F[n] = gather_node_f32(d, n);
     if (d.hasContact) d.contactState[n] = 0;
 }
 

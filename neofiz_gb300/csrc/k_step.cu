@@ -13,7 +13,7 @@
 //
 // Every kernel reads the solver's scalars (dt, time, ...) from device memory, so a sequence
 // of steps is a fixed sequence of launches with no host decision between them.
-#include "nf_internal.h"
+#include "nf_bodies.cuh"
 
 namespace nf {
 
@@ -74,89 +74,10 @@ __global__ void __launch_bounds__(BLOCK) k_nodal(Dev d) {
     const double decay = s->decay, gain = s->gain, dtAvg = s->dtAvg, dt = s->dt;
     double impulse = 0.0, loss = 0.0, fric = 0.0;
     for (int i = blockIdx.x * blockDim.x + threadIdx.x; i < d.N; i += gridDim.x * blockDim.x) {
-        uint8_t fl = d.flags[i];
-        const bool fixedR = fl & 1, fixedZ = fl & 2;
-        bool onWall = fl & 4;
-        double2 u = d.U[i], v = d.V[i];
-        const double2 f = d.F[i];
-        const double m = d.mass[i];
-        const double invM = d.invMass[i];
-        const bool resting = d.hasWall && onWall && f.y <= 0.0;
-        uint8_t ws = 0;
-        if (fixedR) {
-            v.x = 0.0;
-        } else if (resting && d.wallFriction > 0.0) {
-            // RigidWall.slide, RigidWall.java:236-259
-            const double normal = -f.y;
-            const double trial = -m * decay * v.x / gain - f.x;
-            const double limit = isinf(d.wallFriction) ? INFINITY : d.wallFriction * normal;
-            if (fabs(trial) <= limit) {
-                loss += 0.5 * m * v.x * v.x;
-                atomicAdd(&d.s->wStuck, 1);
-                ws |= NF_WALL_STUCK;
-                v.x = 0.0;
-            } else {
-                const double tangential = copysign(limit, trial);
-                const double slid = decay * v.x + gain * (f.x + tangential) / m;
-                fric += -tangential * slid * dt;
-                ws |= NF_WALL_SLID;
-                v.x = slid;
-            }
-            u.x += v.x * dt;
-        } else {
-            v.x = decay * v.x + gain * f.x * invM;
-            u.x += v.x * dt;
-        }
-        const double2 x0 = d.X0[i];
-        if (fixedZ) {
-            v.y = 0.0;
-        } else if (resting) {
-            impulse += -f.y * dtAvg;                         // RigidWall.hold :178-181
-            atomicAdd(&d.s->wContact, 1);
-            ws |= NF_WALL_HELD;
-        } else {
-            const double trial = decay * v.y + gain * f.y * invM;
-            const double zc = x0.y + u.y;
-            if (d.hasWall && zc + trial * dt < d.wallPlane) {
-                impulse += -m * trial;                       // RigidWall.arrive :205-209
-                loss += 0.5 * m * trial * trial;
-                atomicAdd(&d.s->wContact, 1);
-                u.y += d.wallPlane - zc;
-                v.y = 0.0;
-                onWall = true;
-                ws |= NF_WALL_ARRIVED;
-            } else {
-                v.y = trial;
-                u.y += v.y * dt;
-                if (d.hasWall) onWall = false;
-            }
-        }
-        d.U[i] = u;
-        d.V[i] = v;
-        if (d.hasWall) {
-            d.flags[i] = (uint8_t)((fl & 3) | (onWall ? 4 : 0));
-            d.wallState[i] = ws;
-        }
-        if (!(isfinite(u.x) && isfinite(u.y) && isfinite(v.x) && isfinite(v.y)))
-            atomicOr(&d.s->status, STATUS_NONFINITE);
-        if (d.mixed) {
-            // the geometry of the coming assembly: mid-step and current positions as float
-            // pairs, and v dt (see k_prepare_mixed)
-            const double mid = -0.5 * dt;
-            double pr, pz;
-            if (d.finite) {
-                pr = x0.x + u.x + mid * v.x;
-                pz = x0.y + u.y + mid * v.y;
-            } else {
-                pr = x0.x;
-                pz = x0.y;
-            }
-            const double cr = x0.x + u.x, cz = x0.y + u.y;
-            const float prh = (float)pr, pzh = (float)pz, crh = (float)cr, czh = (float)cz;
-            d.pMid[i] = make_float4(prh, (float)(pr - (double)prh), pzh, (float)(pz - (double)pzh));
-            d.pCur[i] = make_float4(crh, (float)(cr - (double)crh), czh, (float)(cz - (double)czh));
-            d.vdt[i] = make_float2((float)(v.x * dt), (float)(v.y * dt));
-        }
+        nodal_node(d, i, NodalCoef{decay, gain, dtAvg, dt},
+                   WallRef{d.hasWall, d.wallPlane, d.wallFriction, &d.s->wContact, &d.s->wStuck},
+                   d.mixed ? MixedGeo{d.pMid, d.pCur, d.vdt, 0} : MixedGeo{nullptr, nullptr, nullptr, 0},
+                   &d.s->status, impulse, loss, fric);
     }
     if (d.hasWall) {
         const double a = block_sum(impulse, sh);
@@ -281,149 +202,7 @@ __global__ void __launch_bounds__(BLOCK) k_element_reduced(Dev d, int zeroStrain
     const int e = blockIdx.x * blockDim.x + threadIdx.x;
     double minEdge = DMAX;
     if (e < d.E) {
-        double *ef = d.contribution + 8 * (size_t)e;
-        if (d.gone != nullptr && d.gone[e]) {
-            for (int k = 0; k < 8; k++) ef[k] = 0.0;
-        } else {
-            const double strainDt = zeroStrain ? 0.0 : d.s->dt;
-            const MatDev &fl = d.mats[d.emat[e]];
-            const double lambda = fl.lambda, mu = fl.mu;
-            const int4 c = d.conn[e];
-            const double mid = -0.5 * strainDt;
-            const double2 x0 = d.X0[c.x], x1 = d.X0[c.y], x2 = d.X0[c.z], x3 = d.X0[c.w];
-            const double2 u0 = d.U[c.x], u1 = d.U[c.y], u2 = d.U[c.z], u3 = d.U[c.w];
-            const double2 v0 = d.V[c.x], v1 = d.V[c.y], v2 = d.V[c.z], v3 = d.V[c.w];
-            double r0, r1, r2, r3, z0, z1, z2, z3;
-            if (d.finite) {                                  // cr/cz, :1176-1182
-                r0 = x0.x + u0.x + mid * v0.x; r1 = x1.x + u1.x + mid * v1.x;
-                r2 = x2.x + u2.x + mid * v2.x; r3 = x3.x + u3.x + mid * v3.x;
-                z0 = x0.y + u0.y + mid * v0.y; z1 = x1.y + u1.y + mid * v1.y;
-                z2 = x2.y + u2.y + mid * v2.y; z3 = x3.y + u3.y + mid * v3.y;
-            } else {
-                r0 = x0.x; r1 = x1.x; r2 = x2.x; r3 = x3.x;
-                z0 = x0.y; z1 = x1.y; z2 = x2.y; z3 = x3.y;
-            }
-            const double a0 = v0.x * strainDt, a1 = v1.x * strainDt;
-            const double a2 = v2.x * strainDt, a3 = v3.x * strainDt;
-            const double c0 = v0.y * strainDt, c1 = v1.y * strainDt;
-            const double c2 = v2.y * strainDt, c3 = v3.y * strainDt;
-
-            if (d.finite) minEdge = shortestEdge(minEdge, r0, r1, r2, r3, z0, z1, z2, z3);
-
-            const double J00 = 0.25 * (-r0 + r1 + r2 - r3);
-            const double J01 = 0.25 * (-z0 + z1 + z2 - z3);
-            const double J10 = 0.25 * (-r0 - r1 + r2 + r3);
-            const double J11 = 0.25 * (-z0 - z1 + z2 + z3);
-            const double det = J00 * J11 - J01 * J10;
-            const double inv = 1.0 / det;
-
-            const double d0r = 0.25 * (J01 - J11) * inv;
-            const double d1r = 0.25 * (J01 + J11) * inv;
-            const double d2r = -d0r;
-            const double d3r = -d1r;
-            const double d0z = 0.25 * (J10 - J00) * inv;
-            const double d1z = -0.25 * (J10 + J00) * inv;
-            const double d2z = -d0z;
-            const double d3z = -d1z;
-
-            const double dEpsR = d0r * a0 + d1r * a1 + d2r * a2 + d3r * a3;
-            const double dEpsZ = d0z * c0 + d1z * c1 + d2z * c2 + d3z * c3;
-            const double dRdZ = d0z * a0 + d1z * a1 + d2z * a2 + d3z * a3;
-            const double dZdR = d0r * c0 + d1r * c1 + d2r * c2 + d3r * c3;
-            const double dGamRZ = dRdZ + dZdR;
-
-            double rg = 0.0, dEpsT = 0.0;
-            if (d.axi) {
-                rg = 0.25 * (r0 + r1 + r2 + r3);
-                dEpsT = 0.25 * (a0 + a1 + a2 + a3) / rg;
-            }
-            double sg[4], bk[4];
-            {
-                const double2 *ps = reinterpret_cast<const double2 *>(d.sig + 4 * (size_t)e);
-                const double2 *pb = reinterpret_cast<const double2 *>(d.back + 4 * (size_t)e);
-                const double2 s01 = ps[0], s23 = ps[1], b01 = pb[0], b23 = pb[1];
-                sg[0] = s01.x; sg[1] = s01.y; sg[2] = s23.x; sg[3] = s23.y;
-                bk[0] = b01.x; bk[1] = b01.y; bk[2] = b23.x; bk[3] = b23.y;
-            }
-            if (d.finite) {
-                const double spinDt = 0.5 * (dZdR - dRdZ);
-                if (spinDt != 0.0) {
-                    const double cs = corot_cos(spinDt), sn = corot_sin(spinDt);
-                    corot_rotate(sg, cs, sn);
-                    corot_rotate(bk, cs, sn);
-                }
-            }
-            double epsP = d.epsP[e], work = d.wP[e];
-            if (d.hasDamage) {
-                DamageRef dr;
-                dr.failureStrain = d.dFail[e];
-                dr.strength = d.dStrength + e;
-                dr.softening = d.dSoft + e;
-                dr.width = d.dWidth + e;
-                dr.geometry = d.dGeom + 5 * (size_t)e;
-                dr.fractureEnergy = d.dGf[e];
-                dr.youngs = fl.youngs;
-                j2_update(sg, bk, epsP, work, dEpsR, dEpsZ, dEpsT, dGamRZ, lambda, mu, fl,
-                          strainDt, &dr, d.dStrength[e], d.dSoft[e]);
-            } else {
-                j2_update(sg, bk, epsP, work, dEpsR, dEpsZ, dEpsT, dGamRZ, lambda, mu, fl,
-                          strainDt, (const DamageRef *)nullptr, 0.0, 0.0);
-            }
-            {
-                double2 *ps = reinterpret_cast<double2 *>(d.sig + 4 * (size_t)e);
-                double2 *pb = reinterpret_cast<double2 *>(d.back + 4 * (size_t)e);
-                ps[0] = make_double2(sg[0], sg[1]); ps[1] = make_double2(sg[2], sg[3]);
-                pb[0] = make_double2(bk[0], bk[1]); pb[1] = make_double2(bk[2], bk[3]);
-                d.epsP[e] = epsP;
-                d.wP[e] = work;
-            }
-            const double sR = sg[0], sZ = sg[1], sT = sg[2], sRZ = sg[3];
-            const double dV = 4.0 * (d.axi ? 2.0 * NF_PI * rg * det : d.thickness * det);
-
-            double g0r, g1r, g2r, g3r;
-            if (d.axi) {
-                const double hh = sT / rg * dV * 0.25;
-                g0r = -((d0r * sR + d0z * sRZ) * dV + hh);
-                g1r = -((d1r * sR + d1z * sRZ) * dV + hh);
-                g2r = -((d2r * sR + d2z * sRZ) * dV + hh);
-                g3r = -((d3r * sR + d3z * sRZ) * dV + hh);
-            } else {
-                g0r = -(d0r * sR + d0z * sRZ) * dV;
-                g1r = -(d1r * sR + d1z * sRZ) * dV;
-                g2r = -(d2r * sR + d2z * sRZ) * dV;
-                g3r = -(d3r * sR + d3z * sRZ) * dV;
-            }
-            double g0z = -(d0z * sZ + d0r * sRZ) * dV;
-            double g1z = -(d1z * sZ + d1r * sRZ) * dV;
-            double g2z = -(d2z * sZ + d2r * sRZ) * dV;
-            double g3z = -(d3z * sZ + d3r * sRZ) * dV;
-
-            const double qhg = d.hourglass;
-            if (qhg > 0.0) {
-                const double hr = r0 - r1 + r2 - r3;
-                const double hz = z0 - z1 + z2 - z3;
-                const double y0 = 1.0 - hr * d0r - hz * d0z;
-                const double y1 = -1.0 - hr * d1r - hz * d1z;
-                const double y2 = 1.0 - hr * d2r - hz * d2z;
-                const double y3 = -1.0 - hr * d3r - hz * d3z;
-                const double k = qhg * mu * dV
-                                 * (d0r * d0r + d1r * d1r + d2r * d2r + d3r * d3r
-                                    + d0z * d0z + d1z * d1z + d2z * d2z + d3z * d3z);
-                double2 hg = d.hg[e];
-                hg.x += k * (y0 * a0 + y1 * a1 + y2 * a2 + y3 * a3);
-                hg.y += k * (y0 * c0 + y1 * c1 + y2 * c2 + y3 * c3);
-                d.hg[e] = hg;
-                const double qr = hg.x, qz = hg.y;
-                g0r -= y0 * qr; g1r -= y1 * qr; g2r -= y2 * qr; g3r -= y3 * qr;
-                g0z -= y0 * qz; g1z -= y1 * qz; g2z -= y2 * qz; g3z -= y3 * qz;
-                d.hgK[e] = k;
-            }
-            double2 *ef2 = reinterpret_cast<double2 *>(ef);
-            ef2[0] = make_double2(g0r, g1r);
-            ef2[1] = make_double2(g2r, g3r);
-            ef2[2] = make_double2(g0z, g1z);
-            ef2[3] = make_double2(g2z, g3z);
-        }
+        element_reduced(d, e, zeroStrain ? 0.0 : d.s->dt, d.hourglass, minEdge);
     }
     min_edge_commit(d, minEdge);
 }
@@ -629,15 +408,7 @@ __global__ void __launch_bounds__(BLOCK) k_gather(Dev d) {
     if (!d.s->active) return;
     const int n = blockIdx.x * blockDim.x + threadIdx.x;
     if (n >= d.N) return;
-    double sr = 0.0, sz = 0.0;
-    const int end = d.nodeSlotStart[n + 1];
-    for (int k = d.nodeSlotStart[n]; k < end; k++) {
-        const int slot = d.nodeSlot[k];
-        sr += d.contribution[slot];
-        sz += d.contribution[slot + 4];
-    }
-    const double m = d.mass[n];
-    d.F[n] = make_double2(sr + m * d.gravR, sz + m * d.gravZ);
+    d.F[n] = gather_node(d, n);
     if (d.hasContact) d.contactState[n] = 0;
 }
 

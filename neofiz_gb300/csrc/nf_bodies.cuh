@@ -1,0 +1,456 @@
+// nf_bodies.cuh -- the per-node and per-element arithmetic of the timestep, shared by the
+// single-scene kernels (k_step.cu, k_mixed.cu) and the batched kernel (k_batch.cu). One copy
+// of each body means a batched instance computes exactly what a single scene does.
+#pragma once
+
+#include "nf_internal.h"
+
+namespace nf {
+
+// One node of nodalUpdate, ExplicitSolver.java:998-1062, with RigidWall.hold/crosses/arrive/
+// slide (RigidWall.java:163-259): shared by the single-scene kernel and the batched one. Adds
+// the node's wall terms to impulse/loss/fric. When geo.pMid is set (the mixed form) it also
+// writes the FP32 geometry of the coming assembly: mid-step and current positions as float
+// pairs (hi, lo) and v dt, at index geo.base + i.
+struct NodalCoef {
+    double decay, gain, dtAvg, dt;
+};
+struct WallRef {
+    int present;
+    double plane, friction;
+    int *contact, *stuck;
+};
+struct MixedGeo {
+    float4 *pMid, *pCur;
+    float2 *vdt;
+    int base;
+};
+
+static __device__ __forceinline__ void nodal_node(const Dev &d, int i, const NodalCoef &co,
+                                                  const WallRef &w, const MixedGeo &geo,
+                                                  uint32_t *status, double &impulse,
+                                                  double &loss, double &fric) {
+    const double decay = co.decay, gain = co.gain, dtAvg = co.dtAvg, dt = co.dt;
+    uint8_t fl = d.flags[i];
+    const bool fixedR = fl & 1, fixedZ = fl & 2;
+    bool onWall = fl & 4;
+    double2 u = d.U[i], v = d.V[i];
+    const double2 f = d.F[i];
+    const double m = d.mass[i];
+    const double invM = d.invMass[i];
+    const bool resting = w.present && onWall && f.y <= 0.0;
+    uint8_t ws = 0;
+    if (fixedR) {
+        v.x = 0.0;
+    } else if (resting && w.friction > 0.0) {
+        // RigidWall.slide, RigidWall.java:236-259
+        const double normal = -f.y;
+        const double trial = -m * decay * v.x / gain - f.x;
+        const double limit = isinf(w.friction) ? INFINITY : w.friction * normal;
+        if (fabs(trial) <= limit) {
+            loss += 0.5 * m * v.x * v.x;
+            atomicAdd(w.stuck, 1);
+            ws |= NF_WALL_STUCK;
+            v.x = 0.0;
+        } else {
+            const double tangential = copysign(limit, trial);
+            const double slid = decay * v.x + gain * (f.x + tangential) / m;
+            fric += -tangential * slid * dt;
+            ws |= NF_WALL_SLID;
+            v.x = slid;
+        }
+        u.x += v.x * dt;
+    } else {
+        v.x = decay * v.x + gain * f.x * invM;
+        u.x += v.x * dt;
+    }
+    const double2 x0 = d.X0[i];
+    if (fixedZ) {
+        v.y = 0.0;
+    } else if (resting) {
+        impulse += -f.y * dtAvg;                         // RigidWall.hold :178-181
+        atomicAdd(w.contact, 1);
+        ws |= NF_WALL_HELD;
+    } else {
+        const double trial = decay * v.y + gain * f.y * invM;
+        const double zc = x0.y + u.y;
+        if (w.present && zc + trial * dt < w.plane) {
+            impulse += -m * trial;                       // RigidWall.arrive :205-209
+            loss += 0.5 * m * trial * trial;
+            atomicAdd(w.contact, 1);
+            u.y += w.plane - zc;
+            v.y = 0.0;
+            onWall = true;
+            ws |= NF_WALL_ARRIVED;
+        } else {
+            v.y = trial;
+            u.y += v.y * dt;
+            if (w.present) onWall = false;
+        }
+    }
+    d.U[i] = u;
+    d.V[i] = v;
+    if (w.present) {
+        d.flags[i] = (uint8_t)((fl & 3) | (onWall ? 4 : 0));
+        d.wallState[i] = ws;
+    }
+    if (!(isfinite(u.x) && isfinite(u.y) && isfinite(v.x) && isfinite(v.y)))
+        atomicOr(status, STATUS_NONFINITE);
+    if (geo.pMid) {
+        // the geometry of the coming assembly: mid-step and current positions as float
+        // pairs, and v dt (see k_prepare_mixed)
+        const double mid = -0.5 * dt;
+        double pr, pz;
+        if (d.finite) {
+            pr = x0.x + u.x + mid * v.x;
+            pz = x0.y + u.y + mid * v.y;
+        } else {
+            pr = x0.x;
+            pz = x0.y;
+        }
+        const double cr = x0.x + u.x, cz = x0.y + u.y;
+        const float prh = (float)pr, pzh = (float)pz, crh = (float)cr, czh = (float)cz;
+        geo.pMid[geo.base + i] = make_float4(prh, (float)(pr - (double)prh), pzh, (float)(pz - (double)pzh));
+        if (geo.pCur) geo.pCur[geo.base + i] = make_float4(crh, (float)(cr - (double)crh), czh, (float)(cz - (double)czh));
+        geo.vdt[geo.base + i] = make_float2((float)(v.x * dt), (float)(v.y * dt));
+    }
+}
+
+// The mixed form's geometry of an assembly on its own (the initial one, and steps without the
+// fused nodal update): node i's mid-step and current positions as float pairs and v sdt.
+static __device__ __forceinline__ void prepare_node(const Dev &d, int i, double sdt,
+                                                    const MixedGeo &geo) {
+    const double mid = -0.5 * sdt;
+    const double2 x = d.X0[i], u = d.U[i], v = d.V[i];
+    double pr, pz;
+    if (d.finite) {
+        pr = x.x + u.x + mid * v.x;
+        pz = x.y + u.y + mid * v.y;
+    } else {
+        pr = x.x;
+        pz = x.y;
+    }
+    const double cr = x.x + u.x, cz = x.y + u.y;
+    const float prh = (float)pr, pzh = (float)pz, crh = (float)cr, czh = (float)cz;
+    geo.pMid[geo.base + i] = make_float4(prh, (float)(pr - (double)prh), pzh, (float)(pz - (double)pzh));
+    if (geo.pCur)
+        geo.pCur[geo.base + i] = make_float4(crh, (float)(cr - (double)crh), czh, (float)(cz - (double)czh));
+    geo.vdt[geo.base + i] = make_float2((float)(v.x * sdt), (float)(v.y * sdt));
+}
+
+// reducedIntegration, ExplicitSolver.java:1373-1504, for element e: B at the centroid, strain
+// increments, Cayley co-rotation, J2/Johnson-Cook return, FB hourglass, the eight force
+// terms into the element's contribution slots; folds its shortest edge into minEdge.
+static __device__ __forceinline__ void element_reduced(const Dev &d, int e, double strainDt,
+                                                       double hourglass, double &minEdge) {
+    double *ef = d.contribution + 8 * (size_t)e;
+    if (d.gone != nullptr && d.gone[e]) {
+        for (int k = 0; k < 8; k++) ef[k] = 0.0;
+    } else {
+        const MatDev &fl = d.mats[d.emat[e]];
+        const double lambda = fl.lambda, mu = fl.mu;
+        const int4 c = d.conn[e];
+        const double mid = -0.5 * strainDt;
+        const double2 x0 = d.X0[c.x], x1 = d.X0[c.y], x2 = d.X0[c.z], x3 = d.X0[c.w];
+        const double2 u0 = d.U[c.x], u1 = d.U[c.y], u2 = d.U[c.z], u3 = d.U[c.w];
+        const double2 v0 = d.V[c.x], v1 = d.V[c.y], v2 = d.V[c.z], v3 = d.V[c.w];
+        double r0, r1, r2, r3, z0, z1, z2, z3;
+        if (d.finite) {                                  // cr/cz, :1176-1182
+            r0 = x0.x + u0.x + mid * v0.x; r1 = x1.x + u1.x + mid * v1.x;
+            r2 = x2.x + u2.x + mid * v2.x; r3 = x3.x + u3.x + mid * v3.x;
+            z0 = x0.y + u0.y + mid * v0.y; z1 = x1.y + u1.y + mid * v1.y;
+            z2 = x2.y + u2.y + mid * v2.y; z3 = x3.y + u3.y + mid * v3.y;
+        } else {
+            r0 = x0.x; r1 = x1.x; r2 = x2.x; r3 = x3.x;
+            z0 = x0.y; z1 = x1.y; z2 = x2.y; z3 = x3.y;
+        }
+        const double a0 = v0.x * strainDt, a1 = v1.x * strainDt;
+        const double a2 = v2.x * strainDt, a3 = v3.x * strainDt;
+        const double c0 = v0.y * strainDt, c1 = v1.y * strainDt;
+        const double c2 = v2.y * strainDt, c3 = v3.y * strainDt;
+
+        if (d.finite) minEdge = shortestEdge(minEdge, r0, r1, r2, r3, z0, z1, z2, z3);
+
+        const double J00 = 0.25 * (-r0 + r1 + r2 - r3);
+        const double J01 = 0.25 * (-z0 + z1 + z2 - z3);
+        const double J10 = 0.25 * (-r0 - r1 + r2 + r3);
+        const double J11 = 0.25 * (-z0 - z1 + z2 + z3);
+        const double det = J00 * J11 - J01 * J10;
+        const double inv = 1.0 / det;
+
+        const double d0r = 0.25 * (J01 - J11) * inv;
+        const double d1r = 0.25 * (J01 + J11) * inv;
+        const double d2r = -d0r;
+        const double d3r = -d1r;
+        const double d0z = 0.25 * (J10 - J00) * inv;
+        const double d1z = -0.25 * (J10 + J00) * inv;
+        const double d2z = -d0z;
+        const double d3z = -d1z;
+
+        const double dEpsR = d0r * a0 + d1r * a1 + d2r * a2 + d3r * a3;
+        const double dEpsZ = d0z * c0 + d1z * c1 + d2z * c2 + d3z * c3;
+        const double dRdZ = d0z * a0 + d1z * a1 + d2z * a2 + d3z * a3;
+        const double dZdR = d0r * c0 + d1r * c1 + d2r * c2 + d3r * c3;
+        const double dGamRZ = dRdZ + dZdR;
+
+        double rg = 0.0, dEpsT = 0.0;
+        if (d.axi) {
+            rg = 0.25 * (r0 + r1 + r2 + r3);
+            dEpsT = 0.25 * (a0 + a1 + a2 + a3) / rg;
+        }
+        double sg[4], bk[4];
+        {
+            const double2 *ps = reinterpret_cast<const double2 *>(d.sig + 4 * (size_t)e);
+            const double2 *pb = reinterpret_cast<const double2 *>(d.back + 4 * (size_t)e);
+            const double2 s01 = ps[0], s23 = ps[1], b01 = pb[0], b23 = pb[1];
+            sg[0] = s01.x; sg[1] = s01.y; sg[2] = s23.x; sg[3] = s23.y;
+            bk[0] = b01.x; bk[1] = b01.y; bk[2] = b23.x; bk[3] = b23.y;
+        }
+        if (d.finite) {
+            const double spinDt = 0.5 * (dZdR - dRdZ);
+            if (spinDt != 0.0) {
+                const double cs = corot_cos(spinDt), sn = corot_sin(spinDt);
+                corot_rotate(sg, cs, sn);
+                corot_rotate(bk, cs, sn);
+            }
+        }
+        double epsP = d.epsP[e], work = d.wP[e];
+        if (d.hasDamage) {
+            DamageRef dr;
+            dr.failureStrain = d.dFail[e];
+            dr.strength = d.dStrength + e;
+            dr.softening = d.dSoft + e;
+            dr.width = d.dWidth + e;
+            dr.geometry = d.dGeom + 5 * (size_t)e;
+            dr.fractureEnergy = d.dGf[e];
+            dr.youngs = fl.youngs;
+            j2_update(sg, bk, epsP, work, dEpsR, dEpsZ, dEpsT, dGamRZ, lambda, mu, fl,
+                      strainDt, &dr, d.dStrength[e], d.dSoft[e]);
+        } else {
+            j2_update(sg, bk, epsP, work, dEpsR, dEpsZ, dEpsT, dGamRZ, lambda, mu, fl,
+                      strainDt, (const DamageRef *)nullptr, 0.0, 0.0);
+        }
+        {
+            double2 *ps = reinterpret_cast<double2 *>(d.sig + 4 * (size_t)e);
+            double2 *pb = reinterpret_cast<double2 *>(d.back + 4 * (size_t)e);
+            ps[0] = make_double2(sg[0], sg[1]); ps[1] = make_double2(sg[2], sg[3]);
+            pb[0] = make_double2(bk[0], bk[1]); pb[1] = make_double2(bk[2], bk[3]);
+            d.epsP[e] = epsP;
+            d.wP[e] = work;
+        }
+        const double sR = sg[0], sZ = sg[1], sT = sg[2], sRZ = sg[3];
+        const double dV = 4.0 * (d.axi ? 2.0 * NF_PI * rg * det : d.thickness * det);
+
+        double g0r, g1r, g2r, g3r;
+        if (d.axi) {
+            const double hh = sT / rg * dV * 0.25;
+            g0r = -((d0r * sR + d0z * sRZ) * dV + hh);
+            g1r = -((d1r * sR + d1z * sRZ) * dV + hh);
+            g2r = -((d2r * sR + d2z * sRZ) * dV + hh);
+            g3r = -((d3r * sR + d3z * sRZ) * dV + hh);
+        } else {
+            g0r = -(d0r * sR + d0z * sRZ) * dV;
+            g1r = -(d1r * sR + d1z * sRZ) * dV;
+            g2r = -(d2r * sR + d2z * sRZ) * dV;
+            g3r = -(d3r * sR + d3z * sRZ) * dV;
+        }
+        double g0z = -(d0z * sZ + d0r * sRZ) * dV;
+        double g1z = -(d1z * sZ + d1r * sRZ) * dV;
+        double g2z = -(d2z * sZ + d2r * sRZ) * dV;
+        double g3z = -(d3z * sZ + d3r * sRZ) * dV;
+
+        const double qhg = hourglass;
+        if (qhg > 0.0) {
+            const double hr = r0 - r1 + r2 - r3;
+            const double hz = z0 - z1 + z2 - z3;
+            const double y0 = 1.0 - hr * d0r - hz * d0z;
+            const double y1 = -1.0 - hr * d1r - hz * d1z;
+            const double y2 = 1.0 - hr * d2r - hz * d2z;
+            const double y3 = -1.0 - hr * d3r - hz * d3z;
+            const double k = qhg * mu * dV
+                             * (d0r * d0r + d1r * d1r + d2r * d2r + d3r * d3r
+                                + d0z * d0z + d1z * d1z + d2z * d2z + d3z * d3z);
+            double2 hg = d.hg[e];
+            hg.x += k * (y0 * a0 + y1 * a1 + y2 * a2 + y3 * a3);
+            hg.y += k * (y0 * c0 + y1 * c1 + y2 * c2 + y3 * c3);
+            d.hg[e] = hg;
+            const double qr = hg.x, qz = hg.y;
+            g0r -= y0 * qr; g1r -= y1 * qr; g2r -= y2 * qr; g3r -= y3 * qr;
+            g0z -= y0 * qz; g1z -= y1 * qz; g2z -= y2 * qz; g3z -= y3 * qz;
+            d.hgK[e] = k;
+        }
+        double2 *ef2 = reinterpret_cast<double2 *>(ef);
+        ef2[0] = make_double2(g0r, g1r);
+        ef2[1] = make_double2(g2r, g3r);
+        ef2[2] = make_double2(g0z, g1z);
+        ef2[3] = make_double2(g2z, g3z);
+    }
+}
+
+static __device__ __forceinline__ float diff_hl(float4 a, float4 b, int comp) {
+    // (a - b) for component comp (0: r, 1: z) of two hi/lo pairs
+    return comp == 0 ? (a.x - b.x) + (a.y - b.y) : (a.z - b.z) + (a.w - b.w);
+}
+
+// One point's update in FP32; shared by the reduced and full kernels.
+static __device__ __forceinline__ void point_update_mixed(const Dev &d, int e, int p, const MatF &fl,
+                                                   float dEpsR, float dEpsZ, float dEpsT,
+                                                   float dGamRZ, float spinDt, float strainDt,
+                                                   float *sg) {
+    float bk[4];
+    {
+        const float4 s = reinterpret_cast<const float4 *>(d.sigF)[p];
+        const float4 b = reinterpret_cast<const float4 *>(d.backF)[p];
+        sg[0] = s.x; sg[1] = s.y; sg[2] = s.z; sg[3] = s.w;
+        bk[0] = b.x; bk[1] = b.y; bk[2] = b.z; bk[3] = b.w;
+    }
+    if (d.finite && spinDt != 0.0f) {
+        const float cs = corot_cos(spinDt), sn = corot_sin(spinDt);
+        corot_rotate(sg, cs, sn);
+        corot_rotate(bk, cs, sn);
+    }
+    float epsP = d.epsPF[p], work = d.wPF[p];
+    if (d.hasDamage) {
+        DamageRefT<float> dr;
+        dr.failureStrain = d.dFailF[e];
+        dr.strength = d.dStrF + p;
+        dr.softening = d.dSoftF + p;
+        dr.width = d.dWidthF + p;
+        dr.geometry = d.dGeomF + 5 * (size_t)e;
+        dr.fractureEnergy = d.dGfF[e];
+        dr.youngs = fl.youngs;
+        j2_update(sg, bk, epsP, work, dEpsR, dEpsZ, dEpsT, dGamRZ, fl.lambda, fl.mu, fl,
+                  strainDt, &dr, d.dStrF[p], d.dSoftF[p]);
+    } else {
+        j2_update(sg, bk, epsP, work, dEpsR, dEpsZ, dEpsT, dGamRZ, fl.lambda, fl.mu, fl,
+                  strainDt, (const DamageRefT<float> *)nullptr, 0.0f, 0.0f);
+    }
+    reinterpret_cast<float4 *>(d.sigF)[p] = make_float4(sg[0], sg[1], sg[2], sg[3]);
+    reinterpret_cast<float4 *>(d.backF)[p] = make_float4(bk[0], bk[1], bk[2], bk[3]);
+    d.epsPF[p] = epsP;
+    d.wPF[p] = work;
+}
+
+// reducedIntegration (ExplicitSolver.java:1373-1504) in FP32 for element e, on the float
+// geometry pMid/vdt of its nodes (node n at index n - base). Shared by the single-scene and
+// batched kernels.
+static __device__ __forceinline__ void element_reduced_f32(const Dev &d, int e, float strainDt,
+                                                           float hourglass, const float4 *pMid,
+                                                           const float2 *vdt, int base,
+                                                           float &minEdge) {
+    float4 *ef = reinterpret_cast<float4 *>(d.contribF + 8 * (size_t)e);
+    if (d.gone != nullptr && d.gone[e]) {
+        ef[0] = make_float4(0.f, 0.f, 0.f, 0.f);
+        ef[1] = make_float4(0.f, 0.f, 0.f, 0.f);
+    } else {
+        const MatF &fl = d.matsF[d.emat[e]];
+        const float mu = fl.mu;
+        const int4 c = d.conn[e];
+        const float4 p0 = pMid[c.x - base], p1 = pMid[c.y - base], p2 = pMid[c.z - base],
+                     p3 = pMid[c.w - base];
+        const float2 w0 = vdt[c.x - base], w1 = vdt[c.y - base], w2 = vdt[c.z - base],
+                     w3 = vdt[c.w - base];
+        const float r0 = 0.0f, z0 = 0.0f;
+        const float r1 = diff_hl(p1, p0, 0), r2 = diff_hl(p2, p0, 0), r3 = diff_hl(p3, p0, 0);
+        const float z1 = diff_hl(p1, p0, 1), z2 = diff_hl(p2, p0, 1), z3 = diff_hl(p3, p0, 1);
+        const float a0 = w0.x, a1 = w1.x, a2 = w2.x, a3 = w3.x;
+        const float c0 = w0.y, c1 = w1.y, c2 = w2.y, c3 = w3.y;
+        if (d.finite) minEdge = shortestEdge(minEdge, r0, r1, r2, r3, z0, z1, z2, z3);
+
+        const float J00 = 0.25f * (-r0 + r1 + r2 - r3);
+        const float J01 = 0.25f * (-z0 + z1 + z2 - z3);
+        const float J10 = 0.25f * (-r0 - r1 + r2 + r3);
+        const float J11 = 0.25f * (-z0 - z1 + z2 + z3);
+        const float det = J00 * J11 - J01 * J10;
+        const float inv = 1.0f / det;
+        const float d0r = 0.25f * (J01 - J11) * inv;
+        const float d1r = 0.25f * (J01 + J11) * inv;
+        const float d2r = -d0r, d3r = -d1r;
+        const float d0z = 0.25f * (J10 - J00) * inv;
+        const float d1z = -0.25f * (J10 + J00) * inv;
+        const float d2z = -d0z, d3z = -d1z;
+
+        const float dEpsR = d0r * a0 + d1r * a1 + d2r * a2 + d3r * a3;
+        const float dEpsZ = d0z * c0 + d1z * c1 + d2z * c2 + d3z * c3;
+        const float dRdZ = d0z * a0 + d1z * a1 + d2z * a2 + d3z * a3;
+        const float dZdR = d0r * c0 + d1r * c1 + d2r * c2 + d3r * c3;
+        const float dGamRZ = dRdZ + dZdR;
+        float rg = 0.0f, dEpsT = 0.0f;
+        if (d.axi) {
+            rg = 0.25f * (p0.x + p1.x + p2.x + p3.x);
+            dEpsT = 0.25f * (a0 + a1 + a2 + a3) / rg;
+        }
+        float sg[4];
+        point_update_mixed(d, e, e, fl, dEpsR, dEpsZ, dEpsT, dGamRZ,
+                           0.5f * (dZdR - dRdZ), strainDt, sg);
+        const float sR = sg[0], sZ = sg[1], sT = sg[2], sRZ = sg[3];
+        const float dV = 4.0f * (d.axi ? 2.0f * 3.14159265358979f * rg * det
+                                       : (float)d.thickness * det);
+        float g0r, g1r, g2r, g3r;
+        if (d.axi) {
+            const float hh = sT / rg * dV * 0.25f;
+            g0r = -((d0r * sR + d0z * sRZ) * dV + hh);
+            g1r = -((d1r * sR + d1z * sRZ) * dV + hh);
+            g2r = -((d2r * sR + d2z * sRZ) * dV + hh);
+            g3r = -((d3r * sR + d3z * sRZ) * dV + hh);
+        } else {
+            g0r = -(d0r * sR + d0z * sRZ) * dV;
+            g1r = -(d1r * sR + d1z * sRZ) * dV;
+            g2r = -(d2r * sR + d2z * sRZ) * dV;
+            g3r = -(d3r * sR + d3z * sRZ) * dV;
+        }
+        float g0z = -(d0z * sZ + d0r * sRZ) * dV;
+        float g1z = -(d1z * sZ + d1r * sRZ) * dV;
+        float g2z = -(d2z * sZ + d2r * sRZ) * dV;
+        float g3z = -(d3z * sZ + d3r * sRZ) * dV;
+        const float qhg = hourglass;
+        if (qhg > 0.0f) {
+            const float hr = r0 - r1 + r2 - r3;
+            const float hz = z0 - z1 + z2 - z3;
+            const float y0 = 1.0f - hr * d0r - hz * d0z;
+            const float y1 = -1.0f - hr * d1r - hz * d1z;
+            const float y2 = 1.0f - hr * d2r - hz * d2z;
+            const float y3 = -1.0f - hr * d3r - hz * d3z;
+            const float k = qhg * mu * dV
+                            * (d0r * d0r + d1r * d1r + d2r * d2r + d3r * d3r
+                               + d0z * d0z + d1z * d1z + d2z * d2z + d3z * d3z);
+            float2 hg = d.hgF[e];
+            hg.x += k * (y0 * a0 + y1 * a1 + y2 * a2 + y3 * a3);
+            hg.y += k * (y0 * c0 + y1 * c1 + y2 * c2 + y3 * c3);
+            d.hgF[e] = hg;
+            g0r -= y0 * hg.x; g1r -= y1 * hg.x; g2r -= y2 * hg.x; g3r -= y3 * hg.x;
+            g0z -= y0 * hg.y; g1z -= y1 * hg.y; g2z -= y2 * hg.y; g3z -= y3 * hg.y;
+            d.hgKF[e] = k;
+        }
+        ef[0] = make_float4(g0r, g1r, g2r, g3r);
+        ef[1] = make_float4(g0z, g1z, g2z, g3z);
+    }
+}
+
+// gather, ExplicitSolver.java:1147-1165: node n's sources in ascending order, then m g.
+static __device__ __forceinline__ double2 gather_node(const Dev &d, int n) {
+    double sr = 0.0, sz = 0.0;
+    const int end = d.nodeSlotStart[n + 1];
+    for (int k = d.nodeSlotStart[n]; k < end; k++) {
+        const int slot = d.nodeSlot[k];
+        sr += d.contribution[slot];
+        sz += d.contribution[slot + 4];
+    }
+    const double m = d.mass[n];
+    return make_double2(sr + m * d.gravR, sz + m * d.gravZ);
+}
+
+// The same gather of float contributions into FP64 sums (the mixed form).
+static __device__ __forceinline__ double2 gather_node_f32(const Dev &d, int n) {
+    double sr = 0.0, sz = 0.0;
+    const int end = d.nodeSlotStart[n + 1];
+    for (int k = d.nodeSlotStart[n]; k < end; k++) {
+        const int slot = d.nodeSlot[k];
+        sr += (double)d.contribF[slot];
+        sz += (double)d.contribF[slot + 4];
+    }
+    const double m = d.mass[n];
+    return make_double2(sr + m * d.gravR, sz + m * d.gravZ);
+}
+
+}  // namespace nf

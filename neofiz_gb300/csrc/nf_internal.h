@@ -197,6 +197,68 @@ struct Solver {
     void mark(int group, bool begin);
 };
 
+// ------------------------------------------------------------------------------------ batches
+// Many independent scenes of one formulation in one set of concatenated arrays, described by
+// one Dev (conn and node slots hold global indices; emat[e] is the element's instance, whose
+// material is mats[instance]). Each instance keeps its own step, time and totals.
+struct BatchInst {
+    int n0, n1, e0, e1;                      // its nodes and elements
+    int hasWall, pad;
+    double cfl, wave, massScale, damping, hourglass;
+    double wallPlane, wallFriction, tEnd;
+};
+
+struct BatchScalars {
+    double dt, dtPrevious, time, minEdgeSquared;
+    double wImpulse, wEnergyLoss, wFriction;
+    long long steps, stepLimit;
+    int wContact, wStuck;
+    uint32_t status;
+    int done;                                // time >= tEnd or the step limit reached
+};
+
+struct BatchDev {
+    const BatchInst *inst;
+    BatchScalars *sc;
+    const int32_t *order;                    // instances, most expensive first
+    int32_t *queue;                          // next position in order (per launch)
+    int32_t *remaining;                      // instances not done
+    unsigned long long *measure;             // [3 per instance] order-preserving extrema
+    int count;
+    int maxNodes;                            // the largest instance's node count
+};
+
+// A launch configuration of the batched step (chosen by the autotuner).
+struct BatchShape {
+    int threads;                             // 128 or 256
+    int stage;                               // mixed: node geometry in shared memory
+    int blocksPerSm;
+    int chunk;                               // steps per instance per launch
+};
+
+// Launchers (k_batch.cu).
+int batch_max_blocks_per_sm(bool mixed, const BatchShape &shape, int maxNodes);
+size_t batch_shared_bytes(bool mixed, const BatchShape &shape, int maxNodes);
+void launch_batch_initial(const Dev &d, const BatchDev &b, bool mixed, cudaStream_t st);
+void launch_batch_arm(const BatchDev &b, long long maxSteps, cudaStream_t st);
+cudaError_t launch_batch_steps(const Dev &d, const BatchDev &b, bool mixed,
+                               const BatchShape &shape, int sms, cudaStream_t st);
+void launch_batch_measure(const Dev &d, const BatchDev &b, cudaStream_t st);
+
+// Set-up helpers of api.cu shared with api_batch.cu.
+const char *validate_material(const nf_material &m);
+MatDev material_constants(const nf_material &m, int formulation);
+double material_wave(const nf_material &m);
+MatF material_constants_f32(const MatDev &m);
+double element_signed_area(const double *r, const double *z, const int32_t *conn, int e);
+void setup_lumped_mass(const double *r, const double *z, const int32_t *conn, int E,
+                       const nf_material *materials, const int32_t *emat, bool axi,
+                       double thickness, double *mass);
+void setup_node_slots(const int32_t *conn, int N, int E, const int32_t *pedges, int K,
+                      int32_t *slotStart, int32_t *slots);
+double setup_min_edge(const double *r, const double *z, const int32_t *conn, int E);
+void set_thread_error(const char *message);
+
 // Launchers (k_step.cu). Each returns the number of kernels it enqueued.
 int launch_initial_assembly(Solver &S);
 int launch_step(Solver &S, bool predicated);

@@ -12,7 +12,10 @@ and through the CPU oracle) and returns ``(solver, mesh, info)``.
 * ``two_blocks``   -- Bench.build (Bench.java:142-169): two copper bodies, optional damage,
                      floor and contact;
 * ``tube``         -- the pressurised thin wall of DefectBurst.fire / BurstCase.run
-                     (QuadMesh.cylinderWall, smoothstep pressure ramp, relaxation damping).
+                     (QuadMesh.cylinderWall, smoothstep pressure ramp, relaxation damping);
+* ``taylor_sweep`` -- a sweep of Taylor rods with drawn meshes, Johnson-Cook constants,
+                     friction and speeds (the batched workload; Sweep.over over
+                     TaylorImpactCase.run).
 """
 from __future__ import annotations
 
@@ -194,3 +197,86 @@ def tube(cls, inner=19.6e-3, outer=20.4e-3, height=4.0e-3, nr=4, nz=20, pressure
         eps = field.sampleOnto(mesh)
         s.setDamage(np.full(mesh.elementCount, 60.0e3), eps)
     return s, mesh, {}
+
+
+# ---------------------------------------------------------------------------- the Taylor sweep
+
+SWEEP_SEED = 20250611
+SWEEP_T_END = 80.0e-6
+
+
+class SplitMix64:
+    """The SplitMix64 generator (Steele, Lea and Flood, "Fast splittable pseudorandom number
+    generators", OOPSLA 2014): a Weyl sequence through a 64-bit finaliser."""
+
+    MASK = (1 << 64) - 1
+
+    def __init__(self, seed: int):
+        self.state = seed & self.MASK
+
+    def next(self) -> int:
+        self.state = (self.state + 0x9E3779B97F4A7C15) & self.MASK
+        z = self.state
+        z = ((z ^ (z >> 30)) * 0xBF58476D1CE4E5B9) & self.MASK
+        z = ((z ^ (z >> 27)) * 0x94D049BB133111EB) & self.MASK
+        return z ^ (z >> 31)
+
+    def uniform(self, lo: float = 0.0, hi: float = 1.0) -> float:
+        return lo + (hi - lo) * ((self.next() >> 11) * (1.0 / (1 << 53)))
+
+    def integer(self, lo: int, hi: int) -> int:
+        """Uniform on lo .. hi inclusive."""
+        return lo + int(self.uniform() * (hi - lo + 1))
+
+
+def rod_material_with(jc: JohnsonCook) -> Material:
+    """The rod steel with a drawn Johnson-Cook law; the kinematic modulus follows the law's
+    secant at the fit strain, as for the 10 x 60 rod."""
+    secant = jc.b * ROD_FIT_STRAIN ** jc.n / ROD_FIT_STRAIN
+    base = Material("rod steel", 200.0e9, 0.29, 7850.0)
+    return base.withKinematicHardening(ROD_KINEMATIC_FRACTION * secant).withJohnsonCook(jc)
+
+
+def taylor_sweep(count: int = 4096, seed: int = SWEEP_SEED, t_end: float = SWEEP_T_END):
+    """Draws the rods of the Taylor sweep: nr uniform on 6..24, nz on 30..120; Johnson-Cook A,
+    B, n and C each uniform within +-20 % of the 10 x 60 rod's; friction uniform on [0, 0.2];
+    impact speed uniform on [150, 250] m/s. Returns one dict per rod, in draw order."""
+    g = SplitMix64(seed)
+    rods = []
+    for _ in range(count):
+        nr = g.integer(6, 24)
+        nz = g.integer(30, 120)
+        a = ROD_JC.a * g.uniform(0.8, 1.2)
+        b = ROD_JC.b * g.uniform(0.8, 1.2)
+        n = ROD_JC.n * g.uniform(0.8, 1.2)
+        c = ROD_JC.c * g.uniform(0.8, 1.2)
+        mu = g.uniform(0.0, 0.2)
+        speed = g.uniform(150.0, 250.0)
+        rods.append({"nr": nr, "nz": nz, "a": a, "b": b, "n": n, "c": c, "mu": mu,
+                     "speed": speed, "t_end": t_end})
+    return rods
+
+
+def _rod_jc(rod) -> JohnsonCook:
+    j = ROD_JC
+    return JohnsonCook(rod["a"], rod["b"], rod["n"], rod["c"], j.m, j.referenceStrainRate,
+                       j.roomTemperature, j.meltTemperature, j.specificHeat, j.taylorQuinney)
+
+
+def sweep_instances(rods, radius=3.8e-3, length=25.0e-3, hourglass=0.10):
+    """The batch instances of drawn rods (what taylor_rod builds, one per rod)."""
+    from .batch import Instance
+    out = []
+    for rod in rods:
+        nr, nz = rod["nr"], rod["nz"]
+        out.append(Instance(mesh=QuadMesh.solidCylinder(radius, length, nr, nz),
+                            material=rod_material_with(_rod_jc(rod)), t_end=rod["t_end"],
+                            velocity=(0.0, -rod["speed"]), wall=(0.0, rod["mu"]),
+                            hourglass=hourglass, fixed_radial=QuadMesh.axisNodes(nr, nz)))
+    return out
+
+
+def sweep_rod(cls, rod, **kw):
+    """One drawn rod as a single scene (the twin of its batch instance)."""
+    return taylor_rod(cls, nr=rod["nr"], nz=rod["nz"], speed=rod["speed"], friction=rod["mu"],
+                      material=rod_material_with(_rod_jc(rod)), **kw)

@@ -10,6 +10,7 @@ import os
 import subprocess
 
 from neofiz_gb300 import _abi
+from neofiz_gb300.batch import BatchSolver
 from neofiz_gb300.solver import ExplicitSolver
 
 HERE = os.path.dirname(os.path.abspath(__file__))
@@ -53,6 +54,15 @@ def api():
 
 class OracleSolver(ExplicitSolver):
     """The reference algorithm on the CPU, behind the product's facade."""
+
+    @classmethod
+    def _binding(cls):
+        return api()
+
+
+class OracleBatch(BatchSolver):
+    """The reference's sweep (one CPU solver per instance, a thread pool over instances)
+    behind the product's batch facade. NFO_THREADS sets the pool size."""
 
     @classmethod
     def _binding(cls):

@@ -45,6 +45,7 @@
 #include <stdlib.h>
 #include <string.h>
 #include <float.h>
+#include <time.h>
 
 #define COMPONENTS 4
 #define GEOMETRY_STRIDE 5
@@ -2022,3 +2023,198 @@ API nf_status nfo_profile_read(nfo_solver *h, double *ms, int64_t *steps) {
     return NF_OK;
 }
 API nf_status nfo_launch_count(nfo_solver *h, int64_t *launches) { (void)h; *launches = 0; return NF_OK; }
+
+/* ------------------------------------------------------------------ batched scenes */
+
+/* The batched surface of include/neofiz.h as the reference runs a sweep: one solver per
+ * instance, a pool of host threads over the instances (Sweep.over, app/Sweep.java:82-105),
+ * each instance stepped while time < t_end. Every instance is FP64 whatever precision is
+ * asked for (the oracle has one precision); launch shapes do not exist here, so the config
+ * calls only store and echo what they are given. */
+struct nfo_batch {
+    int count;
+    nfo_solver **s;
+    double *tEnd;
+    int32_t *nodeOff, *elemOff;
+    int threads;
+    double lastMs;
+    nf_batch_config config;
+    char err[512];
+    /* the pool's shared cursor */
+    pthread_mutex_t lock;
+    int next;
+    int64_t maxSteps;
+};
+typedef struct nfo_batch nfo_batch;
+
+static char g_batch_err[512];
+
+static nf_status bfail(nfo_batch *b, nf_status st, const char *fmt, ...) {
+    va_list ap;
+    va_start(ap, fmt);
+    vsnprintf(b ? b->err : g_batch_err, 512, fmt, ap);
+    va_end(ap);
+    return st;
+}
+
+API const char *nfo_batch_last_error(const nfo_batch *b) { return b ? b->err : g_batch_err; }
+
+API nf_status nfo_batch_destroy(nfo_batch *b) {
+    if (!b) return NF_OK;
+    for (int k = 0; k < b->count; k++) nfo_destroy(b->s[k]);
+    free(b->s); free(b->tEnd); free(b->nodeOff); free(b->elemOff);
+    pthread_mutex_destroy(&b->lock);
+    free(b);
+    return NF_OK;
+}
+
+API nf_status nfo_batch_create(const nf_batch_mesh *mesh, const nf_batch_instance *inst,
+                               int32_t formulation, int32_t kinematics, double thickness,
+                               double cfl_safety, int32_t precision, nfo_batch **out) {
+    *out = NULL;
+    if (!mesh || !inst || mesh->instance_count < 1)
+        return bfail(NULL, NF_EINVAL, "a batch needs at least one instance and its mesh arrays");
+    if (precision != NF_PRECISION_FP64 && precision != NF_PRECISION_MIXED)
+        return bfail(NULL, NF_EINVAL, "unknown precision %d", precision);
+    const int count = mesh->instance_count;
+    nfo_batch *b = (nfo_batch *)calloc(1, sizeof *b);
+    b->count = count;
+    b->s = (nfo_solver **)calloc((size_t)count, sizeof *b->s);
+    b->tEnd = (double *)calloc((size_t)count, sizeof(double));
+    b->nodeOff = ialloc((size_t)count + 1);
+    b->elemOff = ialloc((size_t)count + 1);
+    pthread_mutex_init(&b->lock, NULL);
+    b->config.threads = 1;
+    b->config.blocks_per_sm = 1;
+    b->config.chunk_steps = 1;
+    const char *env = getenv("NFO_THREADS");
+    b->threads = env ? atoi(env) : 1;
+    if (b->threads < 1) b->threads = 1;
+    memcpy(b->nodeOff, mesh->node_offset, sizeof(int32_t) * ((size_t)count + 1));
+    memcpy(b->elemOff, mesh->element_offset, sizeof(int32_t) * ((size_t)count + 1));
+    for (int k = 0; k < count; k++) {
+        const int n0 = mesh->node_offset[k], e0 = mesh->element_offset[k];
+        nf_mesh m;
+        m.node_count = mesh->node_offset[k + 1] - n0;
+        m.element_count = mesh->element_offset[k + 1] - e0;
+        m.pressure_edge_count = 0;
+        m.r = mesh->r + n0;
+        m.z = mesh->z + n0;
+        m.conn = mesh->conn + 4 * (size_t)e0;
+        m.pressure_edges = NULL;
+        nf_status st = nfo_create(&m, &inst[k].material, 1, NULL, formulation, NF_REDUCED,
+                                  kinematics, thickness, cfl_safety, &b->s[k]);
+        if (!st) st = nfo_set_hourglass_coefficient(b->s[k], inst[k].hourglass);
+        for (int i = 0; !st && mesh->fixed && i < m.node_count; i++) {
+            if (mesh->fixed[n0 + i] & 1) st = nfo_fix_radial(b->s[k], i);
+            if (!st && (mesh->fixed[n0 + i] & 2)) st = nfo_fix_axial(b->s[k], i);
+        }
+        if (!st && inst[k].wall_plane == inst[k].wall_plane)
+            st = nfo_set_rigid_wall(b->s[k], inst[k].wall_plane, inst[k].wall_friction);
+        if (!st) st = nfo_set_uniform_velocity(b->s[k], inst[k].velocity_r, inst[k].velocity_z);
+        if (st) {
+            bfail(NULL, st, "instance %d: %s", k, b->s[k] ? nfo_last_error(b->s[k]) : nfo_last_error(NULL));
+            nfo_batch_destroy(b);
+            return st;
+        }
+        b->tEnd[k] = inst[k].t_end;
+    }
+    *out = b;
+    return NF_OK;
+}
+
+API nf_status nfo_batch_tune(nfo_batch *b, int32_t trial_steps, nf_batch_config *chosen) {
+    (void)trial_steps;
+    if (chosen) *chosen = b->config;
+    return NF_OK;
+}
+API nf_status nfo_batch_set_config(nfo_batch *b, const nf_batch_config *c) {
+    b->config = *c;
+    return NF_OK;
+}
+API nf_status nfo_batch_get_config(nfo_batch *b, nf_batch_config *c) {
+    *c = b->config;
+    return NF_OK;
+}
+
+static void *batch_worker(void *arg) {
+    nfo_batch *b = (nfo_batch *)arg;
+    for (;;) {
+        pthread_mutex_lock(&b->lock);
+        const int k = b->next++;
+        pthread_mutex_unlock(&b->lock);
+        if (k >= b->count) return NULL;
+        nfo_run_until(b->s[k], b->tEnd[k], b->maxSteps, NULL);
+    }
+}
+
+API nf_status nfo_batch_run(nfo_batch *b, int64_t max_steps) {
+    struct timespec t0, t1;
+    clock_gettime(CLOCK_MONOTONIC, &t0);
+    b->next = 0;
+    b->maxSteps = max_steps;
+    const int n = b->threads < b->count ? b->threads : b->count;
+    pthread_t *tid = (pthread_t *)calloc((size_t)n, sizeof(pthread_t));
+    for (int t = 1; t < n; t++) pthread_create(&tid[t], NULL, batch_worker, b);
+    batch_worker(b);
+    for (int t = 1; t < n; t++) pthread_join(tid[t], NULL);
+    free(tid);
+    clock_gettime(CLOCK_MONOTONIC, &t1);
+    b->lastMs = (double)(t1.tv_sec - t0.tv_sec) * 1e3 + (double)(t1.tv_nsec - t0.tv_nsec) * 1e-6;
+    return NF_OK;
+}
+
+API nf_status nfo_batch_elapsed(nfo_batch *b, double *ms) { *ms = b->lastMs; return NF_OK; }
+API nf_status nfo_batch_launch_count(nfo_batch *b, int64_t *n) { (void)b; *n = 0; return NF_OK; }
+
+API nf_status nfo_batch_field_size(nfo_batch *b, int32_t field, size_t *count, size_t *bytes) {
+    size_t total = 0, eb = 8;
+    for (int k = 0; k < b->count; k++) {
+        size_t c;
+        nf_status st = nfo_field_size(b->s[k], field, &c, &eb);
+        if (st) return bfail(b, st, "%s", nfo_last_error(b->s[k]));
+        total += c;
+    }
+    *count = total;
+    *bytes = eb;
+    return NF_OK;
+}
+
+API nf_status nfo_batch_read(nfo_batch *b, int32_t field, void *dst, size_t nbytes) {
+    size_t total, eb;
+    nf_status st = nfo_batch_field_size(b, field, &total, &eb);
+    if (st) return st;
+    if (nbytes < total * eb) return bfail(b, NF_EINVAL, "buffer smaller than the field");
+    char *o = (char *)dst;
+    for (int k = 0; k < b->count; k++) {
+        size_t c;
+        nfo_field_size(b->s[k], field, &c, &eb);
+        st = nfo_read_field(b->s[k], field, o, c * eb);
+        if (st) return bfail(b, st, "%s", nfo_last_error(b->s[k]));
+        o += c * eb;
+    }
+    return NF_OK;
+}
+
+API nf_status nfo_batch_state(nfo_batch *b, nf_batch_progress *out) {
+    for (int k = 0; k < b->count; k++) {
+        nf_state s;
+        nfo_get_state(b->s[k], &s);
+        out[k].time = s.time;
+        out[k].timestep = s.timestep;
+        out[k].steps = s.steps;
+        out[k].status = 0;
+        out[k].done = !(s.time < b->tEnd[k]);
+    }
+    return NF_OK;
+}
+
+API nf_status nfo_batch_measure(nfo_batch *b, nf_measure *out) {
+    for (int k = 0; k < b->count; k++) nfo_measure_body(b->s[k], &out[k]);
+    return NF_OK;
+}
+
+API nf_status nfo_batch_wall_stats(nfo_batch *b, nf_wall_info *out) {
+    for (int k = 0; k < b->count; k++) nfo_wall_stats(b->s[k], &out[k]);
+    return NF_OK;
+}

@@ -62,9 +62,11 @@ def test_struct_layouts_match_the_header():
     """Sizes of the ctypes mirrors against a C compile of the header."""
     from neofiz_gb300 import _abi
     src = ("#include <stdio.h>\n#include \"neofiz.h\"\nint main(){printf(\"%zu %zu %zu %zu %zu "
-           "%zu %zu %zu\\n\", sizeof(nf_mesh), sizeof(nf_material), sizeof(nf_state), "
-           "sizeof(nf_audit), sizeof(nf_wall_info), sizeof(nf_contact_info), sizeof(nf_measure), "
-           "sizeof(nf_damage_points)); return 0;}\n")
+           "%zu %zu %zu %zu %zu %zu %zu\\n\", sizeof(nf_mesh), sizeof(nf_material), "
+           "sizeof(nf_state), sizeof(nf_audit), sizeof(nf_wall_info), sizeof(nf_contact_info), "
+           "sizeof(nf_measure), sizeof(nf_damage_points), sizeof(nf_batch_mesh), "
+           "sizeof(nf_batch_instance), sizeof(nf_batch_config), sizeof(nf_batch_progress)); "
+           "return 0;}\n")
     import tempfile
     with tempfile.TemporaryDirectory() as d:
         c = os.path.join(d, "s.c")
@@ -74,7 +76,8 @@ def test_struct_layouts_match_the_header():
         sizes = [int(x) for x in subprocess.check_output([exe]).split()]
     mine = [ctypes.sizeof(t) for t in (_abi.Mesh, _abi.MaterialC, _abi.State, _abi.Audit,
                                         _abi.WallInfo, _abi.ContactInfo, _abi.Measure,
-                                        _abi.DamagePoints)]
+                                        _abi.DamagePoints, _abi.BatchMesh, _abi.BatchInstance,
+                                        _abi.BatchConfig, _abi.BatchProgress)]
     assert sizes == mine
 
 
