@@ -395,6 +395,33 @@ nf_status nf_batch_state(nf_batch *b, nf_batch_progress *out);
 nf_status nf_batch_measure(nf_batch *b, nf_measure *out);
 nf_status nf_batch_wall_stats(nf_batch *b, nf_wall_info *out);
 
+/* ------------------------------------------------------------------ adjoint */
+
+/* No counterpart in the reference. Gradients of a batch's final measurements with respect to
+ * material and wall parameters, by a hand-written reverse sweep of the whole timestep: the
+ * forward pass runs every instance to its t_end (N steps) keeping a checkpoint every
+ * checkpoint_every steps; the backward pass recomputes each segment from its checkpoint and
+ * runs the adjoint of every step in reverse. The elastic/plastic branch of each point, the
+ * rate and temperature clamps, the wall's hold/stick/slip/arrive state of each node and the
+ * element that sets each CFL step are those of the forward pass (frozen). Objectives are
+ * taken after the N steps: the length ratio L/L0 (TaylorImpactCase.java:272-279) or the
+ * mushroom diameter 2 max(r + ur) (:281-288). FP64 batches with reduced integration and no
+ * damage, erosion, contact or pressure. */
+enum { NF_OBJECTIVE_LENGTH_RATIO = 0, NF_OBJECTIVE_MUSHROOM = 1 };
+/* Gradient components: Johnson-Cook A, B, n, C, m (JohnsonCook.java:66-69), the kinematic
+ * hardening modulus (Material.java:20-21) and the wall friction coefficient
+ * (RigidWall.atZ, RigidWall.java:121-136). */
+enum { NF_PARAM_A = 0, NF_PARAM_B, NF_PARAM_N, NF_PARAM_C, NF_PARAM_M, NF_PARAM_KINEMATIC,
+       NF_PARAM_FRICTION, NF_PARAM_COUNT };
+
+nf_status nf_batch_adjoint_forward(nf_batch *b, int32_t checkpoint_every);
+/* values[instance_count]; gradients[instance_count * NF_PARAM_COUNT]. May be called once per
+ * objective after one forward pass. */
+nf_status nf_batch_adjoint_backward(nf_batch *b, int32_t objective, double *values,
+                                    double *gradients);
+/* Device (or, for the CPU restatement, wall) time of the last forward and backward passes. */
+nf_status nf_batch_adjoint_elapsed(nf_batch *b, double *forward_ms, double *backward_ms);
+
 #ifdef __cplusplus
 }
 #endif

@@ -26,6 +26,11 @@ GROUP_NAMES = ("nodal", "erode", "element", "pressure", "gather", "contact", "en
 
 PRECISION_FP64, PRECISION_MIXED = 0, 1
 
+OBJECTIVE_LENGTH_RATIO, OBJECTIVE_MUSHROOM = 0, 1
+(PARAM_A, PARAM_B, PARAM_N, PARAM_C, PARAM_M, PARAM_KINEMATIC, PARAM_FRICTION) = range(7)
+PARAM_COUNT = 7
+PARAM_NAMES = ("A", "B", "n", "C", "m", "kinematic", "friction")
+
 WALL_HELD, WALL_STUCK, WALL_SLID, WALL_ARRIVED = 1, 2, 4, 8
 CONTACT_PAIR, CONTACT_STICK, CONTACT_SLIP = 1, 2, 4
 
@@ -177,6 +182,9 @@ _PROTOS = {
     "batch_state": (_S, [_H, C.POINTER(BatchProgress)]),
     "batch_measure": (_S, [_H, C.POINTER(Measure)]),
     "batch_wall_stats": (_S, [_H, C.POINTER(WallInfo)]),
+    "batch_adjoint_forward": (_S, [_H, C.c_int32]),
+    "batch_adjoint_backward": (_S, [_H, C.c_int32, c_double_p, c_double_p]),
+    "batch_adjoint_elapsed": (_S, [_H, C.POINTER(C.c_double), C.POINTER(C.c_double)]),
 }
 
 ENTRY_POINTS = tuple("nf_" + name for name in _PROTOS)

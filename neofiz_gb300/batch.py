@@ -196,6 +196,28 @@ class BatchSolver:
         self._check(self._api.batch_wall_stats(self._handle, w))
         return list(w)
 
+    # ------------------------------------------------------------------ adjoint
+
+    def adjointForward(self, checkpointEvery: int = 200) -> float:
+        """Runs every instance to its t_end keeping checkpoints (FP64 batches); device ms."""
+        self._check(self._api.batch_adjoint_forward(self._handle, int(checkpointEvery)))
+        return self.adjointElapsed()[0]
+
+    def adjointBackward(self, objective: int = _abi.OBJECTIVE_LENGTH_RATIO):
+        """(values[count], gradients[count, PARAM_COUNT]) of the objective after the forward
+        pass's steps, with respect to A, B, n, C, m, the kinematic modulus and friction."""
+        values = np.zeros(self.count)
+        grads = np.zeros((self.count, _abi.PARAM_COUNT))
+        self._check(self._api.batch_adjoint_backward(
+            self._handle, int(objective), values.ctypes.data_as(_abi.c_double_p),
+            grads.ctypes.data_as(_abi.c_double_p)))
+        return values, grads
+
+    def adjointElapsed(self):
+        f, b = C.c_double(), C.c_double()
+        self._check(self._api.batch_adjoint_elapsed(self._handle, C.byref(f), C.byref(b)))
+        return f.value, b.value
+
     def elementCycles(self) -> int:
         """Element-steps taken so far: sum over instances of elements x steps."""
         steps = self.state()["steps"]

@@ -38,6 +38,13 @@ struct Batch {
     double lastMs = 0.0;
     long long launches = 0;
     std::vector<void *> allocs;
+    // the adjoint's buffers (nf_batch_adjoint_*)
+    AdjDev adj{};
+    std::vector<void *> adjAllocs;
+    bool adjForward = false;
+    double adjForwardMs = 0.0, adjBackwardMs = 0.0;
+    long long adjTapeBytes = 0, adjBarBytes = 0;
+    std::vector<long long> adjBarOff;
 };
 
 constexpr int GRAPH_CHUNKS = 4;              // chunked launches per graph replay
@@ -82,10 +89,18 @@ nf_status bsync(Batch &B) {
     return NF_OK;
 }
 
+void free_adjoint(Batch &B) {
+    for (void *p : B.adjAllocs) cudaFree(p);
+    B.adjAllocs.clear();
+    B.adj = AdjDev{};
+    B.adjForward = false;
+}
+
 void destroy(Batch *B) {
     if (!B) return;
     if (B->stream) cudaStreamSynchronize(B->stream);
     if (B->graph) cudaGraphExecDestroy(B->graph);
+    free_adjoint(*B);
     for (void *p : B->allocs) cudaFree(p);
     if (B->hostRemaining) cudaFreeHost(B->hostRemaining);
     if (B->ev0) cudaEventDestroy(B->ev0);
@@ -649,6 +664,166 @@ nf_status nf_batch_wall_stats(nf_batch *h, nf_wall_info *out) {
         o.contact_count = sc[k].wContact;
         o.stuck_count = sc[k].wStuck;
     }
+    return NF_OK;
+}
+
+}  // extern "C"
+
+// ------------------------------------------------------------------------------------ adjoint
+
+namespace {
+
+template <typename T>
+cudaError_t aalloc(Batch &B, T **p, size_t count) {
+    void *v = nullptr;
+    cudaError_t e = cudaMalloc(&v, sizeof(T) * (count ? count : 1));
+    if (e != cudaSuccess) return e;
+    B.adjAllocs.push_back(v);
+    *p = (T *)v;
+    return cudaMemsetAsync(v, 0, sizeof(T) * (count ? count : 1), B.stream);
+}
+
+}  // namespace
+
+extern "C" {
+
+nf_status nf_batch_adjoint_forward(nf_batch *h, int32_t checkpoint_every) {
+    Batch &B = *reinterpret_cast<Batch *>(h);
+    if (checkpoint_every < 1) return bfail(&B, NF_EINVAL, "checkpoint interval must be positive");
+    if (B.mixed) return bfail(&B, NF_EINVAL, "the adjoint runs on FP64 batches");
+    std::vector<BatchScalars> sc(B.count);
+    BCK(&B, cudaMemcpyAsync(sc.data(), B.b.sc, sizeof(BatchScalars) * B.count,
+                            cudaMemcpyDeviceToHost, B.stream));
+    nf_status st = bsync(B);
+    if (st) return st;
+    for (int k = 0; k < B.count; k++)
+        if (sc[k].steps != 0)
+            return bfail(&B, NF_ESTATE, "the adjoint's forward pass starts from a fresh batch");
+    free_adjoint(B);
+    // checkpoint capacity: 8x the step count the initial CFL step predicts, plus margin
+    std::vector<long long> ckptOff(B.count), finOff(B.count), tapeOff(B.count), barOff(B.count);
+    std::vector<long long> cap(B.count), bytes(B.count);
+    long long ck = 0, fi = 0, ta = 0, ba = 0;
+    for (int k = 0; k < B.count; k++) {
+        const BatchInst &in = B.inst[k];
+        const int n = in.n1 - in.n0, e = in.e1 - in.e0;
+        bytes[k] = (long long)adj_state_bytes(n, e);
+        const double est = sc[k].dt > 0.0 ? 8.0 * in.tEnd / sc[k].dt : 1.0;
+        cap[k] = (long long)(est / checkpoint_every) + 4;
+        ckptOff[k] = ck; ck += cap[k] * bytes[k];
+        finOff[k] = fi; fi += bytes[k];
+        tapeOff[k] = ta; ta += (long long)checkpoint_every * bytes[k];
+        barOff[k] = ba; ba += (long long)adj_bar_bytes(n, e);
+    }
+    AdjDev &a = B.adj;
+    cudaError_t e_ = cudaSuccess;
+    long long *dCkptOff = nullptr, *dFinOff = nullptr, *dTapeOff = nullptr, *dBarOff = nullptr;
+    long long *dCap = nullptr, *dBytes = nullptr;
+#define A(ptr, n) if (e_ == cudaSuccess) e_ = aalloc(B, &(ptr), (n))
+    A(a.ckpt, (size_t)ck); A(a.fin, (size_t)fi);
+    A(dCkptOff, B.count); A(dFinOff, B.count); A(dTapeOff, B.count); A(dBarOff, B.count);
+    A(dCap, B.count); A(dBytes, B.count);
+    A(a.steps, B.count); A(a.grad, (size_t)B.count * NF_PARAM_COUNT); A(a.overflow, 1);
+#undef A
+    if (e_ != cudaSuccess) {
+        free_adjoint(B);
+        return bfail(&B, NF_ENOMEM, "adjoint allocation failed: %s", cudaGetErrorString(e_));
+    }
+    BCK(&B, cudaMemcpyAsync(dCkptOff, ckptOff.data(), 8 * B.count, cudaMemcpyHostToDevice, B.stream));
+    BCK(&B, cudaMemcpyAsync(dFinOff, finOff.data(), 8 * B.count, cudaMemcpyHostToDevice, B.stream));
+    BCK(&B, cudaMemcpyAsync(dTapeOff, tapeOff.data(), 8 * B.count, cudaMemcpyHostToDevice, B.stream));
+    BCK(&B, cudaMemcpyAsync(dBarOff, barOff.data(), 8 * B.count, cudaMemcpyHostToDevice, B.stream));
+    BCK(&B, cudaMemcpyAsync(dCap, cap.data(), 8 * B.count, cudaMemcpyHostToDevice, B.stream));
+    BCK(&B, cudaMemcpyAsync(dBytes, bytes.data(), 8 * B.count, cudaMemcpyHostToDevice, B.stream));
+    a.ckptOff = dCkptOff; a.finOff = dFinOff; a.tapeOff = dTapeOff; a.barOff = dBarOff;
+    a.ckptCap = dCap; a.stateBytes = dBytes;
+    a.every = checkpoint_every;
+    // the tape and adjoint arrays are allocated by the backward pass
+    a.tape = nullptr;
+    a.bar = nullptr;
+    B.adjTapeBytes = ta;
+    B.adjBarBytes = ba;
+    B.adjBarOff = barOff;
+    BCK(&B, cudaEventRecord(B.ev0, B.stream));
+    launch_adjoint_forward(B.d, B.b, a, B.stream);
+    B.launches += 1;
+    BCK(&B, cudaEventRecord(B.ev1, B.stream));
+    st = bsync(B);
+    if (st) return st;
+    int overflow = 0;
+    BCK(&B, cudaMemcpy(&overflow, a.overflow, sizeof overflow, cudaMemcpyDeviceToHost));
+    if (overflow) {
+        free_adjoint(B);
+        return bfail(&B, NF_ESTATE, "an instance took more steps than its checkpoint capacity");
+    }
+    float ms = 0.0f;
+    BCK(&B, cudaEventElapsedTime(&ms, B.ev0, B.ev1));
+    B.adjForwardMs = ms;
+    B.adjForward = true;
+    return NF_OK;
+}
+
+nf_status nf_batch_adjoint_backward(nf_batch *h, int32_t objective, double *values,
+                                    double *gradients) {
+    Batch &B = *reinterpret_cast<Batch *>(h);
+    if (!B.adjForward) return bfail(&B, NF_ESTATE, "run the adjoint's forward pass first");
+    if (objective != NF_OBJECTIVE_LENGTH_RATIO && objective != NF_OBJECTIVE_MUSHROOM)
+        return bfail(&B, NF_EINVAL, "unknown objective %d", objective);
+    AdjDev &a = B.adj;
+    cudaError_t e_ = cudaSuccess;
+    if (!a.tape) {
+        e_ = aalloc(B, &a.tape, (size_t)B.adjTapeBytes);
+        if (e_ == cudaSuccess) e_ = aalloc(B, &a.bar, (size_t)B.adjBarBytes);
+        if (e_ != cudaSuccess) return bfail(&B, NF_ENOMEM, "adjoint allocation failed: %s",
+                                            cudaGetErrorString(e_));
+    }
+    // the objective and its seed (the adjoint of the final displacements), per instance
+    std::vector<double2> X0(B.N), U(B.N);
+    BCK(&B, cudaMemcpy(X0.data(), B.d.X0, 16 * (size_t)B.N, cudaMemcpyDeviceToHost));
+    BCK(&B, cudaMemcpy(U.data(), B.d.U, 16 * (size_t)B.N, cudaMemcpyDeviceToHost));
+    std::vector<char> bar((size_t)B.adjBarBytes, 0);
+    for (int k = 0; k < B.count; k++) {
+        const BatchInst &in = B.inst[k];
+        double zmax = -DBL_MAX, zmin = DBL_MAX, z0max = -DBL_MAX, z0min = DBL_MAX, rmax = -DBL_MAX;
+        int imax = in.n0, imin = in.n0, irmax = in.n0;
+        for (int i = in.n0; i < in.n1; i++) {
+            const double z = X0[i].y + U[i].y, r = X0[i].x + U[i].x;
+            if (z > zmax) { zmax = z; imax = i; }
+            if (z < zmin) { zmin = z; imin = i; }
+            if (r > rmax) { rmax = r; irmax = i; }
+            if (X0[i].y > z0max) z0max = X0[i].y;
+            if (X0[i].y < z0min) z0min = X0[i].y;
+        }
+        double2 *ub = reinterpret_cast<double2 *>(bar.data() + B.adjBarOff[k]);
+        if (objective == NF_OBJECTIVE_LENGTH_RATIO) {
+            const double L0 = z0max - z0min;
+            ub[imax - in.n0].y += 1.0 / L0;
+            ub[imin - in.n0].y -= 1.0 / L0;
+            values[k] = (zmax - zmin) / L0;
+        } else {
+            ub[irmax - in.n0].x += 2.0;
+            values[k] = 2.0 * rmax;
+        }
+    }
+    BCK(&B, cudaMemcpyAsync(a.bar, bar.data(), bar.size(), cudaMemcpyHostToDevice, B.stream));
+    BCK(&B, cudaEventRecord(B.ev0, B.stream));
+    launch_adjoint_backward(B.d, B.b, a, B.stream);
+    B.launches += 1;
+    BCK(&B, cudaEventRecord(B.ev1, B.stream));
+    nf_status st = bsync(B);
+    if (st) return st;
+    float ms = 0.0f;
+    BCK(&B, cudaEventElapsedTime(&ms, B.ev0, B.ev1));
+    B.adjBackwardMs = ms;
+    BCK(&B, cudaMemcpy(gradients, a.grad, sizeof(double) * NF_PARAM_COUNT * B.count,
+                       cudaMemcpyDeviceToHost));
+    return NF_OK;
+}
+
+nf_status nf_batch_adjoint_elapsed(nf_batch *h, double *forward_ms, double *backward_ms) {
+    const Batch &B = *reinterpret_cast<Batch *>(h);
+    *forward_ms = B.adjForwardMs;
+    *backward_ms = B.adjBackwardMs;
     return NF_OK;
 }
 

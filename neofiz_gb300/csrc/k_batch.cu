@@ -15,57 +15,11 @@
 // Launch shape: block size (128, 256), whether the mixed form stages each instance's float
 // node geometry in shared memory, blocks per SM and the chunk length are chosen by the
 // autotuner (api_batch.cu); none of them changes the trajectory.
-#include "nf_bodies.cuh"
+#include "nf_batch_step.cuh"
 
 namespace nf {
 
 constexpr int MEASURE_BLOCK = 256;
-
-__device__ __forceinline__ unsigned long long bbits(double x) {
-    return (unsigned long long)__double_as_longlong(x);
-}
-__device__ __forceinline__ double bdouble(unsigned long long u) {
-    return __longlong_as_double((long long)u);
-}
-
-// Exact block minimum of the per-thread shortest squared edges, returned to every thread. The
-// warps combine with jmin and the warps' results by the integer order of their bits, as the
-// single-scene kernels do with shuffles and atomicMin.
-template <int T>
-__device__ double block_min_edge(double v, double *sh) {
-    for (int o = 16; o > 0; o >>= 1) v = jmin(v, __shfl_down_sync(0xffffffffu, v, o));
-    const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
-    if (lane == 0) sh[warp] = v;
-    __syncthreads();
-    if (threadIdx.x == 0) {
-        unsigned long long m = bbits(sh[0]);
-        for (int w = 1; w < T / 32; w++) m = min(m, bbits(sh[w]));
-        sh[T / 32] = bdouble(m);
-    }
-    __syncthreads();
-    return sh[T / 32];
-}
-
-template <int T>
-__device__ double block_min_edge_f(float v, double *sh) {
-    for (int o = 16; o > 0; o >>= 1) v = fminf(v, __shfl_down_sync(0xffffffffu, v, o));
-    return block_min_edge<T>((double)v, sh);
-}
-
-// Fixed-tree block sum; valid in thread 0.
-template <int T>
-__device__ double block_total(double v, double *sh) {
-    for (int o = 16; o > 0; o >>= 1) v += __shfl_down_sync(0xffffffffu, v, o);
-    const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
-    __syncthreads();
-    if (lane == 0) sh[warp] = v;
-    __syncthreads();
-    double t = 0.0;
-    if (threadIdx.x == 0)
-        for (int w = 0; w < T / 32; w++) t += sh[w];
-    __syncthreads();
-    return t;
-}
 
 // Up to `chunk` steps of instance k by the whole block: ExplicitSolver.step, :940-991, with the
 // loop condition of TaylorImpactCase.java:250-253 (step while time < t_end).
@@ -101,37 +55,9 @@ __device__ void run_instance(const Dev &d, const BatchDev &b, int k, int chunk, 
             wallCount[par ^ 1][0] = 0;
             wallCount[par ^ 1][1] = 0;
         }
-        const double dtAvg = 0.5 * (dtPrev + dt);                   // :947-956
-        const double half = 0.5 * in.damping * dtAvg;
-        const NodalCoef co{(1.0 - half) / (1.0 + half), dtAvg / (1.0 + half), dtAvg, dt};
-        const WallRef w{in.hasWall, in.wallPlane, in.wallFriction, &wallCount[par][0],
-                        &wallCount[par][1]};
-        for (int i = in.n0 + tid; i < in.n1; i += T)
-            nodal_node(d, i, co, w, geo, &scp->status, impulse, loss, fric);
-        __syncthreads();
-        time += dt;                                                   // :973-974
-        steps += 1;
-        double me;
-        if (MIXED) {
-            float m = 3.4028235e38f;
-            const float sdt = (float)dt, qhg = (float)in.hourglass;
-            for (int e = in.e0 + tid; e < in.e1; e += T)
-                element_reduced_f32(d, e, sdt, qhg, pMid, vdt, base, m);
-            me = block_min_edge_f<T>(m, shMin);
-        } else {
-            double m = DMAX;
-            for (int e = in.e0 + tid; e < in.e1; e += T) element_reduced(d, e, dt, in.hourglass, m);
-            me = block_min_edge<T>(m, shMin);
-        }
-        // the gather keeps the nodal loop's node-to-thread map, so the next nodal update reads
-        // only forces its own thread wrote
-        for (int i = in.n0 + tid; i < in.n1; i += T)
-            d.F[i] = MIXED ? gather_node_f32(d, i) : gather_node(d, i);
-        minEdge = me;                                                 // :985-990
-        if (d.finite) {
-            dtPrev = dt;
-            dt = in.cfl * sqrt(me * in.massScale) / in.wave;
-        }
+        minEdge = batch_step<MIXED, T>(d, in, dt, dtPrev, time, steps, geo, pMid, vdt, base,
+                                       &scp->status, &wallCount[par][0], &wallCount[par][1],
+                                       impulse, loss, fric, shMin);
     }
     const double ti = block_total<T>(impulse, shMin);
     const double tl = block_total<T>(loss, shMin);

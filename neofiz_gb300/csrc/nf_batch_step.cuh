@@ -1,0 +1,98 @@
+// nf_batch_step.cuh -- one step of one batched instance by a whole block, shared by the
+// batched kernel (k_batch.cu) and the adjoint kernels (k_adjoint.cu).
+#pragma once
+
+#include "nf_bodies.cuh"
+
+namespace nf {
+
+__device__ __forceinline__ unsigned long long bbits(double x) {
+    return (unsigned long long)__double_as_longlong(x);
+}
+__device__ __forceinline__ double bdouble(unsigned long long u) {
+    return __longlong_as_double((long long)u);
+}
+
+// Exact block minimum of the per-thread shortest squared edges, returned to every thread. The
+// warps combine with jmin and the warps' results by the integer order of their bits, as the
+// single-scene kernels do with shuffles and atomicMin.
+template <int T>
+__device__ double block_min_edge(double v, double *sh) {
+    for (int o = 16; o > 0; o >>= 1) v = jmin(v, __shfl_down_sync(0xffffffffu, v, o));
+    const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
+    if (lane == 0) sh[warp] = v;
+    __syncthreads();
+    if (threadIdx.x == 0) {
+        unsigned long long m = bbits(sh[0]);
+        for (int w = 1; w < T / 32; w++) m = min(m, bbits(sh[w]));
+        sh[T / 32] = bdouble(m);
+    }
+    __syncthreads();
+    return sh[T / 32];
+}
+
+template <int T>
+__device__ double block_min_edge_f(float v, double *sh) {
+    for (int o = 16; o > 0; o >>= 1) v = fminf(v, __shfl_down_sync(0xffffffffu, v, o));
+    return block_min_edge<T>((double)v, sh);
+}
+
+// Fixed-tree block sum; valid in thread 0.
+template <int T>
+__device__ double block_total(double v, double *sh) {
+    for (int o = 16; o > 0; o >>= 1) v += __shfl_down_sync(0xffffffffu, v, o);
+    const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
+    __syncthreads();
+    if (lane == 0) sh[warp] = v;
+    __syncthreads();
+    double t = 0.0;
+    if (threadIdx.x == 0)
+        for (int w = 0; w < T / 32; w++) t += sh[w];
+    __syncthreads();
+    return t;
+}
+
+// One step of instance `in` by the whole block, ExplicitSolver.step :940-991: the nodal update
+// (with the mixed form's float geometry when geo.pMid is set), the assembly with the block's
+// exact shortest squared edge, the per-node gather, the next CFL step. dt, dtPrev, time and
+// steps advance in place; returns the shortest squared edge.
+template <bool MIXED, int T>
+__device__ __forceinline__ double batch_step(const Dev &d, const BatchInst &in, double &dt,
+                                             double &dtPrev, double &time, long long &steps,
+                                             const MixedGeo &geo, const float4 *pMid,
+                                             const float2 *vdt, int base, uint32_t *status,
+                                             int *wallContact, int *wallStuck, double &impulse,
+                                             double &loss, double &fric, double *shMin) {
+    const double dtAvg = 0.5 * (dtPrev + dt);                       // :947-956
+    const double half = 0.5 * in.damping * dtAvg;
+    const NodalCoef co{(1.0 - half) / (1.0 + half), dtAvg / (1.0 + half), dtAvg, dt};
+    const WallRef w{in.hasWall, in.wallPlane, in.wallFriction, wallContact, wallStuck};
+    for (int i = in.n0 + threadIdx.x; i < in.n1; i += T)
+        nodal_node(d, i, co, w, geo, status, impulse, loss, fric);
+    __syncthreads();
+    time += dt;                                                       // :973-974
+    steps += 1;
+    double me;
+    if (MIXED) {
+        float m = 3.4028235e38f;
+        const float sdt = (float)dt, qhg = (float)in.hourglass;
+        for (int e = in.e0 + threadIdx.x; e < in.e1; e += T)
+            element_reduced_f32(d, e, sdt, qhg, pMid, vdt, base, m);
+        me = block_min_edge_f<T>(m, shMin);
+    } else {
+        double m = DMAX;
+        for (int e = in.e0 + threadIdx.x; e < in.e1; e += T) element_reduced(d, e, dt, in.hourglass, m);
+        me = block_min_edge<T>(m, shMin);
+    }
+    // the gather keeps the nodal loop's node-to-thread map, so the next nodal update reads
+    // only forces its own thread wrote
+    for (int i = in.n0 + threadIdx.x; i < in.n1; i += T)
+        d.F[i] = MIXED ? gather_node_f32(d, i) : gather_node(d, i);
+    if (d.finite) {                                                   // :985-990
+        dtPrev = dt;
+        dt = in.cfl * sqrt(me * in.massScale) / in.wave;
+    }
+    return me;
+}
+
+}  // namespace nf

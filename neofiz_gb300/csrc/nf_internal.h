@@ -228,6 +228,23 @@ struct BatchDev {
     int maxNodes;                            // the largest instance's node count
 };
 
+// The adjoint's device buffers (k_adjoint.cu): per instance a run of checkpoint blocks, one
+// final-state block, a tape of `every` blocks and the adjoint arrays; byte offsets by instance.
+struct AdjDev {
+    char *ckpt, *fin, *tape, *bar;
+    const long long *ckptOff, *finOff, *tapeOff, *barOff;
+    const long long *ckptCap;                // checkpoints available per instance
+    const long long *stateBytes;             // bytes of one state block per instance
+    long long *steps;                        // the forward's step count per instance
+    double *grad;                            // [count * 7]
+    int *overflow;
+    int every;
+};
+size_t adj_state_bytes(int n, int e);
+size_t adj_bar_bytes(int n, int e);
+void launch_adjoint_forward(const Dev &d, const BatchDev &b, const AdjDev &a, cudaStream_t st);
+void launch_adjoint_backward(const Dev &d, const BatchDev &b, const AdjDev &a, cudaStream_t st);
+
 // A launch configuration of the batched step (chosen by the autotuner).
 struct BatchShape {
     int threads;                             // 128 or 256

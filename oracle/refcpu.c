@@ -38,6 +38,7 @@
  */
 #include "../include/neofiz.h"
 #include "../neofiz_gb300/csrc/nf_math.h"
+#include "../neofiz_gb300/csrc/nf_adjoint.h"
 
 #include <pthread.h>
 #include <stdarg.h>
@@ -1338,8 +1339,12 @@ static void erode(nfo_solver *h) {
 }
 
 /* step, ExplicitSolver.java:940-991 */
+static void step_body(nfo_solver *h);
 static void step(nfo_solver *h) {
     if (h->stepCount == 0) advanceMaterialAndAssemble(h, 0.0);
+    step_body(h);
+}
+static void step_body(nfo_solver *h) {
     const double dtAvg = 0.5 * (h->dtPrevious + h->dt);
     const double half = 0.5 * h->damping * dtAvg;
     h->nodalDecay = (1.0 - half) / (1.0 + half);
@@ -2044,6 +2049,9 @@ struct nfo_batch {
     pthread_mutex_t lock;
     int next;
     int64_t maxSteps;
+    /* the adjoint's checkpoints, per instance */
+    struct adj_ctx_s *adj;
+    double adjForwardMs, adjBackwardMs;
 };
 typedef struct nfo_batch nfo_batch;
 
@@ -2059,8 +2067,11 @@ static nf_status bfail(nfo_batch *b, nf_status st, const char *fmt, ...) {
 
 API const char *nfo_batch_last_error(const nfo_batch *b) { return b ? b->err : g_batch_err; }
 
+static void adj_free_all(nfo_batch *b);
+
 API nf_status nfo_batch_destroy(nfo_batch *b) {
     if (!b) return NF_OK;
+    adj_free_all(b);
     for (int k = 0; k < b->count; k++) nfo_destroy(b->s[k]);
     free(b->s); free(b->tEnd); free(b->nodeOff); free(b->elemOff);
     pthread_mutex_destroy(&b->lock);
@@ -2216,5 +2227,313 @@ API nf_status nfo_batch_measure(nfo_batch *b, nf_measure *out) {
 
 API nf_status nfo_batch_wall_stats(nfo_batch *b, nf_wall_info *out) {
     for (int k = 0; k < b->count; k++) nfo_wall_stats(b->s[k], &out[k]);
+    return NF_OK;
+}
+
+
+/* ------------------------------------------------------------------ reference adjoint */
+
+/* The FP64 reference adjoint (no counterpart in the reference): gradients of the length
+ * ratio L/L0 or the mushroom diameter after the forward run's N steps with respect to the
+ * Johnson-Cook A, B, n, C, m, the kinematic hardening modulus and the wall friction, by the
+ * reverse sweep of nf_adjoint.h over checkpointed segments. Reduced integration, no damage,
+ * erosion, contact or pressure (the Taylor scene); the first (zero-strain) assembly of a
+ * stress-free start depends on no parameter. */
+typedef struct {
+    double *ur, *uz, *vr, *vz, *fr, *fz;
+    uint8_t *onWall;
+    double *sig, *back, *epsP, *work, *hgR, *hgZ, *hgK;
+    double dt, dtPrevious, minEdgeSquared, time;
+    int64_t stepCount;
+} adj_state;
+
+static void adj_alloc(const nfo_solver *h, adj_state *s) {
+    const size_t N = (size_t)h->N, E = (size_t)h->E;
+    s->ur = dalloc(N); s->uz = dalloc(N); s->vr = dalloc(N); s->vz = dalloc(N);
+    s->fr = dalloc(N); s->fz = dalloc(N); s->onWall = balloc(N);
+    s->sig = dalloc(4 * E); s->back = dalloc(4 * E); s->epsP = dalloc(E); s->work = dalloc(E);
+    s->hgR = dalloc(E); s->hgZ = dalloc(E); s->hgK = dalloc(E);
+}
+static void adj_free(adj_state *s) {
+    free(s->ur); free(s->uz); free(s->vr); free(s->vz); free(s->fr); free(s->fz); free(s->onWall);
+    free(s->sig); free(s->back); free(s->epsP); free(s->work); free(s->hgR); free(s->hgZ);
+    free(s->hgK);
+}
+static void adj_copy(nfo_solver *h, adj_state *s, int save) {
+    const size_t N = (size_t)h->N, E = (size_t)h->E;
+#define C_(a, b, n) do { if (save) memcpy(a, b, n); else memcpy(b, a, n); } while (0)
+    C_(s->ur, h->ur, 8 * N); C_(s->uz, h->uz, 8 * N); C_(s->vr, h->vr, 8 * N);
+    C_(s->vz, h->vz, 8 * N); C_(s->fr, h->fr, 8 * N); C_(s->fz, h->fz, 8 * N);
+    C_(s->onWall, h->onWall, N);
+    C_(s->sig, h->sig, 32 * E); C_(s->back, h->back, 32 * E); C_(s->epsP, h->epsP, 8 * E);
+    C_(s->work, h->wPlastic, 8 * E); C_(s->hgR, h->hgR, 8 * E); C_(s->hgZ, h->hgZ, 8 * E);
+    C_(s->hgK, h->hgK, 8 * E);
+#undef C_
+    if (save) {
+        s->dt = h->dt; s->dtPrevious = h->dtPrevious; s->minEdgeSquared = h->minEdgeSquared;
+        s->time = h->time; s->stepCount = h->stepCount;
+    } else {
+        h->dt = s->dt; h->dtPrevious = s->dtPrevious; h->minEdgeSquared = s->minEdgeSquared;
+        h->time = s->time; h->stepCount = s->stepCount;
+    }
+}
+
+typedef struct adj_ctx_s {
+    int every;
+    int64_t steps;
+    int checkpoints;
+    adj_state *ckpt;
+} adj_ctx;
+
+static void adj_ctx_free(adj_ctx *c) {
+    for (int j = 0; j < c->checkpoints; j++) adj_free(&c->ckpt[j]);
+    free(c->ckpt);
+    c->ckpt = NULL;
+    c->checkpoints = 0;
+}
+
+static void adj_free_all(nfo_batch *b) {
+    if (!b->adj) return;
+    for (int k = 0; k < b->count; k++) adj_ctx_free(&b->adj[k]);
+    free(b->adj);
+    b->adj = NULL;
+}
+
+static nf_adj_mat adj_mat(const nfo_solver *h, int e) {
+    const flow_t *f = &h->flows[h->emat[e]];
+    nf_adj_mat m;
+    m.lambda = h->lambdaOf[e]; m.mu = h->muOf[e];
+    m.sy0 = f->sy0; m.hIso = f->hIso; m.hKin = f->hKin;
+    m.a = f->a; m.b = f->b; m.n = f->n; m.c = f->c; m.m = f->m; m.refRate = f->refRate;
+    m.room = f->room; m.melt = f->melt; m.thermalCoefficient = f->thermalCoefficient;
+    m.jc = f->jc;
+    return m;
+}
+
+static void adj_elem_in(const nfo_solver *h, int e, nf_adj_elem_in *in) {
+    for (int k = 0; k < 4; k++) {
+        const int n = h->conn[4 * e + k];
+        in->x0r[k] = h->r[n]; in->x0z[k] = h->z[n];
+        in->ur[k] = h->ur[n]; in->uz[k] = h->uz[n];
+        in->vr[k] = h->vr[n]; in->vz[k] = h->vz[n];
+        in->sig[k] = h->sig[4 * e + k]; in->back[k] = h->back[4 * e + k];
+    }
+    in->epsP = h->epsP[e]; in->work = h->wPlastic[e];
+    in->hgR = h->hgR[e]; in->hgZ = h->hgZ[e];
+}
+
+typedef struct {
+    double *ur, *uz, *vr, *vz, *fr, *fz;           /* node adjoints */
+    double *sig, *back, *epsP, *work, *hgR, *hgZ;  /* element adjoints */
+    double *corner;                                /* [E][4][4] per-corner node adjoints */
+    double dt, dtPrevious;                         /* of the next step's dt and dtPrevious */
+    double p[NF_ADJ_P_COUNT];
+} adj_bar;
+
+/* The reverse of one step whose pre-step state is `pre` and whose shortest squared edge
+ * (the next step's CFL input) was minEdge. */
+static void adj_reverse_step(nfo_solver *h, adj_state *pre, double minEdge, adj_bar *a) {
+    adj_copy(h, pre, 0);
+    const double dt = h->dt;
+    const double dtAvg = 0.5 * (h->dtPrevious + h->dt);
+    const double half = 0.5 * h->damping * dtAvg;
+    const double decay = (1.0 - half) / (1.0 + half), gain = dtAvg / (1.0 + half);
+    h->nodalDecay = decay; h->nodalGain = gain; h->nodalDtAvg = dtAvg;
+    nodalUpdate(h, 0, h->N);                       /* u', v' of this step */
+    const int axi = h->formulation == NF_AXISYMMETRIC;
+    const int finite = h->kinematics == NF_FINITE_STRAIN;
+    double edgeb = 0.0;
+    int owner = -1, ownerEdge = -1;
+    if (finite && minEdge > 0.0 && minEdge < DBL_MAX) {
+        edgeb = a->dt * h->cflSafety * sqrt(h->massScale) / h->fastestWave * 0.5 / sqrt(minEdge);
+        for (int e = 0; e < h->E && owner < 0; e++) {
+            nf_adj_elem_in in;
+            adj_elem_in(h, e, &in);
+            const int k = nf_adj_edge_owner(&in, dt, finite, minEdge);
+            if (k >= 0) { owner = e; ownerEdge = k; }
+        }
+    }
+    double dtb = a->dtPrevious;
+    for (int e = 0; e < h->E; e++) {
+        nf_adj_elem_in in;
+        adj_elem_in(h, e, &in);
+        nf_adj_elem_bar bar;
+        for (int k = 0; k < 4; k++) {
+            const int n = h->conn[4 * e + k];
+            bar.g[k] = a->fr[n];
+            bar.g[4 + k] = a->fz[n];
+            bar.sig[k] = a->sig[4 * e + k];
+            bar.back[k] = a->back[4 * e + k];
+        }
+        bar.epsP = a->epsP[e]; bar.work = a->work[e]; bar.hgR = a->hgR[e]; bar.hgZ = a->hgZ[e];
+        bar.edgeOwner = e == owner ? ownerEdge : -1;
+        bar.edgeb = edgeb;
+        const nf_adj_mat m = adj_mat(h, e);
+        nf_adj_element_reduced(&in, &m, dt, axi, finite, h->thickness, h->hourglassCoefficient,
+                               &bar, &dtb, a->p);
+        for (int k = 0; k < 4; k++) {
+            a->sig[4 * e + k] = bar.sig[k];
+            a->back[4 * e + k] = bar.back[k];
+            double *c = a->corner + 16 * (size_t)e + 4 * k;
+            c[0] = bar.ur[k]; c[1] = bar.uz[k]; c[2] = bar.vr[k]; c[3] = bar.vz[k];
+        }
+        a->epsP[e] = bar.epsP; a->work[e] = bar.work; a->hgR[e] = bar.hgR; a->hgZ[e] = bar.hgZ;
+    }
+    double acc[4] = {0.0, 0.0, 0.0, 0.0};
+    for (int i = 0; i < h->N; i++) {
+        double ub[2] = {a->ur[i], a->uz[i]}, vb[2] = {a->vr[i], a->vz[i]}, fb[2];
+        for (int s = h->nodeSlotStart[i]; s < h->nodeSlotStart[i + 1]; s++) {
+            const int slot = h->nodeSlot[s];
+            if (slot >= 8 * h->E) continue;
+            const double *c = a->corner + 16 * (size_t)(slot >> 3) + 4 * (slot & 7);
+            ub[0] += c[0]; ub[1] += c[1]; vb[0] += c[2]; vb[1] += c[3];
+        }
+        nf_adj_node(h->z[i], pre->ur[i], pre->uz[i], pre->vr[i], pre->vz[i], pre->fr[i],
+                    pre->fz[i], h->mass[i], 1.0 / h->mass[i], h->fixedR[i], h->fixedZ[i],
+                    pre->onWall[i], h->hasWall, h->wallPlane, h->wallFriction, decay, gain, dt,
+                    ub, vb, fb, acc);
+        a->ur[i] = ub[0]; a->uz[i] = ub[1]; a->vr[i] = vb[0]; a->vz[i] = vb[1];
+        a->fr[i] = fb[0]; a->fz[i] = fb[1];
+    }
+    dtb += acc[2];
+    a->p[NF_ADJ_P_MU] += acc[3];
+    const double dtAvgb = nf_adj_dtavg(acc[0], acc[1], dtAvg, h->damping);
+    dtb += 0.5 * dtAvgb;
+    a->dt = dtb;
+    a->dtPrevious = 0.5 * dtAvgb;
+}
+
+static nf_status adj_check(nfo_solver *h) {
+    if (h->integration != NF_REDUCED || h->gone != NULL || h->hasDamage || h->contact != NULL ||
+        h->K > 0)
+        return fail(h, NF_EINVAL, "the adjoint covers reduced integration without damage, "
+                                  "erosion, contact or pressure");
+    return NF_OK;
+}
+
+static void adj_forward(nfo_solver *h, adj_ctx *c, double tEnd, int every) {
+    c->every = every;
+    int cap = 16;
+    c->ckpt = (adj_state *)calloc((size_t)cap, sizeof(adj_state));
+    c->checkpoints = 0;
+    while (h->time < tEnd) {
+        if (h->stepCount % every == 0) {
+            if (c->checkpoints == cap) {
+                cap *= 2;
+                c->ckpt = (adj_state *)realloc(c->ckpt, (size_t)cap * sizeof(adj_state));
+            }
+            adj_alloc(h, &c->ckpt[c->checkpoints]);
+            adj_copy(h, &c->ckpt[c->checkpoints], 1);
+            c->checkpoints++;
+        }
+        step(h);
+    }
+    c->steps = h->stepCount;
+}
+
+static double adj_objective(const nfo_solver *h, int objective, double *ur, double *uz) {
+    double zmax = -DBL_MAX, zmin = DBL_MAX, z0max = -DBL_MAX, z0min = DBL_MAX, rmax = -DBL_MAX;
+    int imax = 0, imin = 0, irmax = 0;
+    for (int i = 0; i < h->N; i++) {
+        const double z = h->z[i] + h->uz[i], r = h->r[i] + h->ur[i];
+        if (z > zmax) { zmax = z; imax = i; }
+        if (z < zmin) { zmin = z; imin = i; }
+        if (r > rmax) { rmax = r; irmax = i; }
+        if (h->z[i] > z0max) z0max = h->z[i];
+        if (h->z[i] < z0min) z0min = h->z[i];
+    }
+    memset(ur, 0, 8 * (size_t)h->N);
+    memset(uz, 0, 8 * (size_t)h->N);
+    if (objective == 0) {
+        const double L0 = z0max - z0min;
+        uz[imax] += 1.0 / L0;
+        uz[imin] -= 1.0 / L0;
+        return (zmax - zmin) / L0;
+    }
+    ur[irmax] += 2.0;
+    return 2.0 * rmax;
+}
+
+static nf_status adj_backward(nfo_solver *h, adj_ctx *c, int objective, double *value,
+                              double *grad) {
+    const size_t N = (size_t)h->N, E = (size_t)h->E;
+    adj_bar a;
+    memset(&a, 0, sizeof a);
+    a.ur = dalloc(N); a.uz = dalloc(N); a.vr = dalloc(N); a.vz = dalloc(N);
+    a.fr = dalloc(N); a.fz = dalloc(N);
+    a.sig = dalloc(4 * E); a.back = dalloc(4 * E); a.epsP = dalloc(E); a.work = dalloc(E);
+    a.hgR = dalloc(E); a.hgZ = dalloc(E); a.corner = dalloc(16 * E);
+    *value = adj_objective(h, objective, a.ur, a.uz);
+    adj_state final_;
+    adj_alloc(h, &final_);
+    adj_copy(h, &final_, 1);
+    const int every = c->every;
+    adj_state *tape = (adj_state *)calloc((size_t)every, sizeof(adj_state));
+    double *minEdge = (double *)calloc((size_t)every, sizeof(double));
+    for (int j = 0; j < every; j++) adj_alloc(h, &tape[j]);
+    for (int s = c->checkpoints - 1; s >= 0; s--) {
+        adj_copy(h, &c->ckpt[s], 0);
+        const int64_t start = (int64_t)s * every;
+        const int64_t end = start + every < c->steps ? start + every : c->steps;
+        for (int64_t j = start; j < end; j++) {
+            if (h->stepCount == 0) advanceMaterialAndAssemble(h, 0.0);
+            adj_copy(h, &tape[j - start], 1);
+            step_body(h);
+            minEdge[j - start] = h->minEdgeSquared;
+        }
+        for (int64_t j = end - 1; j >= start; j--)
+            adj_reverse_step(h, &tape[j - start], minEdge[j - start], &a);
+    }
+    for (int k = 0; k < NF_ADJ_P_COUNT; k++) grad[k] = a.p[k];
+    adj_copy(h, &final_, 0);
+    adj_free(&final_);
+    for (int j = 0; j < every; j++) adj_free(&tape[j]);
+    free(tape); free(minEdge);
+    free(a.ur); free(a.uz); free(a.vr); free(a.vz); free(a.fr); free(a.fz);
+    free(a.sig); free(a.back); free(a.epsP); free(a.work); free(a.hgR); free(a.hgZ);
+    free(a.corner);
+    return NF_OK;
+}
+
+/* The batch surface: every instance of the oracle's batch, one after another. */
+static double now_ms(void) {
+    struct timespec t;
+    clock_gettime(CLOCK_MONOTONIC, &t);
+    return (double)t.tv_sec * 1e3 + (double)t.tv_nsec * 1e-6;
+}
+
+API nf_status nfo_batch_adjoint_forward(nfo_batch *b, int32_t checkpoint_every) {
+    if (checkpoint_every < 1) return bfail(b, NF_EINVAL, "checkpoint interval must be positive");
+    for (int k = 0; k < b->count; k++) {
+        nf_status st = adj_check(b->s[k]);
+        if (st) return bfail(b, st, "%s", nfo_last_error(b->s[k]));
+        if (b->s[k]->stepCount != 0)
+            return bfail(b, NF_ESTATE, "the adjoint's forward pass starts from a fresh batch");
+    }
+    const double t0 = now_ms();
+    if (b->adj)
+        for (int k = 0; k < b->count; k++) adj_ctx_free(&b->adj[k]);
+    else
+        b->adj = (adj_ctx *)calloc((size_t)b->count, sizeof(adj_ctx));
+    for (int k = 0; k < b->count; k++) adj_forward(b->s[k], &b->adj[k], b->tEnd[k], checkpoint_every);
+    b->adjForwardMs = now_ms() - t0;
+    return NF_OK;
+}
+
+API nf_status nfo_batch_adjoint_backward(nfo_batch *b, int32_t objective, double *values,
+                                         double *gradients) {
+    if (!b->adj) return bfail(b, NF_ESTATE, "run the adjoint's forward pass first");
+    if (objective != NF_OBJECTIVE_LENGTH_RATIO && objective != NF_OBJECTIVE_MUSHROOM)
+        return bfail(b, NF_EINVAL, "unknown objective %d", objective);
+    const double t0 = now_ms();
+    for (int k = 0; k < b->count; k++)
+        adj_backward(b->s[k], &b->adj[k], objective, &values[k], gradients + (size_t)k * NF_ADJ_P_COUNT);
+    b->adjBackwardMs = now_ms() - t0;
+    return NF_OK;
+}
+
+API nf_status nfo_batch_adjoint_elapsed(nfo_batch *b, double *forward_ms, double *backward_ms) {
+    *forward_ms = b->adjForwardMs;
+    *backward_ms = b->adjBackwardMs;
     return NF_OK;
 }

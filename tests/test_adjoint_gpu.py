@@ -1,0 +1,58 @@
+"""The adjoint kernel against the FP64 reference adjoint of the oracle, on a small batch."""
+import numpy as np
+import pytest
+
+from neofiz_gb300 import _abi, scenes
+from neofiz_gb300.batch import BatchSolver
+from oracle.oracle import OracleBatch
+
+pytestmark = pytest.mark.gpu
+
+
+def _rods(t_end=12.0e-6):
+    rods = scenes.taylor_sweep(3, seed=21)
+    for r, (nr, nz) in zip(rods, [(10, 60), (4, 20), (6, 30)]):
+        r["nr"], r["nz"], r["t_end"] = nr, nz, t_end
+    return rods
+
+
+def _grads(cls, rods, every):
+    b = cls(scenes.sweep_instances(rods), scenes.Formulation.AXISYMMETRIC, cfl=0.6)
+    b.adjointForward(every)
+    out = {obj: b.adjointBackward(obj) for obj in (0, 1)}
+    steps = b.state()["steps"].copy()
+    uz = b.read(_abi.FIELD_UZ)
+    b.close()
+    return out, steps, uz
+
+
+def test_adjoint_kernel_matches_the_reference_adjoint(gpu_lib):
+    rods = _rods()
+    g, gsteps, guz = _grads(BatchSolver, rods, every=40)
+    o, osteps, ouz = _grads(OracleBatch, rods, every=40)
+    assert np.array_equal(gsteps, osteps)
+    assert np.array_equal(guz, ouz)                 # the forward pass is the plain path
+    for obj in (0, 1):
+        assert np.array_equal(g[obj][0], o[obj][0])
+        # per-thread partial sums and block trees instead of serial sums: rounding only
+        np.testing.assert_allclose(g[obj][1], o[obj][1], rtol=1e-9, atol=0.0)
+
+
+def test_forward_pass_equals_a_plain_run_and_intervals_agree(gpu_lib):
+    rods = _rods(t_end=8.0e-6)
+    a, asteps, auz = _grads(BatchSolver, rods, every=13)
+    b, bsteps, buz = _grads(BatchSolver, rods, every=200)
+    assert np.array_equal(asteps, bsteps) and np.array_equal(auz, buz)
+    for obj in (0, 1):
+        assert np.array_equal(a[obj][1], b[obj][1])
+    p = BatchSolver(scenes.sweep_instances(rods), scenes.Formulation.AXISYMMETRIC, cfl=0.6)
+    p.run()
+    assert np.array_equal(p.read(_abi.FIELD_UZ), auz)
+    assert np.array_equal(p.state()["steps"], asteps)
+
+
+def test_adjoint_rejects_mixed_batches(gpu_lib):
+    b = BatchSolver(scenes.sweep_instances(_rods()[:1]), scenes.Formulation.AXISYMMETRIC,
+                    cfl=0.6, precision=_abi.PRECISION_MIXED)
+    with pytest.raises(ValueError):
+        b.adjointForward(50)
