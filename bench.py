@@ -48,6 +48,12 @@ def parse():
     p.add_argument("--mixed-steps", type=int, default=600)
     p.add_argument("--no-batched", action="store_true")
     p.add_argument("--batch-count", type=int, default=4096)
+    p.add_argument("--no-adjoint", action="store_true")
+    p.add_argument("--adjoint-count", type=int, default=64)
+    p.add_argument("--only", choices=["batched", "adjoint"],
+                   help="run one form alone and print its JSON (profiling of small cases)")
+    p.add_argument("--t-end", type=float, default=None,
+                   help="with --only: the rods' run length instead of 80 us")
     return p.parse_args()
 
 
@@ -227,6 +233,10 @@ def run_ours(args, world, rank, local):
     if not args.no_batched:
         batched = run_batched(args)
 
+    adjoint = None
+    if not args.no_adjoint:
+        adjoint = run_adjoint(args)
+
     if rank == 0:
         line = {
             "metric": "element-cycles/s, plain FP64 explicit timestep (live elements x steps / s)",
@@ -264,6 +274,7 @@ def run_ours(args, world, rank, local):
             "e2e": e2e,
             "mixed": mixed,
             "batched": batched,
+            "adjoint": adjoint,
             "clocks": clk,
             "gpu_launches": launches,
             "status_word": status,
@@ -388,6 +399,9 @@ def run_batched(args):
     from neofiz_gb300 import ExplicitSolver, _abi, scenes
     from neofiz_gb300.batch import BatchSolver
     rods = scenes.taylor_sweep(args.batch_count)
+    if args.t_end:
+        for r in rods:
+            r["t_end"] = args.t_end
     L0 = 25.0e-3
 
     def make(sel, prec):
@@ -456,6 +470,95 @@ def run_batched(args):
     }
 
 
+def run_adjoint(args):
+    """The adjoint gradient batch: args.adjoint_count rods with the 10 x 60 rod's mesh, 200 m/s
+    and 80 us, Johnson-Cook constants and friction drawn as in the sweep. Times the plain FP64
+    batched forward run, the adjoint's checkpointed forward pass (every 200 steps) and one
+    backward pass per objective (L/L0, mushroom diameter); checks rod 0's gradients against
+    central differences (h = 1e-6 and 1e-5 relative) of FP64 runs of exactly the forward's
+    step count, perturbed one parameter at a time (batched)."""
+    import dataclasses
+    import numpy as np
+    from neofiz_gb300 import _abi, scenes
+    from neofiz_gb300.batch import BatchSolver
+    rods = scenes.adjoint_rods(args.adjoint_count)
+    if args.t_end:
+        for r in rods:
+            r["t_end"] = args.t_end
+
+    def make(insts):
+        return BatchSolver(insts, scenes.Formulation.AXISYMMETRIC, cfl=0.6)
+
+    p = make(scenes.sweep_instances(rods))
+    plain_ms = p.run()
+    steps = p.state()["steps"]
+    p.close()
+    a = make(scenes.sweep_instances(rods))
+    fwd_ms = a.adjointForward(200)
+    grads, values, back_ms = {}, {}, {}
+    for obj, name in ((_abi.OBJECTIVE_LENGTH_RATIO, "length_ratio"),
+                      (_abi.OBJECTIVE_MUSHROOM, "mushroom_diameter")):
+        v, g = a.adjointBackward(obj)
+        values[name], grads[name] = v, g
+        back_ms[name] = a.adjointElapsed()[1]
+    a.close()
+    # central differences on rod 0, the perturbed runs batched
+    N = int(steps[0])
+    jc0 = scenes._rod_jc(rods[0])
+    mat0 = scenes.rod_material_with(jc0)
+    p0 = {"A": jc0.a, "B": jc0.b, "n": jc0.n, "C": jc0.c, "m": jc0.m,
+          "kinematic": mat0.kinematicHardening, "friction": rods[0]["mu"]}
+    fd = {}
+    for h in (1e-6, 1e-5):
+        insts = []
+        for name in _abi.PARAM_NAMES:
+            for sgn in (1.0, -1.0):
+                inst = scenes.sweep_instances(rods[:1])[0]
+                val = p0[name] * (1.0 + sgn * h)
+                if name in ("A", "B", "n", "C", "m"):
+                    f = {"A": "a", "B": "b", "n": "n", "C": "c", "m": "m"}[name]
+                    inst.material = scenes.rod_material_with(
+                        dataclasses.replace(jc0, **{f: val})).withKinematicHardening(
+                            mat0.kinematicHardening)
+                elif name == "kinematic":
+                    inst.material = mat0.withKinematicHardening(val)
+                else:
+                    inst.wall = (0.0, val)
+                inst.t_end = 1.0
+                insts.append(inst)
+        b = make(insts)
+        b.run(max_steps=N)
+        m = b.measure()
+        b.close()
+        fd[h] = np.array([[(m[2 * k].length - m[2 * k + 1].length) / 25.0e-3,
+                           m[2 * k].mushroom_diameter - m[2 * k + 1].mushroom_diameter]
+                          for k in range(len(_abi.PARAM_NAMES))])
+        fd[h] /= np.array([[2.0 * p0[nm] * h] * 2 for nm in _abi.PARAM_NAMES])
+    ad = np.stack([grads["length_ratio"][0], grads["mushroom_diameter"][0]], axis=1)
+    err = np.abs(ad - fd[1e-6]) / np.abs(fd[1e-6])
+    scatter = np.abs(fd[1e-5] - fd[1e-6]) / np.abs(fd[1e-6])
+    per = {nm: {"adjoint_vs_fd_rel": [float(err[k, 0]), float(err[k, 1])],
+                "fd_scatter_h1e-5_vs_1e-6": [float(scatter[k, 0]), float(scatter[k, 1])]}
+           for k, nm in enumerate(_abi.PARAM_NAMES)}
+    both = fwd_ms + back_ms["length_ratio"] + back_ms["mushroom_diameter"]
+    return {
+        "workload": f"{len(rods)} Taylor rods, 10x60 quads, 200 m/s, 80 us (mean "
+                    f"{float(steps.mean()):.0f} steps), JC and friction drawn (seed "
+                    f"{scenes.ADJOINT_SEED}); FP64; checkpoints every 200 steps",
+        "parameters": list(_abi.PARAM_NAMES),
+        "forward_ms": plain_ms, "adjoint_forward_ms": fwd_ms, "backward_ms": back_ms,
+        "cost_vs_forward": {"one_objective": (fwd_ms + back_ms["length_ratio"]) / plain_ms,
+                            "both_objectives": both / plain_ms},
+        "rod0": {"values": {k: float(v[0]) for k, v in values.items()},
+                 "gradients": {k: [float(x) for x in g[0]] for k, g in grads.items()},
+                 "gradients_fraction_convention": {
+                     k: [float(x) for x in scenes.fraction_gradients(g[0], rods[0])]
+                     for k, g in grads.items()},
+                 "central_differences": per,
+                 "max_rel_error": float(err.max())},
+    }
+
+
 def cpu_baseline(args, budget_s=12.0):
     """The reference algorithm on this host's cores (oracle, threaded as the reference's
     Parallel pool), on the same scene; a bounded sample of steps."""
@@ -501,6 +604,12 @@ def run_reference(args, world, rank):
 def main():
     args = parse()
     world, rank, local = dist_setup()
+    if args.only:
+        from neofiz_gb300 import build as nb
+        nb.build()
+        out = run_batched(args) if args.only == "batched" else run_adjoint(args)
+        print(json.dumps(out))
+        return
     if args.impl == "reference":
         run_reference(args, world, rank)
     else:

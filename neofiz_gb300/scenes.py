@@ -280,3 +280,39 @@ def sweep_rod(cls, rod, **kw):
     """One drawn rod as a single scene (the twin of its batch instance)."""
     return taylor_rod(cls, nr=rod["nr"], nz=rod["nz"], speed=rod["speed"], friction=rod["mu"],
                       material=rod_material_with(_rod_jc(rod)), **kw)
+
+
+# ---------------------------------------------------------------------------- the adjoint batch
+
+ADJOINT_SEED = 77
+
+
+def adjoint_rods(count: int = 64, seed: int = ADJOINT_SEED, t_end: float = SWEEP_T_END):
+    """The adjoint gradient batch: rods with the 10 x 60 rod's mesh, speed and run length, and
+    Johnson-Cook constants and friction drawn as in the sweep (so every instance has its own
+    gradient)."""
+    rods = taylor_sweep(count, seed=seed, t_end=t_end)
+    for r in rods:
+        r.update(nr=10, nz=60, speed=200.0)
+    return rods
+
+
+def fraction_gradients(grads, rod):
+    """Gradients in the (A, B, n, C, m, friction, kinematic fraction) convention of the rod's
+    material rule H_kin = f B e^n / e (e the fit strain): chain rule from the adjoint's
+    (A, B, n, C, m, H_kin, friction)."""
+    g = np.asarray(grads, dtype=np.float64)
+    b, n = rod["b"], rod["n"]
+    e = ROD_FIT_STRAIN
+    f = ROD_KINEMATIC_FRACTION
+    secant = b * e ** n / e
+    dH = g[..., 5]
+    out = np.empty_like(g)
+    out[..., 0] = g[..., 0]
+    out[..., 1] = g[..., 1] + dH * f * e ** n / e
+    out[..., 2] = g[..., 2] + dH * f * secant * math.log(e)
+    out[..., 3] = g[..., 3]
+    out[..., 4] = g[..., 4]
+    out[..., 5] = g[..., 6]
+    out[..., 6] = dH * secant
+    return out
