@@ -508,10 +508,11 @@ def run_adjoint(args):
     mat0 = scenes.rod_material_with(jc0)
     p0 = {"A": jc0.a, "B": jc0.b, "n": jc0.n, "C": jc0.c, "m": jc0.m,
           "kinematic": mat0.kinematicHardening, "friction": rods[0]["mu"]}
+    names = _abi.PARAM_NAMES[:7]                    # the rods have no damage
     fd = {}
     for h in (1e-6, 1e-5):
         insts = []
-        for name in _abi.PARAM_NAMES:
+        for name in names:
             for sgn in (1.0, -1.0):
                 inst = scenes.sweep_instances(rods[:1])[0]
                 val = p0[name] * (1.0 + sgn * h)
@@ -532,16 +533,18 @@ def run_adjoint(args):
         b.close()
         fd[h] = np.array([[(m[2 * k].length - m[2 * k + 1].length) / 25.0e-3,
                            m[2 * k].mushroom_diameter - m[2 * k + 1].mushroom_diameter]
-                          for k in range(len(_abi.PARAM_NAMES))])
-        fd[h] /= np.array([[2.0 * p0[nm] * h] * 2 for nm in _abi.PARAM_NAMES])
-    ad = np.stack([grads["length_ratio"][0], grads["mushroom_diameter"][0]], axis=1)
+                          for k in range(len(names))])
+        fd[h] /= np.array([[2.0 * p0[nm] * h] * 2 for nm in names])
+    ad = np.stack([grads["length_ratio"][0][:7], grads["mushroom_diameter"][0][:7]], axis=1)
     err = np.abs(ad - fd[1e-6]) / np.abs(fd[1e-6])
     scatter = np.abs(fd[1e-5] - fd[1e-6]) / np.abs(fd[1e-6])
     per = {nm: {"adjoint_vs_fd_rel": [float(err[k, 0]), float(err[k, 1])],
                 "fd_scatter_h1e-5_vs_1e-6": [float(scatter[k, 0]), float(scatter[k, 1])]}
-           for k, nm in enumerate(_abi.PARAM_NAMES)}
+           for k, nm in enumerate(names)}
     both = fwd_ms + back_ms["length_ratio"] + back_ms["mushroom_diameter"]
+    tube = run_tube_adjoint(args)
     return {
+        "tube": tube,
         "workload": f"{len(rods)} Taylor rods, 10x60 quads, 200 m/s, 80 us (mean "
                     f"{float(steps.mean()):.0f} steps), JC and friction drawn (seed "
                     f"{scenes.ADJOINT_SEED}); FP64; checkpoints every 200 steps",
@@ -557,6 +560,64 @@ def run_adjoint(args):
                  "central_differences": per,
                  "max_rel_error": float(err.max())},
     }
+
+
+def run_tube_adjoint(args):
+    """The tube of the gradient batch: QuadMesh.cylinderWall(19.6, 20.4, 40 mm, 4, 200) in
+    OFHC copper (quasi-static Johnson-Cook law), smoothstep ramp to 60 MPa over 20 us,
+    relaxation damping, Weibull failure strains (seed 7, scale 0.08, so damage begins before
+    the capacity peak) and G_f = 60 kJ/m^2; the wall capacity (BurstCase.loadCapacity) sampled
+    every 10 steps to 60 us. The gradient of its peak with respect to A, B, n and G_f,
+    against central differences (h = 1e-6)."""
+    import dataclasses
+    import numpy as np
+    from neofiz_gb300 import _abi, scenes
+    from neofiz_gb300.batch import BatchSolver
+    from neofiz_gb300.materials import JohnsonCook
+    t_end = args.t_end if args.t_end else 60.0e-6
+    law0 = JohnsonCook.COPPER_OFHC.quasiStatic()
+
+    def tube(name=None, value=None):
+        law, gf = law0, scenes.TUBE_GF
+        if name in ("A", "B", "n"):
+            law = dataclasses.replace(law0, **{{"A": "a", "B": "b", "n": "n"}[name]: value})
+        elif name == "fracture_energy":
+            gf = value
+        return scenes.tube_instance(nz=200, height=40.0e-3, t_end=t_end, scale=0.08,
+                                    material=scenes.tube_material(law), gf=gf)
+
+    def make(insts):
+        return BatchSolver(insts, scenes.Formulation.AXISYMMETRIC, cfl=0.5)
+
+    p = make([tube()])
+    plain_ms = p.run()
+    steps = int(p.state()["steps"][0])
+    p.close()
+    a = make([tube()])
+    fwd_ms = a.adjointForward(200, 10)
+    v, g = a.adjointBackward(_abi.OBJECTIVE_PEAK_CAPACITY)
+    back_ms = a.adjointElapsed()[1]
+    a.close()
+    p0 = {"A": law0.a, "B": law0.b, "n": law0.n, "fracture_energy": scenes.TUBE_GF}
+    h = 1.0e-6
+    insts = [tube(nm, p0[nm] * (1.0 + s * h)) for nm in p0 for s in (1.0, -1.0)]
+    f = make(insts)
+    f.adjointForward(200, 10)
+    fv, _ = f.adjointBackward(_abi.OBJECTIVE_PEAK_CAPACITY)
+    f.close()
+    out = {}
+    for k, nm in enumerate(p0):
+        fd = (fv[2 * k] - fv[2 * k + 1]) / (2.0 * p0[nm] * h)
+        ad = g[0][_abi.PARAM_NAMES.index(nm)]
+        out[nm] = {"adjoint": float(ad), "fd": float(fd), "rel": float(abs(ad - fd) / abs(fd))}
+    return {"workload": "tube 4x200 quads (40 mm), copper, 60 MPa smoothstep ramp over 20 us, "
+                        f"damping, Weibull damage (scale 0.08), {steps} steps, capacity sampled "
+                        "every 10 steps",
+            "peak_capacity_pa": float(v[0]), "forward_ms": plain_ms,
+            "adjoint_forward_ms": fwd_ms, "backward_ms": back_ms,
+            "cost_vs_forward": (fwd_ms + back_ms) / plain_ms,
+            "gradients_vs_central_differences": out,
+            "max_rel_error": max(o["rel"] for o in out.values())}
 
 
 def cpu_baseline(args, budget_s=12.0):

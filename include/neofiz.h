@@ -326,9 +326,11 @@ nf_status nf_material_point_update_static(const nf_material *material, int32_t f
  *   setHourglassCoefficient(q); fixRadial/fixAxial(fixed nodes);
  *   setRigidWall(RigidWall.atZ(plane, friction)) unless plane is NaN;
  *   setUniformVelocity(vr, vz); then step while time < t_end,
+ * plus setPressureRamp on its pressure edges, setRelaxationDamping and setDamage when given,
  * and its trajectory is bit-identical to that scene run alone through nf_create/nf_step in the
  * same precision (NF_PRECISION_FP64 or NF_PRECISION_MIXED). Only reduced integration is
- * batched. Instances may differ in mesh, material, wall, velocity, hourglass and t_end. */
+ * batched, without erosion or contact. Instances may differ in mesh, material, wall,
+ * velocity, hourglass, pressure, damping, damage and t_end. */
 typedef struct nf_batch nf_batch;
 
 typedef struct {
@@ -340,6 +342,11 @@ typedef struct {
     const int32_t *conn;             /* [4 * total elements], node numbers local to the
                                         instance, CCW */
     const uint8_t *fixed;            /* [total nodes] bit 0 radial, bit 1 axial, or NULL */
+    const int32_t *pressure_offset;  /* [count + 1]: instance k owns pressure edges [k] ..
+                                        [k + 1) (QuadMesh pressureEdges), or NULL for none */
+    const int32_t *pressure_edges;   /* [2 * total edges], node numbers local to the instance */
+    const double *failure_strain;    /* [total elements] setDamage(gf, eps), or NULL for no */
+    const double *fracture_energy;   /*   damage in any instance (both or neither) */
 } nf_batch_mesh;
 
 typedef struct {
@@ -349,6 +356,9 @@ typedef struct {
     double wall_friction;
     double hourglass;                /* setHourglassCoefficient */
     double t_end;                    /* the run: step while time < t_end */
+    double pressure, pressure_ramp;  /* setPressureRamp(pascals, seconds) */
+    double damping_fraction;         /* setRelaxationDamping(fraction, omega); omega 0: none */
+    double damping_omega;
 } nf_batch_instance;
 
 /* A launch shape of the batched step; any valid shape gives the same trajectories. */
@@ -405,16 +415,20 @@ nf_status nf_batch_wall_stats(nf_batch *b, nf_wall_info *out);
  * rate and temperature clamps, the wall's hold/stick/slip/arrive state of each node and the
  * element that sets each CFL step are those of the forward pass (frozen). Objectives are
  * taken after the N steps: the length ratio L/L0 (TaylorImpactCase.java:272-279) or the
- * mushroom diameter 2 max(r + ur) (:281-288). FP64 batches with reduced integration and no
- * damage, erosion, contact or pressure. */
-enum { NF_OBJECTIVE_LENGTH_RATIO = 0, NF_OBJECTIVE_MUSHROOM = 1 };
+ * mushroom diameter 2 max(r + ur) (:281-288); or the peak wall capacity, the largest
+ * BurstCase.loadCapacity (BurstCase.java:533-553) sampled every sample_every steps of the
+ * forward pass, its gradient taken at the sampled peak (the step of the peak frozen). FP64
+ * batches with reduced integration (damage, pressure edges, damping and walls included). */
+enum { NF_OBJECTIVE_LENGTH_RATIO = 0, NF_OBJECTIVE_MUSHROOM = 1, NF_OBJECTIVE_PEAK_CAPACITY = 2 };
 /* Gradient components: Johnson-Cook A, B, n, C, m (JohnsonCook.java:66-69), the kinematic
- * hardening modulus (Material.java:20-21) and the wall friction coefficient
- * (RigidWall.atZ, RigidWall.java:121-136). */
+ * hardening modulus (Material.java:20-21), the wall friction coefficient (RigidWall.atZ,
+ * RigidWall.java:121-136) and the fracture energy of every element (setDamage, as a common
+ * value: the sum over elements of the per-element derivatives). */
 enum { NF_PARAM_A = 0, NF_PARAM_B, NF_PARAM_N, NF_PARAM_C, NF_PARAM_M, NF_PARAM_KINEMATIC,
-       NF_PARAM_FRICTION, NF_PARAM_COUNT };
+       NF_PARAM_FRICTION, NF_PARAM_FRACTURE_ENERGY, NF_PARAM_COUNT };
 
-nf_status nf_batch_adjoint_forward(nf_batch *b, int32_t checkpoint_every);
+/* sample_every: the capacity sampling interval (0: no capacity objective). */
+nf_status nf_batch_adjoint_forward(nf_batch *b, int32_t checkpoint_every, int32_t sample_every);
 /* values[instance_count]; gradients[instance_count * NF_PARAM_COUNT]. May be called once per
  * objective after one forward pass. */
 nf_status nf_batch_adjoint_backward(nf_batch *b, int32_t objective, double *values,

@@ -26,10 +26,11 @@ GROUP_NAMES = ("nodal", "erode", "element", "pressure", "gather", "contact", "en
 
 PRECISION_FP64, PRECISION_MIXED = 0, 1
 
-OBJECTIVE_LENGTH_RATIO, OBJECTIVE_MUSHROOM = 0, 1
-(PARAM_A, PARAM_B, PARAM_N, PARAM_C, PARAM_M, PARAM_KINEMATIC, PARAM_FRICTION) = range(7)
-PARAM_COUNT = 7
-PARAM_NAMES = ("A", "B", "n", "C", "m", "kinematic", "friction")
+OBJECTIVE_LENGTH_RATIO, OBJECTIVE_MUSHROOM, OBJECTIVE_PEAK_CAPACITY = 0, 1, 2
+(PARAM_A, PARAM_B, PARAM_N, PARAM_C, PARAM_M, PARAM_KINEMATIC, PARAM_FRICTION,
+ PARAM_FRACTURE_ENERGY) = range(8)
+PARAM_COUNT = 8
+PARAM_NAMES = ("A", "B", "n", "C", "m", "kinematic", "friction", "fracture_energy")
 
 WALL_HELD, WALL_STUCK, WALL_SLID, WALL_ARRIVED = 1, 2, 4, 8
 CONTACT_PAIR, CONTACT_STICK, CONTACT_SLIP = 1, 2, 4
@@ -102,13 +103,17 @@ class DamagePoints(C.Structure):
 class BatchMesh(C.Structure):
     _fields_ = [("instance_count", C.c_int32), ("node_offset", c_int32_p),
                 ("element_offset", c_int32_p), ("r", c_double_p), ("z", c_double_p),
-                ("conn", c_int32_p), ("fixed", C.POINTER(C.c_uint8))]
+                ("conn", c_int32_p), ("fixed", C.POINTER(C.c_uint8)),
+                ("pressure_offset", c_int32_p), ("pressure_edges", c_int32_p),
+                ("failure_strain", c_double_p), ("fracture_energy", c_double_p)]
 
 
 class BatchInstance(C.Structure):
     _fields_ = [("material", MaterialC), ("velocity_r", C.c_double), ("velocity_z", C.c_double),
                 ("wall_plane", C.c_double), ("wall_friction", C.c_double),
-                ("hourglass", C.c_double), ("t_end", C.c_double)]
+                ("hourglass", C.c_double), ("t_end", C.c_double),
+                ("pressure", C.c_double), ("pressure_ramp", C.c_double),
+                ("damping_fraction", C.c_double), ("damping_omega", C.c_double)]
 
 
 class BatchConfig(C.Structure):
@@ -182,7 +187,7 @@ _PROTOS = {
     "batch_state": (_S, [_H, C.POINTER(BatchProgress)]),
     "batch_measure": (_S, [_H, C.POINTER(Measure)]),
     "batch_wall_stats": (_S, [_H, C.POINTER(WallInfo)]),
-    "batch_adjoint_forward": (_S, [_H, C.c_int32]),
+    "batch_adjoint_forward": (_S, [_H, C.c_int32, C.c_int32]),
     "batch_adjoint_backward": (_S, [_H, C.c_int32, c_double_p, c_double_p]),
     "batch_adjoint_elapsed": (_S, [_H, C.POINTER(C.c_double), C.POINTER(C.c_double)]),
 }

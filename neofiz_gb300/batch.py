@@ -36,6 +36,9 @@ class Instance:
     hourglass: float = 0.05
     fixed_radial: Sequence[int] = field(default_factory=tuple)
     fixed_axial: Sequence[int] = field(default_factory=tuple)
+    pressure: tuple = (0.0, 0.0)          # setPressureRamp(pascals, seconds), on the mesh's edges
+    damping: Optional[tuple] = None       # setRelaxationDamping(fraction, omega)
+    damage: Optional[tuple] = None        # setDamage(gf[E], eps[E]); all instances or none
 
 
 def _raise(api, handle, status):
@@ -72,6 +75,20 @@ class BatchSolver:
         self._r = np.concatenate([i.mesh.r for i in self.instances]).astype(np.float64)
         self._z = np.concatenate([i.mesh.z for i in self.instances]).astype(np.float64)
         self._conn = np.concatenate([i.mesh.conn for i in self.instances]).astype(np.int32)
+        edges = np.array([0] + [i.mesh.pressureEdges.size // 2 for i in self.instances],
+                         dtype=np.int64)
+        self.pressure_offset = np.cumsum(edges).astype(np.int32)
+        self._pedges = (np.concatenate([i.mesh.pressureEdges for i in self.instances])
+                        .astype(np.int32) if edges.sum() else np.zeros(2, np.int32))
+        damaged = [i.damage is not None for i in self.instances]
+        if any(damaged) and not all(damaged):
+            raise ValueError("damage is set on every instance of a batch or on none")
+        if all(damaged):
+            self._gf = np.concatenate([np.broadcast_to(np.asarray(i.damage[0], np.float64),
+                                                       (i.mesh.elementCount,))
+                                       for i in self.instances]).astype(np.float64)
+            self._eps = np.concatenate([np.asarray(i.damage[1], np.float64)
+                                        for i in self.instances]).astype(np.float64)
         self._fixed = np.zeros(int(self.node_offset[-1]), dtype=np.uint8)
         for k, inst in enumerate(self.instances):
             n0 = int(self.node_offset[k])
@@ -87,6 +104,11 @@ class BatchSolver:
         cm.z = self._z.ctypes.data_as(_abi.c_double_p)
         cm.conn = self._conn.ctypes.data_as(_abi.c_int32_p)
         cm.fixed = self._fixed.ctypes.data_as(C.POINTER(C.c_uint8))
+        cm.pressure_offset = self.pressure_offset.ctypes.data_as(_abi.c_int32_p)
+        cm.pressure_edges = self._pedges.ctypes.data_as(_abi.c_int32_p)
+        if all(damaged):
+            cm.failure_strain = self._eps.ctypes.data_as(_abi.c_double_p)
+            cm.fracture_energy = self._gf.ctypes.data_as(_abi.c_double_p)
         table = (_abi.BatchInstance * count)()
         for k, inst in enumerate(self.instances):
             t = table[k]
@@ -98,6 +120,9 @@ class BatchSolver:
                 t.wall_plane, t.wall_friction = float(inst.wall[0]), float(inst.wall[1])
             t.hourglass = float(inst.hourglass)
             t.t_end = float(inst.t_end)
+            t.pressure, t.pressure_ramp = float(inst.pressure[0]), float(inst.pressure[1])
+            if inst.damping is not None:
+                t.damping_fraction, t.damping_omega = map(float, inst.damping)
         out = C.c_void_p()
         st = self._api.batch_create(C.byref(cm), table, int(formulation), int(kinematics),
                                     float(thickness), float(cfl), int(precision), C.byref(out))
@@ -198,14 +223,17 @@ class BatchSolver:
 
     # ------------------------------------------------------------------ adjoint
 
-    def adjointForward(self, checkpointEvery: int = 200) -> float:
-        """Runs every instance to its t_end keeping checkpoints (FP64 batches); device ms."""
-        self._check(self._api.batch_adjoint_forward(self._handle, int(checkpointEvery)))
+    def adjointForward(self, checkpointEvery: int = 200, sampleEvery: int = 0) -> float:
+        """Runs every instance to its t_end keeping checkpoints (FP64 batches), sampling the
+        wall capacity every sampleEvery steps (0: not sampled); device ms."""
+        self._check(self._api.batch_adjoint_forward(self._handle, int(checkpointEvery),
+                                                    int(sampleEvery)))
         return self.adjointElapsed()[0]
 
     def adjointBackward(self, objective: int = _abi.OBJECTIVE_LENGTH_RATIO):
         """(values[count], gradients[count, PARAM_COUNT]) of the objective after the forward
-        pass's steps, with respect to A, B, n, C, m, the kinematic modulus and friction."""
+        pass's steps (or at its sampled capacity peak), with respect to A, B, n, C, m, the
+        kinematic modulus, friction and the fracture energy."""
         values = np.zeros(self.count)
         grads = np.zeros((self.count, _abi.PARAM_COUNT))
         self._check(self._api.batch_adjoint_backward(

@@ -43,8 +43,8 @@ struct Batch {
     std::vector<void *> adjAllocs;
     bool adjForward = false;
     double adjForwardMs = 0.0, adjBackwardMs = 0.0;
-    long long adjTapeBytes = 0, adjBarBytes = 0;
-    std::vector<long long> adjBarOff;
+    long long adjTapeBytes = 0, adjBarBytes = 0, adjSeedBytes = 0;
+    std::vector<long long> adjBarOff, adjSeedOff, adjFinOff, adjStateBytes;
 };
 
 constexpr int GRAPH_CHUNKS = 4;              // chunked launches per graph replay
@@ -166,6 +166,11 @@ std::vector<Span> mutable_state(const Batch &B) {
         v.push_back({d.wPF, 4 * E});
         v.push_back({d.hgF, 8 * E});
         v.push_back({d.hgKF, 4 * E});
+        if (d.dStrF) {
+            v.push_back({d.dStrF, 4 * E});
+            v.push_back({d.dSoftF, 4 * E});
+            v.push_back({d.dWidthF, 4 * E});
+        }
     } else {
         v.push_back({d.sig, 32 * E});
         v.push_back({d.back, 32 * E});
@@ -173,6 +178,11 @@ std::vector<Span> mutable_state(const Batch &B) {
         v.push_back({d.wP, 8 * E});
         v.push_back({d.hg, 16 * E});
         v.push_back({d.hgK, 8 * E});
+        if (d.dStrength) {
+            v.push_back({d.dStrength, 8 * E});
+            v.push_back({d.dSoft, 8 * E});
+            v.push_back({d.dWidth, 8 * E});
+        }
     }
     return v;
 }
@@ -216,9 +226,49 @@ nf_status nf_batch_create(const nf_batch_mesh *mesh, const nf_batch_instance *in
             return bfail(nullptr, NF_EINVAL, "instance %d: friction coefficient must be >= 0", k);
     }
     const long long Nl = mesh->node_offset[count], El = mesh->element_offset[count];
-    if (Nl > INT32_MAX / 2 || El > INT32_MAX / 16)
+    const long long Kl = mesh->pressure_offset ? mesh->pressure_offset[count] : 0;
+    if (Nl > INT32_MAX / 2 || El > INT32_MAX / 16 || Kl > INT32_MAX / 16)
         return bfail(nullptr, NF_EINVAL, "batch too large: %lld nodes, %lld elements", Nl, El);
-    const int N = (int)Nl, E = (int)El;
+    const int N = (int)Nl, E = (int)El, K = (int)Kl;
+    if (mesh->pressure_offset) {
+        if (mesh->pressure_offset[0] != 0 || (K > 0 && !mesh->pressure_edges))
+            return bfail(nullptr, NF_EINVAL, "pressure offsets must start at 0 and have edges");
+        for (int k = 0; k < count; k++) {
+            if (mesh->pressure_offset[k + 1] < mesh->pressure_offset[k])
+                return bfail(nullptr, NF_EINVAL, "pressure offsets of instance %d decrease", k);
+            const int nn = mesh->node_offset[k + 1] - mesh->node_offset[k];
+            for (long long j = 2LL * mesh->pressure_offset[k]; j < 2LL * mesh->pressure_offset[k + 1]; j++)
+                if (mesh->pressure_edges[j] < 0 || mesh->pressure_edges[j] >= nn)
+                    return bfail(nullptr, NF_EINVAL, "instance %d: pressure edge refers to node %d of %d",
+                                 k, mesh->pressure_edges[j], nn);
+        }
+    }
+    const bool damage = mesh->failure_strain != nullptr || mesh->fracture_energy != nullptr;
+    if (damage && (!mesh->failure_strain || !mesh->fracture_energy))
+        return bfail(nullptr, NF_EINVAL, "damage needs both failure strains and fracture energies");
+    for (int k = 0; k < count; k++) {
+        const nf_batch_instance &p = instances[k];
+        if (damage) {                                           // ExplicitSolver.java:746-755
+            const nf_material &m = p.material;
+            const double mu = m.youngs_modulus / (2.0 * (1.0 + m.poisson_ratio));
+            const double worst = 2.0 * mu + (2.0 / 3.0) * (m.kinematic_hardening - m.youngs_modulus);
+            if (!(worst > 0.0))
+                return bfail(nullptr, NF_EINVAL,
+                             "instance %d: a fully clamped softening modulus would make the return "
+                             "map singular: 2mu + (2/3)(H_kin - E) = %.17g <= 0", k, worst);
+        }
+        if (p.damping_omega < 0.0)
+            return bfail(nullptr, NF_EINVAL, "instance %d: angular frequency must be positive", k);
+    }
+    if (damage)
+        for (int e = 0; e < E; e++) {                           // Damage.java:232-260
+            if (!(mesh->fracture_energy[e] > 0.0))
+                return bfail(nullptr, NF_EINVAL, "fracture energy must be positive, was %.17g",
+                             mesh->fracture_energy[e]);
+            if (!(mesh->failure_strain[e] > 0.0))
+                return bfail(nullptr, NF_EINVAL, "failure strain must be positive; point %d has %.17g",
+                             e, mesh->failure_strain[e]);
+        }
     for (int k = 0; k < count; k++) {
         const int n0 = mesh->node_offset[k], nn = mesh->node_offset[k + 1] - n0;
         for (int e = mesh->element_offset[k]; e < mesh->element_offset[k + 1]; e++) {
@@ -263,7 +313,9 @@ nf_status nf_batch_create(const nf_batch_mesh *mesh, const nf_batch_instance *in
     std::vector<double> mass(N, 0.0), invMass(N);
     std::vector<uint8_t> flags(N, 0);
     std::vector<int4> conn(E);
-    std::vector<int32_t> emat(E), slotStart(N + 1, 0), slots(4LL * E);
+    std::vector<int32_t> emat(E), slotStart(N + 1, 0), slots(4LL * E + 2LL * K);
+    std::vector<int2> pedges(K);
+    std::vector<double> geom(damage ? 5LL * E : 0);
     std::vector<MatDev> mats(count);
     std::vector<MatF> matsF(count);
     std::vector<BatchScalars> sc(count);
@@ -278,17 +330,37 @@ nf_status nf_batch_create(const nf_batch_mesh *mesh, const nf_batch_instance *in
         maxNodes = std::max(maxNodes, nn);
         const double *r = mesh->r + n0, *z = mesh->z + n0;
         const int32_t *lc = mesh->conn + 4LL * e0;
+        const int k0 = mesh->pressure_offset ? mesh->pressure_offset[k] : 0;
+        const int nk = mesh->pressure_offset ? mesh->pressure_offset[k + 1] - k0 : 0;
+        const int32_t *lp = nk ? mesh->pressure_edges + 2LL * k0 : nullptr;
         setup_lumped_mass(r, z, lc, ne, &p.material, nullptr, axi, thickness, mass.data() + n0);
-        std::vector<int32_t> ls(nn + 1, 0), lsl(4LL * ne);
-        setup_node_slots(lc, nn, ne, nullptr, 0, ls.data(), lsl.data());
+        std::vector<int32_t> ls(nn + 1, 0), lsl(4LL * ne + 2LL * nk);
+        setup_node_slots(lc, nn, ne, lp, nk, ls.data(), lsl.data());
+        const int slotBase = 4 * e0 + 2 * k0;
         for (int i = 0; i < nn; i++) {
             X0[n0 + i] = make_double2(r[i], z[i]);
             V[n0 + i] = make_double2(p.velocity_r, p.velocity_z);
             invMass[n0 + i] = 1.0 / mass[n0 + i];
             flags[n0 + i] = mesh->fixed ? (uint8_t)(mesh->fixed[n0 + i] & 3) : 0;
-            slotStart[n0 + i + 1] = 4 * e0 + ls[i + 1];
+            slotStart[n0 + i + 1] = slotBase + ls[i + 1];
         }
-        for (int j = 0; j < 4 * ne; j++) slots[4LL * e0 + j] = lsl[j] + 8 * e0;
+        // local sources -> global: element slots shift by 8 e0, edge slots move past all elements
+        for (long long j = 0; j < 4LL * ne + 2LL * nk; j++) {
+            const int v = lsl[j];
+            slots[slotBase + j] = v < 8 * ne ? v + 8 * e0 : (E + k0 + (v >> 3) - ne) * 8 + (v & 7);
+        }
+        for (int j = 0; j < nk; j++) pedges[k0 + j] = make_int2(lp[2 * j] + n0, lp[2 * j + 1] + n0);
+        if (damage)
+            for (int e = 0; e < ne; e++) {                      // ExplicitSolver.java:767-789
+                const int b = 4 * e;
+                const int q0 = lc[b], q1 = lc[b + 1], q2 = lc[b + 2], q3 = lc[b + 3];
+                double *g = geom.data() + 5LL * (e0 + e);
+                g[1] = 0.5 * (r[q1] - r[q0] + r[q2] - r[q3]);
+                g[2] = 0.5 * (z[q1] - z[q0] + z[q2] - z[q3]);
+                g[3] = 0.5 * (r[q3] - r[q0] + r[q2] - r[q1]);
+                g[4] = 0.5 * (z[q3] - z[q0] + z[q2] - z[q1]);
+                g[0] = fabs(element_signed_area(r, z, lc, e));
+            }
         for (int e = 0; e < ne; e++) {
             conn[e0 + e] = make_int4(lc[4 * e] + n0, lc[4 * e + 1] + n0, lc[4 * e + 2] + n0,
                                      lc[4 * e + 3] + n0);
@@ -300,11 +372,14 @@ nf_status nf_batch_create(const nf_batch_mesh *mesh, const nf_batch_instance *in
         const double edge = setup_min_edge(r, z, lc, ne);
         BatchInst &in = B->inst[k];
         in.n0 = n0; in.n1 = n1; in.e0 = e0; in.e1 = e1;
+        in.k0 = k0; in.k1 = k0 + nk;
+        in.pressure = p.pressure;
+        in.ramp = p.pressure_ramp;
         in.hasWall = std::isnan(p.wall_plane) ? 0 : 1;
         in.cfl = cfl_safety;
         in.wave = wave;
         in.massScale = 1.0;
-        in.damping = 0.0;
+        in.damping = p.damping_omega > 0.0 ? 2.0 * p.damping_fraction * p.damping_omega : 0.0;
         in.hourglass = p.hourglass;
         in.wallPlane = in.hasWall ? p.wall_plane : 0.0;
         in.wallFriction = in.hasWall ? p.wall_friction : 0.0;
@@ -321,7 +396,8 @@ nf_status nf_batch_create(const nf_batch_mesh *mesh, const nf_batch_instance *in
     std::iota(order.begin(), order.end(), 0);
     std::stable_sort(order.begin(), order.end(), [&](int a, int c) { return cost[a] > cost[c]; });
 
-    d.N = N; d.E = E; d.K = 0; d.ppe = 1;
+    d.N = N; d.E = E; d.K = K; d.ppe = 1;
+    d.hasDamage = damage ? 1 : 0;
     d.axi = axi ? 1 : 0;
     d.finite = kinematics == NF_FINITE_STRAIN ? 1 : 0;
     d.full = 0;
@@ -337,12 +413,21 @@ nf_status nf_batch_create(const nf_batch_mesh *mesh, const nf_batch_instance *in
     A(d.X0, N); A(d.U, N); A(d.V, N); A(d.F, N); A(d.mass, N); A(d.invMass, N);
     A(d.flags, N); A(d.wallState, N);
     A(d.conn, E); A(d.emat, E); A(d.mats, count);
-    A(d.contribution, 8LL * E);
-    A(d.nodeSlotStart, N + 1); A(d.nodeSlot, 4LL * E);
+    A(d.contribution, 8LL * E + 8LL * K);
+    A(d.nodeSlotStart, N + 1); A(d.nodeSlot, 4LL * E + 2LL * K);
+    A(d.pedges, K);
+    if (damage) {
+        A(d.dFail, E); A(d.dGf, E); A(d.dGeom, 5LL * E);
+        A(d.dStrength, E); A(d.dSoft, E); A(d.dWidth, E);
+        if (B->mixed) {
+            A(d.dFailF, E); A(d.dGfF, E); A(d.dGeomF, 5LL * E);
+            A(d.dStrF, E); A(d.dSoftF, E); A(d.dWidthF, E);
+        }
+    }
     if (B->mixed) {
         A(d.matsF, count);
         A(d.sigF, 4LL * E); A(d.backF, 4LL * E); A(d.epsPF, E); A(d.wPF, E);
-        A(d.hgF, E); A(d.hgKF, E); A(d.contribF, 8LL * E);
+        A(d.hgF, E); A(d.hgKF, E); A(d.contribF, 8LL * E + 8LL * K);
         A(d.pMid, N); A(d.vdt, N);
     } else {
         A(d.sig, 4LL * E); A(d.back, 4LL * E); A(d.epsP, E); A(d.wP, E);
@@ -369,7 +454,22 @@ nf_status nf_batch_create(const nf_batch_mesh *mesh, const nf_batch_instance *in
     U(d.X0, X0.data(), N); U(d.V, V.data(), N); U(d.mass, mass.data(), N);
     U(d.invMass, invMass.data(), N); U(d.flags, flags.data(), N);
     U(d.conn, conn.data(), E); U(d.emat, emat.data(), E); U(d.mats, mats.data(), count);
-    U(d.nodeSlotStart, slotStart.data(), N + 1); U(d.nodeSlot, slots.data(), 4LL * E);
+    U(d.nodeSlotStart, slotStart.data(), N + 1); U(d.nodeSlot, slots.data(), 4LL * E + 2LL * K);
+    U(d.pedges, pedges.data(), K);
+    if (damage) {
+        U(d.dFail, mesh->failure_strain, E); U(d.dGf, mesh->fracture_energy, E);
+        U(d.dGeom, geom.data(), 5LL * E);
+        if (B->mixed) {
+            std::vector<float> f(E), gf(E), g5(5LL * E);
+            for (int e = 0; e < E; e++) {
+                f[e] = (float)mesh->failure_strain[e];
+                gf[e] = (float)mesh->fracture_energy[e];
+            }
+            for (size_t j = 0; j < g5.size(); j++) g5[j] = (float)geom[j];
+            U(d.dFailF, f.data(), E); U(d.dGfF, gf.data(), E); U(d.dGeomF, g5.data(), 5LL * E);
+            if (e_ == cudaSuccess) e_ = cudaStreamSynchronize(B->stream);   // f, gf, g5 die here
+        }
+    }
     if (B->mixed) U(d.matsF, matsF.data(), count);
     U(dInst, B->inst.data(), count);
     U(b.sc, sc.data(), count);
@@ -687,10 +787,11 @@ cudaError_t aalloc(Batch &B, T **p, size_t count) {
 
 extern "C" {
 
-nf_status nf_batch_adjoint_forward(nf_batch *h, int32_t checkpoint_every) {
+nf_status nf_batch_adjoint_forward(nf_batch *h, int32_t checkpoint_every, int32_t sample_every) {
     Batch &B = *reinterpret_cast<Batch *>(h);
     if (checkpoint_every < 1) return bfail(&B, NF_EINVAL, "checkpoint interval must be positive");
     if (B.mixed) return bfail(&B, NF_EINVAL, "the adjoint runs on FP64 batches");
+    if (sample_every < 0) return bfail(&B, NF_EINVAL, "sampling interval must not be negative");
     std::vector<BatchScalars> sc(B.count);
     BCK(&B, cudaMemcpyAsync(sc.data(), B.b.sc, sizeof(BatchScalars) * B.count,
                             cudaMemcpyDeviceToHost, B.stream));
@@ -700,10 +801,11 @@ nf_status nf_batch_adjoint_forward(nf_batch *h, int32_t checkpoint_every) {
         if (sc[k].steps != 0)
             return bfail(&B, NF_ESTATE, "the adjoint's forward pass starts from a fresh batch");
     free_adjoint(B);
+    BCK(&B, adjoint_reserve_stack());
     // checkpoint capacity: 8x the step count the initial CFL step predicts, plus margin
     std::vector<long long> ckptOff(B.count), finOff(B.count), tapeOff(B.count), barOff(B.count);
-    std::vector<long long> cap(B.count), bytes(B.count);
-    long long ck = 0, fi = 0, ta = 0, ba = 0;
+    std::vector<long long> seedOff(B.count), cap(B.count), bytes(B.count);
+    long long ck = 0, fi = 0, ta = 0, ba = 0, se = 0;
     for (int k = 0; k < B.count; k++) {
         const BatchInst &in = B.inst[k];
         const int n = in.n1 - in.n0, e = in.e1 - in.e0;
@@ -713,17 +815,19 @@ nf_status nf_batch_adjoint_forward(nf_batch *h, int32_t checkpoint_every) {
         ckptOff[k] = ck; ck += cap[k] * bytes[k];
         finOff[k] = fi; fi += bytes[k];
         tapeOff[k] = ta; ta += (long long)checkpoint_every * bytes[k];
-        barOff[k] = ba; ba += (long long)adj_bar_bytes(n, e);
+        barOff[k] = ba; ba += (long long)adj_bar_bytes(n, e, in.k1 - in.k0);
+        seedOff[k] = se; se += (long long)adj_seed_bytes(n, e);
     }
     AdjDev &a = B.adj;
     cudaError_t e_ = cudaSuccess;
     long long *dCkptOff = nullptr, *dFinOff = nullptr, *dTapeOff = nullptr, *dBarOff = nullptr;
-    long long *dCap = nullptr, *dBytes = nullptr;
+    long long *dCap = nullptr, *dBytes = nullptr, *dSeedOff = nullptr, *dSeedStep = nullptr;
 #define A(ptr, n) if (e_ == cudaSuccess) e_ = aalloc(B, &(ptr), (n))
-    A(a.ckpt, (size_t)ck); A(a.fin, (size_t)fi);
+    A(a.ckpt, (size_t)ck); A(a.fin, (size_t)fi); A(a.peak, (size_t)fi); A(a.seed, (size_t)se);
     A(dCkptOff, B.count); A(dFinOff, B.count); A(dTapeOff, B.count); A(dBarOff, B.count);
-    A(dCap, B.count); A(dBytes, B.count);
-    A(a.steps, B.count); A(a.grad, (size_t)B.count * NF_PARAM_COUNT); A(a.overflow, 1);
+    A(dCap, B.count); A(dBytes, B.count); A(dSeedOff, B.count); A(dSeedStep, B.count);
+    A(a.steps, B.count); A(a.peakStep, B.count); A(a.peakValue, B.count);
+    A(a.grad, (size_t)B.count * NF_PARAM_COUNT); A(a.overflow, 1);
 #undef A
     if (e_ != cudaSuccess) {
         free_adjoint(B);
@@ -735,9 +839,16 @@ nf_status nf_batch_adjoint_forward(nf_batch *h, int32_t checkpoint_every) {
     BCK(&B, cudaMemcpyAsync(dBarOff, barOff.data(), 8 * B.count, cudaMemcpyHostToDevice, B.stream));
     BCK(&B, cudaMemcpyAsync(dCap, cap.data(), 8 * B.count, cudaMemcpyHostToDevice, B.stream));
     BCK(&B, cudaMemcpyAsync(dBytes, bytes.data(), 8 * B.count, cudaMemcpyHostToDevice, B.stream));
+    BCK(&B, cudaMemcpyAsync(dSeedOff, seedOff.data(), 8 * B.count, cudaMemcpyHostToDevice, B.stream));
     a.ckptOff = dCkptOff; a.finOff = dFinOff; a.tapeOff = dTapeOff; a.barOff = dBarOff;
+    a.peakOff = dFinOff; a.seedOff = dSeedOff; a.seedStep = dSeedStep;
     a.ckptCap = dCap; a.stateBytes = dBytes;
     a.every = checkpoint_every;
+    a.sampleEvery = sample_every;
+    B.adjSeedBytes = se;
+    B.adjSeedOff = seedOff;
+    B.adjFinOff = finOff;
+    B.adjStateBytes = bytes;
     // the tape and adjoint arrays are allocated by the backward pass
     a.tape = nullptr;
     a.bar = nullptr;
@@ -763,12 +874,12 @@ nf_status nf_batch_adjoint_forward(nf_batch *h, int32_t checkpoint_every) {
     return NF_OK;
 }
 
+static bool sampled(long long peakStep) { return peakStep > 0; }
+
 nf_status nf_batch_adjoint_backward(nf_batch *h, int32_t objective, double *values,
                                     double *gradients) {
     Batch &B = *reinterpret_cast<Batch *>(h);
     if (!B.adjForward) return bfail(&B, NF_ESTATE, "run the adjoint's forward pass first");
-    if (objective != NF_OBJECTIVE_LENGTH_RATIO && objective != NF_OBJECTIVE_MUSHROOM)
-        return bfail(&B, NF_EINVAL, "unknown objective %d", objective);
     AdjDev &a = B.adj;
     cudaError_t e_ = cudaSuccess;
     if (!a.tape) {
@@ -777,35 +888,113 @@ nf_status nf_batch_adjoint_backward(nf_batch *h, int32_t objective, double *valu
         if (e_ != cudaSuccess) return bfail(&B, NF_ENOMEM, "adjoint allocation failed: %s",
                                             cudaGetErrorString(e_));
     }
-    // the objective and its seed (the adjoint of the final displacements), per instance
-    std::vector<double2> X0(B.N), U(B.N);
+    // the objective and its seed, per instance: the adjoint of the displacements (and, for the
+    // capacity, of the hoop stress) after step m, the final step or the sampled peak
+    if (objective != NF_OBJECTIVE_LENGTH_RATIO && objective != NF_OBJECTIVE_MUSHROOM &&
+        objective != NF_OBJECTIVE_PEAK_CAPACITY)
+        return bfail(&B, NF_EINVAL, "unknown objective %d", objective);
+    std::vector<double2> X0(B.N);
     BCK(&B, cudaMemcpy(X0.data(), B.d.X0, 16 * (size_t)B.N, cudaMemcpyDeviceToHost));
-    BCK(&B, cudaMemcpy(U.data(), B.d.U, 16 * (size_t)B.N, cudaMemcpyDeviceToHost));
-    std::vector<char> bar((size_t)B.adjBarBytes, 0);
+    std::vector<long long> steps(B.count), peakStep(B.count), seedStep(B.count);
+    BCK(&B, cudaMemcpy(steps.data(), a.steps, 8 * B.count, cudaMemcpyDeviceToHost));
+    BCK(&B, cudaMemcpy(peakStep.data(), a.peakStep, 8 * B.count, cudaMemcpyDeviceToHost));
+    std::vector<char> seed((size_t)B.adjSeedBytes, 0);
+    std::vector<int32_t> conn(4 * (size_t)B.E);
+    BCK(&B, cudaMemcpy(conn.data(), B.d.conn, 16 * (size_t)B.E, cudaMemcpyDeviceToHost));
+    const bool finite = B.d.finite != 0;
     for (int k = 0; k < B.count; k++) {
         const BatchInst &in = B.inst[k];
+        const int n = in.n1 - in.n0, e = in.e1 - in.e0;
+        // the state the objective is read from: the final or the peak block (U and sig)
+        const long long blk = B.adjFinOff[k];
+        const char *src = objective == NF_OBJECTIVE_PEAK_CAPACITY ? a.peak : a.fin;
+        std::vector<double2> U(n);
+        std::vector<double> sig(4 * (size_t)e);
+        BCK(&B, cudaMemcpy(U.data(), src + blk, 16 * (size_t)n, cudaMemcpyDeviceToHost));
+        BCK(&B, cudaMemcpy(sig.data(), src + blk + 3 * ((16 * (size_t)n + 15) & ~(size_t)15),
+                           32 * (size_t)e, cudaMemcpyDeviceToHost));
+        double2 *su = reinterpret_cast<double2 *>(seed.data() + B.adjSeedOff[k]);
+        double *ss = reinterpret_cast<double *>(seed.data() + B.adjSeedOff[k]
+                                                + ((16 * (size_t)n + 15) & ~(size_t)15));
+        auto R_ = [&](int i) { return finite ? X0[in.n0 + i].x + U[i].x : X0[in.n0 + i].x; };
+        auto Z_ = [&](int i) { return finite ? X0[in.n0 + i].y + U[i].y : X0[in.n0 + i].y; };
+        if (objective == NF_OBJECTIVE_PEAK_CAPACITY) {
+            if (!(sampled(peakStep[k])))
+                return bfail(&B, NF_ESTATE, "instance %d: no capacity was sampled in the forward "
+                                            "pass (sample_every 0 or no sample before t_end)", k);
+            seedStep[k] = peakStep[k];
+            // BurstCase.loadCapacity (BurstCase.java:533-553) and its derivatives
+            double hoop = 0.0;
+            for (int j = 0; j < e; j++) {
+                double sum = 0.0;
+                for (int c = 0; c < 4; c++) {
+                    const int p = conn[4 * (size_t)(in.e0 + j) + c] - in.n0;
+                    const int q = conn[4 * (size_t)(in.e0 + j) + (c + 1) % 4] - in.n0;
+                    sum += R_(p) * Z_(q) - R_(q) * Z_(p);
+                }
+                hoop += sig[4 * (size_t)j + 2] * (0.5 * sum);
+            }
+            double bore = DBL_MAX, low = DBL_MAX, high = -DBL_MAX;
+            int ib = 0, il = 0, ih = 0;
+            for (int i = 0; i < n; i++) {
+                if (R_(i) < bore) { bore = R_(i); ib = i; }
+                if (Z_(i) < low) { low = Z_(i); il = i; }
+                if (Z_(i) > high) { high = Z_(i); ih = i; }
+            }
+            const double den = bore * (high - low);
+            const double capv = hoop / den;
+            values[k] = capv;
+            for (int j = 0; j < e; j++) {
+                double r[4], z[4];
+                int nn[4];
+                for (int c = 0; c < 4; c++) {
+                    nn[c] = conn[4 * (size_t)(in.e0 + j) + c] - in.n0;
+                    r[c] = R_(nn[c]);
+                    z[c] = Z_(nn[c]);
+                }
+                double sum = 0.0;
+                for (int c = 0; c < 4; c++) sum += r[c] * z[(c + 1) & 3] - r[(c + 1) & 3] * z[c];
+                ss[4 * (size_t)j + 2] += 0.5 * sum / den;
+                if (finite) {
+                    const double w = sig[4 * (size_t)j + 2] / den;
+                    for (int c = 0; c < 4; c++) {
+                        su[nn[c]].x += w * 0.5 * (z[(c + 1) & 3] - z[(c + 3) & 3]);
+                        su[nn[c]].y += w * 0.5 * (r[(c + 3) & 3] - r[(c + 1) & 3]);
+                    }
+                }
+            }
+            if (finite) {
+                su[ib].x -= capv / bore;
+                su[ih].y -= capv / (high - low);
+                su[il].y += capv / (high - low);
+            }
+            continue;
+        }
+        seedStep[k] = steps[k];
         double zmax = -DBL_MAX, zmin = DBL_MAX, z0max = -DBL_MAX, z0min = DBL_MAX, rmax = -DBL_MAX;
-        int imax = in.n0, imin = in.n0, irmax = in.n0;
-        for (int i = in.n0; i < in.n1; i++) {
-            const double z = X0[i].y + U[i].y, r = X0[i].x + U[i].x;
+        int imax = 0, imin = 0, irmax = 0;
+        for (int i = 0; i < n; i++) {
+            const double z = X0[in.n0 + i].y + U[i].y, r = X0[in.n0 + i].x + U[i].x;
             if (z > zmax) { zmax = z; imax = i; }
             if (z < zmin) { zmin = z; imin = i; }
             if (r > rmax) { rmax = r; irmax = i; }
-            if (X0[i].y > z0max) z0max = X0[i].y;
-            if (X0[i].y < z0min) z0min = X0[i].y;
+            if (X0[in.n0 + i].y > z0max) z0max = X0[in.n0 + i].y;
+            if (X0[in.n0 + i].y < z0min) z0min = X0[in.n0 + i].y;
         }
-        double2 *ub = reinterpret_cast<double2 *>(bar.data() + B.adjBarOff[k]);
         if (objective == NF_OBJECTIVE_LENGTH_RATIO) {
             const double L0 = z0max - z0min;
-            ub[imax - in.n0].y += 1.0 / L0;
-            ub[imin - in.n0].y -= 1.0 / L0;
+            su[imax].y += 1.0 / L0;
+            su[imin].y -= 1.0 / L0;
             values[k] = (zmax - zmin) / L0;
         } else {
-            ub[irmax - in.n0].x += 2.0;
+            su[irmax].x += 2.0;
             values[k] = 2.0 * rmax;
         }
     }
-    BCK(&B, cudaMemcpyAsync(a.bar, bar.data(), bar.size(), cudaMemcpyHostToDevice, B.stream));
+    BCK(&B, cudaMemcpyAsync(a.seed, seed.data(), seed.size(), cudaMemcpyHostToDevice, B.stream));
+    BCK(&B, cudaMemcpyAsync(const_cast<long long *>(a.seedStep), seedStep.data(), 8 * B.count,
+                            cudaMemcpyHostToDevice, B.stream));
+    BCK(&B, cudaMemsetAsync(a.bar, 0, (size_t)B.adjBarBytes, B.stream));
     BCK(&B, cudaEventRecord(B.ev0, B.stream));
     launch_adjoint_backward(B.d, B.b, a, B.stream);
     B.launches += 1;

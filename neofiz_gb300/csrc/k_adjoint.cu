@@ -22,6 +22,7 @@ constexpr int ADJ_T = 256;
 struct StateBlock {
     double2 *U, *V, *F, *hg;
     double *sig, *back, *epsP, *wP, *scal;   // scal: dt, dtPrevious, time, steps, minEdge
+    double *dStr, *dSoft, *dWidth;           // damage state
     uint8_t *flags;
 };
 
@@ -29,12 +30,13 @@ __host__ __device__ inline size_t al16(size_t x) { return (x + 15) & ~(size_t)15
 
 size_t adj_state_bytes(int n, int e) {
     return 3 * al16(16 * (size_t)n) + 2 * al16(32 * (size_t)e) + al16(16 * (size_t)e)
-           + 2 * al16(8 * (size_t)e) + 64 + al16((size_t)n);
+           + 5 * al16(8 * (size_t)e) + 64 + al16((size_t)n);
 }
-size_t adj_bar_bytes(int n, int e) {
+size_t adj_bar_bytes(int n, int e, int k) {
     return 3 * al16(16 * (size_t)n) + 2 * al16(32 * (size_t)e) + al16(16 * (size_t)e)
-           + 2 * al16(8 * (size_t)e) + al16(128 * (size_t)e);
+           + 4 * al16(8 * (size_t)e) + al16(128 * (size_t)e) + al16(32 * (size_t)k);
 }
+size_t adj_seed_bytes(int n, int e) { return al16(16 * (size_t)n) + al16(32 * (size_t)e); }
 
 __device__ StateBlock state_at(char *p, int n, int e) {
     StateBlock s;
@@ -46,6 +48,9 @@ __device__ StateBlock state_at(char *p, int n, int e) {
     s.hg = (double2 *)p; p += al16(16 * (size_t)e);
     s.epsP = (double *)p; p += al16(8 * (size_t)e);
     s.wP = (double *)p; p += al16(8 * (size_t)e);
+    s.dStr = (double *)p; p += al16(8 * (size_t)e);
+    s.dSoft = (double *)p; p += al16(8 * (size_t)e);
+    s.dWidth = (double *)p; p += al16(8 * (size_t)e);
     s.scal = (double *)p; p += 64;
     s.flags = (uint8_t *)p;
     return s;
@@ -55,9 +60,11 @@ __device__ StateBlock state_at(char *p, int n, int e) {
 struct BarBlock {
     double2 *U, *V, *F, *hg;
     double *sig, *back, *epsP, *wP, *corner;   // corner: 16 per element (4 corners x ur uz vr vz)
+    double *dStr, *dSoft;                      // damage state
+    double *edge;                              // 4 per pressure edge: a (r, z), b (r, z)
 };
 
-__device__ BarBlock bar_at(char *p, int n, int e) {
+__device__ BarBlock bar_at(char *p, int n, int e, int k) {
     BarBlock s;
     s.U = (double2 *)p; p += al16(16 * (size_t)n);
     s.V = (double2 *)p; p += al16(16 * (size_t)n);
@@ -67,7 +74,10 @@ __device__ BarBlock bar_at(char *p, int n, int e) {
     s.hg = (double2 *)p; p += al16(16 * (size_t)e);
     s.epsP = (double *)p; p += al16(8 * (size_t)e);
     s.wP = (double *)p; p += al16(8 * (size_t)e);
-    s.corner = (double *)p;
+    s.dStr = (double *)p; p += al16(8 * (size_t)e);
+    s.dSoft = (double *)p; p += al16(8 * (size_t)e);
+    s.corner = (double *)p; p += al16(128 * (size_t)e);
+    s.edge = (double *)p; p += al16(32 * (size_t)k);
     return s;
 }
 
@@ -93,9 +103,15 @@ __device__ void copy_state(const Dev &d, const BatchInst &in, StateBlock s, bool
         if (save) {
             sa[0] = a[0]; sa[1] = a[1]; sb[0] = b[0]; sb[1] = b[1];
             s.hg[j] = d.hg[g]; s.epsP[j] = d.epsP[g]; s.wP[j] = d.wP[g];
+            if (d.hasDamage) {
+                s.dStr[j] = d.dStrength[g]; s.dSoft[j] = d.dSoft[g]; s.dWidth[j] = d.dWidth[g];
+            }
         } else {
             a[0] = sa[0]; a[1] = sa[1]; b[0] = sb[0]; b[1] = sb[1];
             d.hg[g] = s.hg[j]; d.epsP[g] = s.epsP[j]; d.wP[g] = s.wP[j];
+            if (d.hasDamage) {
+                d.dStrength[g] = s.dStr[j]; d.dSoft[g] = s.dSoft[j]; d.dWidth[g] = s.dWidth[j];
+            }
         }
     }
 }
@@ -128,6 +144,87 @@ __device__ void elem_in(const Dev &d, const BatchInst &in, const StateBlock &pre
     x->work = pre.wP[le];
     x->hgR = pre.hg[le].x;
     x->hgZ = pre.hg[le].y;
+    x->damaged = d.hasDamage;
+    if (d.hasDamage) {
+        x->dm.failureStrain = d.dFail[e];
+        x->dm.strength = pre.dStr[le];
+        x->dm.softening = pre.dSoft[le];
+        x->dm.fractureEnergy = d.dGf[e];
+        x->dm.youngs = d.mats[d.emat[e]].youngs;
+        x->dm.geometry = d.dGeom + 5 * (size_t)e;
+    }
+}
+
+// BurstCase.loadCapacity (BurstCase.java:533-553) of the instance's current state: the hoop
+// stress times the current element area summed by a fixed tree, over the bore radius and the
+// height (exact extrema). Valid in every thread.
+template <int T>
+__device__ double capacity_of(const Dev &d, const BatchInst &in, double *shRed) {
+    __shared__ double shExt[3];
+    double hoop = 0.0;
+    for (int e = in.e0 + threadIdx.x; e < in.e1; e += T) {
+        const int4 c = d.conn[e];
+        const int nn[4] = {c.x, c.y, c.z, c.w};
+        double sum = 0.0;
+        for (int k = 0; k < 4; k++) {
+            const int i = nn[k], j = nn[(k + 1) & 3];
+            const double2 xi = d.X0[i], xj = d.X0[j];
+            double ri = xi.x, rj = xj.x, zi = xi.y, zj = xj.y;
+            if (d.finite) {
+                const double2 ui = d.U[i], uj = d.U[j];
+                ri = xi.x + ui.x; rj = xj.x + uj.x; zi = xi.y + ui.y; zj = xj.y + uj.y;
+            }
+            sum += ri * zj - rj * zi;
+        }
+        hoop += d.sig[4 * (size_t)e + 2] * (0.5 * sum);
+    }
+    const double total = block_total<T>(hoop, shRed);
+    double bore = DMAX, low = DMAX, high = -DMAX;
+    for (int i = in.n0 + threadIdx.x; i < in.n1; i += T) {
+        const double2 x = d.X0[i];
+        double r = x.x, z = x.y;
+        if (d.finite) {
+            const double2 u = d.U[i];
+            r = x.x + u.x;
+            z = x.y + u.y;
+        }
+        bore = fmin(bore, r);
+        low = fmin(low, z);
+        high = fmax(high, z);
+    }
+    for (int o = 16; o > 0; o >>= 1) {
+        bore = fmin(bore, __shfl_down_sync(0xffffffffu, bore, o));
+        low = fmin(low, __shfl_down_sync(0xffffffffu, low, o));
+        high = fmax(high, __shfl_down_sync(0xffffffffu, high, o));
+    }
+    if (threadIdx.x == 0) {
+        shExt[0] = DMAX; shExt[1] = DMAX; shExt[2] = -DMAX;
+    }
+    __syncthreads();
+    if ((threadIdx.x & 31) == 0) {
+        // order-free extrema of finite values: a lock-free min over warps through shared
+        // memory would need atomics on doubles; the first thread folds the warps instead
+        shRed[threadIdx.x >> 5] = bore;
+    }
+    __syncthreads();
+    if (threadIdx.x == 0)
+        for (int w = 0; w < T / 32; w++) shExt[0] = fmin(shExt[0], shRed[w]);
+    __syncthreads();
+    if ((threadIdx.x & 31) == 0) shRed[threadIdx.x >> 5] = low;
+    __syncthreads();
+    if (threadIdx.x == 0)
+        for (int w = 0; w < T / 32; w++) shExt[1] = fmin(shExt[1], shRed[w]);
+    __syncthreads();
+    if ((threadIdx.x & 31) == 0) shRed[threadIdx.x >> 5] = high;
+    __syncthreads();
+    if (threadIdx.x == 0) {
+        for (int w = 0; w < T / 32; w++) shExt[2] = fmax(shExt[2], shRed[w]);
+        shRed[T / 32] = total / (shExt[0] * (shExt[2] - shExt[1]));
+    }
+    __syncthreads();
+    const double cap = shRed[T / 32];
+    __syncthreads();
+    return cap;
 }
 
 // Forward: every instance to its t_end, a checkpoint every `every` steps, the final state.
@@ -149,6 +246,8 @@ __global__ void __launch_bounds__(ADJ_T) k_adj_forward(Dev d, BatchDev b, AdjDev
     const MixedGeo none{nullptr, nullptr, nullptr, 0};
     char *ckpt = a.ckpt + a.ckptOff[k];
     const size_t bytes = a.stateBytes[k];
+    double peak = -DMAX;
+    long long peakStep = 0;
     int taken = 0;
     for (;; taken++) {
         if (!(time < in.tEnd)) break;
@@ -173,6 +272,20 @@ __global__ void __launch_bounds__(ADJ_T) k_adj_forward(Dev d, BatchDev b, AdjDev
         minEdge = batch_step<false, ADJ_T>(d, in, dt, dtPrev, time, steps, none, nullptr, nullptr,
                                            0, &scp->status, &wallCount[par][0],
                                            &wallCount[par][1], impulse, loss, fric, shMin);
+        if (a.sampleEvery > 0 && steps % a.sampleEvery == 0) {
+            __syncthreads();
+            const double cap = capacity_of<ADJ_T>(d, in, shMin);
+            if (cap > peak) {                  // the same decision in every thread
+                peak = cap;
+                peakStep = steps;
+                StateBlock pk = state_at(a.peak + a.peakOff[k], n, e);
+                copy_state<ADJ_T>(d, in, pk, true);
+                if (threadIdx.x == 0) {
+                    pk.scal[0] = dt; pk.scal[1] = dtPrev; pk.scal[2] = time;
+                    pk.scal[3] = (double)steps; pk.scal[4] = minEdge;
+                }
+            }
+        }
     }
     const double ti = block_total<ADJ_T>(impulse, shMin);
     const double tl = block_total<ADJ_T>(loss, shMin);
@@ -189,6 +302,8 @@ __global__ void __launch_bounds__(ADJ_T) k_adj_forward(Dev d, BatchDev b, AdjDev
         scp->wImpulse += ti; scp->wEnergyLoss += tl; scp->wFriction += tf;
         scp->done = 1;
         a.steps[k] = steps;
+        a.peakStep[k] = peakStep;
+        a.peakValue[k] = peak;
         fin.scal[0] = dt; fin.scal[1] = dtPrev; fin.scal[2] = time; fin.scal[3] = (double)steps;
         fin.scal[4] = minEdge;
     }
@@ -199,7 +314,7 @@ __global__ void __launch_bounds__(ADJ_T) k_adj_forward(Dev d, BatchDev b, AdjDev
 // memory: atomics need a shared or global address).
 __device__ void reverse_step(const Dev &d, const BatchInst &in, const MatDev &mat, StateBlock pre,
                              BarBlock bar, double *pacc, double *shRed, int *shOwner,
-                             double *shDtb, double *shDtPrevb, int *scratch) {
+                             double *shDtb, double *shDtPrevb, double *shTimeb, int *scratch) {
     const int n = in.n1 - in.n0, e = in.e1 - in.e0;
     const double dt = pre.scal[0], dtPrev = pre.scal[1], minEdge = pre.scal[4];
     const double dtAvg = 0.5 * (dtPrev + dt);
@@ -249,6 +364,8 @@ __device__ void reverse_step(const Dev &d, const BatchInst &in, const MatDev &ma
         ab.work = bar.wP[le];
         ab.hgR = bar.hg[le].x;
         ab.hgZ = bar.hg[le].y;
+        ab.strength = d.hasDamage ? bar.dStr[le] : 0.0;
+        ab.softening = d.hasDamage ? bar.dSoft[le] : 0.0;
         ab.edgeOwner = le == owner ? nf_adj_edge_owner(&x, dt, finite, minEdge) : -1;
         ab.edgeb = edgeb;
         nf_adj_element_reduced(&x, &m, dt, d.axi, finite, d.thickness, in.hourglass, &ab, &dtb,
@@ -262,6 +379,22 @@ __device__ void reverse_step(const Dev &d, const BatchInst &in, const MatDev &ma
         bar.epsP[le] = ab.epsP;
         bar.wP[le] = ab.work;
         bar.hg[le] = make_double2(ab.hgR, ab.hgZ);
+        if (d.hasDamage) {
+            bar.dStr[le] = ab.strength;
+            bar.dSoft[le] = ab.softening;
+        }
+    }
+    // pressure edges, loaded at this step's end time (:1203-1207, :1511-1556)
+    double tpress = 0.0;
+    const double tnow = pre.scal[2] + dt;
+    for (int j = threadIdx.x; j < in.k1 - in.k0; j += ADJ_T) {
+        const int2 ed = d.pedges[in.k0 + j];
+        const int la = ed.x - in.n0, lb = ed.y - in.n0;
+        const double cb[4] = {bar.F[la].x, bar.F[lb].x, bar.F[la].y, bar.F[lb].y};
+        const double2 xa = d.X0[ed.x], xb = d.X0[ed.y], ua = d.U[ed.x], ub = d.U[ed.y];
+        nf_adj_pressure_edge(xa.x, xa.y, xb.x, xb.y, ua.x, ua.y, ub.x, ub.y, tnow, in.pressure,
+                             in.ramp, d.axi, finite, d.thickness, cb, bar.edge + 4 * (size_t)j,
+                             bar.edge + 4 * (size_t)j + 2, &tpress);
     }
     __syncthreads();
     double acc[4] = {0.0, 0.0, 0.0, 0.0};
@@ -270,6 +403,11 @@ __device__ void reverse_step(const Dev &d, const BatchInst &in, const MatDev &ma
         double ub[2] = {bar.U[i].x, bar.U[i].y}, vb[2] = {bar.V[i].x, bar.V[i].y}, fb[2];
         for (int s = d.nodeSlotStart[g]; s < d.nodeSlotStart[g + 1]; s++) {
             const int slot = d.nodeSlot[s];
+            if (slot >= 8 * d.E) {              // a pressure edge's slot
+                const double *c = bar.edge + 4 * (size_t)((slot >> 3) - d.E - in.k0) + 2 * (slot & 7);
+                ub[0] += c[0]; ub[1] += c[1];
+                continue;
+            }
             const double *cr = bar.corner + 16 * (size_t)((slot >> 3) - in.e0) + 4 * (slot & 7);
             ub[0] += cr[0]; ub[1] += cr[1]; vb[0] += cr[2]; vb[1] += cr[3];
         }
@@ -286,9 +424,11 @@ __device__ void reverse_step(const Dev &d, const BatchInst &in, const MatDev &ma
     const double tDt = block_total<ADJ_T>(dtb + acc[2], shRed);
     const double tDecay = block_total<ADJ_T>(acc[0], shRed);
     const double tGain = block_total<ADJ_T>(acc[1], shRed);
+    const double tTime = block_total<ADJ_T>(tpress, shRed);
     if (threadIdx.x == 0) {
         const double dtAvgb = nf_adj_dtavg(tDecay, tGain, dtAvg, in.damping);
-        *shDtb = *shDtPrevb + tDt + 0.5 * dtAvgb;
+        *shTimeb += tTime;                      // time' = time + dt
+        *shDtb = *shDtPrevb + tDt + 0.5 * dtAvgb + *shTimeb;
         *shDtPrevb = 0.5 * dtAvgb;
     }
     __syncthreads();
@@ -300,7 +440,7 @@ __global__ void __launch_bounds__(ADJ_T) k_adj_backward(Dev d, BatchDev b, AdjDe
     __shared__ double shRed[ADJ_T / 32 + 1];
     __shared__ int shOwner;
     __shared__ int scratch[3];                   // wall counts and status of recomputed steps
-    __shared__ double shDtb, shDtPrevb;
+    __shared__ double shDtb, shDtPrevb, shTimeb;
     const int k = blockIdx.x;
     const BatchInst in = b.inst[k];
     const MatDev mat = d.mats[k];
@@ -309,12 +449,18 @@ __global__ void __launch_bounds__(ADJ_T) k_adj_backward(Dev d, BatchDev b, AdjDe
     const size_t bytes = a.stateBytes[k];
     char *ckpt = a.ckpt + a.ckptOff[k];
     char *tape = a.tape + a.tapeOff[k];
-    BarBlock bar = bar_at(a.bar + a.barOff[k], n, e);
+    const int nk = in.k1 - in.k0;
+    BarBlock bar = bar_at(a.bar + a.barOff[k], n, e, nk);
+    const long long m = a.seedStep[k];
+    const double2 *seedU = reinterpret_cast<const double2 *>(a.seed + a.seedOff[k]);
+    const double *seedSig = reinterpret_cast<const double *>(a.seed + a.seedOff[k]
+                                                               + al16(16 * (size_t)n));
     double pacc[NF_ADJ_P_COUNT];
     for (int p = 0; p < NF_ADJ_P_COUNT; p++) pacc[p] = 0.0;
     if (threadIdx.x == 0) {
         shDtb = 0.0;
         shDtPrevb = 0.0;
+        shTimeb = 0.0;
         scratch[0] = scratch[1] = scratch[2] = 0;
     }
     __syncthreads();
@@ -343,9 +489,18 @@ __global__ void __launch_bounds__(ADJ_T) k_adj_backward(Dev d, BatchDev b, AdjDe
             if (threadIdx.x == 0) t.scal[4] = me;
         }
         __syncthreads();
-        for (long long j = end - 1; j >= start; j--)
+        for (long long j = end - 1; j >= start; j--) {
+            if (j == m - 1) {                  // the objective's seed enters after step m
+                for (int i = threadIdx.x; i < n; i += ADJ_T) {
+                    bar.U[i].x += seedU[i].x;
+                    bar.U[i].y += seedU[i].y;
+                }
+                for (int q = threadIdx.x; q < 4 * e; q += ADJ_T) bar.sig[q] += seedSig[q];
+                __syncthreads();
+            }
             reverse_step(d, in, mat, state_at(tape + (j - start) * bytes, n, e), bar, pacc, shRed,
-                         &shOwner, &shDtb, &shDtPrevb, scratch);
+                         &shOwner, &shDtb, &shDtPrevb, &shTimeb, scratch);
+        }
     }
     for (int p = 0; p < NF_ADJ_P_COUNT; p++) {
         const double t = block_total<ADJ_T>(pacc[p], shRed);
@@ -354,6 +509,25 @@ __global__ void __launch_bounds__(ADJ_T) k_adj_backward(Dev d, BatchDev b, AdjDe
     // the solver arrays back to the forward's final state
     StateBlock fin = state_at(a.fin + a.finOff[k], n, e);
     copy_state<ADJ_T>(d, in, fin, false);
+}
+
+// Raises the context's per-thread stack limit to what the adjoint kernels' frames need (the
+// reverse sweep spills registers) plus room for their non-inlined callees, if the limit is
+// lower. The device call graph has no cycles, so the frames are fixed at compile time.
+cudaError_t adjoint_reserve_stack() {
+    size_t need = 0;
+    const void *kernels[2] = {(const void *)k_adj_forward, (const void *)k_adj_backward};
+    for (const void *f : kernels) {
+        cudaFuncAttributes at;
+        const cudaError_t e = cudaFuncGetAttributes(&at, f);
+        if (e != cudaSuccess) return e;
+        if (at.localSizeBytes > need) need = at.localSizeBytes;
+    }
+    need += 512;
+    size_t cur = 0;
+    const cudaError_t e = cudaDeviceGetLimit(&cur, cudaLimitStackSize);
+    if (e != cudaSuccess) return e;
+    return need > cur ? cudaDeviceSetLimit(cudaLimitStackSize, need) : cudaSuccess;
 }
 
 void launch_adjoint_forward(const Dev &d, const BatchDev &b, const AdjDev &a, cudaStream_t st) {

@@ -122,6 +122,12 @@ __global__ void __launch_bounds__(256) k_batch_initial(Dev d, BatchDev b) {
             element_reduced(d, e, 0.0, in.hourglass, m);
         me = block_min_edge<256>(m, shMin);
     }
+    const double t0 = b.sc[blockIdx.x].time;
+    for (int k = in.k0 + threadIdx.x; k < in.k1; k += 256) {
+        if (MIXED) pressure_edge_f32(d, k, t0, in.pressure, in.ramp);
+        else pressure_edge(d, k, t0, in.pressure, in.ramp);
+    }
+    __syncthreads();
     for (int i = in.n0 + threadIdx.x; i < in.n1; i += 256)
         d.F[i] = MIXED ? gather_node_f32(d, i) : gather_node(d, i);
     if (threadIdx.x == 0) b.sc[blockIdx.x].minEdgeSquared = me;

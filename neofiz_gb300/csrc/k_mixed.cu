@@ -197,40 +197,7 @@ __global__ void k_pressure_mixed(Dev d) {
     if (!d.s->active) return;
     const int e = blockIdx.x * blockDim.x + threadIdx.x;
     if (e >= d.K) return;
-    const double t = d.s->time;
-    double p = d.targetPressure;
-    if (d.rampDuration > 0.0) {
-        const double s = jmin(1.0, t / d.rampDuration);
-        p = d.targetPressure * s * s * (3.0 - 2.0 * s);
-    }
-    float *c = d.contribF + 8 * (size_t)(d.E + e);
-    const int2 ed = d.pedges[e];
-    const double2 xa = d.X0[ed.x], xb = d.X0[ed.y];
-    double ra = xa.x, rb = xb.x, za = xa.y, zb = xb.y;
-    if (d.finite) {
-        const double2 ua = d.U[ed.x], ub = d.U[ed.y];
-        ra += ua.x; rb += ub.x; za += ua.y; zb += ub.y;
-    }
-    const double tr = rb - ra, tz = zb - za;
-    const double len = sqrt(tr * tr + tz * tz);
-    if (len == 0.0) {
-        c[0] = 0.f; c[1] = 0.f; c[4] = 0.f; c[5] = 0.f;
-        return;
-    }
-    const double nr = tz / len, nz = -tr / len;
-    double wa, wb;
-    if (d.axi) {
-        const double circumference = 2.0 * NF_PI * len;
-        wa = circumference * (ra / 3.0 + rb / 6.0);
-        wb = circumference * (ra / 6.0 + rb / 3.0);
-    } else {
-        wa = d.thickness * len * 0.5;
-        wb = wa;
-    }
-    c[0] = (float)(p * nr * wa);
-    c[1] = (float)(p * nr * wb);
-    c[4] = (float)(p * nz * wa);
-    c[5] = (float)(p * nz * wb);
+    pressure_edge_f32(d, e, d.s->time, d.targetPressure, d.rampDuration);
 }
 
 // The per-node gather (:1147-1165) of float contributions into FP64 forces, same order.

@@ -360,45 +360,7 @@ __global__ void k_pressure(Dev d) {
     if (!d.s->active) return;
     const int e = blockIdx.x * blockDim.x + threadIdx.x;
     if (e >= d.K) return;
-    const double t = d.s->time;
-    double p = d.targetPressure;
-    if (d.rampDuration > 0.0) {
-        const double s = jmin(1.0, t / d.rampDuration);
-        p = d.targetPressure * s * s * (3.0 - 2.0 * s);
-    }
-    double *c = d.contribution + 8 * (size_t)(d.E + e);
-    const int2 ed = d.pedges[e];
-    const double2 xa = d.X0[ed.x], xb = d.X0[ed.y];
-    double ra, rb, za, zb;
-    if (d.finite) {
-        const double2 ua = d.U[ed.x], ub = d.U[ed.y], va = d.V[ed.x], vb = d.V[ed.y];
-        ra = xa.x + ua.x + 0.0 * va.x; rb = xb.x + ub.x + 0.0 * vb.x;
-        za = xa.y + ua.y + 0.0 * va.y; zb = xb.y + ub.y + 0.0 * vb.y;
-    } else {
-        ra = xa.x; rb = xb.x; za = xa.y; zb = xb.y;
-    }
-    const double tr = rb - ra;
-    const double tz = zb - za;
-    const double len = sqrt(tr * tr + tz * tz);
-    if (len == 0.0) {
-        c[0] = 0.0; c[1] = 0.0; c[4] = 0.0; c[5] = 0.0;
-        return;
-    }
-    const double nr = tz / len;
-    const double nz = -tr / len;
-    double wa, wb;
-    if (d.axi) {
-        const double circumference = 2.0 * NF_PI * len;
-        wa = circumference * (ra / 3.0 + rb / 6.0);
-        wb = circumference * (ra / 6.0 + rb / 3.0);
-    } else {
-        wa = d.thickness * len * 0.5;
-        wb = wa;
-    }
-    c[0] = p * nr * wa;
-    c[1] = p * nr * wb;
-    c[4] = p * nz * wa;
-    c[5] = p * nz * wb;
+    pressure_edge(d, e, d.s->time, d.targetPressure, d.rampDuration);
 }
 
 // ------------------------------------------------------------------------------------ gather

@@ -13,7 +13,7 @@
  * map is differentiated through its converged root by the implicit function theorem.
  *
  * Differentiated parameters (NF_ADJ_P_*): Johnson-Cook A, B, n, C, m, the kinematic
- * hardening modulus and the wall friction coefficient.
+ * hardening modulus, the wall friction coefficient and the fracture energy.
  *
  * Plain C (C99) with NF_HD qualifiers, so the oracle (gcc) and the kernels (nvcc) compile the
  * same text; both build with contraction off.
@@ -24,7 +24,7 @@
 #include "nf_math.h"
 
 enum { NF_ADJ_P_A = 0, NF_ADJ_P_B, NF_ADJ_P_N, NF_ADJ_P_C, NF_ADJ_P_M, NF_ADJ_P_HKIN,
-       NF_ADJ_P_MU, NF_ADJ_P_COUNT };
+       NF_ADJ_P_MU, NF_ADJ_P_GF, NF_ADJ_P_COUNT };
 
 #define NF_ADJ_SQRT_2_3 0x1.a20bd700c2c3ep-1
 #define NF_ADJ_TWO_THIRDS (2.0 / 3.0)
@@ -81,115 +81,271 @@ NF_HD double nf_adj_solve(double norm, double stiffness, double plasticStrain,
 
 /* ------------------------------------------------------------------ J2 return map */
 
-/* Reverse of J2.update (J2.java:163-296, no damage) at one point. In: the rotated stress s[4]
- * and back stress bk[4] ({rr, zz, tt, rz}), epsP, work, the strain increments, strainDt, and
- * the adjoints of the outputs (sb, bb, epsPb, workb). Out (overwriting the same arrays):
- * the adjoints of the inputs; *dEb receives the adjoints of dRR, dZZ, dTT, dGamRZ; dt and
- * parameter adjoints are added to *dtb and pb[]. */
-NF_HD void nf_adj_j2(const double *s, const double *bk, double epsP, double work, double dRR,
-                     double dZZ, double dTT, double dGamRZ, const nf_adj_mat *f, double strainDt,
-                     double *sb, double *bb, double *epsPb, double *workb, double *dEb,
-                     double *dtb, double *pb) {
+/* A point's damage state and parameters (Damage.java:166-200): NULL for a material that
+ * cannot fail. */
+typedef struct {
+    double failureStrain, strength, softening, fractureEnergy, youngs;
+    const double *geometry;      /* area, uR, uZ, vR, vZ of the reference element */
+} nf_adj_damage;
+
+/* The return map's forward values at one point (J2.update, J2.java:163-296, with the damage
+ * branches of Damage.java:306-347), kept for its reverse. */
+typedef struct {
+    double t[4], x[4], norm, temperature, flowStress, radius, hardening, stiffness;
+    double dGamma, n[4], pull, alphaDotN, shift, epsP1;
+    int plastic, softening, clamped, fallback, onset;
+    /* onset: the flow stress at onset and the band width (Damage.begin, :306-336) */
+    double fsOnset, width, slope, diff, cross, anisotropy, phi, l1, l2, line;
+    int isotropic, floored;
+} nf_adj_j2_tape;
+
+/* Forward of the return map in the forward kernels' operation order; fills the tape and the
+ * point's new stress, back stress, plastic strain, plastic work and damage state. */
+NF_HD void nf_adj_j2_forward(const double *s, const double *bk, double epsP, double work,
+                             double dRR, double dZZ, double dTT, double dGamRZ,
+                             const nf_adj_mat *f, double strainDt, const nf_adj_damage *dm,
+                             nf_adj_j2_tape *tp, double *sOut, double *bOut) {
     const double lambda = f->lambda, mu = f->mu;
     const double lt = lambda * (dRR + dZZ + dTT);
-    const double tRR = s[0] + lt + 2.0 * mu * dRR;
-    const double tZZ = s[1] + lt + 2.0 * mu * dZZ;
-    const double tTT = s[2] + lt + 2.0 * mu * dTT;
-    const double tRZ = s[3] + mu * dGamRZ;
-    const double p = (tRR + tZZ + tTT) / 3.0;
-    const double x[4] = {tRR - p - bk[0], tZZ - p - bk[1], tTT - p - bk[2], tRZ - bk[3]};
-    const double norm = sqrt(x[0] * x[0] + x[1] * x[1] + x[2] * x[2] + 2.0 * x[3] * x[3]);
+    tp->t[0] = s[0] + lt + 2.0 * mu * dRR;
+    tp->t[1] = s[1] + lt + 2.0 * mu * dZZ;
+    tp->t[2] = s[2] + lt + 2.0 * mu * dTT;
+    tp->t[3] = s[3] + mu * dGamRZ;
+    const double p = (tp->t[0] + tp->t[1] + tp->t[2]) / 3.0;
+    tp->x[0] = tp->t[0] - p - bk[0];
+    tp->x[1] = tp->t[1] - p - bk[1];
+    tp->x[2] = tp->t[2] - p - bk[2];
+    tp->x[3] = tp->t[3] - bk[3];
+    const double *x = tp->x;
+    tp->norm = sqrt(x[0] * x[0] + x[1] * x[1] + x[2] * x[2] + 2.0 * x[3] * x[3]);
     const int jc = f->jc != 0;
-    const double temperature = !jc ? 0.0 : f->room + f->thermalCoefficient * work;
-    double flowStress;
-    if (!jc) flowStress = f->sy0 + f->hIso * epsP;
-    else flowStress = nf_adj_strain_term(f, epsP) * nf_adj_thermal_term(f, temperature);
-    const double radius = NF_ADJ_SQRT_2_3 * flowStress;
-
-    double tb[4] = {0.0, 0.0, 0.0, 0.0};      /* adjoint of the trial stress */
-    if (!(norm > radius)) {                    /* elastic: s' = trial, the rest unchanged */
-        for (int k = 0; k < 4; k++) tb[k] = sb[k];
+    tp->temperature = !jc ? 0.0 : f->room + f->thermalCoefficient * work;
+    tp->softening = dm != 0 && dm->strength > 0.0;
+    tp->clamped = 0;
+    tp->hardening = 0.0;
+    double fs;
+    if (tp->softening) {
+        fs = dm->strength + dm->softening * (epsP - dm->failureStrain);
+        if (fs > 0.0) {
+            tp->hardening = dm->softening;
+        } else {
+            fs = 0.0;
+            tp->clamped = 1;
+        }
+    } else if (!jc) {
+        fs = f->sy0 + f->hIso * epsP;
+        tp->hardening = f->hIso;
     } else {
-        const double stiffness = 2.0 * mu + NF_ADJ_TWO_THIRDS * f->hKin;
-        double dGamma;
-        if (!jc) dGamma = (norm - radius) / (stiffness + NF_ADJ_TWO_THIRDS * f->hIso);
-        else dGamma = nf_adj_solve(norm, stiffness, epsP, temperature, strainDt, f);
-        const double inv = 1.0 / norm;
-        const double n[4] = {x[0] * inv, x[1] * inv, x[2] * inv, x[3] * inv};
-        const double pull = 2.0 * mu * dGamma;
-        const double alphaDotN = bk[0] * n[0] + bk[1] * n[1] + bk[2] * n[2] + 2.0 * bk[3] * n[3];
-        const double shift = NF_ADJ_TWO_THIRDS * f->hKin * dGamma;
+        fs = nf_adj_strain_term(f, epsP) * nf_adj_thermal_term(f, tp->temperature);
+    }
+    tp->flowStress = fs;
+    tp->radius = NF_ADJ_SQRT_2_3 * fs;
+    tp->plastic = tp->norm > tp->radius;
+    tp->onset = 0;
+    tp->fallback = 0;
+    if (!tp->plastic) {
+        for (int k = 0; k < 4; k++) {
+            sOut[k] = tp->t[k];
+            bOut[k] = bk[k];
+        }
+        tp->epsP1 = epsP;
+        return;
+    }
+    tp->stiffness = 2.0 * mu + NF_ADJ_TWO_THIRDS * f->hKin;
+    double dGamma;
+    if (!jc || tp->softening) {
+        dGamma = (tp->norm - tp->radius) / (tp->stiffness + NF_ADJ_TWO_THIRDS * tp->hardening);
+        if (tp->softening && fs + tp->hardening * NF_ADJ_SQRT_2_3 * dGamma < 0.0) {
+            dGamma = tp->norm / tp->stiffness;
+            tp->fallback = 1;
+        }
+    } else {
+        dGamma = nf_adj_solve(tp->norm, tp->stiffness, epsP, tp->temperature, strainDt, f);
+    }
+    tp->dGamma = dGamma;
+    const double inv = 1.0 / tp->norm;
+    for (int k = 0; k < 4; k++) tp->n[k] = x[k] * inv;
+    const double *n = tp->n;
+    tp->pull = 2.0 * mu * dGamma;
+    for (int k = 0; k < 4; k++) sOut[k] = tp->t[k] - tp->pull * n[k];
+    tp->alphaDotN = bk[0] * n[0] + bk[1] * n[1] + bk[2] * n[2] + 2.0 * bk[3] * n[3];
+    tp->shift = NF_ADJ_TWO_THIRDS * f->hKin * dGamma;
+    for (int k = 0; k < 4; k++) bOut[k] = bk[k] + tp->shift * n[k];
+    tp->epsP1 = epsP + NF_ADJ_SQRT_2_3 * dGamma;
+    if (dm != 0 && !tp->softening && tp->epsP1 >= dm->failureStrain) {
+        tp->onset = 1;
+        tp->fsOnset = !jc ? f->sy0 + f->hIso * tp->epsP1
+                          : nf_adj_strain_term(f, tp->epsP1) * nf_adj_thermal_term(f, tp->temperature);
+        const double area = dm->geometry[0];
+        tp->diff = n[0] - n[1];
+        tp->cross = 2.0 * n[3];
+        tp->anisotropy = nf_hypot(tp->diff, tp->cross);
+        if (tp->anisotropy < 1.0e-9) {
+            tp->isotropic = 1;
+            tp->width = sqrt(area);
+        } else {
+            tp->isotropic = 0;
+            tp->phi = 0.5 * nf_atan2(tp->cross, tp->diff);
+            const double tR = -nf_sin(tp->phi), tZ = nf_cos(tp->phi);
+            tp->l1 = dm->geometry[1] * tR + dm->geometry[2] * tZ;
+            tp->l2 = dm->geometry[3] * tR + dm->geometry[4] * tZ;
+            tp->line = fabs(tp->l1) + fabs(tp->l2);
+            tp->width = area / tp->line;
+        }
+        tp->slope = -tp->fsOnset * tp->fsOnset * tp->width / (2.0 * dm->fractureEnergy);
+        tp->floored = tp->slope < -dm->youngs;
+    }
+}
 
+/* Reverse of the return map at one point from its tape. In: the adjoints of the outputs
+ * (sb[4], bb[4], *epsPb, *workb, and the damage state's *strengthb, *softb). Out: the same
+ * arrays hold the adjoints of the inputs; dEb[4] the adjoints of dRR, dZZ, dTT, dGamRZ; dt and
+ * parameter adjoints are added to *dtb and pb[]. */
+NF_HD void nf_adj_j2_reverse(const nf_adj_j2_tape *tp, const double *bk, double epsP,
+                             const nf_adj_mat *f, double strainDt, const nf_adj_damage *dm,
+                             double *sb, double *bb, double *epsPb, double *workb,
+                             double *strengthb, double *softb, double *dEb, double *dtb,
+                             double *pb) {
+    const double mu = f->mu, lambda = f->lambda;
+    const int jc = f->jc != 0;
+    double tb[4] = {0.0, 0.0, 0.0, 0.0};
+    if (!tp->plastic) {
+        for (int k = 0; k < 4; k++) tb[k] = sb[k];
+        /* bb, epsPb, workb and the damage state pass through */
+    } else {
+        const double *n = tp->n, *x = tp->x;
+        const double norm = tp->norm, dGamma = tp->dGamma, inv = 1.0 / norm;
         double nb[4] = {0.0, 0.0, 0.0, 0.0};
-        double dGammab = NF_ADJ_SQRT_2_3 * (*epsPb);          /* epsP' = epsP + sqrt(2/3) dG */
-        /* bk' = bk + shift n */
-        double shiftb = 0.0;
+        double epsP1b = *epsPb;
+        double tempb = 0.0;
+        /* adjoints of the pre-step damage state: unchanged by the step unless it begins here */
+        double strengthIn = strengthb ? *strengthb : 0.0, softIn = softb ? *softb : 0.0;
+        if (tp->onset) {
+            strengthIn = 0.0;
+            softIn = 0.0;
+            /* strength' = fsOnset; softening' = max(slope, -E); width from the band direction */
+            double fsb = strengthb ? *strengthb : 0.0;
+            double widthb = 0.0;
+            if (!tp->floored && softb) {
+                const double sb_ = *softb;
+                fsb -= sb_ * tp->fsOnset * tp->width / dm->fractureEnergy;
+                widthb = -sb_ * tp->fsOnset * tp->fsOnset / (2.0 * dm->fractureEnergy);
+                pb[NF_ADJ_P_GF] += sb_ * tp->fsOnset * tp->fsOnset * tp->width
+                                   / (2.0 * dm->fractureEnergy * dm->fractureEnergy);
+            }
+            if (!jc) {
+                epsP1b += fsb * f->hIso;
+            } else {
+                const double eps = tp->epsP1;
+                const double Th = nf_adj_thermal_term(f, tp->temperature);
+                const double S = nf_adj_strain_term(f, eps);
+                const double en = eps > 0.0 ? nf_pow(eps, f->n) : 0.0;
+                if (eps > 0.0) {
+                    epsP1b += fsb * f->b * f->n * en / eps * Th;
+                    pb[NF_ADJ_P_B] += fsb * Th * en;
+                    pb[NF_ADJ_P_N] += fsb * Th * f->b * en * nf_log(eps);
+                }
+                pb[NF_ADJ_P_A] += fsb * Th;
+                const double h = (tp->temperature - f->room) / (f->melt - f->room);
+                if (h > 0.0 && h < 1.0) {
+                    const double hm = nf_pow(h, f->m);
+                    tempb += fsb * S * (-f->m * hm / h / (f->melt - f->room));
+                    pb[NF_ADJ_P_M] += fsb * S * (-hm * nf_log(h));
+                }
+            }
+            if (!tp->isotropic) {
+                const double area = dm->geometry[0];
+                const double lineb = -widthb * area / (tp->line * tp->line);
+                const double l1b = tp->l1 >= 0.0 ? lineb : -lineb;
+                const double l2b = tp->l2 >= 0.0 ? lineb : -lineb;
+                const double tRb = l1b * dm->geometry[1] + l2b * dm->geometry[3];
+                const double tZb = l1b * dm->geometry[2] + l2b * dm->geometry[4];
+                const double phib = -tRb * cos(tp->phi) - tZb * sin(tp->phi);
+                const double rr = tp->diff * tp->diff + tp->cross * tp->cross;
+                const double crossb = 0.5 * phib * tp->diff / rr;
+                const double diffb = -0.5 * phib * tp->cross / rr;
+                nb[0] += diffb;
+                nb[1] -= diffb;
+                nb[3] += 2.0 * crossb;
+            }
+        }
+        double dGammab = NF_ADJ_SQRT_2_3 * epsP1b;          /* epsP' = epsP + sqrt(2/3) dG */
+        double shiftb = 0.0;                                /* bk' = bk + shift n */
         for (int k = 0; k < 4; k++) {
             shiftb += bb[k] * n[k];
-            nb[k] += shift * bb[k];
+            nb[k] += tp->shift * bb[k];
         }
         pb[NF_ADJ_P_HKIN] += NF_ADJ_TWO_THIRDS * dGamma * shiftb;
         dGammab += NF_ADJ_TWO_THIRDS * f->hKin * shiftb;
-        /* work' = work + dG (norm - pull + alphaDotN) */
-        const double q = norm - pull + alphaDotN;
+        const double q = norm - tp->pull + tp->alphaDotN;  /* work' = work + dG q */
         dGammab += q * (*workb);
         const double qb = dGamma * (*workb);
         double normb = qb, pullb = -qb;
-        const double adnb = qb;
         double bkb[4];
         for (int k = 0; k < 3; k++) {
-            bkb[k] = bb[k] + adnb * n[k];
-            nb[k] += adnb * bk[k];
+            bkb[k] = bb[k] + qb * n[k];
+            nb[k] += qb * bk[k];
         }
-        bkb[3] = bb[3] + 2.0 * adnb * n[3];
-        nb[3] += 2.0 * adnb * bk[3];
-        /* s' = trial - pull n */
-        for (int k = 0; k < 4; k++) {
+        bkb[3] = bb[3] + 2.0 * qb * n[3];
+        nb[3] += 2.0 * qb * bk[3];
+        for (int k = 0; k < 4; k++) {                       /* s' = trial - pull n */
             tb[k] = sb[k];
             pullb -= sb[k] * n[k];
-            nb[k] -= pull * sb[k];
+            nb[k] -= tp->pull * sb[k];
         }
         dGammab += 2.0 * mu * pullb;
-        /* n = x / norm */
-        double xb[4];
-        double nn = 0.0;
+        double xb[4], nn = 0.0;                             /* n = x / norm */
         for (int k = 0; k < 4; k++) {
             xb[k] = nb[k] * inv;
             nn += nb[k] * n[k];
         }
         normb -= nn * inv;
-        /* dGamma(norm, stiffness, epsP, temperature, dt, parameters) */
-        double stiffb = 0.0, epsPbIn = *epsPb, tempb = 0.0;
-        if (!jc) {
-            const double den = stiffness + NF_ADJ_TWO_THIRDS * f->hIso;
-            normb += dGammab / den;
-            const double radiusb = -dGammab / den;
-            stiffb -= dGammab * dGamma / den;
-            epsPbIn += NF_ADJ_SQRT_2_3 * f->hIso * radiusb;
+        double stiffb = 0.0, epsPbIn = epsP1b;             /* epsP' = epsP + ... */
+        if (!jc || tp->softening) {
+            if (tp->fallback) {
+                normb += dGammab / tp->stiffness;
+                stiffb -= dGammab * dGamma / tp->stiffness;
+            } else {
+                const double den = tp->stiffness + NF_ADJ_TWO_THIRDS * tp->hardening;
+                normb += dGammab / den;
+                const double radiusb = -dGammab / den;
+                stiffb -= dGammab * dGamma / den;
+                const double hardb = -dGammab * dGamma / den * NF_ADJ_TWO_THIRDS;
+                const double fsb = NF_ADJ_SQRT_2_3 * radiusb;
+                if (tp->softening) {
+                    if (!tp->clamped) {
+                        softIn += hardb;
+                        strengthIn += fsb;
+                        softIn += fsb * (epsP - dm->failureStrain);
+                        epsPbIn += fsb * dm->softening;
+                    }
+                } else {
+                    epsPbIn += fsb * f->hIso;
+                }
+            }
         } else {
             const double dEps = NF_ADJ_SQRT_2_3 * dGamma;
             const double eps = epsP + dEps;
             const double rate = strainDt > 0.0 ? dEps / strainDt : 0.0;
             const double S = nf_adj_strain_term(f, eps);
             const double R = nf_adj_rate_term(f, rate);
-            const double Th = nf_adj_thermal_term(f, temperature);
+            const double Th = nf_adj_thermal_term(f, tp->temperature);
             const double en = eps > 0.0 ? nf_pow(eps, f->n) : 0.0;
-            const double Sp = eps > 0.0 ? f->b * f->n * en / eps : 0.0;       /* dS/deps */
+            const double Sp = eps > 0.0 ? f->b * f->n * en / eps : 0.0;
             const int rated = !(rate <= f->refRate);
-            const double Rp = rated ? f->c / rate : 0.0;                      /* dR/drate */
-            const double h = (temperature - f->room) / (f->melt - f->room);
+            const double Rp = rated ? f->c / rate : 0.0;
+            const double h = (tp->temperature - f->room) / (f->melt - f->room);
             const int heated = h > 0.0 && h < 1.0;
             const double hm = heated ? nf_pow(h, f->m) : 0.0;
-            const double gdg = -stiffness
+            const double gdg = -tp->stiffness
                                - NF_ADJ_SQRT_2_3 * (Sp * NF_ADJ_SQRT_2_3 * R * Th
                                                     + S * Rp * (strainDt > 0.0 ? NF_ADJ_SQRT_2_3 / strainDt : 0.0) * Th);
-            const double w = -dGammab / gdg;                                  /* dG = -g_x dx / g_dG */
+            const double w = -dGammab / gdg;
             normb += w;
             stiffb += w * (-dGamma);
             epsPbIn += w * (-NF_ADJ_SQRT_2_3 * Sp * R * Th);
             if (heated) {
-                const double dThdT = -f->m * hm / h / (f->melt - f->room);
-                tempb += w * (-NF_ADJ_SQRT_2_3 * S * R * dThdT);
+                tempb += w * (-NF_ADJ_SQRT_2_3 * S * R * (-f->m * hm / h / (f->melt - f->room)));
                 pb[NF_ADJ_P_M] += w * (-NF_ADJ_SQRT_2_3 * S * R * (-hm * nf_log(h)));
             }
             if (rated && strainDt > 0.0) {
@@ -205,11 +361,11 @@ NF_HD void nf_adj_j2(const double *s, const double *bk, double epsP, double work
         pb[NF_ADJ_P_HKIN] += NF_ADJ_TWO_THIRDS * stiffb;
         *workb += f->thermalCoefficient * tempb;
         *epsPb = epsPbIn;
-        /* norm = sqrt(x . x with 2 rz^2) */
-        for (int k = 0; k < 3; k++) xb[k] += normb * x[k] * inv;
+        if (strengthb) *strengthb = strengthIn;
+        if (softb) *softb = softIn;
+        for (int k = 0; k < 3; k++) xb[k] += normb * x[k] * inv;   /* norm */
         xb[3] += normb * 2.0 * x[3] * inv;
-        /* x = dev(trial) - bk */
-        double pbar = 0.0;
+        double pbar = 0.0;                                  /* x = dev(trial) - bk */
         for (int k = 0; k < 3; k++) {
             tb[k] += xb[k];
             pbar -= xb[k];
@@ -219,9 +375,6 @@ NF_HD void nf_adj_j2(const double *s, const double *bk, double epsP, double work
         bkb[3] -= xb[3];
         for (int k = 0; k < 3; k++) tb[k] += pbar / 3.0;
         for (int k = 0; k < 4; k++) bb[k] = bkb[k];
-    }
-    if (!(norm > radius)) {
-        /* elastic: bb, epsPb, workb pass through unchanged */
     }
     /* trial = s + lt I + 2 mu d (normal), s_rz + mu dGamRZ */
     const double ltb = tb[0] + tb[1] + tb[2];
@@ -268,6 +421,8 @@ typedef struct {
     double sig[4], back[4];      /* point state before the step */
     double epsP, work;
     double hgR, hgZ;             /* hourglass force before the step */
+    int damaged;                 /* the element has damage state (dm below) */
+    nf_adj_damage dm;
 } nf_adj_elem_in;
 
 /* Adjoints flowing into and out of one element. In: g[8] (adjoints of the contribution
@@ -279,6 +434,7 @@ typedef struct {
 typedef struct {
     double g[8];
     double sig[4], back[4], epsP, work, hgR, hgZ;
+    double strength, softening;  /* the damage state's */
     int edgeOwner;
     double edgeb;
     double ur[4], uz[4], vr[4], vz[4];
@@ -340,38 +496,12 @@ NF_HD void nf_adj_element_reduced(const nf_adj_elem_in *in, const nf_adj_mat *f,
         nf_adj_rotate_forward(s1, cs, sn);
         nf_adj_rotate_forward(b1, cs, sn);
     }
-    /* the return map, forward, for the stress the forces use */
-    double s2[4];
-    {
-        const double lambda = f->lambda;
-        const double lt = lambda * (dEpsR + dEpsZ + dEpsT);
-        const double tRR = s1[0] + lt + 2.0 * mu * dEpsR;
-        const double tZZ = s1[1] + lt + 2.0 * mu * dEpsZ;
-        const double tTT = s1[2] + lt + 2.0 * mu * dEpsT;
-        const double tRZ = s1[3] + mu * dGamRZ;
-        const double p = (tRR + tZZ + tTT) / 3.0;
-        const double xRR = tRR - p - b1[0], xZZ = tZZ - p - b1[1], xTT = tTT - p - b1[2];
-        const double xRZ = tRZ - b1[3];
-        const double norm = sqrt(xRR * xRR + xZZ * xZZ + xTT * xTT + 2.0 * xRZ * xRZ);
-        const int jc = f->jc != 0;
-        const double temperature = !jc ? 0.0 : f->room + f->thermalCoefficient * in->work;
-        const double flowStress = !jc ? f->sy0 + f->hIso * in->epsP
-                                      : nf_adj_strain_term(f, in->epsP) * nf_adj_thermal_term(f, temperature);
-        const double radius = NF_ADJ_SQRT_2_3 * flowStress;
-        if (!(norm > radius)) {
-            s2[0] = tRR; s2[1] = tZZ; s2[2] = tTT; s2[3] = tRZ;
-        } else {
-            const double stiffness = 2.0 * mu + NF_ADJ_TWO_THIRDS * f->hKin;
-            const double dGamma = !jc ? (norm - radius) / (stiffness + NF_ADJ_TWO_THIRDS * f->hIso)
-                                      : nf_adj_solve(norm, stiffness, in->epsP, temperature, dt, f);
-            const double iv = 1.0 / norm;
-            const double pull = 2.0 * mu * dGamma;
-            s2[0] = tRR - pull * (xRR * iv);
-            s2[1] = tZZ - pull * (xZZ * iv);
-            s2[2] = tTT - pull * (xTT * iv);
-            s2[3] = tRZ - pull * (xRZ * iv);
-        }
-    }
+    /* the return map, forward (taped), for the stress the forces use */
+    double s2[4], b2[4];
+    nf_adj_j2_tape tp;
+    const nf_adj_damage *dm = in->damaged ? &in->dm : 0;
+    nf_adj_j2_forward(s1, b1, in->epsP, in->work, dEpsR, dEpsZ, dEpsT, dGamRZ, f, dt, dm, &tp, s2,
+                      b2);
     const double sR = s2[0], sZ = s2[1], sT = s2[2], sRZ = s2[3];
     const double vol = axi ? 2.0 * NF_PI * rg * det : thickness * det;
     const double dV = 4.0 * vol;
@@ -464,8 +594,8 @@ NF_HD void nf_adj_element_reduced(const nf_adj_elem_in *in, const nf_adj_mat *f,
     double bb4[4] = {ab->back[0], ab->back[1], ab->back[2], ab->back[3]};
     double epsPb = ab->epsP, workb = ab->work;
     double dEb[4];
-    nf_adj_j2(s1, b1, in->epsP, in->work, dEpsR, dEpsZ, dEpsT, dGamRZ, f, dt, sb4, bb4, &epsPb,
-              &workb, dEb, dtb, pb);
+    nf_adj_j2_reverse(&tp, b1, in->epsP, f, dt, dm, sb4, bb4, &epsPb, &workb,
+                      dm ? &ab->strength : 0, dm ? &ab->softening : 0, dEb, dtb, pb);
     ab->epsP = epsPb;
     ab->work = workb;
     double dEpsRb = dEb[0], dEpsZb = dEb[1], dEpsTb = dEb[2], dGamRZb = dEb[3];
@@ -557,6 +687,69 @@ NF_HD int nf_adj_edge_owner(const nf_adj_elem_in *in, double dt, int finite, dou
         if (dr * dr + dz * dz == value) return k;
     }
     return -1;
+}
+
+/* ------------------------------------------------------------------ pressure edge */
+
+/* Reverse of applyPressure + pressureAt (ExplicitSolver.java:1203-1207, :1511-1556) for one
+ * edge (a, b) at time t (after this step's time advance). cb[4]: adjoints of its slots
+ * (radial at a, radial at b, axial at a, axial at b). Out: ab[2], bb[2] the adjoints of the
+ * edge nodes' displacements (r, z) after the nodal update; the time adjoint added to *tb. */
+NF_HD void nf_adj_pressure_edge(double xar, double xaz, double xbr, double xbz, double uar,
+                                double uaz, double ubr, double ubz, double t, double target,
+                                double rampDuration, int axi, int finite, double thickness,
+                                const double *cb, double *ab, double *bb, double *tb) {
+    double p = target, dpdt = 0.0;
+    if (rampDuration > 0.0) {
+        const double s = t / rampDuration < 1.0 ? t / rampDuration : 1.0;
+        p = target * s * s * (3.0 - 2.0 * s);
+        if (t / rampDuration < 1.0) dpdt = target * (6.0 * s - 6.0 * s * s) / rampDuration;
+    }
+    double ra = xar, rb = xbr, za = xaz, zb = xbz;
+    if (finite) {
+        ra = xar + uar; rb = xbr + ubr; za = xaz + uaz; zb = xbz + ubz;
+    }
+    const double tr = rb - ra, tz = zb - za;
+    const double len = sqrt(tr * tr + tz * tz);
+    ab[0] = ab[1] = bb[0] = bb[1] = 0.0;
+    if (len == 0.0) return;
+    const double nr = tz / len, nz = -tr / len;
+    double wa, wb;
+    if (axi) {
+        const double circ = 2.0 * NF_PI * len;
+        wa = circ * (ra / 3.0 + rb / 6.0);
+        wb = circ * (ra / 6.0 + rb / 3.0);
+    } else {
+        wa = thickness * len * 0.5;
+        wb = wa;
+    }
+    /* c0 = p nr wa, c1 = p nr wb, c4 = p nz wa, c5 = p nz wb */
+    const double pb_ = cb[0] * nr * wa + cb[1] * nr * wb + cb[2] * nz * wa + cb[3] * nz * wb;
+    const double nrb = cb[0] * p * wa + cb[1] * p * wb;
+    const double nzb = cb[2] * p * wa + cb[3] * p * wb;
+    const double wab = cb[0] * p * nr + cb[2] * p * nz;
+    const double wbb = cb[1] * p * nr + cb[3] * p * nz;
+    double lenb = 0.0, rab = 0.0, rbb = 0.0;
+    if (axi) {
+        const double circ = 2.0 * NF_PI * len;
+        const double circb = wab * (ra / 3.0 + rb / 6.0) + wbb * (ra / 6.0 + rb / 3.0);
+        rab += circ * (wab / 3.0 + wbb / 6.0);
+        rbb += circ * (wab / 6.0 + wbb / 3.0);
+        lenb += 2.0 * NF_PI * circb;
+    } else {
+        lenb += thickness * 0.5 * (wab + wbb);
+    }
+    double tzb = nrb / len, trb = -nzb / len;
+    lenb += -nrb * tz / (len * len) + nzb * tr / (len * len);
+    trb += lenb * tr / len;
+    tzb += lenb * tz / len;
+    rbb += trb; rab -= trb;
+    const double zbb = tzb, zab = -tzb;
+    if (finite) {
+        ab[0] = rab; ab[1] = zab;
+        bb[0] = rbb; bb[1] = zbb;
+    }
+    if (tb) *tb += pb_ * dpdt;
 }
 
 /* ------------------------------------------------------------------ one node */

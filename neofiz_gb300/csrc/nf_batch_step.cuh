@@ -78,10 +78,14 @@ __device__ __forceinline__ double batch_step(const Dev &d, const BatchInst &in, 
         const float sdt = (float)dt, qhg = (float)in.hourglass;
         for (int e = in.e0 + threadIdx.x; e < in.e1; e += T)
             element_reduced_f32(d, e, sdt, qhg, pMid, vdt, base, m);
+        for (int k = in.k0 + threadIdx.x; k < in.k1; k += T)     // applyPressure, :1203-1207
+            pressure_edge_f32(d, k, time, in.pressure, in.ramp);
         me = block_min_edge_f<T>(m, shMin);
     } else {
         double m = DMAX;
         for (int e = in.e0 + threadIdx.x; e < in.e1; e += T) element_reduced(d, e, dt, in.hourglass, m);
+        for (int k = in.k0 + threadIdx.x; k < in.k1; k += T)
+            pressure_edge(d, k, time, in.pressure, in.ramp);
         me = block_min_edge<T>(m, shMin);
     }
     // the gather keeps the nodal loop's node-to-thread map, so the next nodal update reads

@@ -427,6 +427,88 @@ static __device__ __forceinline__ void element_reduced_f32(const Dev &d, int e, 
     }
 }
 
+// applyPressure + pressureAt, ExplicitSolver.java:1203-1207, :1511-1556, for pressure edge e at
+// time t (the ramp's target and duration given): writes the edge's contribution slots.
+static __device__ __forceinline__ void pressure_edge(const Dev &d, int e, double t, double target,
+                                                     double rampDuration) {
+    double p = target;
+    if (rampDuration > 0.0) {
+        const double s = jmin(1.0, t / rampDuration);
+        p = target * s * s * (3.0 - 2.0 * s);
+    }
+    double *c = d.contribution + 8 * (size_t)(d.E + e);
+    const int2 ed = d.pedges[e];
+    const double2 xa = d.X0[ed.x], xb = d.X0[ed.y];
+    double ra, rb, za, zb;
+    if (d.finite) {
+        const double2 ua = d.U[ed.x], ub = d.U[ed.y], va = d.V[ed.x], vb = d.V[ed.y];
+        ra = xa.x + ua.x + 0.0 * va.x; rb = xb.x + ub.x + 0.0 * vb.x;
+        za = xa.y + ua.y + 0.0 * va.y; zb = xb.y + ub.y + 0.0 * vb.y;
+    } else {
+        ra = xa.x; rb = xb.x; za = xa.y; zb = xb.y;
+    }
+    const double tr = rb - ra;
+    const double tz = zb - za;
+    const double len = sqrt(tr * tr + tz * tz);
+    if (len == 0.0) {
+        c[0] = 0.0; c[1] = 0.0; c[4] = 0.0; c[5] = 0.0;
+        return;
+    }
+    const double nr = tz / len;
+    const double nz = -tr / len;
+    double wa, wb;
+    if (d.axi) {
+        const double circumference = 2.0 * NF_PI * len;
+        wa = circumference * (ra / 3.0 + rb / 6.0);
+        wb = circumference * (ra / 6.0 + rb / 3.0);
+    } else {
+        wa = d.thickness * len * 0.5;
+        wb = wa;
+    }
+    c[0] = p * nr * wa;
+    c[1] = p * nr * wb;
+    c[4] = p * nz * wa;
+    c[5] = p * nz * wb;
+}
+
+// The same edge in the mixed form: FP64 geometry and load, float contribution slots.
+static __device__ __forceinline__ void pressure_edge_f32(const Dev &d, int e, double t,
+                                                         double target, double rampDuration) {
+    double p = target;
+    if (rampDuration > 0.0) {
+        const double s = jmin(1.0, t / rampDuration);
+        p = target * s * s * (3.0 - 2.0 * s);
+    }
+    float *c = d.contribF + 8 * (size_t)(d.E + e);
+    const int2 ed = d.pedges[e];
+    const double2 xa = d.X0[ed.x], xb = d.X0[ed.y];
+    double ra = xa.x, rb = xb.x, za = xa.y, zb = xb.y;
+    if (d.finite) {
+        const double2 ua = d.U[ed.x], ub = d.U[ed.y];
+        ra += ua.x; rb += ub.x; za += ua.y; zb += ub.y;
+    }
+    const double tr = rb - ra, tz = zb - za;
+    const double len = sqrt(tr * tr + tz * tz);
+    if (len == 0.0) {
+        c[0] = 0.f; c[1] = 0.f; c[4] = 0.f; c[5] = 0.f;
+        return;
+    }
+    const double nr = tz / len, nz = -tr / len;
+    double wa, wb;
+    if (d.axi) {
+        const double circumference = 2.0 * NF_PI * len;
+        wa = circumference * (ra / 3.0 + rb / 6.0);
+        wb = circumference * (ra / 6.0 + rb / 3.0);
+    } else {
+        wa = d.thickness * len * 0.5;
+        wb = wa;
+    }
+    c[0] = (float)(p * nr * wa);
+    c[1] = (float)(p * nr * wb);
+    c[4] = (float)(p * nz * wa);
+    c[5] = (float)(p * nz * wb);
+}
+
 // gather, ExplicitSolver.java:1147-1165: node n's sources in ascending order, then m g.
 static __device__ __forceinline__ double2 gather_node(const Dev &d, int n) {
     double sr = 0.0, sz = 0.0;

@@ -203,9 +203,11 @@ struct Solver {
 // material is mats[instance]). Each instance keeps its own step, time and totals.
 struct BatchInst {
     int n0, n1, e0, e1;                      // its nodes and elements
+    int k0, k1;                              // its pressure edges
     int hasWall, pad;
     double cfl, wave, massScale, damping, hourglass;
     double wallPlane, wallFriction, tEnd;
+    double pressure, ramp;                   // setPressureRamp
 };
 
 struct BatchScalars {
@@ -231,17 +233,22 @@ struct BatchDev {
 // The adjoint's device buffers (k_adjoint.cu): per instance a run of checkpoint blocks, one
 // final-state block, a tape of `every` blocks and the adjoint arrays; byte offsets by instance.
 struct AdjDev {
-    char *ckpt, *fin, *tape, *bar;
-    const long long *ckptOff, *finOff, *tapeOff, *barOff;
+    char *ckpt, *fin, *tape, *bar, *peak, *seed;
+    const long long *ckptOff, *finOff, *tapeOff, *barOff, *peakOff, *seedOff;
     const long long *ckptCap;                // checkpoints available per instance
     const long long *stateBytes;             // bytes of one state block per instance
     long long *steps;                        // the forward's step count per instance
-    double *grad;                            // [count * 7]
+    long long *peakStep;                     // the sampled capacity peak: its step and value
+    double *peakValue;
+    const long long *seedStep;               // the objective's seed enters after this step
+    double *grad;                            // [count * NF_PARAM_COUNT]
     int *overflow;
-    int every;
+    int every, sampleEvery;
 };
 size_t adj_state_bytes(int n, int e);
-size_t adj_bar_bytes(int n, int e);
+size_t adj_bar_bytes(int n, int e, int k);
+size_t adj_seed_bytes(int n, int e);
+cudaError_t adjoint_reserve_stack();
 void launch_adjoint_forward(const Dev &d, const BatchDev &b, const AdjDev &a, cudaStream_t st);
 void launch_adjoint_backward(const Dev &d, const BatchDev &b, const AdjDev &a, cudaStream_t st);
 

@@ -155,16 +155,9 @@ NF_HD void nf_split(double a, double *hi, double *lo) {
     *lo = a - h;
 }
 
-NF_HD double nf_pow(double x, double y) {
-    if (y == 0.0 || x == 1.0) return 1.0;
-    if (x != x || y != y) return NAN;
-    if (x < 0.0) {
-        /* Only integer powers of a negative base are real. Never reached on the solver
-         * path, whose bases are a plastic strain and a homologous temperature in (0, 1). */
-        if (rint(y) != y) return NAN;
-        const double m = nf_pow(-x, y);
-        return fmod(y, 2.0) != 0.0 ? -m : m;
-    }
+/* x^y for x >= 0 (or +inf), y neither 0 nor NaN. */
+NF_HD double nf_pow_nonneg(double x, double y) {
+    if (x == 1.0) return 1.0;
     if (x == 0.0) return y > 0.0 ? 0.0 : INFINITY;
     if (x == INFINITY) return y > 0.0 ? INFINITY : 0.0;
     if (y == INFINITY) return x > 1.0 ? INFINITY : 0.0;
@@ -183,6 +176,21 @@ NF_HD double nf_pow(double x, double y) {
     const int k = (int)kd;
     const double r = ((p - kd * NF_LN2_HI) + plo) - kd * NF_LN2_LO;
     return nf_scale(nf_exp_core(r), k);
+}
+
+/* Not recursive: a device call graph without cycles keeps the kernels' stack depth known at
+ * compile time, so the driver sizes each launch's per-thread stack itself. */
+NF_HD double nf_pow(double x, double y) {
+    if (y == 0.0 || x == 1.0) return 1.0;
+    if (x != x || y != y) return NAN;
+    if (x < 0.0) {
+        /* Only integer powers of a negative base are real. Never reached on the solver
+         * path, whose bases are a plastic strain and a homologous temperature in (0, 1). */
+        if (rint(y) != y) return NAN;
+        const double m = nf_pow_nonneg(-x, y);
+        return fmod(y, 2.0) != 0.0 ? -m : m;
+    }
+    return nf_pow_nonneg(x, y);
 }
 
 /* atan(v) for |v| <= 0.15, Taylor to v^23. */

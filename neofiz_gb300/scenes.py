@@ -179,13 +179,21 @@ def two_blocks(cls, side=10, speed=120.0, damage=True, floor=True, contact=True,
     return s, mesh, {}
 
 
+TUBE_GF = 60.0e3
+
+
+def tube_material(law=None) -> Material:
+    law = law if law is not None else JohnsonCook.COPPER_OFHC.quasiStatic()
+    return Material.COPPER_OFHC.withJohnsonCook(law)
+
+
 def tube(cls, inner=19.6e-3, outer=20.4e-3, height=4.0e-3, nr=4, nz=20, pressure=60.0e6,
          ramp=20.0e-6, integration=Integration.FULL, kinematics=Kinematics.FINITE_STRAIN,
-         damage=True, seed=7):
+         damage=True, seed=7, material=None, gf=TUBE_GF, scale=0.35):
     """A pressurised thin wall with a smoothstep ramp and relaxation damping
-    (DefectBurst.fire, DefectBurst.java:385-411)."""
+    (DefectBurst.fire, DefectBurst.java:385-411); failure strains Weibull(scale, 10)."""
     mesh = QuadMesh.cylinderWall(inner, outer, height, nr, nz)
-    copper = Material.COPPER_OFHC.withJohnsonCook(JohnsonCook.COPPER_OFHC.quasiStatic())
+    copper = material if material is not None else tube_material()
     s = cls(mesh, copper, Formulation.AXISYMMETRIC, integration, kinematics, 1.0, 0.5)
     for n in QuadMesh.axialEndNodes(nr, nz):
         s.fixAxial(n)
@@ -193,10 +201,27 @@ def tube(cls, inner=19.6e-3, outer=20.4e-3, height=4.0e-3, nr=4, nz=20, pressure
     wave = copper.barWaveSpeed()
     s.setRelaxationDamping(0.05, wave / (0.5 * (inner + outer)))
     if damage:
-        field = DefectField(Weibull(0.35, 10.0), 1.0e-9, 1.0e-3, seed)
-        eps = field.sampleOnto(mesh)
-        s.setDamage(np.full(mesh.elementCount, 60.0e3), eps)
+        s.setDamage(np.full(mesh.elementCount, gf), tube_failure_strains(mesh, seed, scale))
     return s, mesh, {}
+
+
+def tube_failure_strains(mesh, seed=7, scale=0.35):
+    field = DefectField(Weibull(scale, 10.0), 1.0e-9, 1.0e-3, seed)
+    return field.sampleOnto(mesh)
+
+
+def tube_instance(inner=19.6e-3, outer=20.4e-3, height=4.0e-3, nr=4, nz=20, pressure=60.0e6,
+                  ramp=20.0e-6, t_end=30.0e-6, damage=True, seed=7, material=None, gf=TUBE_GF,
+                  scale=0.35):
+    """The tube as a batch instance (reduced integration): what tube() builds."""
+    from .batch import Instance
+    mesh = QuadMesh.cylinderWall(inner, outer, height, nr, nz)
+    copper = material if material is not None else tube_material()
+    wave = copper.barWaveSpeed()
+    return Instance(mesh=mesh, material=copper, t_end=t_end, hourglass=0.05,
+                    fixed_axial=QuadMesh.axialEndNodes(nr, nz), pressure=(pressure, ramp),
+                    damping=(0.05, wave / (0.5 * (inner + outer))),
+                    damage=(gf, tube_failure_strains(mesh, seed, scale)) if damage else None)
 
 
 # ---------------------------------------------------------------------------- the Taylor sweep
@@ -298,9 +323,9 @@ def adjoint_rods(count: int = 64, seed: int = ADJOINT_SEED, t_end: float = SWEEP
 
 
 def fraction_gradients(grads, rod):
-    """Gradients in the (A, B, n, C, m, friction, kinematic fraction) convention of the rod's
-    material rule H_kin = f B e^n / e (e the fit strain): chain rule from the adjoint's
-    (A, B, n, C, m, H_kin, friction)."""
+    """Gradients in the (A, B, n, C, m, friction, kinematic fraction, fracture energy)
+    convention of the rod's material rule H_kin = f B e^n / e (e the fit strain): chain rule
+    from the adjoint's (A, B, n, C, m, H_kin, friction, fracture energy)."""
     g = np.asarray(grads, dtype=np.float64)
     b, n = rod["b"], rod["n"]
     e = ROD_FIT_STRAIN
@@ -315,4 +340,5 @@ def fraction_gradients(grads, rod):
     out[..., 4] = g[..., 4]
     out[..., 5] = g[..., 6]
     out[..., 6] = dH * secant
+    out[..., 7:] = g[..., 7:]
     return out

@@ -2108,14 +2108,20 @@ API nf_status nfo_batch_create(const nf_batch_mesh *mesh, const nf_batch_instanc
         nf_mesh m;
         m.node_count = mesh->node_offset[k + 1] - n0;
         m.element_count = mesh->element_offset[k + 1] - e0;
-        m.pressure_edge_count = 0;
+        const int k0 = mesh->pressure_offset ? mesh->pressure_offset[k] : 0;
+        m.pressure_edge_count = mesh->pressure_offset ? mesh->pressure_offset[k + 1] - k0 : 0;
         m.r = mesh->r + n0;
         m.z = mesh->z + n0;
         m.conn = mesh->conn + 4 * (size_t)e0;
-        m.pressure_edges = NULL;
+        m.pressure_edges = m.pressure_edge_count ? mesh->pressure_edges + 2 * (size_t)k0 : NULL;
         nf_status st = nfo_create(&m, &inst[k].material, 1, NULL, formulation, NF_REDUCED,
                                   kinematics, thickness, cfl_safety, &b->s[k]);
         if (!st) st = nfo_set_hourglass_coefficient(b->s[k], inst[k].hourglass);
+        if (!st) st = nfo_set_pressure_ramp(b->s[k], inst[k].pressure, inst[k].pressure_ramp);
+        if (!st && inst[k].damping_omega > 0.0)
+            st = nfo_set_relaxation_damping(b->s[k], inst[k].damping_fraction, inst[k].damping_omega);
+        if (!st && mesh->failure_strain)
+            st = nfo_set_damage(b->s[k], mesh->fracture_energy + e0, mesh->failure_strain + e0);
         for (int i = 0; !st && mesh->fixed && i < m.node_count; i++) {
             if (mesh->fixed[n0 + i] & 1) st = nfo_fix_radial(b->s[k], i);
             if (!st && (mesh->fixed[n0 + i] & 2)) st = nfo_fix_axial(b->s[k], i);
@@ -2243,6 +2249,7 @@ typedef struct {
     double *ur, *uz, *vr, *vz, *fr, *fz;
     uint8_t *onWall;
     double *sig, *back, *epsP, *work, *hgR, *hgZ, *hgK;
+    double *dStrength, *dSoft, *dWidth;          /* when the solver has damage */
     double dt, dtPrevious, minEdgeSquared, time;
     int64_t stepCount;
 } adj_state;
@@ -2253,11 +2260,14 @@ static void adj_alloc(const nfo_solver *h, adj_state *s) {
     s->fr = dalloc(N); s->fz = dalloc(N); s->onWall = balloc(N);
     s->sig = dalloc(4 * E); s->back = dalloc(4 * E); s->epsP = dalloc(E); s->work = dalloc(E);
     s->hgR = dalloc(E); s->hgZ = dalloc(E); s->hgK = dalloc(E);
+    s->dStrength = h->hasDamage ? dalloc(E) : NULL;
+    s->dSoft = h->hasDamage ? dalloc(E) : NULL;
+    s->dWidth = h->hasDamage ? dalloc(E) : NULL;
 }
 static void adj_free(adj_state *s) {
     free(s->ur); free(s->uz); free(s->vr); free(s->vz); free(s->fr); free(s->fz); free(s->onWall);
     free(s->sig); free(s->back); free(s->epsP); free(s->work); free(s->hgR); free(s->hgZ);
-    free(s->hgK);
+    free(s->hgK); free(s->dStrength); free(s->dSoft); free(s->dWidth);
 }
 static void adj_copy(nfo_solver *h, adj_state *s, int save) {
     const size_t N = (size_t)h->N, E = (size_t)h->E;
@@ -2268,6 +2278,10 @@ static void adj_copy(nfo_solver *h, adj_state *s, int save) {
     C_(s->sig, h->sig, 32 * E); C_(s->back, h->back, 32 * E); C_(s->epsP, h->epsP, 8 * E);
     C_(s->work, h->wPlastic, 8 * E); C_(s->hgR, h->hgR, 8 * E); C_(s->hgZ, h->hgZ, 8 * E);
     C_(s->hgK, h->hgK, 8 * E);
+    if (h->hasDamage) {
+        C_(s->dStrength, h->dStrength, 8 * E); C_(s->dSoft, h->dSoft, 8 * E);
+        C_(s->dWidth, h->dWidth, 8 * E);
+    }
 #undef C_
     if (save) {
         s->dt = h->dt; s->dtPrevious = h->dtPrevious; s->minEdgeSquared = h->minEdgeSquared;
@@ -2279,10 +2293,15 @@ static void adj_copy(nfo_solver *h, adj_state *s, int save) {
 }
 
 typedef struct adj_ctx_s {
-    int every;
+    int every, sampleEvery;
     int64_t steps;
     int checkpoints;
     adj_state *ckpt;
+    /* the largest sampled capacity (BurstCase.loadCapacity) and the state it was read from */
+    double peak;
+    int64_t peakStep;
+    adj_state peakState;
+    int hasPeak;
 } adj_ctx;
 
 static void adj_ctx_free(adj_ctx *c) {
@@ -2290,6 +2309,8 @@ static void adj_ctx_free(adj_ctx *c) {
     free(c->ckpt);
     c->ckpt = NULL;
     c->checkpoints = 0;
+    if (c->hasPeak) adj_free(&c->peakState);
+    c->hasPeak = 0;
 }
 
 static void adj_free_all(nfo_batch *b) {
@@ -2320,13 +2341,24 @@ static void adj_elem_in(const nfo_solver *h, int e, nf_adj_elem_in *in) {
     }
     in->epsP = h->epsP[e]; in->work = h->wPlastic[e];
     in->hgR = h->hgR[e]; in->hgZ = h->hgZ[e];
+    in->damaged = h->hasDamage;
+    if (h->hasDamage) {
+        in->dm.failureStrain = h->dFailure[e];
+        in->dm.strength = h->dStrength[e];
+        in->dm.softening = h->dSoft[e];
+        in->dm.fractureEnergy = h->dGf[e];
+        in->dm.youngs = h->dE[e];
+        in->dm.geometry = h->dGeom + GEOMETRY_STRIDE * (size_t)e;
+    }
 }
 
 typedef struct {
     double *ur, *uz, *vr, *vz, *fr, *fz;           /* node adjoints */
     double *sig, *back, *epsP, *work, *hgR, *hgZ;  /* element adjoints */
+    double *strength, *soft;                       /* damage state adjoints */
     double *corner;                                /* [E][4][4] per-corner node adjoints */
-    double dt, dtPrevious;                         /* of the next step's dt and dtPrevious */
+    double *edge;                                  /* [K][4] pressure edges: a (r, z), b (r, z) */
+    double dt, dtPrevious, time;                   /* of the next step's dt, dtPrevious, time */
     double p[NF_ADJ_P_COUNT];
 } adj_bar;
 
@@ -2366,6 +2398,8 @@ static void adj_reverse_step(nfo_solver *h, adj_state *pre, double minEdge, adj_
             bar.back[k] = a->back[4 * e + k];
         }
         bar.epsP = a->epsP[e]; bar.work = a->work[e]; bar.hgR = a->hgR[e]; bar.hgZ = a->hgZ[e];
+        bar.strength = h->hasDamage ? a->strength[e] : 0.0;
+        bar.softening = h->hasDamage ? a->soft[e] : 0.0;
         bar.edgeOwner = e == owner ? ownerEdge : -1;
         bar.edgeb = edgeb;
         const nf_adj_mat m = adj_mat(h, e);
@@ -2378,13 +2412,32 @@ static void adj_reverse_step(nfo_solver *h, adj_state *pre, double minEdge, adj_
             c[0] = bar.ur[k]; c[1] = bar.uz[k]; c[2] = bar.vr[k]; c[3] = bar.vz[k];
         }
         a->epsP[e] = bar.epsP; a->work[e] = bar.work; a->hgR[e] = bar.hgR; a->hgZ[e] = bar.hgZ;
+        if (h->hasDamage) {
+            a->strength[e] = bar.strength;
+            a->soft[e] = bar.softening;
+        }
+    }
+    /* pressure edges (their load at this step's end time) */
+    double tpress = 0.0;
+    const double tnow = pre->time + dt;
+    for (int j = 0; j < h->K; j++) {
+        const int na = h->pedges[2 * j], nb = h->pedges[2 * j + 1];
+        const double cb[4] = {a->fr[na], a->fr[nb], a->fz[na], a->fz[nb]};
+        nf_adj_pressure_edge(h->r[na], h->z[na], h->r[nb], h->z[nb], h->ur[na], h->uz[na],
+                             h->ur[nb], h->uz[nb], tnow, h->targetPressure, h->rampDuration, axi,
+                             finite, h->thickness, cb, a->edge + 4 * (size_t)j,
+                             a->edge + 4 * (size_t)j + 2, &tpress);
     }
     double acc[4] = {0.0, 0.0, 0.0, 0.0};
     for (int i = 0; i < h->N; i++) {
         double ub[2] = {a->ur[i], a->uz[i]}, vb[2] = {a->vr[i], a->vz[i]}, fb[2];
         for (int s = h->nodeSlotStart[i]; s < h->nodeSlotStart[i + 1]; s++) {
             const int slot = h->nodeSlot[s];
-            if (slot >= 8 * h->E) continue;
+            if (slot >= 8 * h->E) {
+                const double *c = a->edge + 4 * (size_t)((slot >> 3) - h->E) + 2 * (slot & 7);
+                ub[0] += c[0]; ub[1] += c[1];
+                continue;
+            }
             const double *c = a->corner + 16 * (size_t)(slot >> 3) + 4 * (slot & 7);
             ub[0] += c[0]; ub[1] += c[1]; vb[0] += c[2]; vb[1] += c[3];
         }
@@ -2397,6 +2450,8 @@ static void adj_reverse_step(nfo_solver *h, adj_state *pre, double minEdge, adj_
     }
     dtb += acc[2];
     a->p[NF_ADJ_P_MU] += acc[3];
+    a->time += tpress;                             /* time' = time + dt */
+    dtb += a->time;
     const double dtAvgb = nf_adj_dtavg(acc[0], acc[1], dtAvg, h->damping);
     dtb += 0.5 * dtAvgb;
     a->dt = dtb;
@@ -2404,15 +2459,47 @@ static void adj_reverse_step(nfo_solver *h, adj_state *pre, double minEdge, adj_
 }
 
 static nf_status adj_check(nfo_solver *h) {
-    if (h->integration != NF_REDUCED || h->gone != NULL || h->hasDamage || h->contact != NULL ||
-        h->K > 0)
-        return fail(h, NF_EINVAL, "the adjoint covers reduced integration without damage, "
-                                  "erosion, contact or pressure");
+    if (h->integration != NF_REDUCED || h->gone != NULL || h->contact != NULL)
+        return fail(h, NF_EINVAL, "the adjoint covers reduced integration without erosion or "
+                                  "contact");
     return NF_OK;
 }
 
-static void adj_forward(nfo_solver *h, adj_ctx *c, double tEnd, int every) {
+/* BurstCase.loadCapacity (BurstCase.java:533-553) of the solver's current state; with the
+ * extremal nodes, for the seed. */
+static double adj_capacity(const nfo_solver *h, const double *ur, const double *uz,
+                           const double *sig, int *iBore, int *iLow, int *iHigh) {
+    const int finite = h->kinematics == NF_FINITE_STRAIN;
+    double hoop = 0.0;
+    for (int e = 0; e < h->E; e++) {
+        double sum = 0.0;
+        for (int k = 0; k < 4; k++) {
+            const int i = h->conn[4 * e + k], j = h->conn[4 * e + (k + 1) % 4];
+            const double ri = finite ? h->r[i] + ur[i] : h->r[i];
+            const double rj = finite ? h->r[j] + ur[j] : h->r[j];
+            const double zi = finite ? h->z[i] + uz[i] : h->z[i];
+            const double zj = finite ? h->z[j] + uz[j] : h->z[j];
+            sum += ri * zj - rj * zi;
+        }
+        hoop += sig[4 * e + 2] * (0.5 * sum);
+    }
+    double bore = DBL_MAX, low = DBL_MAX, high = -DBL_MAX;
+    for (int i = 0; i < h->N; i++) {
+        const double r = finite ? h->r[i] + ur[i] : h->r[i];
+        const double z = finite ? h->z[i] + uz[i] : h->z[i];
+        if (r < bore) { bore = r; *iBore = i; }
+        if (z < low) { low = z; *iLow = i; }
+        if (z > high) { high = z; *iHigh = i; }
+    }
+    return hoop / (bore * (high - low));
+}
+
+static void adj_forward(nfo_solver *h, adj_ctx *c, double tEnd, int every, int sampleEvery) {
     c->every = every;
+    c->sampleEvery = sampleEvery;
+    c->hasPeak = 0;
+    c->peak = -DBL_MAX;
+    c->peakStep = 0;
     int cap = 16;
     c->ckpt = (adj_state *)calloc((size_t)cap, sizeof(adj_state));
     c->checkpoints = 0;
@@ -2427,8 +2514,56 @@ static void adj_forward(nfo_solver *h, adj_ctx *c, double tEnd, int every) {
             c->checkpoints++;
         }
         step(h);
+        if (sampleEvery > 0 && h->stepCount % sampleEvery == 0) {
+            int ib, il, ih;
+            const double cap = adj_capacity(h, h->ur, h->uz, h->sig, &ib, &il, &ih);
+            if (cap > c->peak) {
+                c->peak = cap;
+                c->peakStep = h->stepCount;
+                if (!c->hasPeak) adj_alloc(h, &c->peakState);
+                c->hasPeak = 1;
+                adj_copy(h, &c->peakState, 1);
+            }
+        }
     }
     c->steps = h->stepCount;
+}
+
+/* The capacity's seed: adjoints of the displacements and of the hoop stress in `s`. */
+static double adj_capacity_seed(const nfo_solver *h, const adj_state *s, double *urb,
+                                double *uzb, double *sigb) {
+    const int finite = h->kinematics == NF_FINITE_STRAIN;
+    int ib = 0, il = 0, ih = 0;
+    const double cap = adj_capacity(h, s->ur, s->uz, s->sig, &ib, &il, &ih);
+    const double bore = finite ? h->r[ib] + s->ur[ib] : h->r[ib];
+    const double zl = finite ? h->z[il] + s->uz[il] : h->z[il];
+    const double zh = finite ? h->z[ih] + s->uz[ih] : h->z[ih];
+    const double den = bore * (zh - zl);
+    for (int e = 0; e < h->E; e++) {
+        double r[4], z[4];
+        int nn[4];
+        for (int k = 0; k < 4; k++) {
+            nn[k] = h->conn[4 * e + k];
+            r[k] = finite ? h->r[nn[k]] + s->ur[nn[k]] : h->r[nn[k]];
+            z[k] = finite ? h->z[nn[k]] + s->uz[nn[k]] : h->z[nn[k]];
+        }
+        double sum = 0.0;
+        for (int k = 0; k < 4; k++) sum += r[k] * z[(k + 1) & 3] - r[(k + 1) & 3] * z[k];
+        sigb[4 * e + 2] += 0.5 * sum / den;
+        if (finite) {
+            const double w = s->sig[4 * e + 2] / den;
+            for (int k = 0; k < 4; k++) {
+                urb[nn[k]] += w * 0.5 * (z[(k + 1) & 3] - z[(k + 3) & 3]);
+                uzb[nn[k]] += w * 0.5 * (r[(k + 3) & 3] - r[(k + 1) & 3]);
+            }
+        }
+    }
+    if (finite) {
+        urb[ib] -= cap / bore;
+        uzb[ih] -= cap / (zh - zl);
+        uzb[il] += cap / (zh - zl);
+    }
+    return cap;
 }
 
 static double adj_objective(const nfo_solver *h, int objective, double *ur, double *uz) {
@@ -2463,7 +2598,21 @@ static nf_status adj_backward(nfo_solver *h, adj_ctx *c, int objective, double *
     a.fr = dalloc(N); a.fz = dalloc(N);
     a.sig = dalloc(4 * E); a.back = dalloc(4 * E); a.epsP = dalloc(E); a.work = dalloc(E);
     a.hgR = dalloc(E); a.hgZ = dalloc(E); a.corner = dalloc(16 * E);
-    *value = adj_objective(h, objective, a.ur, a.uz);
+    a.strength = dalloc(E); a.soft = dalloc(E); a.edge = dalloc(4 * (size_t)h->K);
+    /* the objective's seed enters the sweep after step m (the final step, or the capacity's
+       sampled peak) */
+    int64_t m = c->steps;
+    double *seedR = dalloc(N), *seedZ = dalloc(N), *seedSig = dalloc(4 * E);
+    if (objective == NF_OBJECTIVE_PEAK_CAPACITY) {
+        if (!c->hasPeak) {
+            free(seedR); free(seedZ); free(seedSig);
+            return fail(h, NF_ESTATE, "no capacity was sampled in the forward pass");
+        }
+        m = c->peakStep;
+        *value = adj_capacity_seed(h, &c->peakState, seedR, seedZ, seedSig);
+    } else {
+        *value = adj_objective(h, objective, seedR, seedZ);
+    }
     adj_state final_;
     adj_alloc(h, &final_);
     adj_copy(h, &final_, 1);
@@ -2481,8 +2630,13 @@ static nf_status adj_backward(nfo_solver *h, adj_ctx *c, int objective, double *
             step_body(h);
             minEdge[j - start] = h->minEdgeSquared;
         }
-        for (int64_t j = end - 1; j >= start; j--)
+        for (int64_t j = end - 1; j >= start; j--) {
+            if (j == m - 1) {
+                for (size_t i = 0; i < N; i++) { a.ur[i] += seedR[i]; a.uz[i] += seedZ[i]; }
+                for (size_t i = 0; i < 4 * E; i++) a.sig[i] += seedSig[i];
+            }
             adj_reverse_step(h, &tape[j - start], minEdge[j - start], &a);
+        }
     }
     for (int k = 0; k < NF_ADJ_P_COUNT; k++) grad[k] = a.p[k];
     adj_copy(h, &final_, 0);
@@ -2491,7 +2645,8 @@ static nf_status adj_backward(nfo_solver *h, adj_ctx *c, int objective, double *
     free(tape); free(minEdge);
     free(a.ur); free(a.uz); free(a.vr); free(a.vz); free(a.fr); free(a.fz);
     free(a.sig); free(a.back); free(a.epsP); free(a.work); free(a.hgR); free(a.hgZ);
-    free(a.corner);
+    free(a.corner); free(a.strength); free(a.soft); free(a.edge);
+    free(seedR); free(seedZ); free(seedSig);
     return NF_OK;
 }
 
@@ -2502,8 +2657,10 @@ static double now_ms(void) {
     return (double)t.tv_sec * 1e3 + (double)t.tv_nsec * 1e-6;
 }
 
-API nf_status nfo_batch_adjoint_forward(nfo_batch *b, int32_t checkpoint_every) {
+API nf_status nfo_batch_adjoint_forward(nfo_batch *b, int32_t checkpoint_every,
+                                        int32_t sample_every) {
     if (checkpoint_every < 1) return bfail(b, NF_EINVAL, "checkpoint interval must be positive");
+    if (sample_every < 0) return bfail(b, NF_EINVAL, "sampling interval must not be negative");
     for (int k = 0; k < b->count; k++) {
         nf_status st = adj_check(b->s[k]);
         if (st) return bfail(b, st, "%s", nfo_last_error(b->s[k]));
@@ -2515,7 +2672,8 @@ API nf_status nfo_batch_adjoint_forward(nfo_batch *b, int32_t checkpoint_every) 
         for (int k = 0; k < b->count; k++) adj_ctx_free(&b->adj[k]);
     else
         b->adj = (adj_ctx *)calloc((size_t)b->count, sizeof(adj_ctx));
-    for (int k = 0; k < b->count; k++) adj_forward(b->s[k], &b->adj[k], b->tEnd[k], checkpoint_every);
+    for (int k = 0; k < b->count; k++)
+        adj_forward(b->s[k], &b->adj[k], b->tEnd[k], checkpoint_every, sample_every);
     b->adjForwardMs = now_ms() - t0;
     return NF_OK;
 }
@@ -2523,11 +2681,15 @@ API nf_status nfo_batch_adjoint_forward(nfo_batch *b, int32_t checkpoint_every) 
 API nf_status nfo_batch_adjoint_backward(nfo_batch *b, int32_t objective, double *values,
                                          double *gradients) {
     if (!b->adj) return bfail(b, NF_ESTATE, "run the adjoint's forward pass first");
-    if (objective != NF_OBJECTIVE_LENGTH_RATIO && objective != NF_OBJECTIVE_MUSHROOM)
+    if (objective != NF_OBJECTIVE_LENGTH_RATIO && objective != NF_OBJECTIVE_MUSHROOM &&
+        objective != NF_OBJECTIVE_PEAK_CAPACITY)
         return bfail(b, NF_EINVAL, "unknown objective %d", objective);
     const double t0 = now_ms();
-    for (int k = 0; k < b->count; k++)
-        adj_backward(b->s[k], &b->adj[k], objective, &values[k], gradients + (size_t)k * NF_ADJ_P_COUNT);
+    for (int k = 0; k < b->count; k++) {
+        nf_status st = adj_backward(b->s[k], &b->adj[k], objective, &values[k],
+                                    gradients + (size_t)k * NF_ADJ_P_COUNT);
+        if (st) return bfail(b, st, "instance %d: %s", k, nfo_last_error(b->s[k]));
+    }
     b->adjBackwardMs = now_ms() - t0;
     return NF_OK;
 }

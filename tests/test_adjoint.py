@@ -64,7 +64,7 @@ def test_reference_adjoint_matches_central_differences():
     jc0 = scenes._rod_jc(rod)
     p0 = {"A": jc0.a, "B": jc0.b, "n": jc0.n, "C": jc0.c, "m": jc0.m,
           "kinematic": scenes.rod_material_with(jc0).kinematicHardening, "friction": rod["mu"]}
-    for k, name in enumerate(_abi.PARAM_NAMES):
+    for k, name in enumerate(_abi.PARAM_NAMES[:7]):
         dp = H * p0[name]
         fd = (_measure(rod, steps, name, p0[name] + dp)
               - _measure(rod, steps, name, p0[name] - dp)) / (2.0 * dp)
@@ -93,3 +93,72 @@ def test_adjoint_needs_a_fresh_fp64_batch():
     b.run()
     with pytest.raises(RuntimeError):
         b.adjointForward(10)
+
+
+def _tube_law():
+    """Copper with rate and thermal terms (C, m, Taylor-Quinney) and kinematic hardening, so
+    every parameter of the capacity gradient is exercised."""
+    from neofiz_gb300.materials import JohnsonCook
+    return JohnsonCook.COPPER_OFHC
+
+
+def _tube(name=None, value=None, t_end=50.0e-6):
+    law = _tube_law()
+    hkin = 2.0e8
+    gf = scenes.TUBE_GF
+    if name in ("A", "B", "n", "C", "m"):
+        field = {"A": "a", "B": "b", "n": "n", "C": "c", "m": "m"}[name]
+        law = dataclasses.replace(law, **{field: value})
+    elif name == "kinematic":
+        hkin = value
+    elif name == "fracture_energy":
+        gf = value
+    mat = scenes.tube_material(law).withKinematicHardening(hkin)
+    return scenes.tube_instance(nz=10, height=2.0e-3, t_end=t_end, scale=0.04, material=mat, gf=gf)
+
+
+def _capacity(name=None, value=None):
+    b = OracleBatch([_tube(name, value)], scenes.Formulation.AXISYMMETRIC, cfl=0.5)
+    b.adjointForward(64, 10)
+    v, g = b.adjointBackward(_abi.OBJECTIVE_PEAK_CAPACITY)
+    b.close()
+    return v[0], g[0]
+
+
+def test_capacity_gradient_matches_central_differences():
+    """The tube: pressure edges with a smoothstep ramp, relaxation damping and damage that
+    begins before the capacity peak; the peak sampled every 10 steps."""
+    value, grad = _capacity()
+    law = _tube_law()
+    p0 = {"A": law.a, "B": law.b, "n": law.n, "C": law.c, "m": law.m, "kinematic": 2.0e8,
+          "fracture_energy": scenes.TUBE_GF}
+    assert grad[_abi.PARAM_FRACTURE_ENERGY] != 0.0        # damage shapes the peak
+    assert grad[_abi.PARAM_FRICTION] == 0.0               # no wall
+    for k, name in enumerate(_abi.PARAM_NAMES):
+        if name not in p0:
+            continue
+        dp = H * p0[name]
+        fd = (_capacity(name, p0[name] + dp)[0] - _capacity(name, p0[name] - dp)[0]) / (2 * dp)
+        assert grad[k] == pytest.approx(fd, rel=1e-4), (name, grad[k], fd)
+
+
+def test_fraction_convention_is_the_chain_rule():
+    """(A, B, n, C, m, H_kin, mu, Gf) -> (A, B, n, C, m, mu, f, Gf) with H_kin = f B e^n / e:
+    the kinematic column by its three dependencies, the others carried over."""
+    rod = scenes.taylor_sweep(1, seed=5)[0]
+    g = np.arange(1.0, 9.0)
+    out = scenes.fraction_gradients(g, rod)
+    e, f, b, n = scenes.ROD_FIT_STRAIN, scenes.ROD_KINEMATIC_FRACTION, rod["b"], rod["n"]
+
+    def hkin(bb, nn, ff):
+        return ff * bb * e ** nn / e
+
+    h = 1e-7
+    dHdB = (hkin(b * (1 + h), n, f) - hkin(b * (1 - h), n, f)) / (2 * b * h)
+    dHdn = (hkin(b, n * (1 + h), f) - hkin(b, n * (1 - h), f)) / (2 * n * h)
+    dHdf = (hkin(b, n, f * (1 + h)) - hkin(b, n, f * (1 - h))) / (2 * f * h)
+    np.testing.assert_allclose(out[[0, 3, 4]], g[[0, 3, 4]])
+    np.testing.assert_allclose(out[1], g[1] + g[5] * dHdB, rtol=1e-7)
+    np.testing.assert_allclose(out[2], g[2] + g[5] * dHdn, rtol=1e-7)
+    assert out[5] == g[6] and out[7] == g[7]
+    np.testing.assert_allclose(out[6], g[5] * dHdf, rtol=1e-7)

@@ -56,3 +56,27 @@ def test_adjoint_rejects_mixed_batches(gpu_lib):
                     cfl=0.6, precision=_abi.PRECISION_MIXED)
     with pytest.raises(ValueError):
         b.adjointForward(50)
+
+
+def _tubes():
+    from neofiz_gb300.materials import JohnsonCook
+    a = scenes.tube_material(JohnsonCook.COPPER_OFHC).withKinematicHardening(2.0e8)
+    return [scenes.tube_instance(nz=10, height=2.0e-3, t_end=50.0e-6, scale=0.04, material=a),
+            scenes.tube_instance(nz=14, height=2.8e-3, t_end=40.0e-6, scale=0.06, seed=11)]
+
+
+def test_capacity_adjoint_kernel_matches_the_reference_adjoint(gpu_lib):
+    """Pressure edges, damping, damage and the sampled capacity peak on the GPU."""
+    out = {}
+    for cls in (BatchSolver, OracleBatch):
+        b = cls(_tubes(), scenes.Formulation.AXISYMMETRIC, cfl=0.5)
+        b.adjointForward(64, 10)
+        out[cls] = (b.adjointBackward(_abi.OBJECTIVE_PEAK_CAPACITY), b.state()["steps"].copy(),
+                    b.read(_abi.FIELD_UR))
+        b.close()
+    (gv, gg), gs, gu = out[BatchSolver]
+    (ov, og), os_, ou = out[OracleBatch]
+    assert np.array_equal(gs, os_) and np.array_equal(gu, ou)
+    np.testing.assert_allclose(gv, ov, rtol=1e-13)
+    assert og[0][_abi.PARAM_FRACTURE_ENERGY] != 0.0
+    np.testing.assert_allclose(gg, og, rtol=1e-9, atol=1e-12 * np.abs(og).max())

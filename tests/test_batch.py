@@ -64,3 +64,18 @@ def test_batch_rejects_bad_input():
     inst[1].hourglass = -1.0
     with pytest.raises(ValueError):
         OracleBatch(inst, scenes.Formulation.AXISYMMETRIC)
+
+
+def test_oracle_batch_tube_equals_single_scene():
+    """Pressure edges, relaxation damping and damage through the batch surface."""
+    from neofiz_gb300 import Integration
+    inst = scenes.tube_instance(t_end=8.0e-6)
+    b = OracleBatch([inst, scenes.tube_instance(t_end=6.0e-6, seed=9)],
+                    scenes.Formulation.AXISYMMETRIC, cfl=0.5)
+    b.run()
+    s, mesh, _ = scenes.tube(OracleSolver, integration=Integration.REDUCED)
+    s.runUntil(8.0e-6)
+    assert b.state()["steps"][0] == s.steps()
+    for f in (_abi.FIELD_UR, _abi.FIELD_UZ, _abi.FIELD_VR, _abi.FIELD_STRESS,
+              _abi.FIELD_PLASTIC_STRAIN):
+        assert np.array_equal(b.readInstance(f, 0), s.readField(f)), f

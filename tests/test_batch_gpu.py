@@ -141,3 +141,21 @@ def test_mixed_length_ratio_within_1e4_of_fp64(gpu_lib):
         b.close()
     l64, l32 = lengths[_abi.PRECISION_FP64], lengths[_abi.PRECISION_MIXED]
     assert np.all(np.abs(l32 - l64) <= 1e-4 * l64), np.abs(l32 - l64) / l64
+
+
+@pytest.mark.parametrize("precision", [_abi.PRECISION_FP64, _abi.PRECISION_MIXED])
+def test_batch_tube_equals_single_scene(gpu_lib, precision):
+    """Pressure edges, relaxation damping and damage: the batched tube is the single tube."""
+    from neofiz_gb300 import Integration
+    # failure strains Weibull(0.04, 10): damage begins well before 25 us
+    insts = [scenes.tube_instance(t_end=25.0e-6, scale=0.04),
+             scenes.tube_instance(t_end=20.0e-6, seed=3, nz=12, scale=0.04)]
+    b = BatchSolver(insts, scenes.Formulation.AXISYMMETRIC, cfl=0.5, precision=precision)
+    b.run()
+    s, mesh, _ = scenes.tube(ExplicitSolver, integration=Integration.REDUCED, scale=0.04)
+    s.setPrecision(precision)
+    s.runUntil(25.0e-6)
+    assert b.state()["steps"][0] == s.steps()
+    assert s._auditC().max_damage > 0.0 or precision == _abi.PRECISION_MIXED
+    for f in FIELDS:
+        assert np.array_equal(b.readInstance(f, 0), s.readField(f)), f
