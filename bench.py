@@ -54,6 +54,9 @@ def parse():
                    help="run one form alone and print its JSON (profiling of small cases)")
     p.add_argument("--t-end", type=float, default=None,
                    help="with --only: the rods' run length instead of 80 us")
+    p.add_argument("--batch-shape", default=None,
+                   help="threads,stage_nodes,blocks_per_sm for the sweep instead of the "
+                        "autotuner's choice (profiling a given shape)")
     return p.parse_args()
 
 
@@ -231,7 +234,7 @@ def run_ours(args, world, rank, local):
 
     batched = None
     if not args.no_batched:
-        batched = run_batched(args)
+        batched = run_batched(args, plain_fp64=value)
 
     adjoint = None
     if not args.no_adjoint:
@@ -387,14 +390,17 @@ def run_mixed(args, torch):
     }
 
 
-def run_batched(args):
-    """The batched mixed-precision Taylor sweep: args.batch_count axisymmetric rods (nr 6..24,
-    nz 30..120, Johnson-Cook A, B, n, C within +-20 %, friction 0..0.2, 150..250 m/s, drawn
-    by SplitMix64 from a fixed seed), each run to 80 us, in one handle: autotuned shape,
-    graph-replayed chunks of the persistent kernel. Its state (~0.7 GB) is larger than L2.
-    Errors in L/L0 against FP64 on every eighth rod (the FP64 batch, whose instances are
-    bit-identical to single-scene FP64 runs; checked here on four rods); the FP64 baseline is a
-    loop of plain single-scene FP64 runs on a sample of eight rods."""
+def run_batched(args, plain_fp64=None):
+    """The batched Taylor sweep: args.batch_count axisymmetric rods (nr 6..24, nz 30..120,
+    Johnson-Cook A, B, n, C within +-20 %, friction 0..0.2, 150..250 m/s, drawn by SplitMix64
+    from a fixed seed), each run to 80 us, in one handle: autotuned shape, graph-replayed
+    chunks of the persistent kernel. Its state (~0.7 GB) is larger than L2. Two reduced-
+    precision forms: mixed (FP32 element arithmetic, FP64 nodal update and gather) and
+    compensated (also the nodal update and gather in FP32, displacements as compensated float
+    pairs); the line's value is the compensated form. Errors in L/L0 against FP64 on every
+    eighth rod (the FP64 batch, whose instances are bit-identical to single-scene FP64 runs;
+    checked here on four rods); the FP64 baselines are that batch and a loop of plain
+    single-scene FP64 runs on a sample of eight rods."""
     import numpy as np
     from neofiz_gb300 import ExplicitSolver, _abi, scenes
     from neofiz_gb300.batch import BatchSolver
@@ -408,20 +414,29 @@ def run_batched(args):
         return BatchSolver(scenes.sweep_instances(sel), scenes.Formulation.AXISYMMETRIC,
                            cfl=0.6, precision=prec)
 
-    b = make(rods, _abi.PRECISION_MIXED)
-    t0 = time.perf_counter()
-    shape = b.tune(32)
-    tune_s = time.perf_counter() - t0
-    clocks = Clocks(0)
-    clocks.start()
-    launches0 = b.launchCount()
-    ms = b.run()
-    clk = clocks.stop()
-    cycles = b.elementCycles()
-    st = b.state()
-    L32 = np.array([m.length for m in b.measure()]) / L0
-    launches = b.launchCount() - launches0
-    b.close()
+    def timed(prec):
+        b = make(rods, prec)
+        t0 = time.perf_counter()
+        if args.batch_shape:
+            t, sn, bps = (int(x) for x in args.batch_shape.split(","))
+            b.setConfig(t, sn, bps, b.config()["chunk_steps"])
+            shape = b.config()
+        else:
+            shape = b.tune(32)
+        tune_s = time.perf_counter() - t0
+        clocks = Clocks(0)
+        clocks.start()
+        launches0 = b.launchCount()
+        ms = b.run()
+        clk = clocks.stop()
+        out = {"ms": ms, "cycles": b.elementCycles(), "state": b.state(),
+               "L": np.array([m.length for m in b.measure()]) / L0,
+               "launches": b.launchCount() - launches0, "shape": shape, "tune_s": tune_s,
+               "clocks": clk}
+        b.close()
+        return out
+
+    runs = {"compensated": timed(_abi.PRECISION_COMPENSATED), "mixed": timed(_abi.PRECISION_MIXED)}
 
     sub = list(range(0, len(rods), 8))
     f = make([rods[k] for k in sub], _abi.PRECISION_FP64)
@@ -430,7 +445,6 @@ def run_batched(args):
     L64 = np.array([m.length for m in f.measure()]) / L0
     ur64 = [f.readInstance(_abi.FIELD_UZ, j) for j in range(4)]
     f.close()
-    err = np.abs(L32[sub] - L64) / L64
     identical = True
     loop_cycles, loop_s = 0, 0.0
     for j, k in enumerate(sub[:4]):
@@ -446,28 +460,44 @@ def run_batched(args):
         s.synchronize()
         loop_s += time.perf_counter() - t0
         loop_cycles += mesh.elementCount * (s.steps() - 1)
-    rate = cycles / (ms * 1e-3)
     loop_rate = loop_cycles / loop_s
-    return {
+    batch64 = cycles64 / (ms64 * 1e-3)
+
+    def summary(r):
+        rate = r["cycles"] / (r["ms"] * 1e-3)
+        err = np.abs(r["L"][sub] - L64) / L64
+        st = r["state"]
+        o = {"value": rate, "unit": "element-cycles/s", "ms": r["ms"],
+             "element_cycles": r["cycles"],
+             "steps_per_rod": {"mean": float(st["steps"].mean()), "max": int(st["steps"].max())},
+             "shape": r["shape"], "tune_s": r["tune_s"], "gpu_launches": r["launches"],
+             "speedup_vs_fp64_loop": rate / loop_rate,
+             "speedup_vs_fp64_batched": rate / batch64,
+             "L_over_L0_error_vs_fp64": {"max": float(err.max()), "median": float(np.median(err)),
+                                         "p99": float(np.percentile(err, 99)), "rods": len(sub)},
+             "status": int(st["status"].max()), "clocks": r["clocks"]}
+        if plain_fp64:
+            o["speedup_vs_plain_fp64_path"] = rate / plain_fp64
+        return o
+
+    comp = summary(runs["compensated"])
+    line = {
         "workload": f"{len(rods)} axisymmetric Taylor rods (nr 6..24, nz 30..120, JC +-20 %, "
                     f"mu 0..0.2, 150..250 m/s, SplitMix64 seed {scenes.SWEEP_SEED}) to 80 us, "
-                    f"mixed precision, one handle",
-        "value": rate, "unit": "element-cycles/s", "ms": ms, "element_cycles": cycles,
+                    f"one handle",
+        "precision": "compensated (FP32 element, nodal and gather arithmetic; displacements "
+                     "as compensated float pairs; FP64 time, step and audits)",
+        **comp,
         "elements": int(sum(r["nr"] * r["nz"] for r in rods)),
-        "steps_per_rod": {"mean": float(st["steps"].mean()), "max": int(st["steps"].max())},
-        "shape": shape, "tune_s": tune_s, "gpu_launches": launches,
         "l2": "state ~0.7 GB, larger than L2; no flush",
-        "fp64_batched": {"value": cycles64 / (ms64 * 1e-3), "rods": len(sub)},
+        "mixed": summary(runs["mixed"]),
+        "fp64_batched": {"value": batch64, "rods": len(sub)},
         "fp64_loop": {"value": loop_rate, "rods": len(range(0, len(rods), max(1, len(rods) // 8))),
                       "note": "plain single-scene FP64 runs one after another (runUntil), "
                               "host wall clock"},
-        "speedup_vs_fp64_loop": rate / loop_rate,
-        "L_over_L0_error_vs_fp64": {"max": float(err.max()), "median": float(np.median(err)),
-                                    "p99": float(np.percentile(err, 99)), "rods": len(sub)},
         "fp64_batch_equals_single_scene": identical,
-        "status": int(st["status"].max()),
-        "clocks": clk,
     }
+    return line
 
 
 def run_adjoint(args):

@@ -248,7 +248,10 @@ nf_status nf_set_stream(nf_solver *h, void *stream);
  * force arithmetic and keeps the element state in FP32, while nodal kinematics, the force
  * gather, contact and all audits stay FP64. Switching converts the current state. No
  * reference counterpart. */
-enum { NF_PRECISION_FP64 = 0, NF_PRECISION_MIXED = 1 };
+/* NF_PRECISION_COMPENSATED (batches only) also runs the nodal update and the force gather in
+ * FP32, each displacement carried as a compensated float pair (hi + lo, about 48 significant
+ * bits); time, step size and the audits stay FP64. */
+enum { NF_PRECISION_FP64 = 0, NF_PRECISION_MIXED = 1, NF_PRECISION_COMPENSATED = 2 };
 nf_status nf_set_precision(nf_solver *h, int32_t precision);
 
 /* ------------------------------------------------------------------ instrumentation */
@@ -328,7 +331,8 @@ nf_status nf_material_point_update_static(const nf_material *material, int32_t f
  *   setUniformVelocity(vr, vz); then step while time < t_end,
  * plus setPressureRamp on its pressure edges, setRelaxationDamping and setDamage when given,
  * and its trajectory is bit-identical to that scene run alone through nf_create/nf_step in the
- * same precision (NF_PRECISION_FP64 or NF_PRECISION_MIXED). Only reduced integration is
+ * same precision (NF_PRECISION_FP64 or NF_PRECISION_MIXED); NF_PRECISION_COMPENSATED has no
+ * single-scene form, its error is stated against FP64. Only reduced integration is
  * batched, without erosion or contact. Instances may differ in mesh, material, wall,
  * velocity, hourglass, pressure, damping, damage and t_end. */
 typedef struct nf_batch nf_batch;

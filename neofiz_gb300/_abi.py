@@ -24,7 +24,7 @@ NF_OK, NF_EINVAL, NF_ESTATE, NF_EDEVICE, NF_ETIMEOUT, NF_ENOMEM = range(6)
  GROUP_END) = range(7)
 GROUP_NAMES = ("nodal", "erode", "element", "pressure", "gather", "contact", "end")
 
-PRECISION_FP64, PRECISION_MIXED = 0, 1
+PRECISION_FP64, PRECISION_MIXED, PRECISION_COMPENSATED = 0, 1, 2
 
 OBJECTIVE_LENGTH_RATIO, OBJECTIVE_MUSHROOM, OBJECTIVE_PEAK_CAPACITY = 0, 1, 2
 (PARAM_A, PARAM_B, PARAM_N, PARAM_C, PARAM_M, PARAM_KINEMATIC, PARAM_FRICTION,

@@ -923,6 +923,8 @@ nf_status nf_profile_read(nf_solver *h, double *ms, int64_t *steps) {
 
 nf_status nf_set_precision(nf_solver *h, int32_t precision) {
     Solver &S = *reinterpret_cast<Solver *>(h);
+    if (precision == NF_PRECISION_COMPENSATED)
+        return fail(&S, NF_EINVAL, "the compensated form runs in batches (nf_batch_create)");
     if (precision != NF_PRECISION_FP64 && precision != NF_PRECISION_MIXED)
         return fail(&S, NF_EINVAL, "unknown precision %d", precision);
     nf_status st = sync_check(S);

@@ -26,7 +26,9 @@ struct Batch {
     BatchDev b{};
     cudaStream_t stream = nullptr;
     int device = 0, sms = 1;
-    bool mixed = false;
+    bool mixed = false;                      // FP32 element state (mixed or compensated)
+    bool comp = false;                       // the compensated form's FP32 nodal state
+    int mode = NF_PRECISION_FP64;
     std::string err;
     std::vector<BatchInst> inst;
     int N = 0, E = 0, count = 0;
@@ -113,7 +115,7 @@ bool shape_valid(const Batch &B, const BatchShape &s) {
     if (s.threads != 128 && s.threads != 256) return false;
     if (s.stage && !B.mixed) return false;
     if (s.chunk < 1 || s.blocksPerSm < 1) return false;
-    return batch_max_blocks_per_sm(B.mixed, s, B.b.maxNodes) >= s.blocksPerSm;
+    return batch_max_blocks_per_sm(B.mode, s, B.b.maxNodes) >= s.blocksPerSm;
 }
 
 // The run's launches: reset the queue, launch one chunk; GRAPH_CHUNKS times.
@@ -121,7 +123,7 @@ cudaError_t enqueue_chunks(Batch &B, int chunks) {
     for (int c = 0; c < chunks; c++) {
         cudaError_t e = cudaMemsetAsync(B.b.queue, 0, sizeof(int32_t), B.stream);
         if (e != cudaSuccess) return e;
-        e = launch_batch_steps(B.d, B.b, B.mixed, B.shape, B.sms, B.stream);
+        e = launch_batch_steps(B.d, B.b, B.mode, B.shape, B.sms, B.stream);
         if (e != cudaSuccess) return e;
     }
     return cudaSuccess;
@@ -159,6 +161,11 @@ std::vector<Span> mutable_state(const Batch &B) {
     const size_t N = B.N, E = B.E;
     std::vector<Span> v = {{d.U, 16 * N}, {d.V, 16 * N}, {d.F, 16 * N}, {d.flags, N},
                            {d.wallState, N}, {B.b.sc, sizeof(BatchScalars) * B.count}};
+    if (B.comp) {
+        v.push_back({d.uC, 16 * N});
+        v.push_back({d.vC, 8 * N});
+        v.push_back({d.fC, 8 * N});
+    }
     if (B.mixed) {
         v.push_back({d.sigF, 16 * E});
         v.push_back({d.backF, 16 * E});
@@ -205,7 +212,8 @@ nf_status nf_batch_create(const nf_batch_mesh *mesh, const nf_batch_instance *in
         return bfail(nullptr, NF_EINVAL, "a batch needs at least one instance and its mesh arrays");
     if (formulation < 0 || formulation > 2 || kinematics < 0 || kinematics > 1)
         return bfail(nullptr, NF_EINVAL, "unknown formulation or kinematics");
-    if (precision != NF_PRECISION_FP64 && precision != NF_PRECISION_MIXED)
+    if (precision != NF_PRECISION_FP64 && precision != NF_PRECISION_MIXED &&
+        precision != NF_PRECISION_COMPENSATED)
         return bfail(nullptr, NF_EINVAL, "unknown precision %d", precision);
     const int count = mesh->instance_count;
     if (mesh->node_offset[0] != 0 || mesh->element_offset[0] != 0)
@@ -293,7 +301,9 @@ nf_status nf_batch_create(const nf_batch_mesh *mesh, const nf_batch_instance *in
     Batch *B = new Batch();
     Dev &d = B->d;
     BatchDev &b = B->b;
-    B->mixed = precision == NF_PRECISION_MIXED;
+    B->mixed = precision != NF_PRECISION_FP64;
+    B->comp = precision == NF_PRECISION_COMPENSATED;
+    B->mode = precision;
     B->N = N;
     B->E = E;
     B->count = count;
@@ -407,6 +417,7 @@ nf_status nf_batch_create(const nf_batch_mesh *mesh, const nf_batch_instance *in
     d.massScale = 1.0;
     d.nmat = count;
     d.mixed = B->mixed ? 1 : 0;
+    d.comp = B->comp ? 1 : 0;
     d.sms = B->sms;
     cudaError_t e_ = cudaSuccess;
 #define A(ptr, n) if (e_ == cudaSuccess) e_ = balloc(*B, &(ptr), (n))
@@ -429,6 +440,9 @@ nf_status nf_batch_create(const nf_batch_mesh *mesh, const nf_batch_instance *in
         A(d.sigF, 4LL * E); A(d.backF, 4LL * E); A(d.epsPF, E); A(d.wPF, E);
         A(d.hgF, E); A(d.hgKF, E); A(d.contribF, 8LL * E + 8LL * K);
         A(d.pMid, N); A(d.vdt, N);
+        if (B->comp) {
+            A(d.uC, N); A(d.x0C, N); A(d.vC, N); A(d.fC, N); A(d.mC, N);
+        }
     } else {
         A(d.sig, 4LL * E); A(d.back, 4LL * E); A(d.epsP, E); A(d.wP, E);
         A(d.hg, E); A(d.hgK, E);
@@ -481,9 +495,13 @@ nf_status nf_batch_create(const nf_batch_mesh *mesh, const nf_batch_instance *in
     }
     launch_batch_initial(d, b, B->mixed, B->stream);
     B->launches += 1;
+    if (B->comp) {
+        launch_batch_comp(d, true, B->stream);
+        B->launches += 1;
+    }
     // default shape: the most resident blocks of 256 threads, capped at 8 per SM
     BatchShape s{256, 0, 1, 256};
-    const int occ = batch_max_blocks_per_sm(B->mixed, s, maxNodes);
+    const int occ = batch_max_blocks_per_sm(B->mode, s, maxNodes);
     s.blocksPerSm = std::max(1, std::min(occ, 8));
     B->shape = s;
     nf_status st = bsync(*B);
@@ -542,6 +560,10 @@ nf_status nf_batch_run(nf_batch *h, int64_t max_steps) {
         st = bsync(B);
         if (st) return st;
     }
+    if (B.comp) {                            // the FP64 arrays that reads see
+        launch_batch_comp(B.d, false, B.stream);
+        B.launches += 1;
+    }
     BCK(&B, cudaEventRecord(B.ev1, B.stream));
     st = bsync(B);
     if (st) return st;
@@ -573,7 +595,7 @@ nf_status nf_batch_tune(nf_batch *h, int32_t trial_steps, nf_batch_config *chose
     for (int threads : {128, 256})
         for (int stage = 0; stage <= (B.mixed ? 1 : 0); stage++) {
             BatchShape s{threads, stage, 1, trial_steps};
-            const int occ = batch_max_blocks_per_sm(B.mixed, s, B.b.maxNodes);
+            const int occ = batch_max_blocks_per_sm(B.mode, s, B.b.maxNodes);
             for (int bps : {1, 2, 4, 8, 16}) {
                 if (bps > occ) break;
                 s.blocksPerSm = bps;

@@ -23,7 +23,7 @@ constexpr int MEASURE_BLOCK = 256;
 
 // Up to `chunk` steps of instance k by the whole block: ExplicitSolver.step, :940-991, with the
 // loop condition of TaylorImpactCase.java:250-253 (step while time < t_end).
-template <bool MIXED, bool STAGE, int T>
+template <bool MIXED, bool STAGE, int T, bool COMP>
 __device__ void run_instance(const Dev &d, const BatchDev &b, int k, int chunk, float4 *sPMid,
                              float2 *sVdt, double *shMin, int (*wallCount)[2]) {
     const BatchInst in = b.inst[k];
@@ -55,9 +55,9 @@ __device__ void run_instance(const Dev &d, const BatchDev &b, int k, int chunk, 
             wallCount[par ^ 1][0] = 0;
             wallCount[par ^ 1][1] = 0;
         }
-        minEdge = batch_step<MIXED, T>(d, in, dt, dtPrev, time, steps, geo, pMid, vdt, base,
-                                       &scp->status, &wallCount[par][0], &wallCount[par][1],
-                                       impulse, loss, fric, shMin);
+        minEdge = batch_step<MIXED, T, COMP>(d, in, dt, dtPrev, time, steps, geo, pMid, vdt,
+                                             base, &scp->status, &wallCount[par][0],
+                                             &wallCount[par][1], impulse, loss, fric, shMin);
     }
     const double ti = block_total<T>(impulse, shMin);
     const double tl = block_total<T>(loss, shMin);
@@ -83,7 +83,7 @@ __device__ void run_instance(const Dev &d, const BatchDev &b, int k, int chunk, 
     __syncthreads();
 }
 
-template <bool MIXED, bool STAGE, int T>
+template <bool MIXED, bool STAGE, int T, bool COMP>
 __global__ void __launch_bounds__(T) k_batch_steps(Dev d, BatchDev b, int chunk) {
     extern __shared__ __align__(16) unsigned char dyn[];
     __shared__ double shMin[T / 32 + 1];
@@ -97,7 +97,8 @@ __global__ void __launch_bounds__(T) k_batch_steps(Dev d, BatchDev b, int chunk)
         const int q = next;
         __syncthreads();
         if (q >= b.count) return;
-        run_instance<MIXED, STAGE, T>(d, b, b.order[q], chunk, sPMid, sVdt, shMin, wallCount);
+        run_instance<MIXED, STAGE, T, COMP>(d, b, b.order[q], chunk, sPMid, sVdt, shMin,
+                                            wallCount);
     }
 }
 
@@ -131,6 +132,30 @@ __global__ void __launch_bounds__(256) k_batch_initial(Dev d, BatchDev b) {
     for (int i = in.n0 + threadIdx.x; i < in.n1; i += 256)
         d.F[i] = MIXED ? gather_node_f32(d, i) : gather_node(d, i);
     if (threadIdx.x == 0) b.sc[blockIdx.x].minEdgeSquared = me;
+}
+
+// The compensated form's FP32 node state from the FP64 arrays (after the first assembly), and
+// back (after a run, so reads and measurements see FP64 arrays).
+__global__ void k_batch_comp_init(Dev d) {
+    const int i = blockIdx.x * blockDim.x + threadIdx.x;
+    if (i >= d.N) return;
+    const double2 x = d.X0[i], u = d.U[i], v = d.V[i], f = d.F[i];
+    const float2 xr = ff_from(x.x), xz = ff_from(x.y), ur = ff_from(u.x), uz = ff_from(u.y);
+    d.x0C[i] = make_float4(xr.x, xr.y, xz.x, xz.y);
+    d.uC[i] = make_float4(ur.x, ur.y, uz.x, uz.y);
+    d.vC[i] = make_float2((float)v.x, (float)v.y);
+    d.fC[i] = make_float2((float)f.x, (float)f.y);
+    d.mC[i] = make_float2((float)d.mass[i], (float)d.invMass[i]);
+}
+
+__global__ void k_batch_comp_sync(Dev d) {
+    const int i = blockIdx.x * blockDim.x + threadIdx.x;
+    if (i >= d.N) return;
+    const float4 u = d.uC[i];
+    const float2 v = d.vC[i], f = d.fC[i];
+    d.U[i] = make_double2((double)u.x + (double)u.y, (double)u.z + (double)u.w);
+    d.V[i] = make_double2((double)v.x, (double)v.y);
+    d.F[i] = make_double2((double)f.x, (double)f.y);
 }
 
 // Arms a run: every instance may take maxSteps more steps; counts the instances left to run.
@@ -189,27 +214,35 @@ __global__ void __launch_bounds__(MEASURE_BLOCK) k_batch_measure(Dev d, BatchDev
 
 // ------------------------------------------------------------------------------------ launch
 
-template <bool MIXED, bool STAGE, int T>
+template <bool MIXED, bool STAGE, int T, bool COMP>
 static const void *steps_kernel() {
-    return (const void *)k_batch_steps<MIXED, STAGE, T>;
+    return (const void *)k_batch_steps<MIXED, STAGE, T, COMP>;
 }
 
-static const void *select_kernel(bool mixed, const BatchShape &s) {
-    if (mixed) {
-        if (s.stage) return s.threads == 128 ? steps_kernel<true, true, 128>() : steps_kernel<true, true, 256>();
-        return s.threads == 128 ? steps_kernel<true, false, 128>() : steps_kernel<true, false, 256>();
-    }
-    return s.threads == 128 ? steps_kernel<false, false, 128>() : steps_kernel<false, false, 256>();
+template <bool MIXED, bool COMP>
+static const void *by_shape(const BatchShape &s) {
+    if (MIXED && s.stage)
+        return s.threads == 128 ? steps_kernel<MIXED, true, 128, COMP>()
+                                : steps_kernel<MIXED, true, 256, COMP>();
+    return s.threads == 128 ? steps_kernel<MIXED, false, 128, COMP>()
+                            : steps_kernel<MIXED, false, 256, COMP>();
 }
 
-size_t batch_shared_bytes(bool mixed, const BatchShape &s, int maxNodes) {
-    return mixed && s.stage ? (sizeof(float4) + sizeof(float2)) * (size_t)maxNodes : 0;
+static const void *select_kernel(int mode, const BatchShape &s) {
+    if (mode == NF_PRECISION_COMPENSATED) return by_shape<true, true>(s);
+    if (mode == NF_PRECISION_MIXED) return by_shape<true, false>(s);
+    return by_shape<false, false>(s);
+}
+
+size_t batch_shared_bytes(int mode, const BatchShape &s, int maxNodes) {
+    return mode != NF_PRECISION_FP64 && s.stage ? (sizeof(float4) + sizeof(float2)) * (size_t)maxNodes
+                                                : 0;
 }
 
 // Resident blocks per SM of a shape (0 when it cannot launch, e.g. too much shared memory).
-int batch_max_blocks_per_sm(bool mixed, const BatchShape &s, int maxNodes) {
-    const void *k = select_kernel(mixed, s);
-    const size_t smem = batch_shared_bytes(mixed, s, maxNodes);
+int batch_max_blocks_per_sm(int mode, const BatchShape &s, int maxNodes) {
+    const void *k = select_kernel(mode, s);
+    const size_t smem = batch_shared_bytes(mode, s, maxNodes);
     if (smem > 48 * 1024 &&
         cudaFuncSetAttribute(k, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem) != cudaSuccess) {
         (void)cudaGetLastError();
@@ -223,10 +256,10 @@ int batch_max_blocks_per_sm(bool mixed, const BatchShape &s, int maxNodes) {
     return n;
 }
 
-cudaError_t launch_batch_steps(const Dev &d, const BatchDev &b, bool mixed, const BatchShape &s,
+cudaError_t launch_batch_steps(const Dev &d, const BatchDev &b, int mode, const BatchShape &s,
                                int sms, cudaStream_t st) {
-    const void *k = select_kernel(mixed, s);
-    const size_t smem = batch_shared_bytes(mixed, s, b.maxNodes);
+    const void *k = select_kernel(mode, s);
+    const size_t smem = batch_shared_bytes(mode, s, b.maxNodes);
     int blocks = sms * s.blocksPerSm;
     if (blocks > b.count) blocks = b.count;
     if (blocks < 1) blocks = 1;
@@ -241,6 +274,12 @@ void launch_batch_initial(const Dev &d, const BatchDev &b, bool mixed, cudaStrea
     if (b.count <= 0) return;
     if (mixed) k_batch_initial<true><<<b.count, 256, 0, st>>>(d, b);
     else k_batch_initial<false><<<b.count, 256, 0, st>>>(d, b);
+}
+
+void launch_batch_comp(const Dev &d, bool toFloat, cudaStream_t st) {
+    if (d.N <= 0) return;
+    if (toFloat) k_batch_comp_init<<<grid_for(d.N, 256), 256, 0, st>>>(d);
+    else k_batch_comp_sync<<<grid_for(d.N, 256), 256, 0, st>>>(d);
 }
 
 void launch_batch_arm(const BatchDev &b, long long maxSteps, cudaStream_t st) {

@@ -55,20 +55,29 @@ __device__ double block_total(double v, double *sh) {
 // One step of instance `in` by the whole block, ExplicitSolver.step :940-991: the nodal update
 // (with the mixed form's float geometry when geo.pMid is set), the assembly with the block's
 // exact shortest squared edge, the per-node gather, the next CFL step. dt, dtPrev, time and
-// steps advance in place; returns the shortest squared edge.
-template <bool MIXED, int T>
+// steps advance in place; returns the shortest squared edge. COMP (with MIXED): the
+// compensated form's FP32 nodal update and gather (nf_bodies.cuh).
+template <bool MIXED, int T, bool COMP = false>
 __device__ __forceinline__ double batch_step(const Dev &d, const BatchInst &in, double &dt,
                                              double &dtPrev, double &time, long long &steps,
                                              const MixedGeo &geo, const float4 *pMid,
                                              const float2 *vdt, int base, uint32_t *status,
                                              int *wallContact, int *wallStuck, double &impulse,
                                              double &loss, double &fric, double *shMin) {
+    static_assert(!COMP || MIXED, "the compensated form assembles in FP32");
     const double dtAvg = 0.5 * (dtPrev + dt);                       // :947-956
     const double half = 0.5 * in.damping * dtAvg;
     const NodalCoef co{(1.0 - half) / (1.0 + half), dtAvg / (1.0 + half), dtAvg, dt};
     const WallRef w{in.hasWall, in.wallPlane, in.wallFriction, wallContact, wallStuck};
-    for (int i = in.n0 + threadIdx.x; i < in.n1; i += T)
-        nodal_node(d, i, co, w, geo, status, impulse, loss, fric);
+    if (COMP) {
+        const float decay = (float)co.decay, gain = (float)co.gain, fa = (float)dtAvg,
+                    fdt = (float)dt;
+        for (int i = in.n0 + threadIdx.x; i < in.n1; i += T)
+            nodal_node_comp(d, i, decay, gain, fa, fdt, w, geo, status, impulse, loss, fric);
+    } else {
+        for (int i = in.n0 + threadIdx.x; i < in.n1; i += T)
+            nodal_node(d, i, co, w, geo, status, impulse, loss, fric);
+    }
     __syncthreads();
     time += dt;                                                       // :973-974
     steps += 1;
@@ -78,8 +87,10 @@ __device__ __forceinline__ double batch_step(const Dev &d, const BatchInst &in, 
         const float sdt = (float)dt, qhg = (float)in.hourglass;
         for (int e = in.e0 + threadIdx.x; e < in.e1; e += T)
             element_reduced_f32(d, e, sdt, qhg, pMid, vdt, base, m);
-        for (int k = in.k0 + threadIdx.x; k < in.k1; k += T)     // applyPressure, :1203-1207
-            pressure_edge_f32(d, k, time, in.pressure, in.ramp);
+        for (int k = in.k0 + threadIdx.x; k < in.k1; k += T) {   // applyPressure, :1203-1207
+            if (COMP) pressure_edge_comp(d, k, time, in.pressure, in.ramp);
+            else pressure_edge_f32(d, k, time, in.pressure, in.ramp);
+        }
         me = block_min_edge_f<T>(m, shMin);
     } else {
         double m = DMAX;
@@ -90,8 +101,10 @@ __device__ __forceinline__ double batch_step(const Dev &d, const BatchInst &in, 
     }
     // the gather keeps the nodal loop's node-to-thread map, so the next nodal update reads
     // only forces its own thread wrote
-    for (int i = in.n0 + threadIdx.x; i < in.n1; i += T)
-        d.F[i] = MIXED ? gather_node_f32(d, i) : gather_node(d, i);
+    for (int i = in.n0 + threadIdx.x; i < in.n1; i += T) {
+        if (COMP) d.fC[i] = gather_node_comp(d, i);
+        else d.F[i] = MIXED ? gather_node_f32(d, i) : gather_node(d, i);
+    }
     if (d.finite) {                                                   // :985-990
         dtPrev = dt;
         dt = in.cfl * sqrt(me * in.massScale) / in.wave;

@@ -509,6 +509,189 @@ static __device__ __forceinline__ void pressure_edge_f32(const Dev &d, int e, do
     c[5] = (float)(p * nz * wb);
 }
 
+// ---------------------------------------------------------------- the compensated form
+// FP32 nodal arithmetic with each displacement carried as an unevaluated float pair hi + lo
+// (Kahan-style compensated accumulation, about 48 significant bits), FP32 velocities and an
+// FP32 gather. Built with contraction off, so the error-free transformations hold.
+
+// TwoSum (Knuth): s + e == a + b exactly.
+static __device__ __forceinline__ float2 two_sum_f(float a, float b) {
+    const float s = a + b;
+    const float bb = s - a;
+    return make_float2(s, (a - (s - bb)) + (b - bb));
+}
+
+// (hi, lo) += x, renormalised (|lo| <= ulp(hi) / 2).
+static __device__ __forceinline__ void ff_add(float &hi, float &lo, float x) {
+    const float2 s = two_sum_f(hi, x);
+    const float l = s.y + lo;
+    hi = s.x + l;
+    lo = l - (hi - s.x);
+}
+
+// The pair nearest xh + xl + uh + ul + c for a small c (a node's position, mid-step or current).
+static __device__ __forceinline__ float2 ff_point(float xh, float xl, float uh, float ul, float c) {
+    const float2 s = two_sum_f(xh, uh);
+    const float l = s.y + ((xl + ul) + c);
+    const float hi = s.x + l;
+    return make_float2(hi, l - (hi - s.x));
+}
+
+static __device__ __forceinline__ float2 ff_from(double x) {
+    const float hi = (float)x;
+    return make_float2(hi, (float)(x - (double)hi));
+}
+
+// nodalUpdate (:998-1062) with the rigid wall (RigidWall.java:163-259) for node i in the
+// compensated form, the same branch structure as nodal_node; also writes the node's float
+// geometry for the coming assembly. The audit terms are summed in FP64.
+static __device__ __forceinline__ void nodal_node_comp(const Dev &d, int i, float decay,
+                                                       float gain, float dtAvg, float dt,
+                                                       const WallRef &w, const MixedGeo &geo,
+                                                       uint32_t *status, double &impulse,
+                                                       double &loss, double &fric) {
+    const uint8_t fl = d.flags[i];
+    const bool fixedR = fl & 1, fixedZ = fl & 2;
+    bool onWall = fl & 4;
+    float4 u = d.uC[i];
+    float2 v = d.vC[i];
+    const float2 f = d.fC[i];
+    const float2 mm = d.mC[i];
+    const float m = mm.x, invM = mm.y;
+    const float4 x0 = d.x0C[i];
+    const float friction = (float)w.friction;
+    const bool resting = w.present && onWall && f.y <= 0.0f;
+    uint8_t ws = 0;
+    if (fixedR) {
+        v.x = 0.0f;
+    } else if (resting && friction > 0.0f) {
+        const float normal = -f.y;
+        const float trial = -m * decay * v.x / gain - f.x;
+        const float limit = isinf(friction) ? INFINITY : friction * normal;
+        if (fabsf(trial) <= limit) {
+            loss += 0.5 * (double)m * (double)v.x * (double)v.x;
+            atomicAdd(w.stuck, 1);
+            ws |= NF_WALL_STUCK;
+            v.x = 0.0f;
+        } else {
+            const float tangential = copysignf(limit, trial);
+            const float slid = decay * v.x + gain * (f.x + tangential) / m;
+            fric += -(double)tangential * (double)slid * (double)dt;
+            ws |= NF_WALL_SLID;
+            v.x = slid;
+        }
+        ff_add(u.x, u.y, v.x * dt);
+    } else {
+        v.x = decay * v.x + gain * f.x * invM;
+        ff_add(u.x, u.y, v.x * dt);
+    }
+    if (fixedZ) {
+        v.y = 0.0f;
+    } else if (resting) {
+        impulse += -(double)f.y * (double)dtAvg;
+        atomicAdd(w.contact, 1);
+        ws |= NF_WALL_HELD;
+    } else {
+        const float trial = decay * v.y + gain * f.y * invM;
+        const float plane = (float)w.plane;
+        // z + trial dt < plane, with z = x0 + u as a pair
+        const float2 s = two_sum_f(x0.z, u.z);
+        const float below = (s.x - plane) + ((s.y + (x0.w + u.w)) + trial * dt);
+        if (w.present && below < 0.0f) {
+            impulse += -(double)m * (double)trial;
+            loss += 0.5 * (double)m * (double)trial * (double)trial;
+            atomicAdd(w.contact, 1);
+            // u = plane - x0
+            const float2 t = two_sum_f(plane, -x0.z);
+            const float l = t.y - x0.w;
+            u.z = t.x + l;
+            u.w = l - (u.z - t.x);
+            v.y = 0.0f;
+            onWall = true;
+            ws |= NF_WALL_ARRIVED;
+        } else {
+            v.y = trial;
+            ff_add(u.z, u.w, v.y * dt);
+            if (w.present) onWall = false;
+        }
+    }
+    d.uC[i] = u;
+    d.vC[i] = v;
+    if (w.present) {
+        d.flags[i] = (uint8_t)((fl & 3) | (onWall ? 4 : 0));
+        d.wallState[i] = ws;
+    }
+    if (!(isfinite(u.x) && isfinite(u.z) && isfinite(v.x) && isfinite(v.y)))
+        atomicOr(status, STATUS_NONFINITE);
+    if (geo.pMid) {
+        const float mid = -0.5f * dt;
+        float2 pr, pz;
+        if (d.finite) {
+            pr = ff_point(x0.x, x0.y, u.x, u.y, mid * v.x);
+            pz = ff_point(x0.z, x0.w, u.z, u.w, mid * v.y);
+        } else {
+            pr = make_float2(x0.x, x0.y);
+            pz = make_float2(x0.z, x0.w);
+        }
+        geo.pMid[geo.base + i] = make_float4(pr.x, pr.y, pz.x, pz.y);
+        geo.vdt[geo.base + i] = make_float2(v.x * dt, v.y * dt);
+    }
+}
+
+// The pressure edge of the mixed form with the edge's current geometry read from the
+// compensated pairs.
+static __device__ __forceinline__ void pressure_edge_comp(const Dev &d, int e, double t,
+                                                          double target, double rampDuration) {
+    double p = target;
+    if (rampDuration > 0.0) {
+        const double s = jmin(1.0, t / rampDuration);
+        p = target * s * s * (3.0 - 2.0 * s);
+    }
+    float *c = d.contribF + 8 * (size_t)(d.E + e);
+    const int2 ed = d.pedges[e];
+    const float4 xa = d.x0C[ed.x], xb = d.x0C[ed.y];
+    double ra = (double)xa.x + (double)xa.y, rb = (double)xb.x + (double)xb.y;
+    double za = (double)xa.z + (double)xa.w, zb = (double)xb.z + (double)xb.w;
+    if (d.finite) {
+        const float4 ua = d.uC[ed.x], ub = d.uC[ed.y];
+        ra += (double)ua.x + (double)ua.y; rb += (double)ub.x + (double)ub.y;
+        za += (double)ua.z + (double)ua.w; zb += (double)ub.z + (double)ub.w;
+    }
+    const double tr = rb - ra, tz = zb - za;
+    const double len = sqrt(tr * tr + tz * tz);
+    if (len == 0.0) {
+        c[0] = 0.f; c[1] = 0.f; c[4] = 0.f; c[5] = 0.f;
+        return;
+    }
+    const double nr = tz / len, nz = -tr / len;
+    double wa, wb;
+    if (d.axi) {
+        const double circumference = 2.0 * NF_PI * len;
+        wa = circumference * (ra / 3.0 + rb / 6.0);
+        wb = circumference * (ra / 6.0 + rb / 3.0);
+    } else {
+        wa = d.thickness * len * 0.5;
+        wb = wa;
+    }
+    c[0] = (float)(p * nr * wa);
+    c[1] = (float)(p * nr * wb);
+    c[4] = (float)(p * nz * wa);
+    c[5] = (float)(p * nz * wb);
+}
+
+// The gather of float contributions into float sums, in CSR order, then m g.
+static __device__ __forceinline__ float2 gather_node_comp(const Dev &d, int n) {
+    float sr = 0.0f, sz = 0.0f;
+    const int end = d.nodeSlotStart[n + 1];
+    for (int k = d.nodeSlotStart[n]; k < end; k++) {
+        const int slot = d.nodeSlot[k];
+        sr += d.contribF[slot];
+        sz += d.contribF[slot + 4];
+    }
+    const float m = d.mC[n].x;
+    return make_float2(sr + m * (float)d.gravR, sz + m * (float)d.gravZ);
+}
+
 // gather, ExplicitSolver.java:1147-1165: node n's sources in ascending order, then m g.
 static __device__ __forceinline__ double2 gather_node(const Dev &d, int n) {
     double sr = 0.0, sz = 0.0;

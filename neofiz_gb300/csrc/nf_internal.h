@@ -130,6 +130,11 @@ struct Dev {
     float2 *hgF;
     float *dStrF, *dSoftF, *dWidthF, *dFailF, *dGfF, *dGeomF;
     float4 *pMid, *pCur;
+    // compensated form (batches): displacement and reference position as float pairs
+    // (r hi, r lo, z hi, z lo), velocity, gathered force and (mass, 1/mass) in FP32
+    float4 *uC, *x0C;
+    float2 *vC, *fC, *mC;
+    int comp;
     float2 *vdt;
     double *gaussVol;                        // reference volume of each point
     // scan workspace; the cooperative contact pass's grid and its per-block scan sums
@@ -261,11 +266,13 @@ struct BatchShape {
 };
 
 // Launchers (k_batch.cu).
-int batch_max_blocks_per_sm(bool mixed, const BatchShape &shape, int maxNodes);
-size_t batch_shared_bytes(bool mixed, const BatchShape &shape, int maxNodes);
+// mode: NF_PRECISION_FP64, NF_PRECISION_MIXED or NF_PRECISION_COMPENSATED
+int batch_max_blocks_per_sm(int mode, const BatchShape &shape, int maxNodes);
+size_t batch_shared_bytes(int mode, const BatchShape &shape, int maxNodes);
 void launch_batch_initial(const Dev &d, const BatchDev &b, bool mixed, cudaStream_t st);
 void launch_batch_arm(const BatchDev &b, long long maxSteps, cudaStream_t st);
-cudaError_t launch_batch_steps(const Dev &d, const BatchDev &b, bool mixed,
+void launch_batch_comp(const Dev &d, bool toFloat, cudaStream_t st);
+cudaError_t launch_batch_steps(const Dev &d, const BatchDev &b, int mode,
                                const BatchShape &shape, int sms, cudaStream_t st);
 void launch_batch_measure(const Dev &d, const BatchDev &b, cudaStream_t st);
 

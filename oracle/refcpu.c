@@ -2085,7 +2085,8 @@ API nf_status nfo_batch_create(const nf_batch_mesh *mesh, const nf_batch_instanc
     *out = NULL;
     if (!mesh || !inst || mesh->instance_count < 1)
         return bfail(NULL, NF_EINVAL, "a batch needs at least one instance and its mesh arrays");
-    if (precision != NF_PRECISION_FP64 && precision != NF_PRECISION_MIXED)
+    if (precision != NF_PRECISION_FP64 && precision != NF_PRECISION_MIXED &&
+        precision != NF_PRECISION_COMPENSATED)
         return bfail(NULL, NF_EINVAL, "unknown precision %d", precision);
     const int count = mesh->instance_count;
     nfo_batch *b = (nfo_batch *)calloc(1, sizeof *b);
