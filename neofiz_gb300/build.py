@@ -6,6 +6,8 @@ neofiz_gb300/_build. Flags that matter for correctness:
                             rounds where the reference's Java does;
   -Xcompiler -ffp-contract=off   the same for the host-side set-up arithmetic (lumped mass,
                             node slots, initial step), which matters on the aarch64 host.
+k_batch_comp.cu alone (the compensated batch form, which has no bit-level twin) is built with
+float contraction, fast float division/square root and denormal flushing instead.
 """
 from __future__ import annotations
 
@@ -20,11 +22,24 @@ CSRC = os.path.join(HERE, "csrc")
 BUILD = os.path.join(HERE, "_build")
 LIBRARY = os.path.join(BUILD, "libneofiz_gpu.so")
 SOURCES = ["api.cu", "api_batch.cu", "k_step.cu", "k_contact.cu", "k_scan.cu", "k_mixed.cu",
-           "k_batch.cu", "k_adjoint.cu", "noalloc.cu"]
+           "k_batch.cu", "k_batch_comp.cu", "k_adjoint.cu", "noalloc.cu"]
 ARCH = ["-gencode", "arch=compute_103a,code=sm_103a"]
 NVCC_FLAGS = ["-O3", "-std=c++17", "-lineinfo", "--fmad=false", "-prec-div=true",
               "-prec-sqrt=true", "-Xcompiler", "-fPIC,-ffp-contract=off,-O2",
               "-Xptxas", "-O3"]
+
+
+# The compensated batch form has no bit-level twin; its translation unit is built for speed
+# (float multiply-add contraction, fast float division and square root, denormals flushed).
+FAST_FLOAT_SOURCES = {"k_batch_comp.cu"}
+FAST_FLOAT_FLAGS = ["--fmad=true", "-prec-div=false", "-prec-sqrt=false", "-ftz=true"]
+
+
+def flags_for(src: str):
+    if src not in FAST_FLOAT_SOURCES:
+        return NVCC_FLAGS
+    strict = ("--fmad=false", "-prec-div=true", "-prec-sqrt=true")
+    return [f for f in NVCC_FLAGS if f not in strict] + FAST_FLOAT_FLAGS
 
 
 def nvcc() -> str:
@@ -50,7 +65,7 @@ def build(force: bool = False, verbose: bool = False, extra=()) -> str:
 
     def compile_one(src):
         obj = os.path.join(BUILD, src.replace(".cu", ".o"))
-        cmd = [cc, *ARCH, *NVCC_FLAGS, *extra, "-c", os.path.join(CSRC, src), "-o", obj]
+        cmd = [cc, *ARCH, *flags_for(src), *extra, "-c", os.path.join(CSRC, src), "-o", obj]
         r = subprocess.run(cmd, capture_output=True, text=True)
         if r.returncode != 0:
             raise RuntimeError(f"nvcc failed on {src}:\n{r.stderr}")

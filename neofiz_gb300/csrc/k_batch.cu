@@ -15,92 +15,11 @@
 // Launch shape: block size (128, 256), whether the mixed form stages each instance's float
 // node geometry in shared memory, blocks per SM and the chunk length are chosen by the
 // autotuner (api_batch.cu); none of them changes the trajectory.
-#include "nf_batch_step.cuh"
+#include "nf_batch_kernels.cuh"
 
 namespace nf {
 
 constexpr int MEASURE_BLOCK = 256;
-
-// Up to `chunk` steps of instance k by the whole block: ExplicitSolver.step, :940-991, with the
-// loop condition of TaylorImpactCase.java:250-253 (step while time < t_end).
-template <bool MIXED, bool STAGE, int T, bool COMP>
-__device__ void run_instance(const Dev &d, const BatchDev &b, int k, int chunk, float4 *sPMid,
-                             float2 *sVdt, double *shMin, int (*wallCount)[2]) {
-    const BatchInst in = b.inst[k];
-    BatchScalars *scp = b.sc + k;
-    if (scp->done) return;
-    const int tid = threadIdx.x;
-    double dt = scp->dt, dtPrev = scp->dtPrevious, time = scp->time;
-    double minEdge = scp->minEdgeSquared;
-    long long steps = scp->steps;
-    const long long limit = scp->stepLimit;
-    double impulse = 0.0, loss = 0.0, fric = 0.0;
-    if (tid == 0) {
-        wallCount[0][0] = wallCount[0][1] = 0;
-        wallCount[1][0] = wallCount[1][1] = 0;
-    }
-    __syncthreads();
-    float4 *pMid = STAGE ? sPMid : d.pMid;
-    float2 *vdt = STAGE ? sVdt : d.vdt;
-    const int base = STAGE ? in.n0 : 0;
-    const MixedGeo geo = MIXED ? MixedGeo{pMid, nullptr, vdt, -base}
-                               : MixedGeo{nullptr, nullptr, nullptr, 0};
-    int taken = 0;
-    for (; taken < chunk; taken++) {
-        if (!(time < in.tEnd) || steps >= limit) break;
-        // RigidWall.beginStep: this step's counts go to buffer `par`; the other is cleared for
-        // the next step (its last users passed this step's first barrier already)
-        const int par = taken & 1;
-        if (tid == 0) {
-            wallCount[par ^ 1][0] = 0;
-            wallCount[par ^ 1][1] = 0;
-        }
-        minEdge = batch_step<MIXED, T, COMP>(d, in, dt, dtPrev, time, steps, geo, pMid, vdt,
-                                             base, &scp->status, &wallCount[par][0],
-                                             &wallCount[par][1], impulse, loss, fric, shMin);
-    }
-    const double ti = block_total<T>(impulse, shMin);
-    const double tl = block_total<T>(loss, shMin);
-    const double tf = block_total<T>(fric, shMin);
-    if (tid == 0) {
-        scp->dt = dt;
-        scp->dtPrevious = dtPrev;
-        scp->time = time;
-        scp->steps = steps;
-        scp->minEdgeSquared = minEdge;
-        if (taken > 0) {
-            scp->wContact = wallCount[(taken - 1) & 1][0];
-            scp->wStuck = wallCount[(taken - 1) & 1][1];
-        }
-        scp->wImpulse += ti;
-        scp->wEnergyLoss += tl;
-        scp->wFriction += tf;
-        if (!(time < in.tEnd) || steps >= limit) {
-            scp->done = 1;
-            atomicSub(b.remaining, 1);
-        }
-    }
-    __syncthreads();
-}
-
-template <bool MIXED, bool STAGE, int T, bool COMP>
-__global__ void __launch_bounds__(T) k_batch_steps(Dev d, BatchDev b, int chunk) {
-    extern __shared__ __align__(16) unsigned char dyn[];
-    __shared__ double shMin[T / 32 + 1];
-    __shared__ int wallCount[2][2];
-    __shared__ int next;
-    float4 *sPMid = reinterpret_cast<float4 *>(dyn);
-    float2 *sVdt = reinterpret_cast<float2 *>(dyn + sizeof(float4) * (size_t)b.maxNodes);
-    for (;;) {
-        if (threadIdx.x == 0) next = atomicAdd(b.queue, 1);
-        __syncthreads();
-        const int q = next;
-        __syncthreads();
-        if (q >= b.count) return;
-        run_instance<MIXED, STAGE, T, COMP>(d, b, b.order[q], chunk, sPMid, sVdt, shMin,
-                                            wallCount);
-    }
-}
 
 // The first assembly of every instance (zero strain increment), in the batch's precision, as
 // the single-scene path runs it before its first step; records the shortest edge.
@@ -132,30 +51,6 @@ __global__ void __launch_bounds__(256) k_batch_initial(Dev d, BatchDev b) {
     for (int i = in.n0 + threadIdx.x; i < in.n1; i += 256)
         d.F[i] = MIXED ? gather_node_f32(d, i) : gather_node(d, i);
     if (threadIdx.x == 0) b.sc[blockIdx.x].minEdgeSquared = me;
-}
-
-// The compensated form's FP32 node state from the FP64 arrays (after the first assembly), and
-// back (after a run, so reads and measurements see FP64 arrays).
-__global__ void k_batch_comp_init(Dev d) {
-    const int i = blockIdx.x * blockDim.x + threadIdx.x;
-    if (i >= d.N) return;
-    const double2 x = d.X0[i], u = d.U[i], v = d.V[i], f = d.F[i];
-    const float2 xr = ff_from(x.x), xz = ff_from(x.y), ur = ff_from(u.x), uz = ff_from(u.y);
-    d.x0C[i] = make_float4(xr.x, xr.y, xz.x, xz.y);
-    d.uC[i] = make_float4(ur.x, ur.y, uz.x, uz.y);
-    d.vC[i] = make_float2((float)v.x, (float)v.y);
-    d.fC[i] = make_float2((float)f.x, (float)f.y);
-    d.mC[i] = make_float2((float)d.mass[i], (float)d.invMass[i]);
-}
-
-__global__ void k_batch_comp_sync(Dev d) {
-    const int i = blockIdx.x * blockDim.x + threadIdx.x;
-    if (i >= d.N) return;
-    const float4 u = d.uC[i];
-    const float2 v = d.vC[i], f = d.fC[i];
-    d.U[i] = make_double2((double)u.x + (double)u.y, (double)u.z + (double)u.w);
-    d.V[i] = make_double2((double)v.x, (double)v.y);
-    d.F[i] = make_double2((double)f.x, (double)f.y);
 }
 
 // Arms a run: every instance may take maxSteps more steps; counts the instances left to run.
@@ -229,7 +124,7 @@ static const void *by_shape(const BatchShape &s) {
 }
 
 static const void *select_kernel(int mode, const BatchShape &s) {
-    if (mode == NF_PRECISION_COMPENSATED) return by_shape<true, true>(s);
+    if (mode == NF_PRECISION_COMPENSATED) return comp_steps_kernel(s);
     if (mode == NF_PRECISION_MIXED) return by_shape<true, false>(s);
     return by_shape<false, false>(s);
 }
@@ -274,12 +169,6 @@ void launch_batch_initial(const Dev &d, const BatchDev &b, bool mixed, cudaStrea
     if (b.count <= 0) return;
     if (mixed) k_batch_initial<true><<<b.count, 256, 0, st>>>(d, b);
     else k_batch_initial<false><<<b.count, 256, 0, st>>>(d, b);
-}
-
-void launch_batch_comp(const Dev &d, bool toFloat, cudaStream_t st) {
-    if (d.N <= 0) return;
-    if (toFloat) k_batch_comp_init<<<grid_for(d.N, 256), 256, 0, st>>>(d);
-    else k_batch_comp_sync<<<grid_for(d.N, 256), 256, 0, st>>>(d);
 }
 
 void launch_batch_arm(const BatchDev &b, long long maxSteps, cudaStream_t st) {

@@ -52,22 +52,68 @@ __device__ double block_total(double v, double *sh) {
     return t;
 }
 
+// The coming step's size and nodal coefficients (:947-956, :985-990), computed once per block
+// by thread 0 and read by every thread: the same formulas as each thread would evaluate, so
+// the same bits, without every thread spending FP64 divisions and a square root on them.
+struct BlockStep {
+    double dt, decay, gain, dtAvg;
+};
+
+__device__ __forceinline__ void block_step_coef(BlockStep &bs, const BatchInst &in, double dt,
+                                                double dtPrev) {
+    const double dtAvg = 0.5 * (dtPrev + dt);
+    const double half = 0.5 * in.damping * dtAvg;
+    bs.dt = dt;
+    bs.decay = (1.0 - half) / (1.0 + half);
+    bs.gain = dtAvg / (1.0 + half);
+    bs.dtAvg = dtAvg;
+}
+
+// block_min_edge, with thread 0 also preparing the next step in bs between the barriers.
+template <int T>
+__device__ double block_min_edge_next(double v, double *sh, BlockStep *bs, const BatchInst &in,
+                                      double dt, double dtPrev, int finite) {
+    for (int o = 16; o > 0; o >>= 1) v = jmin(v, __shfl_down_sync(0xffffffffu, v, o));
+    const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
+    if (lane == 0) sh[warp] = v;
+    __syncthreads();
+    if (threadIdx.x == 0) {
+        unsigned long long m = bbits(sh[0]);
+        for (int w = 1; w < T / 32; w++) m = min(m, bbits(sh[w]));
+        const double me = bdouble(m);
+        sh[T / 32] = me;
+        if (finite) block_step_coef(*bs, in, in.cfl * sqrt(me * in.massScale) / in.wave, dt);
+        else block_step_coef(*bs, in, dt, dtPrev);
+    }
+    __syncthreads();
+    return sh[T / 32];
+}
+
 // One step of instance `in` by the whole block, ExplicitSolver.step :940-991: the nodal update
 // (with the mixed form's float geometry when geo.pMid is set), the assembly with the block's
 // exact shortest squared edge, the per-node gather, the next CFL step. dt, dtPrev, time and
 // steps advance in place; returns the shortest squared edge. COMP (with MIXED): the
-// compensated form's FP32 nodal update and gather (nf_bodies.cuh).
+// compensated form's FP32 nodal update and gather (nf_bodies.cuh). With bs (a block-shared
+// BlockStep prepared for this step), the step's coefficients and the next step size come from
+// thread 0 through it; without, every thread evaluates them.
 template <bool MIXED, int T, bool COMP = false>
 __device__ __forceinline__ double batch_step(const Dev &d, const BatchInst &in, double &dt,
                                              double &dtPrev, double &time, long long &steps,
                                              const MixedGeo &geo, const float4 *pMid,
                                              const float2 *vdt, int base, uint32_t *status,
                                              int *wallContact, int *wallStuck, double &impulse,
-                                             double &loss, double &fric, double *shMin) {
+                                             double &loss, double &fric, double *shMin,
+                                             BlockStep *bs = nullptr) {
     static_assert(!COMP || MIXED, "the compensated form assembles in FP32");
-    const double dtAvg = 0.5 * (dtPrev + dt);                       // :947-956
-    const double half = 0.5 * in.damping * dtAvg;
-    const NodalCoef co{(1.0 - half) / (1.0 + half), dtAvg / (1.0 + half), dtAvg, dt};
+    NodalCoef co;
+    if (bs) {
+        co = NodalCoef{bs->decay, bs->gain, bs->dtAvg, dt};
+    } else {
+        const double dtAvg = 0.5 * (dtPrev + dt);                   // :947-956
+        const double half = 0.5 * in.damping * dtAvg;
+        co = NodalCoef{(1.0 - half) / (1.0 + half), dtAvg / (1.0 + half), dtAvg, dt};
+    }
+    const double dtAvg = co.dtAvg;
     const WallRef w{in.hasWall, in.wallPlane, in.wallFriction, wallContact, wallStuck};
     if (COMP) {
         const float decay = (float)co.decay, gain = (float)co.gain, fa = (float)dtAvg,
@@ -91,13 +137,19 @@ __device__ __forceinline__ double batch_step(const Dev &d, const BatchInst &in, 
             if (COMP) pressure_edge_comp(d, k, time, in.pressure, in.ramp);
             else pressure_edge_f32(d, k, time, in.pressure, in.ramp);
         }
-        me = block_min_edge_f<T>(m, shMin);
+        if (bs) {
+            for (int o = 16; o > 0; o >>= 1) m = fminf(m, __shfl_down_sync(0xffffffffu, m, o));
+            me = block_min_edge_next<T>((double)m, shMin, bs, in, dt, dtPrev, d.finite);
+        } else {
+            me = block_min_edge_f<T>(m, shMin);
+        }
     } else {
         double m = DMAX;
         for (int e = in.e0 + threadIdx.x; e < in.e1; e += T) element_reduced(d, e, dt, in.hourglass, m);
         for (int k = in.k0 + threadIdx.x; k < in.k1; k += T)
             pressure_edge(d, k, time, in.pressure, in.ramp);
-        me = block_min_edge<T>(m, shMin);
+        me = bs ? block_min_edge_next<T>(m, shMin, bs, in, dt, dtPrev, d.finite)
+                : block_min_edge<T>(m, shMin);
     }
     // the gather keeps the nodal loop's node-to-thread map, so the next nodal update reads
     // only forces its own thread wrote
@@ -107,7 +159,7 @@ __device__ __forceinline__ double batch_step(const Dev &d, const BatchInst &in, 
     }
     if (d.finite) {                                                   // :985-990
         dtPrev = dt;
-        dt = in.cfl * sqrt(me * in.massScale) / in.wave;
+        dt = bs ? bs->dt : in.cfl * sqrt(me * in.massScale) / in.wave;
     }
     return me;
 }

@@ -512,7 +512,9 @@ static __device__ __forceinline__ void pressure_edge_f32(const Dev &d, int e, do
 // ---------------------------------------------------------------- the compensated form
 // FP32 nodal arithmetic with each displacement carried as an unevaluated float pair hi + lo
 // (Kahan-style compensated accumulation, about 48 significant bits), FP32 velocities and an
-// FP32 gather. Built with contraction off, so the error-free transformations hold.
+// FP32 gather. The error-free transformations are additions only; the increment v dt that
+// feeds one is rounded on its own (__fmul_rn), so a contracted multiply-add cannot change
+// what the compensation sees.
 
 // TwoSum (Knuth): s + e == a + b exactly.
 static __device__ __forceinline__ float2 two_sum_f(float a, float b) {
@@ -580,10 +582,10 @@ static __device__ __forceinline__ void nodal_node_comp(const Dev &d, int i, floa
             ws |= NF_WALL_SLID;
             v.x = slid;
         }
-        ff_add(u.x, u.y, v.x * dt);
+        ff_add(u.x, u.y, __fmul_rn(v.x, dt));
     } else {
         v.x = decay * v.x + gain * f.x * invM;
-        ff_add(u.x, u.y, v.x * dt);
+        ff_add(u.x, u.y, __fmul_rn(v.x, dt));
     }
     if (fixedZ) {
         v.y = 0.0f;
@@ -611,7 +613,7 @@ static __device__ __forceinline__ void nodal_node_comp(const Dev &d, int i, floa
             ws |= NF_WALL_ARRIVED;
         } else {
             v.y = trial;
-            ff_add(u.z, u.w, v.y * dt);
+            ff_add(u.z, u.w, __fmul_rn(v.y, dt));
             if (w.present) onWall = false;
         }
     }

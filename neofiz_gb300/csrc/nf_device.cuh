@@ -49,9 +49,12 @@ template <> struct Fn<double> {
     static __device__ __forceinline__ double abs(double a) { return ::fabs(a); }
     static constexpr double tolerance = SOLVE_TOLERANCE;
 };
+// The FP32 forms run well inside their error budget with CUDA's fast pow and log (a few ulp
+// instead of correctly rounded): the Johnson-Cook solve of a plastic point calls them in
+// every Newton iteration.
 template <> struct Fn<float> {
-    static __device__ __forceinline__ float pow(float a, float b) { return ::powf(a, b); }
-    static __device__ __forceinline__ float log(float a) { return ::logf(a); }
+    static __device__ __forceinline__ float pow(float a, float b) { return __powf(a, b); }
+    static __device__ __forceinline__ float log(float a) { return __logf(a); }
     static __device__ __forceinline__ float sqrt(float a) { return ::sqrtf(a); }
     static __device__ __forceinline__ float hypot(float a, float b) { return ::hypotf(a, b); }
     static __device__ __forceinline__ float atan2(float a, float b) { return ::atan2f(a, b); }

@@ -272,6 +272,7 @@ size_t batch_shared_bytes(int mode, const BatchShape &shape, int maxNodes);
 void launch_batch_initial(const Dev &d, const BatchDev &b, bool mixed, cudaStream_t st);
 void launch_batch_arm(const BatchDev &b, long long maxSteps, cudaStream_t st);
 void launch_batch_comp(const Dev &d, bool toFloat, cudaStream_t st);
+const void *comp_steps_kernel(const BatchShape &shape);      // k_batch_comp.cu
 cudaError_t launch_batch_steps(const Dev &d, const BatchDev &b, int mode,
                                const BatchShape &shape, int sms, cudaStream_t st);
 void launch_batch_measure(const Dev &d, const BatchDev &b, cudaStream_t st);
