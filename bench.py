@@ -422,7 +422,7 @@ def run_batched(args, plain_fp64=None):
             b.setConfig(t, sn, bps, b.config()["chunk_steps"])
             shape = b.config()
         else:
-            shape = b.tune(32)
+            shape = b.tune(64)
         tune_s = time.perf_counter() - t0
         clocks = Clocks(0)
         clocks.start()

@@ -111,7 +111,7 @@ __global__ void __launch_bounds__(MEASURE_BLOCK) k_batch_measure(Dev d, BatchDev
 
 template <bool MIXED, bool STAGE, int T, bool COMP>
 static const void *steps_kernel() {
-    return (const void *)k_batch_steps<MIXED, STAGE, T, COMP>;
+    return (const void *)k_batch_steps<MIXED, STAGE, T>;
 }
 
 template <bool MIXED, bool COMP>

@@ -33,10 +33,10 @@ __global__ void k_batch_comp_sync(Dev d) {
 
 const void *comp_steps_kernel(const BatchShape &s) {
     if (s.stage)
-        return s.threads == 128 ? (const void *)k_batch_steps<true, true, 128, true>
-                                : (const void *)k_batch_steps<true, true, 256, true>;
-    return s.threads == 128 ? (const void *)k_batch_steps<true, false, 128, true>
-                            : (const void *)k_batch_steps<true, false, 256, true>;
+        return s.threads == 128 ? (const void *)k_batch_steps_comp<true, 128>
+                                : (const void *)k_batch_steps_comp<true, 256>;
+    return s.threads == 128 ? (const void *)k_batch_steps_comp<false, 128>
+                            : (const void *)k_batch_steps_comp<false, 256>;
 }
 
 void launch_batch_comp(const Dev &d, bool toFloat, cudaStream_t st) {

@@ -24,7 +24,7 @@ __device__ void run_instance(const Dev &d, const BatchDev &b, int k, int chunk, 
     if (tid == 0) {
         wallCount[0][0] = wallCount[0][1] = 0;
         wallCount[1][0] = wallCount[1][1] = 0;
-        block_step_coef(*bs, in, dt, dtPrev);
+        block_step_init(*bs, d, in, dt, dtPrev);
     }
     __syncthreads();
     float4 *pMid = STAGE ? sPMid : d.pMid;
@@ -71,8 +71,10 @@ __device__ void run_instance(const Dev &d, const BatchDev &b, int k, int chunk, 
     __syncthreads();
 }
 
+// The queue loop of the persistent kernel: each block takes the next instance (most
+// expensive first) for a chunk of steps until none is left.
 template <bool MIXED, bool STAGE, int T, bool COMP>
-__global__ void __launch_bounds__(T) k_batch_steps(Dev d, BatchDev b, int chunk) {
+__device__ __forceinline__ void batch_queue(const Dev &d, const BatchDev &b, int chunk) {
     extern __shared__ __align__(16) unsigned char dyn[];
     __shared__ double shMin[T / 32 + 1];
     __shared__ int wallCount[2][2];
@@ -89,6 +91,19 @@ __global__ void __launch_bounds__(T) k_batch_steps(Dev d, BatchDev b, int chunk)
         run_instance<MIXED, STAGE, T, COMP>(d, b, b.order[q], chunk, sPMid, sVdt, shMin,
                                             wallCount, &bs);
     }
+}
+
+// The FP64 and mixed forms (the compiler's register choice).
+template <bool MIXED, bool STAGE, int T>
+__global__ void __launch_bounds__(T) k_batch_steps(Dev d, BatchDev b, int chunk) {
+    batch_queue<MIXED, STAGE, T, false>(d, b, chunk);
+}
+
+// The compensated form keeps few values live across its FP32 phases: capped at 85 registers
+// (768 resident threads per SM) it hides more memory latency than with the compiler's choice.
+template <bool STAGE, int T>
+__global__ void __launch_bounds__(T, 768 / T) k_batch_steps_comp(Dev d, BatchDev b, int chunk) {
+    batch_queue<true, STAGE, T, true>(d, b, chunk);
 }
 
 }  // namespace nf

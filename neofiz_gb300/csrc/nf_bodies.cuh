@@ -549,6 +549,7 @@ static __device__ __forceinline__ float2 ff_from(double x) {
 // geometry for the coming assembly. The audit terms are summed in FP64.
 static __device__ __forceinline__ void nodal_node_comp(const Dev &d, int i, float decay,
                                                        float gain, float dtAvg, float dt,
+                                                       float plane, float friction,
                                                        const WallRef &w, const MixedGeo &geo,
                                                        uint32_t *status, double &impulse,
                                                        double &loss, double &fric) {
@@ -561,7 +562,6 @@ static __device__ __forceinline__ void nodal_node_comp(const Dev &d, int i, floa
     const float2 mm = d.mC[i];
     const float m = mm.x, invM = mm.y;
     const float4 x0 = d.x0C[i];
-    const float friction = (float)w.friction;
     const bool resting = w.present && onWall && f.y <= 0.0f;
     uint8_t ws = 0;
     if (fixedR) {
@@ -595,7 +595,6 @@ static __device__ __forceinline__ void nodal_node_comp(const Dev &d, int i, floa
         ws |= NF_WALL_HELD;
     } else {
         const float trial = decay * v.y + gain * f.y * invM;
-        const float plane = (float)w.plane;
         // z + trial dt < plane, with z = x0 + u as a pair
         const float2 s = two_sum_f(x0.z, u.z);
         const float below = (s.x - plane) + ((s.y + (x0.w + u.w)) + trial * dt);
@@ -682,7 +681,8 @@ static __device__ __forceinline__ void pressure_edge_comp(const Dev &d, int e, d
 }
 
 // The gather of float contributions into float sums, in CSR order, then m g.
-static __device__ __forceinline__ float2 gather_node_comp(const Dev &d, int n) {
+static __device__ __forceinline__ float2 gather_node_comp(const Dev &d, int n, float gR,
+                                                          float gZ) {
     float sr = 0.0f, sz = 0.0f;
     const int end = d.nodeSlotStart[n + 1];
     for (int k = d.nodeSlotStart[n]; k < end; k++) {
@@ -691,7 +691,7 @@ static __device__ __forceinline__ float2 gather_node_comp(const Dev &d, int n) {
         sz += d.contribF[slot + 4];
     }
     const float m = d.mC[n].x;
-    return make_float2(sr + m * (float)d.gravR, sz + m * (float)d.gravZ);
+    return make_float2(sr + m * gR, sz + m * gZ);
 }
 
 // gather, ExplicitSolver.java:1147-1165: node n's sources in ascending order, then m g.
