@@ -437,6 +437,12 @@ nf_status nf_batch_adjoint_forward(nf_batch *b, int32_t checkpoint_every, int32_
  * objective after one forward pass. */
 nf_status nf_batch_adjoint_backward(nf_batch *b, int32_t objective, double *values,
                                     double *gradients);
+/* Several objectives in one backward pass (count 1 to 3, each at most once per call): the
+ * segments are recomputed once and each objective's reverse sweep reads the same recomputed
+ * values, so its gradients are bit-identical to a pass of its own. values[count *
+ * instance_count] and gradients[count * instance_count * NF_PARAM_COUNT], objective-major. */
+nf_status nf_batch_adjoint_backward_many(nf_batch *b, const int32_t *objectives, int32_t count,
+                                         double *values, double *gradients);
 /* Device (or, for the CPU restatement, wall) time of the last forward and backward passes. */
 nf_status nf_batch_adjoint_elapsed(nf_batch *b, double *forward_ms, double *backward_ms);
 

@@ -189,6 +189,7 @@ _PROTOS = {
     "batch_wall_stats": (_S, [_H, C.POINTER(WallInfo)]),
     "batch_adjoint_forward": (_S, [_H, C.c_int32, C.c_int32]),
     "batch_adjoint_backward": (_S, [_H, C.c_int32, c_double_p, c_double_p]),
+    "batch_adjoint_backward_many": (_S, [_H, c_int32_p, C.c_int32, c_double_p, c_double_p]),
     "batch_adjoint_elapsed": (_S, [_H, C.POINTER(C.c_double), C.POINTER(C.c_double)]),
 }
 

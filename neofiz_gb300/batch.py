@@ -241,6 +241,18 @@ class BatchSolver:
             grads.ctypes.data_as(_abi.c_double_p)))
         return values, grads
 
+    def adjointBackwardMany(self, objectives: Sequence[int]):
+        """Several objectives in one backward pass (one segment recompute shared):
+        (values[len, count], gradients[len, count, PARAM_COUNT]), each objective's gradients
+        bit-identical to adjointBackward(objective)."""
+        obj = np.asarray(list(objectives), dtype=np.int32)
+        values = np.zeros((obj.size, self.count))
+        grads = np.zeros((obj.size, self.count, _abi.PARAM_COUNT))
+        self._check(self._api.batch_adjoint_backward_many(
+            self._handle, obj.ctypes.data_as(_abi.c_int32_p), int(obj.size),
+            values.ctypes.data_as(_abi.c_double_p), grads.ctypes.data_as(_abi.c_double_p)))
+        return values, grads
+
     def adjointElapsed(self):
         f, b = C.c_double(), C.c_double()
         self._check(self._api.batch_adjoint_elapsed(self._handle, C.byref(f), C.byref(b)))

@@ -850,11 +850,13 @@ nf_status nf_batch_adjoint_forward(nf_batch *h, int32_t checkpoint_every, int32_
     long long *dCkptOff = nullptr, *dFinOff = nullptr, *dTapeOff = nullptr, *dBarOff = nullptr;
     long long *dCap = nullptr, *dBytes = nullptr, *dSeedOff = nullptr, *dSeedStep = nullptr;
 #define A(ptr, n) if (e_ == cudaSuccess) e_ = aalloc(B, &(ptr), (n))
-    A(a.ckpt, (size_t)ck); A(a.fin, (size_t)fi); A(a.peak, (size_t)fi); A(a.seed, (size_t)se);
+    A(a.ckpt, (size_t)ck); A(a.fin, (size_t)fi); A(a.peak, (size_t)fi);
+    A(a.seed, (size_t)se * NF_ADJ_MAX_WIDTH);
     A(dCkptOff, B.count); A(dFinOff, B.count); A(dTapeOff, B.count); A(dBarOff, B.count);
-    A(dCap, B.count); A(dBytes, B.count); A(dSeedOff, B.count); A(dSeedStep, B.count);
+    A(dCap, B.count); A(dBytes, B.count); A(dSeedOff, B.count);
+    A(dSeedStep, (size_t)B.count * NF_ADJ_MAX_WIDTH);
     A(a.steps, B.count); A(a.peakStep, B.count); A(a.peakValue, B.count);
-    A(a.grad, (size_t)B.count * NF_PARAM_COUNT); A(a.overflow, 1);
+    A(a.grad, (size_t)B.count * NF_PARAM_COUNT * NF_ADJ_MAX_WIDTH); A(a.overflow, 1);
 #undef A
     if (e_ != cudaSuccess) {
         free_adjoint(B);
@@ -872,6 +874,8 @@ nf_status nf_batch_adjoint_forward(nf_batch *h, int32_t checkpoint_every, int32_
     a.ckptCap = dCap; a.stateBytes = dBytes;
     a.every = checkpoint_every;
     a.sampleEvery = sample_every;
+    a.width = 1;
+    a.seedPlane = se;
     B.adjSeedBytes = se;
     B.adjSeedOff = seedOff;
     B.adjFinOff = finOff;
@@ -881,6 +885,7 @@ nf_status nf_batch_adjoint_forward(nf_batch *h, int32_t checkpoint_every, int32_
     a.bar = nullptr;
     B.adjTapeBytes = ta;
     B.adjBarBytes = ba;
+    a.barPlane = ba;
     B.adjBarOff = barOff;
     BCK(&B, cudaEventRecord(B.ev0, B.stream));
     launch_adjoint_forward(B.d, B.b, a, B.stream);
@@ -903,125 +908,148 @@ nf_status nf_batch_adjoint_forward(nf_batch *h, int32_t checkpoint_every, int32_
 
 static bool sampled(long long peakStep) { return peakStep > 0; }
 
-nf_status nf_batch_adjoint_backward(nf_batch *h, int32_t objective, double *values,
-                                    double *gradients) {
+// The objective of instance k and its seed in one plane of the seed buffer: the adjoint of
+// the displacements (and, for the capacity, of the hoop stress) after step *seedStep, the
+// final step or the sampled peak.
+static nf_status adjoint_seed(Batch &B, int32_t objective, int k,
+                              const std::vector<double2> &X0, const std::vector<int32_t> &conn,
+                              const std::vector<long long> &steps,
+                              const std::vector<long long> &peakStep, char *plane,
+                              double *value, long long *seedStep) {
+    const AdjDev &a = B.adj;
+    const bool finite = B.d.finite != 0;
+    const BatchInst &in = B.inst[k];
+    const int n = in.n1 - in.n0, e = in.e1 - in.e0;
+    // the state the objective is read from: the final or the peak block (U and sig)
+    const long long blk = B.adjFinOff[k];
+    const char *src = objective == NF_OBJECTIVE_PEAK_CAPACITY ? a.peak : a.fin;
+    std::vector<double2> U(n);
+    std::vector<double> sig(4 * (size_t)e);
+    BCK(&B, cudaMemcpy(U.data(), src + blk, 16 * (size_t)n, cudaMemcpyDeviceToHost));
+    BCK(&B, cudaMemcpy(sig.data(), src + blk + 3 * ((16 * (size_t)n + 15) & ~(size_t)15),
+                       32 * (size_t)e, cudaMemcpyDeviceToHost));
+    double2 *su = reinterpret_cast<double2 *>(plane + B.adjSeedOff[k]);
+    double *ss = reinterpret_cast<double *>(plane + B.adjSeedOff[k]
+                                            + ((16 * (size_t)n + 15) & ~(size_t)15));
+    auto R_ = [&](int i) { return finite ? X0[in.n0 + i].x + U[i].x : X0[in.n0 + i].x; };
+    auto Z_ = [&](int i) { return finite ? X0[in.n0 + i].y + U[i].y : X0[in.n0 + i].y; };
+    if (objective == NF_OBJECTIVE_PEAK_CAPACITY) {
+        if (!(sampled(peakStep[k])))
+            return bfail(&B, NF_ESTATE, "instance %d: no capacity was sampled in the forward "
+                                        "pass (sample_every 0 or no sample before t_end)", k);
+        *seedStep = peakStep[k];
+        // BurstCase.loadCapacity (BurstCase.java:533-553) and its derivatives
+        double hoop = 0.0;
+        for (int j = 0; j < e; j++) {
+            double sum = 0.0;
+            for (int c = 0; c < 4; c++) {
+                const int p = conn[4 * (size_t)(in.e0 + j) + c] - in.n0;
+                const int q = conn[4 * (size_t)(in.e0 + j) + (c + 1) % 4] - in.n0;
+                sum += R_(p) * Z_(q) - R_(q) * Z_(p);
+            }
+            hoop += sig[4 * (size_t)j + 2] * (0.5 * sum);
+        }
+        double bore = DBL_MAX, low = DBL_MAX, high = -DBL_MAX;
+        int ib = 0, il = 0, ih = 0;
+        for (int i = 0; i < n; i++) {
+            if (R_(i) < bore) { bore = R_(i); ib = i; }
+            if (Z_(i) < low) { low = Z_(i); il = i; }
+            if (Z_(i) > high) { high = Z_(i); ih = i; }
+        }
+        const double den = bore * (high - low);
+        const double capv = hoop / den;
+        *value = capv;
+        for (int j = 0; j < e; j++) {
+            double r[4], z[4];
+            int nn[4];
+            for (int c = 0; c < 4; c++) {
+                nn[c] = conn[4 * (size_t)(in.e0 + j) + c] - in.n0;
+                r[c] = R_(nn[c]);
+                z[c] = Z_(nn[c]);
+            }
+            double sum = 0.0;
+            for (int c = 0; c < 4; c++) sum += r[c] * z[(c + 1) & 3] - r[(c + 1) & 3] * z[c];
+            ss[4 * (size_t)j + 2] += 0.5 * sum / den;
+            if (finite) {
+                const double w = sig[4 * (size_t)j + 2] / den;
+                for (int c = 0; c < 4; c++) {
+                    su[nn[c]].x += w * 0.5 * (z[(c + 1) & 3] - z[(c + 3) & 3]);
+                    su[nn[c]].y += w * 0.5 * (r[(c + 3) & 3] - r[(c + 1) & 3]);
+                }
+            }
+        }
+        if (finite) {
+            su[ib].x -= capv / bore;
+            su[ih].y -= capv / (high - low);
+            su[il].y += capv / (high - low);
+        }
+        return NF_OK;
+    }
+    *seedStep = steps[k];
+    double zmax = -DBL_MAX, zmin = DBL_MAX, z0max = -DBL_MAX, z0min = DBL_MAX, rmax = -DBL_MAX;
+    int imax = 0, imin = 0, irmax = 0;
+    for (int i = 0; i < n; i++) {
+        const double z = X0[in.n0 + i].y + U[i].y, r = X0[in.n0 + i].x + U[i].x;
+        if (z > zmax) { zmax = z; imax = i; }
+        if (z < zmin) { zmin = z; imin = i; }
+        if (r > rmax) { rmax = r; irmax = i; }
+        if (X0[in.n0 + i].y > z0max) z0max = X0[in.n0 + i].y;
+        if (X0[in.n0 + i].y < z0min) z0min = X0[in.n0 + i].y;
+    }
+    if (objective == NF_OBJECTIVE_LENGTH_RATIO) {
+        const double L0 = z0max - z0min;
+        su[imax].y += 1.0 / L0;
+        su[imin].y -= 1.0 / L0;
+        *value = (zmax - zmin) / L0;
+    } else {
+        su[irmax].x += 2.0;
+        *value = 2.0 * rmax;
+    }
+    return NF_OK;
+}
+
+nf_status nf_batch_adjoint_backward_many(nf_batch *h, const int32_t *objectives, int32_t count,
+                                         double *values, double *gradients) {
     Batch &B = *reinterpret_cast<Batch *>(h);
     if (!B.adjForward) return bfail(&B, NF_ESTATE, "run the adjoint's forward pass first");
+    if (count < 1 || count > NF_ADJ_MAX_WIDTH)
+        return bfail(&B, NF_EINVAL, "1 to %d objectives per backward pass, not %d",
+                     NF_ADJ_MAX_WIDTH, count);
+    for (int w = 0; w < count; w++)
+        if (objectives[w] != NF_OBJECTIVE_LENGTH_RATIO && objectives[w] != NF_OBJECTIVE_MUSHROOM &&
+            objectives[w] != NF_OBJECTIVE_PEAK_CAPACITY)
+            return bfail(&B, NF_EINVAL, "unknown objective %d", objectives[w]);
     AdjDev &a = B.adj;
     cudaError_t e_ = cudaSuccess;
     if (!a.tape) {
         e_ = aalloc(B, &a.tape, (size_t)B.adjTapeBytes);
-        if (e_ == cudaSuccess) e_ = aalloc(B, &a.bar, (size_t)B.adjBarBytes);
+        if (e_ == cudaSuccess)
+            e_ = aalloc(B, &a.bar, (size_t)B.adjBarBytes * NF_ADJ_MAX_WIDTH);
         if (e_ != cudaSuccess) return bfail(&B, NF_ENOMEM, "adjoint allocation failed: %s",
                                             cudaGetErrorString(e_));
     }
-    // the objective and its seed, per instance: the adjoint of the displacements (and, for the
-    // capacity, of the hoop stress) after step m, the final step or the sampled peak
-    if (objective != NF_OBJECTIVE_LENGTH_RATIO && objective != NF_OBJECTIVE_MUSHROOM &&
-        objective != NF_OBJECTIVE_PEAK_CAPACITY)
-        return bfail(&B, NF_EINVAL, "unknown objective %d", objective);
     std::vector<double2> X0(B.N);
     BCK(&B, cudaMemcpy(X0.data(), B.d.X0, 16 * (size_t)B.N, cudaMemcpyDeviceToHost));
-    std::vector<long long> steps(B.count), peakStep(B.count), seedStep(B.count);
+    std::vector<long long> steps(B.count), peakStep(B.count);
+    std::vector<long long> seedStep((size_t)B.count * count);
     BCK(&B, cudaMemcpy(steps.data(), a.steps, 8 * B.count, cudaMemcpyDeviceToHost));
     BCK(&B, cudaMemcpy(peakStep.data(), a.peakStep, 8 * B.count, cudaMemcpyDeviceToHost));
-    std::vector<char> seed((size_t)B.adjSeedBytes, 0);
     std::vector<int32_t> conn(4 * (size_t)B.E);
     BCK(&B, cudaMemcpy(conn.data(), B.d.conn, 16 * (size_t)B.E, cudaMemcpyDeviceToHost));
-    const bool finite = B.d.finite != 0;
-    for (int k = 0; k < B.count; k++) {
-        const BatchInst &in = B.inst[k];
-        const int n = in.n1 - in.n0, e = in.e1 - in.e0;
-        // the state the objective is read from: the final or the peak block (U and sig)
-        const long long blk = B.adjFinOff[k];
-        const char *src = objective == NF_OBJECTIVE_PEAK_CAPACITY ? a.peak : a.fin;
-        std::vector<double2> U(n);
-        std::vector<double> sig(4 * (size_t)e);
-        BCK(&B, cudaMemcpy(U.data(), src + blk, 16 * (size_t)n, cudaMemcpyDeviceToHost));
-        BCK(&B, cudaMemcpy(sig.data(), src + blk + 3 * ((16 * (size_t)n + 15) & ~(size_t)15),
-                           32 * (size_t)e, cudaMemcpyDeviceToHost));
-        double2 *su = reinterpret_cast<double2 *>(seed.data() + B.adjSeedOff[k]);
-        double *ss = reinterpret_cast<double *>(seed.data() + B.adjSeedOff[k]
-                                                + ((16 * (size_t)n + 15) & ~(size_t)15));
-        auto R_ = [&](int i) { return finite ? X0[in.n0 + i].x + U[i].x : X0[in.n0 + i].x; };
-        auto Z_ = [&](int i) { return finite ? X0[in.n0 + i].y + U[i].y : X0[in.n0 + i].y; };
-        if (objective == NF_OBJECTIVE_PEAK_CAPACITY) {
-            if (!(sampled(peakStep[k])))
-                return bfail(&B, NF_ESTATE, "instance %d: no capacity was sampled in the forward "
-                                            "pass (sample_every 0 or no sample before t_end)", k);
-            seedStep[k] = peakStep[k];
-            // BurstCase.loadCapacity (BurstCase.java:533-553) and its derivatives
-            double hoop = 0.0;
-            for (int j = 0; j < e; j++) {
-                double sum = 0.0;
-                for (int c = 0; c < 4; c++) {
-                    const int p = conn[4 * (size_t)(in.e0 + j) + c] - in.n0;
-                    const int q = conn[4 * (size_t)(in.e0 + j) + (c + 1) % 4] - in.n0;
-                    sum += R_(p) * Z_(q) - R_(q) * Z_(p);
-                }
-                hoop += sig[4 * (size_t)j + 2] * (0.5 * sum);
-            }
-            double bore = DBL_MAX, low = DBL_MAX, high = -DBL_MAX;
-            int ib = 0, il = 0, ih = 0;
-            for (int i = 0; i < n; i++) {
-                if (R_(i) < bore) { bore = R_(i); ib = i; }
-                if (Z_(i) < low) { low = Z_(i); il = i; }
-                if (Z_(i) > high) { high = Z_(i); ih = i; }
-            }
-            const double den = bore * (high - low);
-            const double capv = hoop / den;
-            values[k] = capv;
-            for (int j = 0; j < e; j++) {
-                double r[4], z[4];
-                int nn[4];
-                for (int c = 0; c < 4; c++) {
-                    nn[c] = conn[4 * (size_t)(in.e0 + j) + c] - in.n0;
-                    r[c] = R_(nn[c]);
-                    z[c] = Z_(nn[c]);
-                }
-                double sum = 0.0;
-                for (int c = 0; c < 4; c++) sum += r[c] * z[(c + 1) & 3] - r[(c + 1) & 3] * z[c];
-                ss[4 * (size_t)j + 2] += 0.5 * sum / den;
-                if (finite) {
-                    const double w = sig[4 * (size_t)j + 2] / den;
-                    for (int c = 0; c < 4; c++) {
-                        su[nn[c]].x += w * 0.5 * (z[(c + 1) & 3] - z[(c + 3) & 3]);
-                        su[nn[c]].y += w * 0.5 * (r[(c + 3) & 3] - r[(c + 1) & 3]);
-                    }
-                }
-            }
-            if (finite) {
-                su[ib].x -= capv / bore;
-                su[ih].y -= capv / (high - low);
-                su[il].y += capv / (high - low);
-            }
-            continue;
+    std::vector<char> seed((size_t)B.adjSeedBytes * count, 0);
+    for (int w = 0; w < count; w++)
+        for (int k = 0; k < B.count; k++) {
+            const nf_status st = adjoint_seed(B, objectives[w], k, X0, conn, steps, peakStep,
+                                              seed.data() + (size_t)w * B.adjSeedBytes,
+                                              &values[(size_t)w * B.count + k],
+                                              &seedStep[(size_t)w * B.count + k]);
+            if (st) return st;
         }
-        seedStep[k] = steps[k];
-        double zmax = -DBL_MAX, zmin = DBL_MAX, z0max = -DBL_MAX, z0min = DBL_MAX, rmax = -DBL_MAX;
-        int imax = 0, imin = 0, irmax = 0;
-        for (int i = 0; i < n; i++) {
-            const double z = X0[in.n0 + i].y + U[i].y, r = X0[in.n0 + i].x + U[i].x;
-            if (z > zmax) { zmax = z; imax = i; }
-            if (z < zmin) { zmin = z; imin = i; }
-            if (r > rmax) { rmax = r; irmax = i; }
-            if (X0[in.n0 + i].y > z0max) z0max = X0[in.n0 + i].y;
-            if (X0[in.n0 + i].y < z0min) z0min = X0[in.n0 + i].y;
-        }
-        if (objective == NF_OBJECTIVE_LENGTH_RATIO) {
-            const double L0 = z0max - z0min;
-            su[imax].y += 1.0 / L0;
-            su[imin].y -= 1.0 / L0;
-            values[k] = (zmax - zmin) / L0;
-        } else {
-            su[irmax].x += 2.0;
-            values[k] = 2.0 * rmax;
-        }
-    }
     BCK(&B, cudaMemcpyAsync(a.seed, seed.data(), seed.size(), cudaMemcpyHostToDevice, B.stream));
-    BCK(&B, cudaMemcpyAsync(const_cast<long long *>(a.seedStep), seedStep.data(), 8 * B.count,
-                            cudaMemcpyHostToDevice, B.stream));
-    BCK(&B, cudaMemsetAsync(a.bar, 0, (size_t)B.adjBarBytes, B.stream));
+    BCK(&B, cudaMemcpyAsync(const_cast<long long *>(a.seedStep), seedStep.data(),
+                            8 * seedStep.size(), cudaMemcpyHostToDevice, B.stream));
+    BCK(&B, cudaMemsetAsync(a.bar, 0, (size_t)B.adjBarBytes * count, B.stream));
+    a.width = count;
     BCK(&B, cudaEventRecord(B.ev0, B.stream));
     launch_adjoint_backward(B.d, B.b, a, B.stream);
     B.launches += 1;
@@ -1031,9 +1059,14 @@ nf_status nf_batch_adjoint_backward(nf_batch *h, int32_t objective, double *valu
     float ms = 0.0f;
     BCK(&B, cudaEventElapsedTime(&ms, B.ev0, B.ev1));
     B.adjBackwardMs = ms;
-    BCK(&B, cudaMemcpy(gradients, a.grad, sizeof(double) * NF_PARAM_COUNT * B.count,
+    BCK(&B, cudaMemcpy(gradients, a.grad, sizeof(double) * NF_PARAM_COUNT * B.count * count,
                        cudaMemcpyDeviceToHost));
     return NF_OK;
+}
+
+nf_status nf_batch_adjoint_backward(nf_batch *h, int32_t objective, double *values,
+                                    double *gradients) {
+    return nf_batch_adjoint_backward_many(h, &objective, 1, values, gradients);
 }
 
 nf_status nf_batch_adjoint_elapsed(nf_batch *h, double *forward_ms, double *backward_ms) {

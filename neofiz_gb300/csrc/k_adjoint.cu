@@ -440,8 +440,10 @@ __global__ void __launch_bounds__(ADJ_T) k_adj_backward(Dev d, BatchDev b, AdjDe
     __shared__ double shRed[ADJ_T / 32 + 1];
     __shared__ int shOwner;
     __shared__ int scratch[3];                   // wall counts and status of recomputed steps
-    __shared__ double shDtb, shDtPrevb, shTimeb;
+    __shared__ double shDtb[NF_ADJ_MAX_WIDTH], shDtPrevb[NF_ADJ_MAX_WIDTH];
+    __shared__ double shTimeb[NF_ADJ_MAX_WIDTH];
     const int k = blockIdx.x;
+    const int W = a.width;
     const BatchInst in = b.inst[k];
     const MatDev mat = d.mats[k];
     const int n = in.n1 - in.n0, e = in.e1 - in.e0;
@@ -450,17 +452,12 @@ __global__ void __launch_bounds__(ADJ_T) k_adj_backward(Dev d, BatchDev b, AdjDe
     char *ckpt = a.ckpt + a.ckptOff[k];
     char *tape = a.tape + a.tapeOff[k];
     const int nk = in.k1 - in.k0;
-    BarBlock bar = bar_at(a.bar + a.barOff[k], n, e, nk);
-    const long long m = a.seedStep[k];
-    const double2 *seedU = reinterpret_cast<const double2 *>(a.seed + a.seedOff[k]);
-    const double *seedSig = reinterpret_cast<const double *>(a.seed + a.seedOff[k]
-                                                               + al16(16 * (size_t)n));
-    double pacc[NF_ADJ_P_COUNT];
-    for (int p = 0; p < NF_ADJ_P_COUNT; p++) pacc[p] = 0.0;
+    // per objective: its parameter adjoints, summed per thread over every step
+    double pacc[NF_ADJ_MAX_WIDTH][NF_ADJ_P_COUNT];
+    for (int w = 0; w < NF_ADJ_MAX_WIDTH; w++)
+        for (int p = 0; p < NF_ADJ_P_COUNT; p++) pacc[w][p] = 0.0;
     if (threadIdx.x == 0) {
-        shDtb = 0.0;
-        shDtPrevb = 0.0;
-        shTimeb = 0.0;
+        for (int w = 0; w < NF_ADJ_MAX_WIDTH; w++) shDtb[w] = shDtPrevb[w] = shTimeb[w] = 0.0;
         scratch[0] = scratch[1] = scratch[2] = 0;
     }
     __syncthreads();
@@ -490,22 +487,35 @@ __global__ void __launch_bounds__(ADJ_T) k_adj_backward(Dev d, BatchDev b, AdjDe
         }
         __syncthreads();
         for (long long j = end - 1; j >= start; j--) {
-            if (j == m - 1) {                  // the objective's seed enters after step m
-                for (int i = threadIdx.x; i < n; i += ADJ_T) {
-                    bar.U[i].x += seedU[i].x;
-                    bar.U[i].y += seedU[i].y;
+            const StateBlock pre = state_at(tape + (j - start) * bytes, n, e);
+            for (int w = 0; w < W; w++) {
+                BarBlock bar = bar_at(a.bar + w * a.barPlane + a.barOff[k], n, e, nk);
+                if (j == a.seedStep[(size_t)w * b.count + k] - 1) {
+                    // objective w's seed enters after its step m
+                    const char *sd = a.seed + w * a.seedPlane + a.seedOff[k];
+                    const double2 *seedU = reinterpret_cast<const double2 *>(sd);
+                    const double *seedSig =
+                        reinterpret_cast<const double *>(sd + al16(16 * (size_t)n));
+                    for (int i = threadIdx.x; i < n; i += ADJ_T) {
+                        bar.U[i].x += seedU[i].x;
+                        bar.U[i].y += seedU[i].y;
+                    }
+                    for (int q = threadIdx.x; q < 4 * e; q += ADJ_T) bar.sig[q] += seedSig[q];
+                    __syncthreads();
                 }
-                for (int q = threadIdx.x; q < 4 * e; q += ADJ_T) bar.sig[q] += seedSig[q];
-                __syncthreads();
+                // the forward values each objective's reverse reads are recomputed from the
+                // same tape entry, so every objective sees the same bits
+                reverse_step(d, in, mat, pre, bar, pacc[w], shRed, &shOwner, &shDtb[w],
+                             &shDtPrevb[w], &shTimeb[w], scratch);
             }
-            reverse_step(d, in, mat, state_at(tape + (j - start) * bytes, n, e), bar, pacc, shRed,
-                         &shOwner, &shDtb, &shDtPrevb, &shTimeb, scratch);
         }
     }
-    for (int p = 0; p < NF_ADJ_P_COUNT; p++) {
-        const double t = block_total<ADJ_T>(pacc[p], shRed);
-        if (threadIdx.x == 0) a.grad[NF_ADJ_P_COUNT * (size_t)k + p] = t;
-    }
+    for (int w = 0; w < W; w++)
+        for (int p = 0; p < NF_ADJ_P_COUNT; p++) {
+            const double t = block_total<ADJ_T>(pacc[w][p], shRed);
+            if (threadIdx.x == 0)
+                a.grad[((size_t)w * b.count + k) * NF_ADJ_P_COUNT + p] = t;
+        }
     // the solver arrays back to the forward's final state
     StateBlock fin = state_at(a.fin + a.finOff[k], n, e);
     copy_state<ADJ_T>(d, in, fin, false);

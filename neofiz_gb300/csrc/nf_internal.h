@@ -245,11 +245,16 @@ struct AdjDev {
     long long *steps;                        // the forward's step count per instance
     long long *peakStep;                     // the sampled capacity peak: its step and value
     double *peakValue;
+    // The backward pass carries `width` objectives (1..NF_ADJ_MAX_WIDTH) through one segment
+    // recompute: objective w's adjoint arrays, seed, seed step and gradients sit in plane w
+    // (bar + w barPlane, seed + w seedPlane, seedStep[w count + k], grad[(w count + k) P + p]).
     const long long *seedStep;               // the objective's seed enters after this step
-    double *grad;                            // [count * NF_PARAM_COUNT]
+    double *grad;
     int *overflow;
-    int every, sampleEvery;
+    int every, sampleEvery, width;
+    long long barPlane, seedPlane;
 };
+constexpr int NF_ADJ_MAX_WIDTH = 3;
 size_t adj_state_bytes(int n, int e);
 size_t adj_bar_bytes(int n, int e, int k);
 size_t adj_seed_bytes(int n, int e);

@@ -2695,6 +2695,23 @@ API nf_status nfo_batch_adjoint_backward(nfo_batch *b, int32_t objective, double
     return NF_OK;
 }
 
+/* Several objectives: one reference backward pass per objective (the reference adjoint has
+ * no shared recompute; its gradients are those of the single passes). */
+API nf_status nfo_batch_adjoint_backward_many(nfo_batch *b, const int32_t *objectives,
+                                              int32_t count, double *values, double *gradients) {
+    if (count < 1 || count > 3)
+        return bfail(b, NF_EINVAL, "1 to 3 objectives per backward pass, not %d", count);
+    double total = 0.0;
+    for (int w = 0; w < count; w++) {
+        nf_status st = nfo_batch_adjoint_backward(b, objectives[w], values + (size_t)w * b->count,
+                                                  gradients + (size_t)w * b->count * NF_ADJ_P_COUNT);
+        if (st) return st;
+        total += b->adjBackwardMs;
+    }
+    b->adjBackwardMs = total;
+    return NF_OK;
+}
+
 API nf_status nfo_batch_adjoint_elapsed(nfo_batch *b, double *forward_ms, double *backward_ms) {
     *forward_ms = b->adjForwardMs;
     *backward_ms = b->adjBackwardMs;

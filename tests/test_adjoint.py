@@ -162,3 +162,19 @@ def test_fraction_convention_is_the_chain_rule():
     np.testing.assert_allclose(out[2], g[2] + g[5] * dHdn, rtol=1e-7)
     assert out[5] == g[6] and out[7] == g[7]
     np.testing.assert_allclose(out[6], g[5] * dHdf, rtol=1e-7)
+
+
+def test_several_objectives_in_one_pass_match_single_passes():
+    """backward_many([L/L0, mushroom]) on the reference adjoint gives the single passes'
+    values and gradients."""
+    rods = scenes.adjoint_rods(2)
+    for r in rods:
+        r["nr"], r["nz"], r["t_end"] = 4, 20, 4.0e-6
+    b = OracleBatch(scenes.sweep_instances(rods), scenes.Formulation.AXISYMMETRIC, cfl=0.6)
+    b.adjointForward(17)
+    v, g = b.adjointBackwardMany([_abi.OBJECTIVE_LENGTH_RATIO, _abi.OBJECTIVE_MUSHROOM])
+    for w, obj in enumerate((_abi.OBJECTIVE_LENGTH_RATIO, _abi.OBJECTIVE_MUSHROOM)):
+        v1, g1 = b.adjointBackward(obj)
+        assert np.array_equal(v[w], v1) and np.array_equal(g[w], g1)
+    with pytest.raises(ValueError):
+        b.adjointBackwardMany([0, 1, 2, 0])

@@ -80,3 +80,25 @@ def test_capacity_adjoint_kernel_matches_the_reference_adjoint(gpu_lib):
     np.testing.assert_allclose(gv, ov, rtol=1e-13)
     assert og[0][_abi.PARAM_FRACTURE_ENERGY] != 0.0
     np.testing.assert_allclose(gg, og, rtol=1e-9, atol=1e-12 * np.abs(og).max())
+
+
+def test_several_objectives_in_one_pass_are_bit_identical_to_single_passes(gpu_lib):
+    """One recompute carries L/L0 and the mushroom diameter (and a tube's capacity): each
+    objective's values and gradients equal its own pass bit for bit."""
+    rods = _rods(t_end=6.0e-6)
+    b = BatchSolver(scenes.sweep_instances(rods), scenes.Formulation.AXISYMMETRIC, cfl=0.6)
+    b.adjointForward(40)
+    objs = [_abi.OBJECTIVE_LENGTH_RATIO, _abi.OBJECTIVE_MUSHROOM]
+    v, g = b.adjointBackwardMany(objs)
+    for w, obj in enumerate(objs):
+        v1, g1 = b.adjointBackward(obj)
+        assert np.array_equal(v[w], v1) and np.array_equal(g[w], g1), obj
+    b.close()
+    t = BatchSolver([scenes.tube_instance(nz=20, t_end=12.0e-6, scale=0.04)],
+                    scenes.Formulation.AXISYMMETRIC, cfl=0.5)
+    t.adjointForward(50, 5)
+    objs = [_abi.OBJECTIVE_PEAK_CAPACITY, _abi.OBJECTIVE_LENGTH_RATIO]
+    v, g = t.adjointBackwardMany(objs)
+    for w, obj in enumerate(objs):
+        v1, g1 = t.adjointBackward(obj)
+        assert np.array_equal(v[w], v1) and np.array_equal(g[w], g1), obj
