@@ -417,11 +417,15 @@ def run_batched(args, plain_fp64=None):
     def timed(prec):
         b = make(rods, prec)
         t0 = time.perf_counter()
+        shape = None
         if args.batch_shape:
             t, sn, bps = (int(x) for x in args.batch_shape.split(","))
-            b.setConfig(t, sn, bps, b.config()["chunk_steps"])
-            shape = b.config()
-        else:
+            try:
+                b.setConfig(t, sn, bps, b.config()["chunk_steps"])
+                shape = b.config()
+            except ValueError:          # not a valid shape for this form: tune instead
+                shape = None
+        if shape is None:
             shape = b.tune(64)
         tune_s = time.perf_counter() - t0
         clocks = Clocks(0)
