@@ -446,6 +446,43 @@ nf_status nf_batch_adjoint_backward_many(nf_batch *b, const int32_t *objectives,
 /* Device (or, for the CPU restatement, wall) time of the last forward and backward passes. */
 nf_status nf_batch_adjoint_elapsed(nf_batch *b, double *forward_ms, double *backward_ms);
 
+/* ------------------------------------------------------------------ film (frame capture) */
+
+/* Film.capture (render/Film.java:148-224) on the device: each capture enqueues, on the
+ * solver's stream and without waiting, a frame into device memory -- the deformed node
+ * positions r + ur, z + uz, the chosen element fields, the live flag of every element
+ * (!isEroded), the solver's scalars and the audit partial sums -- and the frames are copied
+ * back only when read. Positions and fields are kept in FP64, as the reference's frames hold
+ * them. A film belongs to one solver; destroy it before the solver. */
+typedef struct nf_film nf_film;
+enum {
+    NF_FILM_PLASTIC_STRAIN = 0,      /* elementPlasticStrain (ExplicitSolver.java:1897-1901) */
+    NF_FILM_DAMAGE,                  /* elementDamage (:1764-1772) */
+    NF_FILM_VON_MISES_MPA,           /* Mises of centroidStress (:1886-1894), MPa */
+    NF_FILM_HOOP_STRESS_MPA,         /* centroidStress[2], MPa */
+    NF_FILM_SPEED,                   /* elementSpeed (:895-902), m/s */
+    NF_FILM_FIELD_KINDS
+};
+typedef struct {
+    double time;                     /* s */
+    int64_t steps;
+    int32_t eroded;                  /* elements gone */
+    int32_t contact_pairs;
+    double pressure;                 /* the applied bore pressure (pressureAt), Pa */
+} nf_film_info;
+/* fields[field_count] (NF_FILM_*; up to 8); capacity: frames it can hold. */
+nf_status nf_film_create(nf_solver *h, const int32_t *fields, int32_t field_count,
+                         int32_t capacity, nf_film **out);
+nf_status nf_film_destroy(nf_film *f);
+nf_status nf_film_capture(nf_film *f);
+nf_status nf_film_frames(nf_film *f, int32_t *count);
+/* All frames, frame-major; any pointer may be NULL: r, z [count * nodes], values [count *
+ * field_count * elements], live [count * elements], info, audits [count]. */
+nf_status nf_film_read(nf_film *f, double *r, double *z, double *values, uint8_t *live,
+                       nf_film_info *info, nf_audit *audits);
+nf_status nf_film_clear(nf_film *f);
+const char *nf_film_last_error(const nf_film *f);
+
 #ifdef __cplusplus
 }
 #endif

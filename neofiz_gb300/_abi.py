@@ -196,9 +196,33 @@ _PROTOS = {
 ENTRY_POINTS = tuple("nf_" + name for name in _PROTOS)
 
 
+class FilmInfo(C.Structure):
+    _fields_ = [("time", C.c_double), ("steps", C.c_int64), ("eroded", C.c_int32),
+                ("contact_pairs", C.c_int32), ("pressure", C.c_double)]
+
+
+(FILM_PLASTIC_STRAIN, FILM_DAMAGE, FILM_VON_MISES_MPA, FILM_HOOP_STRESS_MPA,
+ FILM_SPEED) = range(5)
+
+# The device film (GPU library only: the oracle has no device to capture from).
+_FILM_PROTOS = {
+    "film_create": (_S, [_H, c_int32_p, C.c_int32, C.c_int32, C.POINTER(C.c_void_p)]),
+    "film_destroy": (_S, [_H]),
+    "film_capture": (_S, [_H]),
+    "film_frames": (_S, [_H, c_int32_p]),
+    "film_read": (_S, [_H, c_double_p, c_double_p, c_double_p, C.POINTER(C.c_uint8),
+                       C.POINTER(FilmInfo), C.POINTER(Audit)]),
+    "film_clear": (_S, [_H]),
+    "film_last_error": (C.c_char_p, [_H]),
+}
+
+
 def bind(lib: C.CDLL, prefix: str) -> types.SimpleNamespace:
     ns = types.SimpleNamespace()
-    for name, (res, args) in _PROTOS.items():
+    protos = dict(_PROTOS)
+    if prefix == "nf_":
+        protos.update(_FILM_PROTOS)
+    for name, (res, args) in protos.items():
         fn = getattr(lib, prefix + name)
         fn.restype = res
         fn.argtypes = args

@@ -1289,4 +1289,10 @@ void setup_node_slots(const int32_t *conn, int N, int E, const int32_t *pedges, 
 double setup_min_edge(const double *r, const double *z, const int32_t *conn, int E) {
     return min_edge_length(r, z, conn, E);
 }
+// Helpers shared with the device film (k_film.cu).
+void solver_state_to_double(Solver &S) { mixed_to_double(S); }
+nf_status solver_fail(Solver &S, nf_status st, const char *message) {
+    return fail(&S, st, "%s", message);
+}
+nf_status solver_sync(Solver &S) { return sync_check(S); }
 }  // namespace nf

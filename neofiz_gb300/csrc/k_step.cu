@@ -665,17 +665,20 @@ __global__ void __launch_bounds__(BLOCK) k_audit_points(Dev d, double *out) {
     }
 }
 
-void launch_audits(Solver &S, nf_audit *o) {
+size_t audit_partial_doubles(const Dev &d) {
+    return 4 * (size_t)grid_for(d.N, BLOCK) + 12 * (size_t)grid_for(d.E, BLOCK);
+}
+
+void launch_audit_partials(Solver &S, double *buf) {
     Dev &d = S.d;
     const int nb = grid_for(d.N, BLOCK), eb = grid_for(d.E, BLOCK);
-    double *buf = nullptr;
-    cudaMalloc(&buf, sizeof(double) * (4 * (size_t)nb + 12 * (size_t)eb));
     k_audit_nodes<<<nb, BLOCK, 0, S.stream>>>(d, buf);
     k_audit_points<<<eb, BLOCK, 0, S.stream>>>(d, buf + 4 * (size_t)nb);
-    std::vector<double> h(4 * (size_t)nb + 12 * (size_t)eb);
-    cudaMemcpyAsync(h.data(), buf, sizeof(double) * h.size(), cudaMemcpyDeviceToHost, S.stream);
-    cudaStreamSynchronize(S.stream);
-    cudaFree(buf);
+}
+
+void reduce_audit_partials(const Solver &S, const double *h, nf_audit *o) {
+    const Dev &d = S.d;
+    const int nb = grid_for(d.N, BLOCK), eb = grid_for(d.E, BLOCK);
     memset(o, 0, sizeof *o);
     for (int b = 0; b < nb; b++) {
         o->kinetic_energy += h[4 * b + 0];
@@ -687,7 +690,7 @@ void launch_audits(Solver &S, nf_audit *o) {
     double yielded = 0, begun = 0, failed = 0, clamped = 0, tmax = -INFINITY;
     double worstVal = 0.0;
     int worst = -1;
-    const double *p = h.data() + 4 * (size_t)nb;
+    const double *p = h + 4 * (size_t)nb;
     for (int b = 0; b < eb; b++) {
         const double *q = p + 12 * (size_t)b;
         o->strain_energy += q[0];
@@ -709,6 +712,18 @@ void launch_audits(Solver &S, nf_audit *o) {
     o->max_temperature = tmax;
     o->most_damaged_element = d.hasDamage ? worst : -1;
     if (S.integration == NF_FULL || S.hourglass == 0.0) o->hourglass_energy = 0.0;
+}
+
+void launch_audits(Solver &S, nf_audit *o) {
+    const size_t n = audit_partial_doubles(S.d);
+    double *buf = nullptr;
+    cudaMalloc(&buf, sizeof(double) * n);
+    launch_audit_partials(S, buf);
+    std::vector<double> h(n);
+    cudaMemcpyAsync(h.data(), buf, sizeof(double) * n, cudaMemcpyDeviceToHost, S.stream);
+    cudaStreamSynchronize(S.stream);
+    cudaFree(buf);
+    reduce_audit_partials(S, h.data(), o);
 }
 
 // Body measurements (TaylorImpactCase.java:272-288): exact extrema, any order.

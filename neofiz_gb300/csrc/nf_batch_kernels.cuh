@@ -99,10 +99,10 @@ __global__ void __launch_bounds__(T) k_batch_steps(Dev d, BatchDev b, int chunk)
     batch_queue<MIXED, STAGE, T, false>(d, b, chunk);
 }
 
-// The compensated form keeps few values live across its FP32 phases: capped at 85 registers
-// (768 resident threads per SM) it hides more memory latency than with the compiler's choice.
+// The compensated form keeps few values live across its FP32 phases: capped at 64 registers
+// (1024 resident threads per SM) it hides more memory latency than with the compiler's choice.
 template <bool STAGE, int T>
-__global__ void __launch_bounds__(T, 768 / T) k_batch_steps_comp(Dev d, BatchDev b, int chunk) {
+__global__ void __launch_bounds__(T, 1024 / T) k_batch_steps_comp(Dev d, BatchDev b, int chunk) {
     batch_queue<true, STAGE, T, true>(d, b, chunk);
 }
 

@@ -301,6 +301,15 @@ int launch_initial_assembly(Solver &S);
 int launch_step(Solver &S, bool predicated);
 int launch_advance(Solver &S);
 void launch_audits(Solver &S, nf_audit *out);
+// The audits in two halves: per-block partial sums into a device buffer of
+// audit_partial_doubles(d) doubles (enqueued, no wait), and their fixed-order host reduction.
+size_t audit_partial_doubles(const Dev &d);
+void launch_audit_partials(Solver &S, double *buf);
+void reduce_audit_partials(const Solver &S, const double *h, nf_audit *out);
+// api.cu helpers for the device film (k_film.cu).
+void solver_state_to_double(Solver &S);
+nf_status solver_fail(Solver &S, nf_status st, const char *message);
+nf_status solver_sync(Solver &S);
 void launch_measure(Solver &S, nf_measure *out);
 void launch_material_points(const MatDev &m, int count, double *sig, double *back, double *epsP,
                             double *work, const double *strain, double strainDt,

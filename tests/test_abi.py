@@ -41,19 +41,23 @@ def test_library_exports_every_declared_symbol(library):
 
 
 DEVICE_ONLY = {"nf_device_count", "nf_material_point_update_static"}
+# the device film has no CPU counterpart (it captures device memory)
+FILM = {"nf_film_create", "nf_film_destroy", "nf_film_capture", "nf_film_frames",
+        "nf_film_read", "nf_film_clear", "nf_film_last_error"}
 
 
 def test_abi_binding_covers_the_header():
     from neofiz_gb300 import _abi
-    declared = set(declared_symbols()) - DEVICE_ONLY
+    declared = set(declared_symbols()) - DEVICE_ONLY - FILM
     assert declared == set(_abi.ENTRY_POINTS)
+    assert FILM == {"nf_" + name for name in _abi._FILM_PROTOS}
 
 
 def test_oracle_exports_the_same_surface():
     from oracle import oracle
     lib = ctypes.CDLL(oracle.build())
     for name in declared_symbols():
-        if name in DEVICE_ONLY:
+        if name in DEVICE_ONLY or name in FILM:
             continue
         assert hasattr(lib, "nfo_" + name[3:]), name
 
@@ -62,10 +66,11 @@ def test_struct_layouts_match_the_header():
     """Sizes of the ctypes mirrors against a C compile of the header."""
     from neofiz_gb300 import _abi
     src = ("#include <stdio.h>\n#include \"neofiz.h\"\nint main(){printf(\"%zu %zu %zu %zu %zu "
-           "%zu %zu %zu %zu %zu %zu %zu\\n\", sizeof(nf_mesh), sizeof(nf_material), "
+           "%zu %zu %zu %zu %zu %zu %zu %zu\\n\", sizeof(nf_mesh), sizeof(nf_material), "
            "sizeof(nf_state), sizeof(nf_audit), sizeof(nf_wall_info), sizeof(nf_contact_info), "
            "sizeof(nf_measure), sizeof(nf_damage_points), sizeof(nf_batch_mesh), "
-           "sizeof(nf_batch_instance), sizeof(nf_batch_config), sizeof(nf_batch_progress)); "
+           "sizeof(nf_batch_instance), sizeof(nf_batch_config), sizeof(nf_batch_progress), "
+           "sizeof(nf_film_info)); "
            "return 0;}\n")
     import tempfile
     with tempfile.TemporaryDirectory() as d:
@@ -77,7 +82,7 @@ def test_struct_layouts_match_the_header():
     mine = [ctypes.sizeof(t) for t in (_abi.Mesh, _abi.MaterialC, _abi.State, _abi.Audit,
                                         _abi.WallInfo, _abi.ContactInfo, _abi.Measure,
                                         _abi.DamagePoints, _abi.BatchMesh, _abi.BatchInstance,
-                                        _abi.BatchConfig, _abi.BatchProgress)]
+                                        _abi.BatchConfig, _abi.BatchProgress, _abi.FilmInfo)]
     assert sizes == mine
 
 
