@@ -409,6 +409,33 @@ nf_status nf_batch_state(nf_batch *b, nf_batch_progress *out);
 nf_status nf_batch_measure(nf_batch *b, nf_measure *out);
 nf_status nf_batch_wall_stats(nf_batch *b, nf_wall_info *out);
 
+/* ------------------------------------------------------------------ burst measurement */
+
+/* BurstCase.run's measurement (validate/BurstCase.java:446-490) on every instance of a batch:
+ * every sample_every steps the wall capacity (loadCapacity, :533-553), the hoop strain
+ * (hoopStrain, :560-569, about mean_radius[instance]) and the applied pressure are sampled and
+ * the peak kept; an instance stops once its pressure ramp has reached its target and the
+ * capacity has fallen `margin` below the peak (BurstCase.PEAK_MARGIN), or at t_end tested at
+ * sample points only (the reference runs whole samples). Up to trace_capacity samples per
+ * instance are kept (BurstCase.Sample without the energy columns). Set before running; setting
+ * again restarts the measurement. No reference counterpart as a batch (the reference runs one
+ * solver per case). */
+typedef struct {
+    int32_t sample_every;            /* BurstCase.SAMPLE_STEPS */
+    int32_t trace_capacity;
+    double margin;                   /* BurstCase.PEAK_MARGIN */
+} nf_batch_burst;
+typedef struct {
+    double peak_capacity, peak_strain, peak_applied;  /* at the capacity's maximum */
+    double capacity, strain, applied;                 /* the last sample */
+    int32_t samples;
+    int32_t traversed;               /* the peak was passed (Result.traversed) */
+} nf_burst_result;
+nf_status nf_batch_set_burst(nf_batch *b, const nf_batch_burst *config, const double *mean_radius);
+nf_status nf_batch_burst_results(nf_batch *b, nf_burst_result *out);
+/* [instance_count * trace_capacity * 4]: time, hoop strain, capacity, applied per sample. */
+nf_status nf_batch_burst_trace(nf_batch *b, double *trace);
+
 /* ------------------------------------------------------------------ adjoint */
 
 /* No counterpart in the reference. Gradients of a batch's final measurements with respect to

@@ -190,10 +190,25 @@ _PROTOS = {
     "batch_adjoint_forward": (_S, [_H, C.c_int32, C.c_int32]),
     "batch_adjoint_backward": (_S, [_H, C.c_int32, c_double_p, c_double_p]),
     "batch_adjoint_backward_many": (_S, [_H, c_int32_p, C.c_int32, c_double_p, c_double_p]),
+    "batch_set_burst": (_S, [_H, C.c_void_p, c_double_p]),
+    "batch_burst_results": (_S, [_H, C.c_void_p]),
+    "batch_burst_trace": (_S, [_H, c_double_p]),
     "batch_adjoint_elapsed": (_S, [_H, C.POINTER(C.c_double), C.POINTER(C.c_double)]),
 }
 
 ENTRY_POINTS = tuple("nf_" + name for name in _PROTOS)
+
+
+class BatchBurst(C.Structure):
+    _fields_ = [("sample_every", C.c_int32), ("trace_capacity", C.c_int32),
+                ("margin", C.c_double)]
+
+
+class BurstResult(C.Structure):
+    _fields_ = [("peak_capacity", C.c_double), ("peak_strain", C.c_double),
+                ("peak_applied", C.c_double), ("capacity", C.c_double),
+                ("strain", C.c_double), ("applied", C.c_double), ("samples", C.c_int32),
+                ("traversed", C.c_int32)]
 
 
 class FilmInfo(C.Structure):

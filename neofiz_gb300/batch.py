@@ -221,6 +221,34 @@ class BatchSolver:
         self._check(self._api.batch_wall_stats(self._handle, w))
         return list(w)
 
+    # ------------------------------------------------------------------ burst measurement
+
+    def setBurst(self, sampleEvery: int, meanRadius, margin: float = 0.005,
+                 traceCapacity: int = 0) -> None:
+        """BurstCase.run's sampling on every instance (nf_batch_set_burst): capacity, hoop
+        strain (about meanRadius[k]) and applied pressure every sampleEvery steps; an instance
+        stops once past its capacity peak. sampleEvery 0 turns it off."""
+        cfg = _abi.BatchBurst(int(sampleEvery), int(traceCapacity), float(margin))
+        self._burstRadius = np.ascontiguousarray(
+            np.broadcast_to(np.asarray(meanRadius, np.float64), (self.count,)))
+        self._traceCapacity = int(traceCapacity)
+        self._check(self._api.batch_set_burst(self._handle, C.byref(cfg),
+                                              self._burstRadius.ctypes.data_as(_abi.c_double_p)))
+
+    def burstResults(self) -> dict:
+        r = (_abi.BurstResult * self.count)()
+        self._check(self._api.batch_burst_results(self._handle, r))
+        keys = ("peak_capacity", "peak_strain", "peak_applied", "capacity", "strain",
+                "applied", "samples", "traversed")
+        return {k: np.array([getattr(x, k) for x in r]) for k in keys}
+
+    def burstTrace(self) -> np.ndarray:
+        """[count, traceCapacity, 4]: time, hoop strain, capacity, applied per sample."""
+        out = np.zeros((self.count, self._traceCapacity, 4))
+        self._check(self._api.batch_burst_trace(self._handle,
+                                                out.ctypes.data_as(_abi.c_double_p)))
+        return out
+
     # ------------------------------------------------------------------ adjoint
 
     def adjointForward(self, checkpointEvery: int = 200, sampleEvery: int = 0) -> float:

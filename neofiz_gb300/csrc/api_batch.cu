@@ -43,6 +43,7 @@ struct Batch {
     // the adjoint's buffers (nf_batch_adjoint_*)
     AdjDev adj{};
     std::vector<void *> adjAllocs;
+    std::vector<void *> burstAllocs;         // nf_batch_set_burst's buffers
     bool adjForward = false;
     double adjForwardMs = 0.0, adjBackwardMs = 0.0;
     long long adjTapeBytes = 0, adjBarBytes = 0, adjSeedBytes = 0;
@@ -103,6 +104,7 @@ void destroy(Batch *B) {
     if (B->stream) cudaStreamSynchronize(B->stream);
     if (B->graph) cudaGraphExecDestroy(B->graph);
     free_adjoint(*B);
+    for (void *p : B->burstAllocs) cudaFree(p);
     for (void *p : B->allocs) cudaFree(p);
     if (B->hostRemaining) cudaFreeHost(B->hostRemaining);
     if (B->ev0) cudaEventDestroy(B->ev0);
@@ -161,6 +163,10 @@ std::vector<Span> mutable_state(const Batch &B) {
     const size_t N = B.N, E = B.E;
     std::vector<Span> v = {{d.U, 16 * N}, {d.V, 16 * N}, {d.F, 16 * N}, {d.flags, N},
                            {d.wallState, N}, {B.b.sc, sizeof(BatchScalars) * B.count}};
+    if (B.b.burst.every > 0) {
+        v.push_back({B.b.burst.state, sizeof(BurstState) * B.count});
+        v.push_back({B.b.burst.trace, 32 * (size_t)B.count * B.b.burst.traceCap});
+    }
     if (B.comp) {
         v.push_back({d.uC, 16 * N});
         v.push_back({d.vC, 8 * N});
@@ -735,6 +741,11 @@ nf_status nf_batch_state(nf_batch *h, nf_batch_progress *out) {
     std::vector<BatchScalars> sc(B.count);
     BCK(&B, cudaMemcpyAsync(sc.data(), B.b.sc, sizeof(BatchScalars) * B.count,
                             cudaMemcpyDeviceToHost, B.stream));
+    const BurstDev &bd = B.b.burst;
+    std::vector<BurstState> burst(bd.every > 0 ? B.count : 0);
+    if (bd.every > 0)
+        BCK(&B, cudaMemcpyAsync(burst.data(), bd.state, sizeof(BurstState) * B.count,
+                                cudaMemcpyDeviceToHost, B.stream));
     nf_status st = bsync(B);
     if (st) return st;
     for (int k = 0; k < B.count; k++) {
@@ -742,7 +753,10 @@ nf_status nf_batch_state(nf_batch *h, nf_batch_progress *out) {
         out[k].timestep = sc[k].dt;
         out[k].steps = sc[k].steps;
         out[k].status = sc[k].status;
-        out[k].done = !(sc[k].time < B.inst[k].tEnd);
+        out[k].done = bd.every > 0 ? (burst[k].traversed ||
+                                      (sc[k].steps % bd.every == 0 &&
+                                       !(sc[k].time < B.inst[k].tEnd)))
+                                   : !(sc[k].time < B.inst[k].tEnd);
     }
     return NF_OK;
 }
@@ -792,6 +806,92 @@ nf_status nf_batch_wall_stats(nf_batch *h, nf_wall_info *out) {
         o.stuck_count = sc[k].wStuck;
     }
     return NF_OK;
+}
+
+}  // extern "C"
+
+// ------------------------------------------------------------------------------------ burst
+
+extern "C" {
+
+nf_status nf_batch_set_burst(nf_batch *h, const nf_batch_burst *config,
+                             const double *mean_radius) {
+    Batch &B = *reinterpret_cast<Batch *>(h);
+    if (!config || config->sample_every < 0 || config->trace_capacity < 0 ||
+        !(config->margin >= 0.0 && config->margin < 1.0))
+        return bfail(&B, NF_EINVAL, "burst sampling needs sample_every >= 0, trace_capacity >= 0 "
+                                    "and a margin in [0, 1)");
+    if (config->sample_every > 0 && !mean_radius)
+        return bfail(&B, NF_EINVAL, "burst sampling needs each instance's mean radius");
+    BurstDev &bd = B.b.burst;
+    for (void *p : B.burstAllocs) cudaFree(p);
+    B.burstAllocs.clear();
+    bd = BurstDev{};
+    if (B.graph) {                           // the captured launches hold the old BatchDev
+        cudaGraphExecDestroy(B.graph);
+        B.graph = nullptr;
+    }
+    if (config->sample_every == 0) return NF_OK;
+    cudaError_t e = cudaSuccess;
+    auto A = [&](void **p, size_t bytes) {
+        if (e != cudaSuccess) return;
+        e = cudaMalloc(p, bytes ? bytes : 1);
+        if (e == cudaSuccess) {
+            B.burstAllocs.push_back(*p);
+            e = cudaMemsetAsync(*p, 0, bytes ? bytes : 1, B.stream);
+        }
+    };
+    double *radius = nullptr;
+    A((void **)&radius, 8 * (size_t)B.count);
+    A((void **)&bd.state, sizeof(BurstState) * (size_t)B.count);
+    A((void **)&bd.trace, 32 * (size_t)B.count * config->trace_capacity);
+    A((void **)&bd.scratch, 8 * (size_t)B.E);
+    if (e == cudaSuccess)
+        e = cudaMemcpyAsync(radius, mean_radius, 8 * (size_t)B.count, cudaMemcpyHostToDevice,
+                            B.stream);
+    if (e != cudaSuccess) {
+        for (void *p : B.burstAllocs) cudaFree(p);
+        B.burstAllocs.clear();
+        bd = BurstDev{};
+        return bfail(&B, NF_ENOMEM, "burst allocation failed: %s", cudaGetErrorString(e));
+    }
+    bd.meanRadius = radius;
+    bd.every = config->sample_every;
+    bd.traceCap = config->trace_capacity;
+    bd.margin = config->margin;
+    return bsync(B);
+}
+
+nf_status nf_batch_burst_results(nf_batch *h, nf_burst_result *out) {
+    Batch &B = *reinterpret_cast<Batch *>(h);
+    const BurstDev &bd = B.b.burst;
+    if (bd.every == 0) return bfail(&B, NF_ESTATE, "burst sampling is not set");
+    std::vector<BurstState> st(B.count);
+    BCK(&B, cudaMemcpyAsync(st.data(), bd.state, sizeof(BurstState) * B.count,
+                            cudaMemcpyDeviceToHost, B.stream));
+    nf_status s = bsync(B);
+    if (s) return s;
+    for (int k = 0; k < B.count; k++) {
+        nf_burst_result &o = out[k];
+        o.peak_capacity = st[k].peakCapacity;
+        o.peak_strain = st[k].peakStrain;
+        o.peak_applied = st[k].peakApplied;
+        o.capacity = st[k].capacity;
+        o.strain = st[k].strain;
+        o.applied = st[k].applied;
+        o.samples = st[k].samples;
+        o.traversed = st[k].traversed;
+    }
+    return NF_OK;
+}
+
+nf_status nf_batch_burst_trace(nf_batch *h, double *trace) {
+    Batch &B = *reinterpret_cast<Batch *>(h);
+    const BurstDev &bd = B.b.burst;
+    if (bd.every == 0) return bfail(&B, NF_ESTATE, "burst sampling is not set");
+    BCK(&B, cudaMemcpyAsync(trace, bd.trace, 32 * (size_t)B.count * bd.traceCap,
+                            cudaMemcpyDeviceToHost, B.stream));
+    return bsync(B);
 }
 
 }  // extern "C"

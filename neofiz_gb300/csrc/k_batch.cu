@@ -60,7 +60,11 @@ __global__ void k_batch_arm(BatchDev b, long long maxSteps) {
     if (k >= b.count) return;
     BatchScalars &s = b.sc[k];
     s.stepLimit = s.steps + maxSteps;
-    const bool done = !(s.time < b.inst[k].tEnd) || maxSteps <= 0;
+    const int every = b.burst.every;
+    const bool ended = every > 0 ? (s.steps % every == 0 && !(s.time < b.inst[k].tEnd)) ||
+                                       b.burst.state[k].traversed
+                                 : !(s.time < b.inst[k].tEnd);
+    const bool done = ended || maxSteps <= 0;
     s.done = done ? 1 : 0;
     if (!done) atomicAdd(b.remaining, 1);
 }

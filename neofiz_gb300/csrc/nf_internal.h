@@ -224,6 +224,24 @@ struct BatchScalars {
     int done;                                // time >= tEnd or the step limit reached
 };
 
+// BurstCase.run's measurement (BurstCase.java:446-490) on the device: every `every` steps each
+// instance samples its wall capacity, hoop strain and applied pressure, keeps the running
+// peak, and stops once the ramp has reached its ceiling and the capacity has fallen `margin`
+// below the peak. every == 0: off.
+struct BurstState {
+    double peakCapacity, peakStrain, peakApplied;
+    double capacity, strain, applied;        // the last sample
+    int samples, traversed;
+};
+struct BurstDev {
+    int every, traceCap;
+    double margin;
+    const double *meanRadius;                // [count] for the hoop strain
+    BurstState *state;                       // [count]
+    double *trace;                           // [count * traceCap * 4]: t, strain, capacity, applied
+    double *scratch;                         // [E]: each element's hoop stress x area
+};
+
 struct BatchDev {
     const BatchInst *inst;
     BatchScalars *sc;
@@ -233,6 +251,7 @@ struct BatchDev {
     unsigned long long *measure;             // [3 per instance] order-preserving extrema
     int count;
     int maxNodes;                            // the largest instance's node count
+    BurstDev burst;
 };
 
 // The adjoint's device buffers (k_adjoint.cu): per instance a run of checkpoint blocks, one

@@ -342,3 +342,75 @@ def fraction_gradients(grads, rod):
     out[..., 6] = dH * secant
     out[..., 7:] = g[..., 7:]
     return out
+
+
+# ---------------------------------------------------------------------------- burst (BurstCase)
+
+BIAXIAL = 2.0 / math.sqrt(3.0)                      # validate/Burst.java
+BIAXIAL_SOFTENING = math.sqrt(3.0)
+BURST_SAMPLE_STEPS = 250                            # BurstCase.java:131-132
+BURST_PEAK_MARGIN = 0.005
+BURST_RAMP_PERIODS = 20.0
+BURST_MAX_PERIODS = 300.0
+BURST_DAMPING = 0.5
+BURST_OVERSHOOT = 1.06
+BURST_THROUGH_WALL = 8
+BURST_ALONG_AXIS = 2
+BURST_CFL = 0.5
+
+
+def _instability_strain(law, softening):
+    """Burst.instabilityStrain (Burst.java:100-113): dsigma/deps = softening sigma, bisected."""
+    def residual(eps):
+        slope = math.inf if eps <= 0.0 else law.b * law.n * math.pow(eps, law.n - 1.0)
+        term = law.a if eps <= 0.0 else law.a + law.b * math.pow(eps, law.n)
+        return slope - softening * term
+    hi = 1.0
+    lo = hi
+    while residual(lo) <= 0.0:
+        lo *= 0.5
+        if lo < 1e-15:
+            return 0.0
+    for _ in range(200):
+        mid = 0.5 * (lo + hi)
+        if residual(mid) > 0.0:
+            lo = mid
+        else:
+            hi = mid
+    return 0.5 * (lo + hi)
+
+
+def burst_pressure(law, thickness, mean_radius):
+    """Burst.burstPressure (Burst.java:168-182): the thin-wall instability pressure."""
+    hoop = _instability_strain(law, BIAXIAL_SOFTENING) / BIAXIAL
+    eq = BIAXIAL * hoop
+    term = law.a if eq <= 0.0 else law.a + law.b * math.pow(eq, law.n)
+    return BIAXIAL * term * (thickness / mean_radius) * math.exp(-2.0 * hoop)
+
+
+def burst_material() -> Material:
+    """BurstCase.COPPER: OFHC copper on its quasi-static flow curve."""
+    return Material.COPPER_OFHC.withJohnsonCook(JohnsonCook.COPPER_OFHC.quasiStatic())
+
+
+def burst_instance(mean_radius=25.0e-3, slenderness=25.0, through_wall=BURST_THROUGH_WALL,
+                   overshoot=BURST_OVERSHOOT, material=None):
+    """BurstCase.run's tube (BurstCase.java:400-444) as a batch instance: a two-element slice
+    of the wall, every node held axially, a smoothstep ramp to overshoot x the closed-form
+    burst pressure over 20 ring periods, relaxation damping at the ring frequency, run to 300
+    periods (the deadline)."""
+    from .batch import Instance
+    material = material if material is not None else burst_material()
+    law = material.johnsonCook
+    thickness = 2.0 * mean_radius / slenderness
+    inner, outer = mean_radius - 0.5 * thickness, mean_radius + 0.5 * thickness
+    h = thickness / through_wall
+    mesh = QuadMesh.cylinderWall(inner, outer, h * BURST_ALONG_AXIS, through_wall,
+                                 BURST_ALONG_AXIS)
+    ceiling = overshoot * burst_pressure(law, thickness, mean_radius)
+    omega = material.barWaveSpeed() / mean_radius
+    period = 2.0 * math.pi / omega
+    return Instance(mesh=mesh, material=material, t_end=BURST_MAX_PERIODS * period,
+                    fixed_axial=np.arange(mesh.nodeCount), pressure=(ceiling,
+                                                                    BURST_RAMP_PERIODS * period),
+                    damping=(BURST_DAMPING, omega))

@@ -2052,6 +2052,11 @@ struct nfo_batch {
     /* the adjoint's checkpoints, per instance */
     struct adj_ctx_s *adj;
     double adjForwardMs, adjBackwardMs;
+    /* burst measurement (nfo_batch_set_burst) */
+    nf_batch_burst burst;
+    double *meanRadius;
+    nf_burst_result *burstRes;
+    double *burstTrace;
 };
 typedef struct nfo_batch nfo_batch;
 
@@ -2074,6 +2079,7 @@ API nf_status nfo_batch_destroy(nfo_batch *b) {
     adj_free_all(b);
     for (int k = 0; k < b->count; k++) nfo_destroy(b->s[k]);
     free(b->s); free(b->tEnd); free(b->nodeOff); free(b->elemOff);
+    free(b->meanRadius); free(b->burstRes); free(b->burstTrace);
     pthread_mutex_destroy(&b->lock);
     free(b);
     return NF_OK;
@@ -2155,6 +2161,8 @@ API nf_status nfo_batch_get_config(nfo_batch *b, nf_batch_config *c) {
     return NF_OK;
 }
 
+static void burst_run_instance(nfo_batch *b, int k);
+
 static void *batch_worker(void *arg) {
     nfo_batch *b = (nfo_batch *)arg;
     for (;;) {
@@ -2162,7 +2170,8 @@ static void *batch_worker(void *arg) {
         const int k = b->next++;
         pthread_mutex_unlock(&b->lock);
         if (k >= b->count) return NULL;
-        nfo_run_until(b->s[k], b->tEnd[k], b->maxSteps, NULL);
+        if (b->burst.sample_every > 0) burst_run_instance(b, k);
+        else nfo_run_until(b->s[k], b->tEnd[k], b->maxSteps, NULL);
     }
 }
 
@@ -2222,7 +2231,10 @@ API nf_status nfo_batch_state(nfo_batch *b, nf_batch_progress *out) {
         out[k].timestep = s.timestep;
         out[k].steps = s.steps;
         out[k].status = 0;
-        out[k].done = !(s.time < b->tEnd[k]);
+        const int every = b->burst.sample_every;
+        out[k].done = every > 0 ? (b->burstRes[k].traversed ||
+                                   (s.steps % every == 0 && !(s.time < b->tEnd[k])))
+                                : !(s.time < b->tEnd[k]);
     }
     return NF_OK;
 }
@@ -2715,5 +2727,88 @@ API nf_status nfo_batch_adjoint_backward_many(nfo_batch *b, const int32_t *objec
 API nf_status nfo_batch_adjoint_elapsed(nfo_batch *b, double *forward_ms, double *backward_ms) {
     *forward_ms = b->adjForwardMs;
     *backward_ms = b->adjBackwardMs;
+    return NF_OK;
+}
+
+/* ---------------------------------------------------------------- burst measurement */
+
+/* BurstCase.run's sampling (validate/BurstCase.java:446-490) for instance k after its step
+ * count reached a multiple of sample_every: loadCapacity (:533-553), hoopStrain (:560-569),
+ * borePressure, the running peak and the turnover test. */
+static void burst_sample(nfo_batch *b, int k) {
+    nfo_solver *h = b->s[k];
+    int ib, il, ih;
+    const double capacity = adj_capacity(h, h->ur, h->uz, h->sig, &ib, &il, &ih);
+    double bore = DBL_MAX, rim = -DBL_MAX;
+    for (int i = 0; i < h->N; i++) {
+        const double r = h->r[i] + h->ur[i];
+        if (r < bore) bore = r;
+        if (r > rim) rim = r;
+    }
+    const double strain = nf_log(0.5 * (bore + rim) / b->meanRadius[k]);
+    const double applied = pressureAt(h, h->time);
+    nf_burst_result *st = &b->burstRes[k];
+    if (b->burst.trace_capacity > 0 && st->samples < b->burst.trace_capacity) {
+        double *t = b->burstTrace + 4 * ((size_t)k * b->burst.trace_capacity + st->samples);
+        t[0] = h->time; t[1] = strain; t[2] = capacity; t[3] = applied;
+    }
+    st->samples += 1;
+    st->capacity = capacity;
+    st->strain = strain;
+    st->applied = applied;
+    if (capacity > st->peak_capacity) {
+        st->peak_capacity = capacity;
+        st->peak_strain = strain;
+        st->peak_applied = applied;
+    } else if (applied >= h->targetPressure && capacity < st->peak_capacity * (1.0 - b->burst.margin)) {
+        st->traversed = 1;
+    }
+}
+
+/* Whole samples of steps until the peak is traversed, the deadline is passed at a sample
+ * point, or the run's step bound is reached. */
+static void burst_run_instance(nfo_batch *b, int k) {
+    nfo_solver *h = b->s[k];
+    const int every = b->burst.sample_every;
+    int64_t taken = 0;
+    for (;;) {
+        if (b->burstRes[k].traversed || taken >= b->maxSteps) break;
+        if (h->stepCount % every == 0 && !(h->time < b->tEnd[k])) break;
+        step(h);
+        taken++;
+        if (h->stepCount % every == 0) burst_sample(b, k);
+    }
+}
+
+API nf_status nfo_batch_set_burst(nfo_batch *b, const nf_batch_burst *config,
+                                  const double *mean_radius) {
+    if (!config || config->sample_every < 0 || config->trace_capacity < 0 ||
+        !(config->margin >= 0.0 && config->margin < 1.0))
+        return bfail(b, NF_EINVAL, "burst sampling needs sample_every >= 0, trace_capacity >= 0 "
+                                   "and a margin in [0, 1)");
+    if (config->sample_every > 0 && !mean_radius)
+        return bfail(b, NF_EINVAL, "burst sampling needs each instance's mean radius");
+    free(b->meanRadius); free(b->burstRes); free(b->burstTrace);
+    b->meanRadius = NULL; b->burstRes = NULL; b->burstTrace = NULL;
+    b->burst = *config;
+    if (config->sample_every == 0) return NF_OK;
+    b->meanRadius = (double *)malloc(sizeof(double) * (size_t)b->count);
+    memcpy(b->meanRadius, mean_radius, sizeof(double) * (size_t)b->count);
+    b->burstRes = (nf_burst_result *)calloc((size_t)b->count, sizeof(nf_burst_result));
+    b->burstTrace = (double *)calloc(4 * (size_t)b->count * (size_t)config->trace_capacity + 1,
+                                     sizeof(double));
+    return NF_OK;
+}
+
+API nf_status nfo_batch_burst_results(nfo_batch *b, nf_burst_result *out) {
+    if (b->burst.sample_every == 0) return bfail(b, NF_ESTATE, "burst sampling is not set");
+    memcpy(out, b->burstRes, sizeof(nf_burst_result) * (size_t)b->count);
+    return NF_OK;
+}
+
+API nf_status nfo_batch_burst_trace(nfo_batch *b, double *trace) {
+    if (b->burst.sample_every == 0) return bfail(b, NF_ESTATE, "burst sampling is not set");
+    memcpy(trace, b->burstTrace,
+           sizeof(double) * 4 * (size_t)b->count * (size_t)b->burst.trace_capacity);
     return NF_OK;
 }
