@@ -50,7 +50,9 @@ def parse():
     p.add_argument("--batch-count", type=int, default=4096)
     p.add_argument("--no-adjoint", action="store_true")
     p.add_argument("--adjoint-count", type=int, default=64)
-    p.add_argument("--only", choices=["batched", "adjoint"],
+    p.add_argument("--no-burst", action="store_true")
+    p.add_argument("--burst-count", type=int, default=1024)
+    p.add_argument("--only", choices=["batched", "adjoint", "burst"],
                    help="run one form alone and print its JSON (profiling of small cases)")
     p.add_argument("--t-end", type=float, default=None,
                    help="with --only: the rods' run length instead of 80 us")
@@ -240,6 +242,10 @@ def run_ours(args, world, rank, local):
     if not args.no_adjoint:
         adjoint = run_adjoint(args)
 
+    burst = None
+    if not args.no_burst:
+        burst = run_burst(args)
+
     if rank == 0:
         line = {
             "metric": "element-cycles/s, plain FP64 explicit timestep (live elements x steps / s)",
@@ -278,6 +284,7 @@ def run_ours(args, world, rank, local):
             "mixed": mixed,
             "batched": batched,
             "adjoint": adjoint,
+            "burst": burst,
             "clocks": clk,
             "gpu_launches": launches,
             "status_word": status,
@@ -604,6 +611,58 @@ def run_adjoint(args):
     }
 
 
+def run_burst(args):
+    """A burst sweep (BurstCase.run over a BarlowSweep-like grid): args.burst_count
+    two-element wall slices, slenderness 15..60 and mean radius 10..40 mm drawn by SplitMix64,
+    OFHC copper, ramp to 1.06 x the closed-form burst pressure, each run on the device until
+    its capacity has turned over (BurstCase's sampling every 250 steps). FP64 (bit-identical to
+    the reference's per-case runs) and compensated; the CPU leg is the oracle on four tubes."""
+    import numpy as np
+    from neofiz_gb300 import _abi, scenes
+    from neofiz_gb300.batch import BatchSolver
+    from oracle.oracle import OracleBatch
+    rng = scenes.SplitMix64(20250703)
+    pars = [(rng.uniform(15.0, 60.0), rng.uniform(10.0e-3, 40.0e-3))
+            for _ in range(args.burst_count)]
+    tubes = [scenes.burst_instance(mean_radius=r, slenderness=sl) for sl, r in pars]
+    radius = np.array([r for _, r in pars])
+    out = {}
+    for name, prec in (("fp64", _abi.PRECISION_FP64),
+                       ("compensated", _abi.PRECISION_COMPENSATED)):
+        b = BatchSolver(tubes, scenes.Formulation.AXISYMMETRIC, cfl=scenes.BURST_CFL,
+                        precision=prec)
+        b.setBurst(scenes.BURST_SAMPLE_STEPS, radius, scenes.BURST_PEAK_MARGIN)
+        shape = b.tune(64)
+        b.setBurst(scenes.BURST_SAMPLE_STEPS, radius, scenes.BURST_PEAK_MARGIN)
+        ms = b.run()
+        res = b.burstResults()
+        cycles = b.elementCycles()
+        exact = np.array([t.pressure[0] for t in tubes]) / scenes.BURST_OVERSHOOT
+        dev = 100.0 * (res["peak_capacity"] / exact - 1.0)
+        out[name] = {"value": cycles / (ms * 1e-3), "unit": "element-cycles/s", "ms": ms,
+                     "element_cycles": cycles, "shape": shape,
+                     "traversed": int(res["traversed"].sum()), "tubes": len(tubes),
+                     "steps_mean": float(b.state()["steps"].mean()),
+                     "peak_vs_closed_form_pct": {"median": float(np.median(dev)),
+                                                 "min": float(dev.min()), "max": float(dev.max())},
+                     "peaks": res["peak_capacity"]}
+        b.close()
+    rel = np.abs(out["compensated"].pop("peaks") / out["fp64"]["peaks"] - 1.0)
+    out["fp64"].pop("peaks")
+    out["compensated"]["peak_capacity_vs_fp64"] = {"max": float(rel.max()),
+                                                   "median": float(np.median(rel))}
+    o = OracleBatch(tubes[:4], scenes.Formulation.AXISYMMETRIC, cfl=scenes.BURST_CFL)
+    o.setBurst(scenes.BURST_SAMPLE_STEPS, radius[:4], scenes.BURST_PEAK_MARGIN)
+    o.run()
+    ocyc = o.elementCycles()
+    out["cpu_oracle"] = {"value": ocyc / (o.elapsed() * 1e-3), "unit": "element-cycles/s",
+                         "tubes": 4, "kind": "port", "threads": "one per tube"}
+    out["workload"] = (f"{len(tubes)} burst slices (8 x 2 quads), slenderness 15..60, mean radius "
+                       "10..40 mm, OFHC copper, ramp to 1.06 x burst over 20 ring periods, "
+                       "sampled every 250 steps until the capacity turns over")
+    return out
+
+
 def run_tube_adjoint(args):
     """The tube of the gradient batch: QuadMesh.cylinderWall(19.6, 20.4, 40 mm, 4, 200) in
     OFHC copper (quasi-static Johnson-Cook law), smoothstep ramp to 60 MPa over 20 us,
@@ -710,7 +769,7 @@ def main():
     if args.only:
         from neofiz_gb300 import build as nb
         nb.build()
-        out = run_batched(args) if args.only == "batched" else run_adjoint(args)
+        out = {"batched": run_batched, "adjoint": run_adjoint, "burst": run_burst}[args.only](args)
         print(json.dumps(out))
         return
     if args.impl == "reference":

@@ -367,7 +367,7 @@ typedef struct {
 
 /* A launch shape of the batched step; any valid shape gives the same trajectories. */
 typedef struct {
-    int32_t threads;                 /* threads per block: 128 or 256 */
+    int32_t threads;                 /* threads per block: 32, 128 or 256 */
     int32_t stage_nodes;             /* mixed form: node geometry staged in shared memory */
     int32_t blocks_per_sm;           /* resident blocks per SM (1 .. occupancy limit) */
     int32_t chunk_steps;             /* steps an instance takes per launch */

@@ -114,7 +114,7 @@ void destroy(Batch *B) {
 }
 
 bool shape_valid(const Batch &B, const BatchShape &s) {
-    if (s.threads != 128 && s.threads != 256) return false;
+    if (s.threads != 32 && s.threads != 128 && s.threads != 256) return false;
     if (s.stage && !B.mixed) return false;
     if (s.chunk < 1 || s.blocksPerSm < 1) return false;
     return batch_max_blocks_per_sm(B.mode, s, B.b.maxNodes) >= s.blocksPerSm;
@@ -598,16 +598,20 @@ nf_status nf_batch_tune(nf_batch *h, int32_t trial_steps, nf_batch_config *chose
     };
     copy(true);
     std::vector<BatchShape> cands;
-    for (int threads : {128, 256})
+    // one-warp blocks serve small instances (a burst slice has 16 elements): more of them
+    // resident per SM instead of mostly idle 128-thread blocks
+    for (int threads : {32, 128, 256})
         for (int stage = 0; stage <= (B.mixed ? 1 : 0); stage++) {
             BatchShape s{threads, stage, 1, trial_steps};
             const int occ = batch_max_blocks_per_sm(B.mode, s, B.b.maxNodes);
-            for (int bps : {1, 2, 4, 8, 16}) {
+            bool atOcc = false;
+            for (int bps : {1, 2, 4, 8, 16, 32}) {
                 if (bps > occ) break;
                 s.blocksPerSm = bps;
                 cands.push_back(s);
+                atOcc = bps == occ;
             }
-            if (occ > 0 && occ != 1 && occ != 2 && occ != 4 && occ != 8 && occ < 16) {
+            if (occ > 0 && !atOcc) {
                 s.blocksPerSm = occ;
                 cands.push_back(s);
             }

@@ -118,13 +118,17 @@ static const void *steps_kernel() {
     return (const void *)k_batch_steps<MIXED, STAGE, T>;
 }
 
+template <bool MIXED, bool STAGE, bool COMP>
+static const void *by_threads(int threads) {
+    if (threads == 32) return steps_kernel<MIXED, STAGE, 32, COMP>();
+    return threads == 128 ? steps_kernel<MIXED, STAGE, 128, COMP>()
+                          : steps_kernel<MIXED, STAGE, 256, COMP>();
+}
+
 template <bool MIXED, bool COMP>
 static const void *by_shape(const BatchShape &s) {
-    if (MIXED && s.stage)
-        return s.threads == 128 ? steps_kernel<MIXED, true, 128, COMP>()
-                                : steps_kernel<MIXED, true, 256, COMP>();
-    return s.threads == 128 ? steps_kernel<MIXED, false, 128, COMP>()
-                            : steps_kernel<MIXED, false, 256, COMP>();
+    if (MIXED && s.stage) return by_threads<MIXED, true, COMP>(s.threads);
+    return by_threads<MIXED, false, COMP>(s.threads);
 }
 
 static const void *select_kernel(int mode, const BatchShape &s) {

@@ -32,9 +32,12 @@ __global__ void k_batch_comp_sync(Dev d) {
 }
 
 const void *comp_steps_kernel(const BatchShape &s) {
-    if (s.stage)
+    if (s.stage) {
+        if (s.threads == 32) return (const void *)k_batch_steps_comp<true, 32>;
         return s.threads == 128 ? (const void *)k_batch_steps_comp<true, 128>
                                 : (const void *)k_batch_steps_comp<true, 256>;
+    }
+    if (s.threads == 32) return (const void *)k_batch_steps_comp<false, 32>;
     return s.threads == 128 ? (const void *)k_batch_steps_comp<false, 128>
                             : (const void *)k_batch_steps_comp<false, 256>;
 }
