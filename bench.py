@@ -30,6 +30,9 @@ sys.path.insert(0, HERE)
 CELL = 0.114e-3
 GAP = 0.5e-3
 L2_FLUSH_BYTES = 256 << 20
+# DRAM bytes (read + write) of one k_element_reduced launch of this workload after 300 steps,
+# from ncu (profiles/launches_perforation_200k_fp64.md; ncu cannot run inside the timed bench)
+ELEMENT_TRAFFIC_BYTES = {CELL: 39_627_008 + 108_032}
 
 
 def parse():
@@ -275,7 +278,8 @@ def run_ours(args, world, rank, local):
                 "frac": (achieved / peaks["hbm_gbs"]) if achieved else None,
                 "peak_source": peak_kind,
                 "bytes_per_launch": elem_bytes, "launch_ms": elem_ms,
-                "traffic": None,
+                "traffic": ELEMENT_TRAFFIC_BYTES.get(args.cell),
+                "traffic_source": "ncu dram__bytes_read.sum + dram__bytes_write.sum, one launch",
                 "note": "FP64 arithmetic, not HBM, bounds this kernel on GB300",
                 "group_ms_per_step": per_step, "top_group": top,
             },
