@@ -86,6 +86,17 @@ def barrier(world):
         dist.barrier()
 
 
+def sum_over_ranks(x, world):
+    if world == 1:
+        return x
+    import torch
+    import torch.distributed as dist
+    dev = "cuda" if dist.get_backend() == "nccl" else "cpu"
+    t = torch.tensor([x], dtype=torch.float64, device=dev)
+    dist.all_reduce(t, op=dist.ReduceOp.SUM)
+    return float(t.item())
+
+
 def max_over_ranks(x, world):
     if world == 1:
         return x
@@ -420,6 +431,14 @@ def run_batched(args, plain_fp64=None):
         for r in rods:
             r["t_end"] = args.t_end
     L0 = 25.0e-3
+    # one process per GPU: each rank steps its share of the rods (no collective in the data
+    # path); element-steps are summed and the time is the slowest rank's
+    world = int(os.environ.get("WORLD_SIZE", "1"))
+    rank = int(os.environ.get("RANK", "0"))
+    if world > 1:
+        from neofiz_gb300.shard import shard
+        mine = shard(scenes.sweep_instances(rods), world, rank, 0.6)
+        rods = [rods[i] for i in mine]
 
     def make(sel, prec):
         return BatchSolver(scenes.sweep_instances(sel), scenes.Formulation.AXISYMMETRIC,
@@ -442,9 +461,11 @@ def run_batched(args, plain_fp64=None):
         clocks = Clocks(0)
         clocks.start()
         launches0 = b.launchCount()
-        ms = b.run()
+        barrier(world)
+        ms = max_over_ranks(b.run(), world)
         clk = clocks.stop()
-        out = {"ms": ms, "cycles": b.elementCycles(), "state": b.state(),
+        out = {"ms": ms, "cycles": int(sum_over_ranks(float(b.elementCycles()), world)),
+               "state": b.state(),
                "L": np.array([m.length for m in b.measure()]) / L0,
                "launches": b.launchCount() - launches0, "shape": shape, "tune_s": tune_s,
                "clocks": clk}
@@ -496,6 +517,9 @@ def run_batched(args, plain_fp64=None):
         return o
 
     comp = summary(runs["compensated"])
+    if world > 1:
+        comp["ranks"] = world
+        comp["sharding"] = "by instance, cost-balanced (neofiz_gb300.shard); errors on rank 0's share"
     line = {
         "workload": f"{len(rods)} axisymmetric Taylor rods (nr 6..24, nz 30..120, JC +-20 %, "
                     f"mu 0..0.2, 150..250 m/s, SplitMix64 seed {scenes.SWEEP_SEED}) to 80 us, "
