@@ -453,10 +453,13 @@ nf_status nf_batch_burst_trace(nf_batch *b, double *trace);
 enum { NF_OBJECTIVE_LENGTH_RATIO = 0, NF_OBJECTIVE_MUSHROOM = 1, NF_OBJECTIVE_PEAK_CAPACITY = 2 };
 /* Gradient components: Johnson-Cook A, B, n, C, m (JohnsonCook.java:66-69), the kinematic
  * hardening modulus (Material.java:20-21), the wall friction coefficient (RigidWall.atZ,
- * RigidWall.java:121-136) and the fracture energy of every element (setDamage, as a common
- * value: the sum over elements of the per-element derivatives). */
+ * RigidWall.java:121-136), the fracture energy of every element (setDamage, as a common
+ * value: the sum over elements of the per-element derivatives), and the yield stress and
+ * isotropic hardening modulus of a material without a Johnson-Cook law (Material.java:20-21,
+ * J2 flow stress sy0 + H_iso eps_p). */
 enum { NF_PARAM_A = 0, NF_PARAM_B, NF_PARAM_N, NF_PARAM_C, NF_PARAM_M, NF_PARAM_KINEMATIC,
-       NF_PARAM_FRICTION, NF_PARAM_FRACTURE_ENERGY, NF_PARAM_COUNT };
+       NF_PARAM_FRICTION, NF_PARAM_FRACTURE_ENERGY, NF_PARAM_YIELD, NF_PARAM_ISOTROPIC,
+       NF_PARAM_COUNT };
 
 /* sample_every: the capacity sampling interval (0: no capacity objective). */
 nf_status nf_batch_adjoint_forward(nf_batch *b, int32_t checkpoint_every, int32_t sample_every);

@@ -28,9 +28,10 @@ PRECISION_FP64, PRECISION_MIXED, PRECISION_COMPENSATED = 0, 1, 2
 
 OBJECTIVE_LENGTH_RATIO, OBJECTIVE_MUSHROOM, OBJECTIVE_PEAK_CAPACITY = 0, 1, 2
 (PARAM_A, PARAM_B, PARAM_N, PARAM_C, PARAM_M, PARAM_KINEMATIC, PARAM_FRICTION,
- PARAM_FRACTURE_ENERGY) = range(8)
-PARAM_COUNT = 8
-PARAM_NAMES = ("A", "B", "n", "C", "m", "kinematic", "friction", "fracture_energy")
+ PARAM_FRACTURE_ENERGY, PARAM_YIELD, PARAM_ISOTROPIC) = range(10)
+PARAM_COUNT = 10
+PARAM_NAMES = ("A", "B", "n", "C", "m", "kinematic", "friction", "fracture_energy", "yield",
+               "isotropic")
 
 WALL_HELD, WALL_STUCK, WALL_SLID, WALL_ARRIVED = 1, 2, 4, 8
 CONTACT_PAIR, CONTACT_STICK, CONTACT_SLIP = 1, 2, 4

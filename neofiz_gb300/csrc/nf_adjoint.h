@@ -13,7 +13,8 @@
  * map is differentiated through its converged root by the implicit function theorem.
  *
  * Differentiated parameters (NF_ADJ_P_*): Johnson-Cook A, B, n, C, m, the kinematic
- * hardening modulus, the wall friction coefficient and the fracture energy.
+ * hardening modulus, the wall friction coefficient, the fracture energy, and the yield stress
+ * and isotropic hardening modulus of a linear-hardening material.
  *
  * Plain C (C99) with NF_HD qualifiers, so the oracle (gcc) and the kernels (nvcc) compile the
  * same text; both build with contraction off.
@@ -24,7 +25,7 @@
 #include "nf_math.h"
 
 enum { NF_ADJ_P_A = 0, NF_ADJ_P_B, NF_ADJ_P_N, NF_ADJ_P_C, NF_ADJ_P_M, NF_ADJ_P_HKIN,
-       NF_ADJ_P_MU, NF_ADJ_P_GF, NF_ADJ_P_COUNT };
+       NF_ADJ_P_MU, NF_ADJ_P_GF, NF_ADJ_P_SY0, NF_ADJ_P_HISO, NF_ADJ_P_COUNT };
 
 #define NF_ADJ_SQRT_2_3 0x1.a20bd700c2c3ep-1
 #define NF_ADJ_TWO_THIRDS (2.0 / 3.0)
@@ -233,8 +234,10 @@ NF_HD void nf_adj_j2_reverse(const nf_adj_j2_tape *tp, const double *bk, double 
                 pb[NF_ADJ_P_GF] += sb_ * tp->fsOnset * tp->fsOnset * tp->width
                                    / (2.0 * dm->fractureEnergy * dm->fractureEnergy);
             }
-            if (!jc) {
+            if (!jc) {                              /* fs = sy0 + H_iso epsP' */
                 epsP1b += fsb * f->hIso;
+                pb[NF_ADJ_P_SY0] += fsb;
+                pb[NF_ADJ_P_HISO] += fsb * tp->epsP1;
             } else {
                 const double eps = tp->epsP1;
                 const double Th = nf_adj_thermal_term(f, tp->temperature);
@@ -319,8 +322,10 @@ NF_HD void nf_adj_j2_reverse(const nf_adj_j2_tape *tp, const double *bk, double 
                         softIn += fsb * (epsP - dm->failureStrain);
                         epsPbIn += fsb * dm->softening;
                     }
-                } else {
+                } else {                            /* fs = sy0 + H_iso epsP */
                     epsPbIn += fsb * f->hIso;
+                    pb[NF_ADJ_P_SY0] += fsb;
+                    pb[NF_ADJ_P_HISO] += fsb * epsP + hardb;   /* hardening = H_iso */
                 }
             }
         } else {

@@ -178,3 +178,48 @@ def test_several_objectives_in_one_pass_match_single_passes():
         assert np.array_equal(v[w], v1) and np.array_equal(g[w], g1)
     with pytest.raises(ValueError):
         b.adjointBackwardMany([0, 1, 2, 0])
+
+
+def _linear_rod_material(sy0=600.0e6, h_iso=2.0e9, h_kin=3.0e8):
+    """A J2 steel with linear isotropic and kinematic hardening (no Johnson-Cook law)."""
+    from neofiz_gb300.materials import Material
+    return Material("linear steel", 200.0e9, 0.29, 7850.0).yielding(sy0, h_iso, h_kin)
+
+
+def _linear_measure(mat, steps):
+    s, mesh, info = scenes.taylor_rod(OracleSolver, nr=3, nz=12, speed=250.0, friction=0.09,
+                                      material=mat)
+    s.run(steps)
+    m = s.measure()
+    return np.array([m.length / info["length"], m.mushroom_diameter])
+
+
+def test_yield_and_isotropic_hardening_gradients_match_central_differences():
+    """The hardening moduli of a linear-hardening material (no Johnson-Cook law): d/d sy0 and
+    d/d H_iso (and H_kin) against central differences of the plain path."""
+    import dataclasses as dc
+    mat = _linear_rod_material()
+    inst = scenes.sweep_instances([dict(nr=3, nz=12, t_end=8.0e-6, mu=0.09, speed=250.0,
+                                        a=1.0, b=1.0, n=0.5, c=0.0)])[0]
+    inst = dc.replace(inst, material=mat)
+    b = OracleBatch([inst], scenes.Formulation.AXISYMMETRIC, cfl=0.6)
+    b.adjointForward(15)
+    steps = int(b.state()["steps"][0])
+    grads = {obj: b.adjointBackward(obj)[1][0] for obj in (0, 1)}
+    base = {"yield": mat.yieldStress, "isotropic": mat.isotropicHardening,
+            "kinematic": mat.kinematicHardening}
+    for name, k in (("yield", _abi.PARAM_YIELD), ("isotropic", _abi.PARAM_ISOTROPIC),
+                    ("kinematic", _abi.PARAM_KINEMATIC)):
+        dp = H * base[name]
+        def at(v):
+            p = dict(base)
+            p[name] = v
+            return _linear_measure(_linear_rod_material(p["yield"], p["isotropic"],
+                                                        p["kinematic"]), steps)
+        fd = (at(base[name] + dp) - at(base[name] - dp)) / (2.0 * dp)
+        for obj in (0, 1):
+            assert grads[obj][k] == pytest.approx(fd[obj], rel=1e-5), (name, obj)
+    # a Johnson-Cook rod has no yield or isotropic-hardening dependence
+    rod = _rod()
+    _, jc = _gradients(rod, every=20)
+    assert jc[0][1][_abi.PARAM_YIELD] == 0.0 and jc[0][1][_abi.PARAM_ISOTROPIC] == 0.0

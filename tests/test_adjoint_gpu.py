@@ -102,3 +102,24 @@ def test_several_objectives_in_one_pass_are_bit_identical_to_single_passes(gpu_l
     for w, obj in enumerate(objs):
         v1, g1 = t.adjointBackward(obj)
         assert np.array_equal(v[w], v1) and np.array_equal(g[w], g1), obj
+
+
+def test_linear_hardening_gradients_match_the_reference_adjoint(gpu_lib):
+    """Yield stress and isotropic hardening modulus of a linear-hardening rod: the kernel's
+    gradients against the oracle's reference adjoint."""
+    import dataclasses as dc
+    from neofiz_gb300.materials import Material
+    mat = Material("linear steel", 200.0e9, 0.29, 7850.0).yielding(600.0e6, 2.0e9, 3.0e8)
+    rods = _rods(t_end=8.0e-6)
+    insts = [dc.replace(x, material=mat) for x in scenes.sweep_instances(rods)]
+    out = {}
+    for cls in (BatchSolver, OracleBatch):
+        b = cls(insts, scenes.Formulation.AXISYMMETRIC, cfl=0.6)
+        b.adjointForward(25)
+        out[cls] = [b.adjointBackward(obj) for obj in (0, 1)]
+        b.close()
+    for obj in (0, 1):
+        g, o = out[BatchSolver][obj], out[OracleBatch][obj]
+        assert np.array_equal(g[0], o[0])
+        np.testing.assert_allclose(g[1], o[1], rtol=1e-9, atol=0.0)
+        assert np.all(g[1][:, _abi.PARAM_YIELD] != 0.0)
