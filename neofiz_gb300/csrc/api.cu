@@ -56,6 +56,31 @@ cudaError_t dalloc(Solver &S, T **p, size_t count) {
     return e;
 }
 
+// The set-up arrays of nf_create carved from one allocation: one cudaMalloc and one memset
+// instead of one each per array (the allocations dominated creating a 200k-element scene).
+struct Arena {
+    std::vector<std::pair<void **, size_t>> items;
+    template <typename T>
+    void add(T **p, size_t count) {
+        items.push_back({reinterpret_cast<void **>(p), sizeof(T) * (count ? count : 1)});
+    }
+    cudaError_t commit(Solver &S) {
+        size_t total = 0;
+        for (auto &it : items) total += (it.second + 255) & ~(size_t)255;
+        void *base = nullptr;
+        cudaError_t e = cudaMalloc(&base, total);
+        if (e != cudaSuccess) return e;
+        S.arena = base;
+        S.arenaBytes = total;
+        char *p = static_cast<char *>(base);
+        for (auto &it : items) {
+            *it.first = p;
+            p += (it.second + 255) & ~(size_t)255;
+        }
+        return cudaMemsetAsync(base, 0, total, S.stream);
+    }
+};
+
 template <typename T>
 cudaError_t upload(Solver &S, T *dst, const T *src, size_t count) {
     if (!count) return cudaSuccess;
@@ -430,8 +455,8 @@ nf_status nf_create(const nf_mesh *mesh, const nf_material *materials, int32_t m
                            std::max(d.coopBlocks, 8 * d.sms)) + 1;
     d.bucketCap = std::max(1 << 14, 2 * N);
     const size_t scanInts = scan_tmp_ints(std::max(std::max(4 * E, N + 1), d.bucketCap + 1)) + 16;
-    cudaError_t e_ = cudaSuccess;
-#define A(ptr, n) if (e_ == cudaSuccess) e_ = dalloc(*S, &(ptr), (n))
+    Arena arena;
+#define A(ptr, n) arena.add(&(ptr), (n))
     A(d.X0, N); A(d.U, N); A(d.V, N); A(d.F, N); A(d.mass, N); A(d.invMass, N);
     A(d.flags, N); A(d.wallState, N); A(d.contactState, N);
     A(d.conn, E); A(d.emat, E); A(d.mats, material_count);
@@ -444,6 +469,7 @@ nf_status nf_create(const nf_mesh *mesh, const nf_material *materials, int32_t m
     A(d.edgeGroup, 4LL * E); A(d.groupStart, groupStart.size()); A(d.groupMember, 4LL * E);
     A(d.s, 1);
 #undef A
+    const cudaError_t e_ = arena.commit(*S);
     if (e_ != cudaSuccess) {
         nf_status st = fail(nullptr, NF_ENOMEM, "device allocation failed: %s", cudaGetErrorString(e_));
         nf_destroy(reinterpret_cast<nf_solver *>(S));
@@ -500,8 +526,12 @@ nf_status nf_destroy(nf_solver *h) {
                     d.scanTmp, d.s, d.matsF, d.sigF, d.backF, d.epsPF, d.wPF, d.hgKF,
                     d.contribF, d.hgF, d.dStrF, d.dSoftF, d.dWidthF, d.dFailF, d.dGfF, d.dGeomF,
                     d.pMid, d.pCur, d.vdt, d.gaussVol, d.coopSums, d.incSlots, d.bucketA, d.bucketN, d.slaveXY};
-    for (void *p : ptrs)
-        if (p) cudaFree(p);
+    const char *a0 = static_cast<const char *>(S->arena), *a1 = a0 + S->arenaBytes;
+    for (void *p : ptrs) {
+        const char *c = static_cast<const char *>(p);
+        if (p && !(S->arena && c >= a0 && c < a1)) cudaFree(p);      // arena arrays go below
+    }
+    if (S->arena) cudaFree(S->arena);
     if (S->ownStream) cudaStreamDestroy(S->ownStream);
     delete S;
     return NF_OK;

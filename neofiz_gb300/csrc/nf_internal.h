@@ -193,6 +193,8 @@ struct Solver {
     Dev graphDev{};
     bool graphValid = false;
     bool noGraphs = false;       // capture failed once: steps are enqueued directly
+    void *arena = nullptr;       // nf_create's set-up arrays, one allocation
+    size_t arenaBytes = 0;
     // per-group event profiling
     bool profiling = false;
     struct Rec { int group; cudaEvent_t a, b; };

@@ -169,6 +169,17 @@ class Materials:
     def __init__(self, one: Optional[Material], each: Optional[Sequence[Material]]):
         self._one = one
         self._each = list(each) if each is not None else None
+        self._table = None
+        if self._each is not None:
+            # the device's layout (distinct materials, per-element index), built once here
+            # with C-level passes rather than per element in Python
+            import numpy as np
+            keys = list(map(id, self._each))
+            objs = dict(zip(keys, self._each))
+            order = list(dict.fromkeys(keys))               # first appearance
+            slot = {k: i for i, k in enumerate(order)}
+            index = np.fromiter(map(slot.__getitem__, keys), dtype=np.int32, count=len(keys))
+            self._table = ([objs[k] for k in order], index)
 
     @staticmethod
     def uniform(material: Material) -> "Materials":
@@ -209,20 +220,14 @@ class Materials:
         """Distinct materials in first-appearance order, compared by identity."""
         if self._one is not None:
             return [self._one]
-        out = []
-        for m in self._each:
-            if not any(k is m for k in out):
-                out.append(m)
-        return out
+        return list(self._table[0])
 
     def table(self, elementCount: int):
         """(distinct materials, per-element index into them)."""
         import numpy as np
-        mats = self.distinct()
         if self._one is not None:
-            return mats, np.zeros(elementCount, dtype=np.int32)
-        ids = {id(m): i for i, m in enumerate(mats)}
-        return mats, np.array([ids[id(m)] for m in self._each], dtype=np.int32)
+            return [self._one], np.zeros(elementCount, dtype=np.int32)
+        return list(self._table[0]), self._table[1]
 
     def fastestWave(self) -> float:
         if self._one is not None:
