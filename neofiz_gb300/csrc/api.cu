@@ -416,15 +416,29 @@ nf_status nf_create(const nf_mesh *mesh, const nf_material *materials, int32_t m
     s0.tEnd = INFINITY;
     d.dt0 = s0.dt;
 
-    // edge groups for the free surface: element-edges with the same undirected node pair
+    // edge groups for the free surface: element-edges with the same undirected node pair, in
+    // (lower node, higher node, element-edge) order -- a counting sort by the lower node (stable
+    // in element-edge order) and an insertion sort by the higher node within each node's few
+    // edges, linear in the mesh where a comparison sort of the 4E keys is not
     std::vector<std::pair<long long, int>> keys(4LL * E);
-    for (int e = 0; e < E; e++)
-        for (int k = 0; k < 4; k++) {
-            const int a = mesh->conn[e * 4 + k], b = mesh->conn[e * 4 + (k + 1) % 4];
-            const long long lo = std::min(a, b), hi = std::max(a, b);
-            keys[e * 4 + k] = std::make_pair((lo << 32) | hi, e * 4 + k);
+    {
+        std::vector<int32_t> start(N + 1, 0);
+        for (long long q = 0; q < 4LL * E; q++) {
+            const int a = mesh->conn[q], b = mesh->conn[(q & ~3LL) + ((q + 1) & 3)];
+            start[std::min(a, b) + 1]++;
         }
-    std::sort(keys.begin(), keys.end());
+        for (int i = 0; i < N; i++) start[i + 1] += start[i];
+        std::vector<int32_t> cursor(start.begin(), start.end() - 1);
+        for (long long q = 0; q < 4LL * E; q++) {
+            const int a = mesh->conn[q], b = mesh->conn[(q & ~3LL) + ((q + 1) & 3)];
+            const long long lo = std::min(a, b), hi = std::max(a, b);
+            keys[cursor[lo]++] = std::make_pair((lo << 32) | hi, (int)q);
+        }
+        for (int i = 0; i < N; i++)
+            for (int j = start[i] + 1; j < start[i + 1]; j++)
+                for (int m = j; m > start[i] && keys[m] < keys[m - 1]; m--)
+                    std::swap(keys[m], keys[m - 1]);
+    }
     std::vector<int32_t> edgeGroup(4LL * E), groupStart, groupMember(4LL * E);
     for (size_t i = 0; i < keys.size();) {
         size_t j = i;
