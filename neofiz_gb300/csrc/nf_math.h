@@ -12,16 +12,25 @@
  * multiply-add contraction (nvcc --fmad=false, gcc -ffp-contract=off) -- the GPU and the CPU
  * produce bit-identical results.
  *
- * Methods (all from the mathematics; coefficients are exact Taylor coefficients rounded to
- * double, computed for this file):
- *   log   : x = 2^k m, m in [sqrt(1/2), sqrt(2)]; with f = m - 1 and s = f/(2+f),
- *           log(1+f) = 2 atanh(s) = f - s (f - R),  R = sum_{j>=1} 2 s^(2j) / (2j+1).
- *           k ln2 is added with a Cody-Waite split of ln2 (high part has 32 significant
- *           bits, so k*hi is exact). A double-double form feeds pow.
- *   exp   : Cody-Waite reduction x = k ln2 + r, |r| <= ln2/2, Taylor series to r^13.
- *   pow   : exp(y log x) with log in double-double and the product y*log x split exactly by
- *           Veltkamp/Dekker two-product (no fma), so the result is accurate to a few ulp
- *           rather than |y log x| ulp.
+ * Methods (from the mathematics and published methods; every constant is an exact value
+ * rounded to double, computed for this file -- the tables by gen_nf_math_tables.py):
+ *   log   : Tang's table-driven logarithm (ACM TOMS 16, 1990). x = 2^k z with z in
+ *           [0.705, 1.41); z's leading mantissa bits pick one of 128 entries holding
+ *           invc ~ 1/c and -log(invc) as hi + lo; r = z invc - 1 is formed exactly as a
+ *           product and its fused-multiply-add error (no division), and
+ *           log x = k ln2 + (-log invc) + log1p(r), log1p by its Taylor series to r^7
+ *           (|r| <= 2^-8). The large terms are summed with their rounding errors, so the
+ *           result comes as a double-double (hi + lo) for pow, and rounded once for log.
+ *   exp   : Tang's table-driven exponential (ACM TOMS 15, 1989). x = (128 m + j) ln2/128 + r
+ *           with ln2/128 split in a 35-bit head (exact products) and a tail, |r| <= ln2/256;
+ *           exp x = 2^m 2^(j/128) (1 + r + r^2/2 + ... + r^5/120), 2^(j/128) from a table as
+ *           hi + lo. A double-double argument (pow's y log x) enters through r.
+ *   pow   : exp(y log x) with log as double-double and y log x formed exactly by a fused
+ *           multiply-add, so the result is accurate to about half an ulp rather than
+ *           |y log x| ulp.
+ * Fused multiply-add is an exactly rounded IEEE operation (fma() in C, the DFMA instruction on
+ * the GPU), so it gives the same bits on both sides; only contraction of separate operations
+ * is switched off.
  *   atan2 : quadrant folding to atan(t), t in [0,1]; t > tan(pi/8) maps through
  *           atan(t) = pi/4 + atan((t-1)/(t+1)); |u| > 1/8 maps through
  *           atan(u) = atan(1/4) + atan((u-1/4)/(1+u/4)); Taylor series for |v| <= 0.15.
@@ -36,6 +45,8 @@
 #include <stdint.h>
 #include <string.h>
 #include <math.h>
+
+#include "nf_math_tables.h"
 
 #if defined(__CUDACC__)
 #define NF_HD static __host__ __device__ inline
@@ -73,70 +84,97 @@ NF_HD double nf_scale(double er, int k) {
     return er * nf_pow2i(k);
 }
 
-/* exp(r) for |r| <= ~0.35, Taylor to r^13. */
-NF_HD double nf_exp_core(double r) {
-    double p = 0x1.6124613a86d09p-33;              /* 1/13! */
-    p = 0x1.1eed8eff8d898p-29 + r * p;             /* 1/12! */
-    p = 0x1.ae64567f544e4p-26 + r * p;             /* 1/11! */
-    p = 0x1.27e4fb7789f5cp-22 + r * p;             /* 1/10! */
-    p = 0x1.71de3a556c734p-19 + r * p;             /* 1/9!  */
-    p = 0x1.a01a01a01a01ap-16 + r * p;             /* 1/8!  */
-    p = 0x1.a01a01a01a01ap-13 + r * p;             /* 1/7!  */
-    p = 0x1.6c16c16c16c17p-10 + r * p;             /* 1/6!  */
-    p = 0x1.1111111111111p-7 + r * p;              /* 1/5!  */
-    p = 0x1.5555555555555p-5 + r * p;              /* 1/4!  */
-    p = 0x1.5555555555555p-3 + r * p;              /* 1/3!  */
-    p = 0x1.0000000000000p-1 + r * p;              /* 1/2!  */
-    return 1.0 + (r + (r * r) * p);
+/* Tables of the logarithm (invc, -log invc hi, lo, 0 per entry) and of 2^(j/128) (hi, lo),
+ * one copy for the host and one in device global memory (read through the read-only cache;
+ * a warp's lanes index different entries, which constant memory would serialise). */
+static const double nf_log_tab_h[4 * 128] = { NF_LOG_TABLE };
+static const double nf_exp_tab_h[2 * 128] = { NF_EXP_TABLE };
+#if defined(__CUDACC__)
+static __device__ const double nf_log_tab_d[4 * 128] = { NF_LOG_TABLE };
+static __device__ const double nf_exp_tab_d[2 * 128] = { NF_EXP_TABLE };
+#endif
+
+NF_HD double nf_log_tab(int i) {
+#if defined(__CUDA_ARCH__)
+    return __ldg(nf_log_tab_d + i);
+#else
+    return nf_log_tab_h[i];
+#endif
+}
+NF_HD double nf_exp_tab(int i) {
+#if defined(__CUDA_ARCH__)
+    return __ldg(nf_exp_tab_d + i);
+#else
+    return nf_exp_tab_h[i];
+#endif
+}
+
+/* exp(p + plo) for p in [-745.2, 709.8] and |plo| <= 2^-40 |p| (or p's own rounding error). */
+NF_HD double nf_exp_dd(double p, double plo) {
+    const double kd = rint(p * NF_EXP_N_OVER_LN2);
+    const int n = (int)kd;
+    const double r1 = fma(-kd, NF_EXP_L_HI, p);          /* exact: kd L_HI exact, Sterbenz */
+    const double r = fma(-kd, NF_EXP_L_LO, r1) + plo;
+    const int j = n & 127;
+    const int m = (n - j) / 128;                          /* exact: n - j is a multiple */
+    const double thi = nf_exp_tab(2 * j), tlo = nf_exp_tab(2 * j + 1);
+    double t = fma(r, 0x1.1111111111111p-7, 0x1.5555555555555p-5);   /* 1/120, 1/24 */
+    t = fma(r, t, 0x1.5555555555555p-3);                               /* 1/6 */
+    t = fma(r, t, 0.5);
+    const double q = fma(r * r, t, r);                    /* exp(r) - 1 */
+    return nf_scale(thi + fma(thi, q, tlo), m);
 }
 
 NF_HD double nf_exp(double x) {
     if (x != x) return x;
     if (x > 709.782712893384) return INFINITY;
     if (x < -745.1332191019412) return 0.0;
-    const double kd = rint(x * NF_INV_LN2);
-    const int k = (int)kd;
-    const double r = (x - kd * NF_LN2_HI) - kd * NF_LN2_LO;
-    return nf_scale(nf_exp_core(r), k);
+    return nf_exp_dd(x, 0.0);
 }
 
 /* log(x) as an unevaluated sum hi + lo, for finite x > 0. */
 NF_HD void nf_log_dd(double x, double *hi, double *lo) {
     uint64_t u = nf_bits(x);
-    int k = 0;
+    int64_t kadj = 0;
     if (u < 0x0010000000000000ULL) {               /* subnormal: renormalise */
-        x *= 0x1p54;
-        u = nf_bits(x);
-        k = -54;
+        u = nf_bits(x * 0x1p54);
+        kadj = -54;
     }
-    k += (int)(u >> 52) - 1023;
-    double m = nf_from_bits((u & 0x000fffffffffffffULL) | 0x3ff0000000000000ULL);
-    if (m > NF_SQRT2) { m *= 0.5; k += 1; }
-    const double f = m - 1.0;                      /* exact */
-    const double s = f / (2.0 + f);
-    const double z = s * s;
-    double R = 0x1.af286bca1af28p-4;               /* 2/19 */
-    R = 0x1.e1e1e1e1e1e1ep-4 + z * R;              /* 2/17 */
-    R = 0x1.1111111111111p-3 + z * R;              /* 2/15 */
-    R = 0x1.3b13b13b13b14p-3 + z * R;              /* 2/13 */
-    R = 0x1.745d1745d1746p-3 + z * R;              /* 2/11 */
-    R = 0x1.c71c71c71c71cp-3 + z * R;              /* 2/9  */
-    R = 0x1.2492492492492p-2 + z * R;              /* 2/7  */
-    R = 0x1.999999999999ap-2 + z * R;              /* 2/5  */
-    R = 0x1.5555555555555p-1 + z * R;              /* 2/3  */
-    R = z * R;
-    const double c = s * (f - R);
-    const double lg = f - c;
-    const double lglo = (f - lg) - c;              /* |f| >= |c|: Fast2Sum error */
+    const uint64_t tmp = u - NF_LOG_OFF;
+    const int64_t k = (int64_t)(tmp & 0xfff0000000000000ULL) / ((int64_t)1 << 52) + kadj;
+    const int j = (int)((tmp >> 45) & 127);
+    const double z = nf_from_bits(u - (tmp & 0xfff0000000000000ULL));
+    const double invc = nf_log_tab(4 * j), chi = nf_log_tab(4 * j + 1);
+    const double clo = nf_log_tab(4 * j + 2);
+    const double pr = z * invc;
+    const double rl = fma(z, invc, -pr);           /* z invc = pr + rl exactly */
+    const double rh = pr - 1.0;                    /* exact (Sterbenz) */
     const double dk = (double)k;
-    const double t1 = dk * NF_LN2_HI;              /* exact */
-    const double sum = t1 + lg;
-    const double bb = sum - t1;
-    const double err = (t1 - (sum - bb)) + (lg - bb);
-    const double l = err + (lglo + dk * NF_LN2_LO);
-    const double h = sum + l;
+    /* k ln2_hi + (-log invc) + rh - rh^2/2, each addition with its error (Fast2Sum: the
+     * running sum is never smaller than the term added, or is zero) */
+    const double a = dk * NF_LN2_HI;               /* exact */
+    const double s1 = a + chi;
+    const double e1 = (a - s1) + chi;
+    const double s2 = s1 + rh;
+    const double e2 = (s1 - s2) + rh;
+    const double q = rh * rh;
+    const double ql = fma(rh, rh, -q);             /* rh^2 = q + ql exactly */
+    const double hq = -0.5 * q;
+    const double s3 = s2 + hq;
+    const double e3 = (s2 - s3) + hq;
+    /* rh^3 (1/3 - rh/4 + rh^2/5 - rh^3/6 + rh^4/7); the remainder is below 2^-67 */
+    double t = fma(rh, 0x1.2492492492492p-3, -0x1.5555555555555p-3);   /* 1/7, -1/6 */
+    t = fma(rh, t, 0x1.999999999999ap-3);                               /* 1/5 */
+    t = fma(rh, t, -0.25);
+    t = fma(rh, t, 0x1.5555555555555p-2);                               /* 1/3 */
+    const double cubic = (q * rh) * t;
+    /* rl (1 - rh) is log1p's first-order response to r's low part */
+    const double small = ((dk * NF_LN2_LO + clo) + ((e1 + e2) + e3))
+                         + (fma(-rh, rl, rl) - 0.5 * ql);
+    const double l = cubic + small;
+    const double h = s3 + l;
     *hi = h;
-    *lo = l - (h - sum);
+    *lo = l - (h - s3);
 }
 
 NF_HD double nf_log(double x) {
@@ -144,46 +182,36 @@ NF_HD double nf_log(double x) {
     if (x == INFINITY) return x;
     double hi, lo;
     nf_log_dd(x, &hi, &lo);
-    return hi + lo;
+    return hi;
 }
 
-/* Veltkamp split of a into hi + lo, each with at most 26 significant bits. */
-NF_HD void nf_split(double a, double *hi, double *lo) {
-    const double c = 134217729.0 * a;              /* 2^27 + 1 */
-    const double h = c - (c - a);
-    *hi = h;
-    *lo = a - h;
-}
-
-/* x^y for x >= 0 (or +inf), y neither 0 nor NaN. */
+/* x^y for x >= 0 (or +inf), y neither 0 nor NaN. Special cases by bit pattern (integer
+ * comparisons, which keep the FP64 pipe for the arithmetic). */
 NF_HD double nf_pow_nonneg(double x, double y) {
-    if (x == 1.0) return 1.0;
-    if (x == 0.0) return y > 0.0 ? 0.0 : INFINITY;
-    if (x == INFINITY) return y > 0.0 ? INFINITY : 0.0;
-    if (y == INFINITY) return x > 1.0 ? INFINITY : 0.0;
-    if (y == -INFINITY) return x > 1.0 ? 0.0 : INFINITY;
+    const uint64_t ux = nf_bits(x), uy = nf_bits(y);
+    if (ux == 0x3ff0000000000000ULL) return 1.0;                   /* x == 1 */
+    if ((ux << 1) == 0) return (uy >> 63) ? INFINITY : 0.0;        /* x == +-0, y > 0 or < 0 */
+    if (ux == 0x7ff0000000000000ULL) return (uy >> 63) ? 0.0 : INFINITY;
+    if ((uy << 1) == 0xffe0000000000000ULL) {                      /* y == +-inf */
+        const int big = ux > 0x3ff0000000000000ULL;
+        return (uy >> 63) ? (big ? 0.0 : INFINITY) : (big ? INFINITY : 0.0);
+    }
     double lh, ll;
     nf_log_dd(x, &lh, &ll);
     const double p = y * lh;
     if (p > 709.8) return INFINITY;
     if (p < -745.2) return 0.0;
-    double yh, yl, hh, hl;
-    nf_split(y, &yh, &yl);
-    nf_split(lh, &hh, &hl);
-    const double perr = ((yh * hh - p) + yh * hl + yl * hh) + yl * hl;  /* exact */
-    const double plo = perr + y * ll;
-    const double kd = rint(p * NF_INV_LN2);
-    const int k = (int)kd;
-    const double r = ((p - kd * NF_LN2_HI) + plo) - kd * NF_LN2_LO;
-    return nf_scale(nf_exp_core(r), k);
+    const double perr = fma(y, lh, -p);            /* y lh = p + perr exactly */
+    return nf_exp_dd(p, fma(y, ll, perr));
 }
 
 /* Not recursive: a device call graph without cycles keeps the kernels' stack depth known at
  * compile time, so the driver sizes each launch's per-thread stack itself. */
 NF_HD double nf_pow(double x, double y) {
-    if (y == 0.0 || x == 1.0) return 1.0;
-    if (x != x || y != y) return NAN;
-    if (x < 0.0) {
+    const uint64_t ux = nf_bits(x), uy = nf_bits(y);
+    if ((uy << 1) == 0 || ux == 0x3ff0000000000000ULL) return 1.0;              /* y == 0, x == 1 */
+    if ((ux << 1) > 0xffe0000000000000ULL || (uy << 1) > 0xffe0000000000000ULL) return NAN;
+    if ((ux >> 63) && (ux << 1) != 0) {                                         /* x < 0 */
         /* Only integer powers of a negative base are real. Never reached on the solver
          * path, whose bases are a plastic strain and a homologous temperature in (0, 1). */
         if (rint(y) != y) return NAN;

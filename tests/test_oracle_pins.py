@@ -477,6 +477,34 @@ def test_threads_are_bit_identical():
 
 # ----------------------------------------------------------------------------- math layer
 
+@pytest.mark.parametrize("name,gen", [
+    ("log", lambda r: (math.exp(r.uniform(-700, 700)),)),
+    ("log", lambda r: (1.0 + r.uniform(-0.01, 0.01),)),
+    ("log", lambda r: (r.uniform(1e-320, 1e-308),)),
+    ("exp", lambda r: (r.uniform(-708, 709),)),
+    ("exp", lambda r: (r.uniform(-1e-3, 1e-3),)),
+    ("pow", lambda r: (math.exp(r.uniform(-20, 2)), r.uniform(0.05, 1.6))),
+    ("pow", lambda r: (math.exp(r.uniform(-50, 50)), r.uniform(-10, 10))),
+    ("pow", lambda r: (1.0 + r.uniform(-1e-6, 1e-6), r.uniform(0.1, 1000))),
+])
+def test_table_driven_functions_within_half_an_ulp(name, gen):
+    """The table-driven log, exp and pow against values exact to 120 bits: within 0.52 ulp
+    (the Johnson-Cook law's strain, rate and thermal terms go through these three)."""
+    mpmath = pytest.importorskip("mpmath")
+    from oracle.oracle import math_fn
+    import random
+    mpmath.mp.prec = 120
+    exact = {"log": mpmath.log, "exp": mpmath.exp, "pow": mpmath.power}[name]
+    rnd = random.Random(7)
+    worst = 0.0
+    for _ in range(4000):
+        args = gen(rnd)
+        got = math_fn(name, *args) if len(args) == 2 else math_fn(name, args[0])
+        want = exact(*[mpmath.mpf(a) for a in args])
+        worst = max(worst, float(abs(mpmath.mpf(got) - want) / math.ulp(float(want))))
+    assert worst <= 0.52
+
+
 @pytest.mark.parametrize("name,fn,gen", [
     ("log", math.log, lambda r: (math.exp(r.uniform(-30, 30)),)),
     ("exp", math.exp, lambda r: (r.uniform(-700, 700),)),
