@@ -364,7 +364,10 @@ __device__ void resolve_pair(const Dev &d, int i, int n, int s, double &energy, 
 // serial loop keeps, so the buckets need no order. A candidate's depth is zero unless its gap
 // is negative; that test is exact and reads only what the fill staged beside the entry, so it
 // runs first, before the exclusions and the divisions.
-__device__ void search_slave(const Dev &d, const Grid &g, int i, double &energy, double &diss) {
+// Contact.nearestPenetrated for surface slot i, one warp: the deepest admissible segment and
+// whether the last step's master was seen too deep. Every lane returns the same answer.
+__device__ void search_slave(const Dev &d, const Grid &g, int i, double &bestOut, int &segOut,
+                             bool &fellOut) {
     const int lane = threadIdx.x & 31;
     const double2 xn = d.slaveXY[i];
     const int n = d.surfNodes[i];
@@ -437,8 +440,16 @@ __device__ void search_slave(const Dev &d, const Grid &g, int i, double &energy,
             bestSeg = os;
         }
     }
-    const bool anyFell = __any_sync(0xffffffffu, fell);
-    if (lane != 0) return;
+    fellOut = __any_sync(0xffffffffu, fell);
+    bestOut = __shfl_sync(0xffffffffu, best, 0);
+    segOut = __shfl_sync(0xffffffffu, bestSeg, 0);
+}
+
+// The pair of surface slot i from its search (Contact.java:446-462): master, last master,
+// the escape count and the pair forces; one lane.
+__device__ void finish_slave(const Dev &d, int i, double best, int bestSeg, bool anyFell,
+                             double &energy, double &diss) {
+    const int last = d.lastMaster[i];
     d.master[i] = best > 0.0 ? bestSeg : -1;
     if (!(best > 0.0)) {                      // no pair: Contact.java:446-452
         if (last >= 0 && anyFell) atomicAdd(&d.s->escaped, 1);
@@ -446,7 +457,7 @@ __device__ void search_slave(const Dev &d, const Grid &g, int i, double &energy,
         return;
     }
     d.lastMaster[i] = bestSeg;
-    resolve_pair(d, i, n, bestSeg, energy, diss);
+    resolve_pair(d, i, d.surfNodes[i], bestSeg, energy, diss);
 }
 
 // ---------------------------------------------------------------------------- the pass
@@ -649,13 +660,36 @@ __global__ void __launch_bounds__(CB, 2) k_contact_pass(Dev d) {
     }
     SYNC();
 
-    // the search and the pair forces: one warp per slave; the totals as per-block partials,
-    // folded in a fixed order at the step's end
+    // the search and the pair forces: one warp searches each slave in turn, and the k-th
+    // slave's answer is kept by lane k; the pair forces, long dependent chains of divisions,
+    // are then computed by those lanes side by side instead of one after another. The totals
+    // are per-block partials, folded in a fixed order at the step's end.
     {
         double energy = 0.0, diss = 0.0;
         const int warpsTotal = gridDim.x * CB_WARPS;
-        for (int i = (threadIdx.x >> 5) * gridDim.x + blockIdx.x; i < nodes; i += warpsTotal)
-            search_slave(d, g, i, energy, diss);
+        const int lane = threadIdx.x & 31;
+        int mine = -1, mySeg = -1;
+        double myBest = 0.0;
+        bool myFell = false;
+        int r = 0;
+        for (int i = (threadIdx.x >> 5) * gridDim.x + blockIdx.x; i < nodes; i += warpsTotal) {
+            double best;
+            int seg;
+            bool fell;
+            search_slave(d, g, i, best, seg, fell);
+            if (r == lane) {
+                mine = i;
+                myBest = best;
+                mySeg = seg;
+                myFell = fell;
+            }
+            if (++r == 32) {
+                if (mine >= 0) finish_slave(d, mine, myBest, mySeg, myFell, energy, diss);
+                mine = -1;
+                r = 0;
+            }
+        }
+        if (mine >= 0) finish_slave(d, mine, myBest, mySeg, myFell, energy, diss);
         const double e1 = block_sum_c(energy, shd);
         const double e2 = block_sum_c(diss, shd);
         if (threadIdx.x == 0) {

@@ -105,7 +105,8 @@ __device__ __forceinline__ T jc_strainTerm(const MatT<T> &f, T eps) {
 template <typename T>
 __device__ __forceinline__ T jc_rateTerm(const MatT<T> &f, T rate) {
     if (rate <= f.refRate) return T(1);
-    return T(1) + f.c * Fn<T>::log(rate / f.refRate);
+    // rate / 1 is rate exactly: the common reference rate of 1/s skips the division
+    return T(1) + f.c * Fn<T>::log(f.refRate == T(1) ? rate : rate / f.refRate);
 }
 template <typename T>
 __device__ __forceinline__ T jc_thermalTerm(const MatT<T> &f, T temperature) {
