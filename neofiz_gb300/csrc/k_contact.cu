@@ -37,6 +37,7 @@ constexpr double MAX_DEPTH = 0.5;
 constexpr double STICK_RELAXATION = 0.5;
 constexpr double FACING = 0.25;
 constexpr int INC_CAP = NF_INC_CAP;      // incident terms a surface node's fixed list holds
+constexpr int SCAN_ITEMS = 8;            // values a thread scans in registers per tile
 constexpr unsigned long long WAIT_LIMIT_NS = 1000000000ULL;   // one second
 constexpr long long WAIT_LIMIT_SPINS = 1LL << 27;             // a bound independent of the timer
 
@@ -184,15 +185,29 @@ __device__ bool grid_scan(const Dev &d, int32_t *in, int32_t *out, int32_t *out2
     int carry;
     block_scan_incl(pre, sh, &carry);
     if (total && threadIdx.x == 0 && (int)blockIdx.x == G - 1) *total = carry + bsum;
-    for (int base = lo; base < hi; base += CB) {
-        const int i = base + threadIdx.x;
-        const int v = i < hi ? in[i] : 0;
+    // tiles of CB x SCAN_ITEMS: each thread scans a run of SCAN_ITEMS in registers, so one
+    // block scan serves SCAN_ITEMS values per thread
+    for (int base = lo; base < hi; base += CB * SCAN_ITEMS) {
+        const int first = base + threadIdx.x * SCAN_ITEMS;
+        int v[SCAN_ITEMS];
+        int run = 0;
+#pragma unroll
+        for (int k = 0; k < SCAN_ITEMS; k++) {
+            v[k] = first + k < hi ? in[first + k] : 0;
+            run += v[k];
+        }
         int tileTotal;
-        const int incl = block_scan_incl(v, sh, &tileTotal);
-        if (i < hi) {
-            out[i] = carry + incl - v;
-            if (out2) out2[i] = carry + incl - v;
-            if (zeroIn) in[i] = 0;
+        const int incl = block_scan_incl(run, sh, &tileTotal);
+        int at = carry + incl - run;
+#pragma unroll
+        for (int k = 0; k < SCAN_ITEMS; k++) {
+            const int i = first + k;
+            if (i < hi) {
+                out[i] = at;
+                if (out2) out2[i] = at;
+                if (zeroIn) in[i] = 0;
+            }
+            at += v[k];
         }
         carry += tileTotal;
     }

@@ -192,7 +192,8 @@ __global__ void __launch_bounds__(BLOCK) k_erode(Dev d) {
 // ------------------------------------------------------------------------------------ element kernels
 
 __device__ __forceinline__ void min_edge_commit(Dev &d, double minEdge) {
-    for (int o = 16; o > 0; o >>= 1) minEdge = jmin(minEdge, __shfl_down_sync(0xffffffffu, minEdge, o));
+    for (int o = 16; o > 0; o >>= 1)
+        minEdge = jmin_nonneg(minEdge, __shfl_down_sync(0xffffffffu, minEdge, o));
     if ((threadIdx.x & 31) == 0) atomicMin(&d.s->minEdgeBits, dbits(minEdge));
 }
 

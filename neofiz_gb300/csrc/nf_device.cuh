@@ -285,12 +285,26 @@ __device__ __forceinline__ T corot_sin(T spinDt) {
 template <typename T>
 __device__ __forceinline__ T sq2(T a, T b) { return a * a + b * b; }
 
-// shortestEdge, ExplicitSolver.java:1191-1197
+// Math.min of two squared lengths (+0, positive, +inf or NaN): their bit patterns order as
+// their values do, every NaN pattern lies above +inf's, and Math.min's NaN rule is kept, so
+// integer comparisons give jmin's answer without using the FP64 pipe.
+__device__ __forceinline__ double jmin_nonneg(double a, double b) {
+    const unsigned long long ua = (unsigned long long)__double_as_longlong(a);
+    const unsigned long long ub = (unsigned long long)__double_as_longlong(b);
+    if (ua > 0x7ff0000000000000ULL) return a;
+    if (ub > 0x7ff0000000000000ULL) return b;
+    return ua <= ub ? a : b;
+}
+__device__ __forceinline__ float jmin_nonneg(float a, float b) { return jmin(a, b); }
+
+// shortestEdge, ExplicitSolver.java:1191-1197 (running is Double.MAX_VALUE or an earlier
+// minimum, so every operand is a squared length)
 template <typename T>
 __device__ __forceinline__ T shortestEdge(T running, T r0, T r1, T r2, T r3, T z0, T z1, T z2,
                                           T z3) {
-    return jmin(running, jmin(jmin(sq2(r1 - r0, z1 - z0), sq2(r2 - r1, z2 - z1)),
-                              jmin(sq2(r3 - r2, z3 - z2), sq2(r0 - r3, z0 - z3))));
+    return jmin_nonneg(running,
+                       jmin_nonneg(jmin_nonneg(sq2(r1 - r0, z1 - z0), sq2(r2 - r1, z2 - z1)),
+                                   jmin_nonneg(sq2(r3 - r2, z3 - z2), sq2(r0 - r3, z0 - z3))));
 }
 
 // Damage.at, Damage.java:342-347
