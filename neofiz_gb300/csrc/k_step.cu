@@ -163,7 +163,7 @@ __global__ void __launch_bounds__(BLOCK) k_erode(Dev d) {
                 const int p = e * d.ppe + g;
                 sum += damage_at(d.dStrength[p], d.dSoft[p], d.dFail[e], d.epsP[p]);
             }
-            failed = sum / d.ppe >= d.erosionDamage;
+            failed = (d.ppe == 1 ? sum : sum / d.ppe) >= d.erosionDamage;   // x / 1 is x
         }
         const int4 c = d.conn[e];                            // currentArea, :681-691
         const int nn[4] = {c.x, c.y, c.z, c.w};
@@ -295,7 +295,7 @@ __global__ void __launch_bounds__(BLOCK) k_element_full(Dev d, int zeroStrain) {
                 }
                 if (d.finite) {
                     const double spinDt = 0.5 * (dZdR - dRdZ);
-                    if (spinDt != 0.0) {
+                    if (!is_zero(spinDt)) {
                         const double cs = corot_cos(spinDt), sn = corot_sin(spinDt);
                         corot_rotate(sg, cs, sn);
                         corot_rotate(bk, cs, sn);

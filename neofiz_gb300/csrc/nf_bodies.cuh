@@ -208,7 +208,7 @@ static __device__ __forceinline__ void element_reduced(const Dev &d, int e, doub
         }
         if (d.finite) {
             const double spinDt = 0.5 * (dZdR - dRdZ);
-            if (spinDt != 0.0) {
+            if (!is_zero(spinDt)) {
                 const double cs = corot_cos(spinDt), sn = corot_sin(spinDt);
                 corot_rotate(sg, cs, sn);
                 corot_rotate(bk, cs, sn);

@@ -108,9 +108,19 @@ __device__ __forceinline__ T jc_rateTerm(const MatT<T> &f, T rate) {
     // rate / 1 is rate exactly: the common reference rate of 1/s skips the division
     return T(1) + f.c * Fn<T>::log(f.refRate == T(1) ? rate : rate / f.refRate);
 }
+// x == +-0 by bit pattern for doubles (an integer test, off the FP64 pipe)
+__device__ __forceinline__ bool is_zero(double x) {
+    return ((unsigned long long)__double_as_longlong(x) << 1) == 0ULL;
+}
+__device__ __forceinline__ bool is_zero(float x) { return x == 0.0f; }
+
 template <typename T>
 __device__ __forceinline__ T jc_thermalTerm(const MatT<T> &f, T temperature) {
-    const T homologous = (temperature - f.room) / (f.melt - f.room);
+    const T above = temperature - f.room, span = f.melt - f.room;
+    // a point that has done no plastic work sits at room temperature: 0 / span is +-0, whose
+    // term is 1, for any span but 0 and NaN (which the division below turns into NaN)
+    if (is_zero(above) && (span > T(0) || span < T(0))) return T(1);
+    const T homologous = above / span;
     if (homologous <= T(0)) return T(1);
     if (homologous >= T(1)) return T(0);
     return T(1) - Fn<T>::pow(homologous, f.m);
