@@ -379,59 +379,90 @@ __device__ void resolve_pair(const Dev &d, int i, int n, int s, double &energy, 
 // serial loop keeps, so the buckets need no order. A candidate's depth is zero unless its gap
 // is negative; that test is exact and reads only what the fill staged beside the entry, so it
 // runs first, before the exclusions and the divisions.
-// Contact.nearestPenetrated for surface slot i, one warp: the deepest admissible segment and
-// whether the last step's master was seen too deep. Every lane returns the same answer.
-__device__ void search_slave(const Dev &d, const Grid &g, int i, double &bestOut, int &segOut,
-                             bool &fellOut) {
-    const int lane = threadIdx.x & 31;
-    const double2 xn = d.slaveXY[i];
-    const int n = d.surfNodes[i];
-    const int last = d.lastMaster[i];
-    const int ci = iclamp(jd2i((xn.x - g.r0) / g.cellSize), g.cols);
-    const int cj = iclamp(jd2i((xn.y - g.z0) / g.cellSize), g.rows);
-    int lo = 0, len = 0;                      // lanes 0..8: the nine cells in visit order
-    long long myCell = -1;
-    if (lane < 9) {
-        const int j = cj + lane / 3 - 1, ii = ci + lane % 3 - 1;
-        if (j >= 0 && j < g.rows && ii >= 0 && ii < g.cols) {
-            myCell = (long long)j * g.cols + ii;
-            const int bkt = bucket_of(d, g, myCell);
-            lo = d.bucketStart[bkt];
-            len = d.bucketStart[bkt + 1] - lo;
+// Contact.nearestPenetrated (Contact.java:570-606) for four surface slots per warp, eight lanes
+// (a group) each: the deepest admissible segment and whether the last step's master was seen
+// too deep. Every candidate carries its visit key (cell in the nine, then the bucket entry),
+// and ties in depth go to the smallest key, the candidate the serial loop keeps. All 32 lanes
+// run every shuffle; a lane's group answer is valid when slot < nodes.
+constexpr int SG = 8;                          // lanes per slave
+__device__ void search_group(const Dev &d, const Grid &g, int slot, int nodes, double &bestOut,
+                             int &segOut, bool &fellOut) {
+    const int lane = threadIdx.x & 31, gl = lane & (SG - 1);
+    const bool live = slot < nodes;
+    double2 xn = make_double2(0.0, 0.0);
+    int n = -1, last = -1, ci = 0, cj = 0;
+    if (live) {
+        xn = d.slaveXY[slot];
+        n = d.surfNodes[slot];
+        last = d.lastMaster[slot];
+        ci = iclamp(jd2i((xn.x - g.r0) / g.cellSize), g.cols);
+        cj = iclamp(jd2i((xn.y - g.z0) / g.cellSize), g.rows);
+    }
+    // the nine cells in visit order: lane gl takes cell gl, lane 0 also cell 8
+    int lo = 0, len = 0, lo8 = 0, len8 = 0;
+    long long myCell = -1, cell8 = -1;
+    if (live) {
+        {
+            const int j = cj + gl / 3 - 1, ii = ci + gl % 3 - 1;
+            if (j >= 0 && j < g.rows && ii >= 0 && ii < g.cols) {
+                myCell = (long long)j * g.cols + ii;
+                const int bkt = bucket_of(d, g, myCell);
+                lo = d.bucketStart[bkt];
+                len = d.bucketStart[bkt + 1] - lo;
+            }
+        }
+        if (gl == 0) {
+            const int j = cj + 1, ii = ci + 1;
+            if (j < g.rows && ii < g.cols) {
+                cell8 = (long long)j * g.cols + ii;
+                const int bkt = bucket_of(d, g, cell8);
+                lo8 = d.bucketStart[bkt];
+                len8 = d.bucketStart[bkt + 1] - lo8;
+            }
         }
     }
-    int off = len;                            // inclusive scan over the nine
-    for (int o = 1; o < 16; o <<= 1) {
-        const int t = __shfl_up_sync(0xffffffffu, off, o);
-        if (lane >= o) off += t;
+    int off = len;                              // inclusive scan over cells 0..7
+    for (int o = 1; o < SG; o <<= 1) {
+        const int t = __shfl_up_sync(0xffffffffu, off, o, SG);
+        if (gl >= o) off += t;
     }
-    const int total = __shfl_sync(0xffffffffu, off, 8);
-    off -= len;                               // exclusive
+    const int off8 = __shfl_sync(0xffffffffu, off, SG - 1, SG);
+    off -= len;                                 // exclusive
+    lo8 = __shfl_sync(0xffffffffu, lo8, 0, SG);
+    len8 = __shfl_sync(0xffffffffu, len8, 0, SG);
+    cell8 = __shfl_sync(0xffffffffu, cell8, 0, SG);
+    const int total = off8 + len8;
+    int rounds = total;                         // the longest group's candidates, warp-wide
+    for (int o = 16; o > 0; o >>= 1) rounds = max(rounds, __shfl_xor_sync(0xffffffffu, rounds, o));
     double best = 0.0;
     unsigned long long bestKey = ~0ULL;
     int bestSeg = -1;
     bool fell = false;
-    for (int base = 0; base < total; base += 32) {
-        const int t = base + lane;
-        int c = 0;                            // which of the nine ranges holds position t
+    for (int base = 0; base < rounds; base += SG) {
+        const int t = base + gl;
+        int c = 0;                              // which of the nine ranges holds position t
 #pragma unroll
-        for (int q = 1; q < 9; q++) {
-            const int oq = __shfl_sync(0xffffffffu, off, q);
+        for (int q = 1; q < SG; q++) {
+            const int oq = __shfl_sync(0xffffffffu, off, q, SG);
             if (t >= oq) c = q;
         }
-        const int oc = __shfl_sync(0xffffffffu, off, c);
-        const int lc = __shfl_sync(0xffffffffu, lo, c);
-        const long long cc = __shfl_sync(0xffffffffu, myCell, c);
+        if (t >= off8) c = 8;
+        const int src = c < SG ? c : 0;
+        const int oc0 = __shfl_sync(0xffffffffu, off, src, SG);
+        const int lc0 = __shfl_sync(0xffffffffu, lo, src, SG);
+        const long long cc0 = __shfl_sync(0xffffffffu, myCell, src, SG);
         if (t >= total) continue;
+        const int oc = c < SG ? oc0 : off8, lc = c < SG ? lc0 : lo8;
+        const long long cc = c < SG ? cc0 : cell8;
         const int k = lc + (t - oc);
         const long long kc = d.bucketCell[k];
         const int entry = d.bucketEntry[k];
         const double2 pa = d.bucketA[k], nrm = d.bucketN[k];
         if (kc != cc) continue;
         const double gap = (xn.x - pa.x) * nrm.x + (xn.y - pa.y) * nrm.y;
-        if (!(gap < 0.0)) continue;           // depth_of would return zero
+        if (!(gap < 0.0)) continue;             // depth_of would return zero
         const int sg = entry >> 1;
-        if (excluded(d, i, n, sg)) continue;
+        if (excluded(d, slot, n, sg)) continue;
         const double depth = depth_of(d, n, sg);
         if (depth <= 0.0) continue;
         if (depth > MAX_DEPTH * d.slen[sg]) {
@@ -445,19 +476,20 @@ __device__ void search_slave(const Dev &d, const Grid &g, int i, double &bestOut
             bestSeg = sg;
         }
     }
-    for (int o = 16; o > 0; o >>= 1) {
-        const double ob = __shfl_down_sync(0xffffffffu, best, o);
-        const unsigned long long ok = __shfl_down_sync(0xffffffffu, bestKey, o);
-        const int os = __shfl_down_sync(0xffffffffu, bestSeg, o);
+    for (int o = SG / 2; o > 0; o >>= 1) {
+        const double ob = __shfl_down_sync(0xffffffffu, best, o, SG);
+        const unsigned long long ok = __shfl_down_sync(0xffffffffu, bestKey, o, SG);
+        const int os = __shfl_down_sync(0xffffffffu, bestSeg, o, SG);
         if (ob > best || (ob == best && ok < bestKey)) {
             best = ob;
             bestKey = ok;
             bestSeg = os;
         }
     }
-    fellOut = __any_sync(0xffffffffu, fell);
-    bestOut = __shfl_sync(0xffffffffu, best, 0);
-    segOut = __shfl_sync(0xffffffffu, bestSeg, 0);
+    const unsigned fellBits = __ballot_sync(0xffffffffu, fell);
+    fellOut = ((fellBits >> (lane & ~(SG - 1))) & ((1u << SG) - 1u)) != 0u;
+    bestOut = __shfl_sync(0xffffffffu, best, 0, SG);
+    segOut = __shfl_sync(0xffffffffu, bestSeg, 0, SG);
 }
 
 // The pair of surface slot i from its search (Contact.java:446-462): master, last master,
@@ -675,36 +707,24 @@ __global__ void __launch_bounds__(CB, 2) k_contact_pass(Dev d) {
     }
     SYNC();
 
-    // the search and the pair forces: one warp searches each slave in turn, and the k-th
-    // slave's answer is kept by lane k; the pair forces, long dependent chains of divisions,
-    // are then computed by those lanes side by side instead of one after another. The totals
-    // are per-block partials, folded in a fixed order at the step's end.
+    // the search and the pair forces: each warp searches four slaves at a time, eight lanes
+    // each, and the groups' first lanes then compute the four pairs' forces side by side (long
+    // dependent chains of divisions). The totals are per-block partials, folded in a fixed
+    // order at the step's end.
     {
         double energy = 0.0, diss = 0.0;
         const int warpsTotal = gridDim.x * CB_WARPS;
-        const int lane = threadIdx.x & 31;
-        int mine = -1, mySeg = -1;
-        double myBest = 0.0;
-        bool myFell = false;
-        int r = 0;
-        for (int i = (threadIdx.x >> 5) * gridDim.x + blockIdx.x; i < nodes; i += warpsTotal) {
+        const int group = (threadIdx.x & 31) / SG;
+        for (int w = (threadIdx.x >> 5) * gridDim.x + blockIdx.x; w * (32 / SG) < nodes;
+             w += warpsTotal) {
+            const int slot = w * (32 / SG) + group;
             double best;
             int seg;
             bool fell;
-            search_slave(d, g, i, best, seg, fell);
-            if (r == lane) {
-                mine = i;
-                myBest = best;
-                mySeg = seg;
-                myFell = fell;
-            }
-            if (++r == 32) {
-                if (mine >= 0) finish_slave(d, mine, myBest, mySeg, myFell, energy, diss);
-                mine = -1;
-                r = 0;
-            }
+            search_group(d, g, slot, nodes, best, seg, fell);
+            if ((threadIdx.x & (SG - 1)) == 0 && slot < nodes)
+                finish_slave(d, slot, best, seg, fell, energy, diss);
         }
-        if (mine >= 0) finish_slave(d, mine, myBest, mySeg, myFell, energy, diss);
         const double e1 = block_sum_c(energy, shd);
         const double e2 = block_sum_c(diss, shd);
         if (threadIdx.x == 0) {
