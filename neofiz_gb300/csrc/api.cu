@@ -482,6 +482,14 @@ nf_status nf_create(const nf_mesh *mesh, const nf_material *materials, int32_t m
     A(d.partials, (size_t)PARTIAL_SLOTS * d.maxBlocks);
     A(d.edgeGroup, 4LL * E); A(d.groupStart, groupStart.size()); A(d.groupMember, 4LL * E);
     A(d.s, 1);
+    // the Johnson-Cook work list of the FP64 one-point element pass
+    bool anyJC = false;
+    for (int m = 0; m < material_count; m++) anyJC = anyJC || mats[m].jc != 0;
+    if (anyJC && !d.full && E > 0) {
+        d.hotCap = std::max(1024, (E / 4 + 127) & ~127);
+        d.hotSmem = listed_pass_smem(S->device);
+        A(d.hot, 1); A(d.hotList, d.hotCap); A(d.hotNext, d.hotCap); A(d.hotStamp, E);
+    }
 #undef A
     const cudaError_t e_ = arena.commit(*S);
     if (e_ != cudaSuccess) {
@@ -504,6 +512,10 @@ nf_status nf_create(const nf_mesh *mesh, const nf_material *materials, int32_t m
     upload(*S, d.groupStart, groupStart.data(), groupStart.size());
     upload(*S, d.groupMember, groupMember.data(), groupMember.size());
     upload(*S, d.s, &s0, 1);
+    if (d.hot) {
+        const HotList h0{0, 0, 1, 0};          // listing stamps start at 0: nothing listed
+        upload(*S, d.hot, &h0, 1);
+    }
     d.scanTmpSize = (int)scanInts;
     d.scanTmp = nullptr;
     nf_status st = sync_check(*S);
@@ -539,7 +551,8 @@ nf_status nf_destroy(nf_solver *h) {
                     d.pairEnergy, d.pairDiss, d.incCount, d.incStart, d.incCursor, d.incEntry,
                     d.scanTmp, d.s, d.matsF, d.sigF, d.backF, d.epsPF, d.wPF, d.hgKF,
                     d.contribF, d.hgF, d.dStrF, d.dSoftF, d.dWidthF, d.dFailF, d.dGfF, d.dGeomF,
-                    d.pMid, d.pCur, d.vdt, d.gaussVol, d.coopSums, d.incSlots, d.bucketA, d.bucketN, d.slaveXY};
+                    d.pMid, d.pCur, d.vdt, d.gaussVol, d.coopSums, d.incSlots, d.bucketA, d.bucketN, d.slaveXY,
+                    d.hot, d.hotList, d.hotNext, d.hotStamp};
     const char *a0 = static_cast<const char *>(S->arena), *a1 = a0 + S->arenaBytes;
     for (void *p : ptrs) {
         const char *c = static_cast<const char *>(p);

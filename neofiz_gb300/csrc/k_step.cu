@@ -208,6 +208,91 @@ __global__ void __launch_bounds__(BLOCK) k_element_reduced(Dev d, int zeroStrain
     min_edge_commit(d, minEdge);
 }
 
+// reducedIntegration over the Johnson-Cook work list: threads [0, count) take the listed
+// elements in list order (most expensive cost class first, so warps hold points of equal solve
+// length and the longest start first), threads [count, count + E) take every element not
+// listed; each element is computed once, by the same code as k_element_reduced. Each warp
+// appends its points' cost classes for the next step's list.
+__global__ void __launch_bounds__(BLOCK) k_element_reduced_listed(Dev d, int zeroStrain) {
+    if (!d.s->active) return;
+    const HotList *h = d.hot;
+    const int listed = h->count;
+    const int g = blockIdx.x * blockDim.x + threadIdx.x;
+    int e = -1;
+    if (g < listed) {
+        e = d.hotList[g];
+    } else if (g - listed < d.E) {
+        const int c = g - listed;
+        if (d.hotStamp[c] != h->epoch) e = c;
+    }
+    double minEdge = DMAX;
+    int cost = 0;
+    if (e >= 0) element_reduced(d, e, zeroStrain ? 0.0 : d.s->dt, d.hourglass, minEdge, &cost);
+    const unsigned want = __ballot_sync(0xffffffffu, cost > 0);
+    if (want) {
+        const int lane = threadIdx.x & 31, leader = __ffs(want) - 1;
+        int base = 0;
+        if (lane == leader) base = atomicAdd(&d.hot->nextCount, __popc(want));
+        base = __shfl_sync(0xffffffffu, base, leader);
+        if (cost > 0) {
+            const int pos = base + __popc(want & ((1u << lane) - 1u));
+            if (pos < d.hotCap) d.hotNext[pos] = make_int2(e, min(cost, HOT_CLASSES - 1));
+        }
+    }
+    min_edge_commit(d, minEdge);
+}
+
+// Dynamic shared memory (unused) that the listed pass requests so that at most two of its
+// blocks share an SM: eight warps per SM keep the FP64 pipe busy, and a listed warp with a long
+// Johnson-Cook solve competes with seven others for it instead of eleven. Needs the device
+// current; sets the kernel's attribute.
+int listed_pass_smem(int device) {
+    int perSm = 0, optin = 0;
+    if (cudaDeviceGetAttribute(&perSm, cudaDevAttrMaxSharedMemoryPerMultiprocessor, device) != cudaSuccess ||
+        cudaDeviceGetAttribute(&optin, cudaDevAttrMaxSharedMemoryPerBlockOptin, device) != cudaSuccess)
+        return 0;
+    const int smem = perSm / 3 + 2048;
+    if (smem > optin || 2 * (smem + 1024) > perSm) return 0;
+    if (cudaFuncSetAttribute(k_element_reduced_listed, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                             smem) != cudaSuccess)
+        return 0;
+    return smem;
+}
+
+// The next step's work list from the entries the pass appended: a counting sort by cost class,
+// most expensive first; listed elements are stamped with the new epoch.
+__global__ void __launch_bounds__(1024) k_hot_build(Dev d) {
+    if (!d.s->active) return;
+    __shared__ int count[HOT_CLASSES], start[HOT_CLASSES];
+    HotList *h = d.hot;
+    const int n = min(h->nextCount, d.hotCap);
+    const int epoch = h->epoch + 1;
+    for (int k = threadIdx.x; k < HOT_CLASSES; k += blockDim.x) count[k] = 0;
+    __syncthreads();
+    for (int i = threadIdx.x; i < n; i += blockDim.x) atomicAdd(&count[d.hotNext[i].y], 1);
+    __syncthreads();
+    if (threadIdx.x == 0) {
+        int acc = 0;
+        for (int k = HOT_CLASSES - 1; k >= 0; k--) {
+            start[k] = acc;
+            acc += count[k];
+        }
+    }
+    __syncthreads();
+    for (int i = threadIdx.x; i < n; i += blockDim.x) {
+        const int2 it = d.hotNext[i];
+        const int pos = atomicAdd(&start[it.y], 1);
+        d.hotList[pos] = it.x;
+        d.hotStamp[it.x] = epoch;
+    }
+    __syncthreads();
+    if (threadIdx.x == 0) {
+        h->count = n;
+        h->epoch = epoch;
+        h->nextCount = 0;
+    }
+}
+
 // fullIntegration, ExplicitSolver.java:1219-1339
 __global__ void __launch_bounds__(BLOCK) k_element_full(Dev d, int zeroStrain) {
     if (!d.s->active) return;
@@ -455,9 +540,18 @@ static int assemble(Solver &S, int zeroStrain, bool prepared = false) {
         if (!prepared) n += launch_prepare_mixed(S, zeroStrain);
         n += launch_element_mixed(S, zeroStrain);
     } else if (d.E > 0) {
-        if (d.full) k_element_full<<<grid_for(d.E, BLOCK), BLOCK, 0, st>>>(d, zeroStrain);
-        else k_element_reduced<<<grid_for(d.E, BLOCK), BLOCK, 0, st>>>(d, zeroStrain);
-        n++;
+        if (d.full) {
+            k_element_full<<<grid_for(d.E, BLOCK), BLOCK, 0, st>>>(d, zeroStrain);
+            n++;
+        } else if (d.hot) {
+            k_element_reduced_listed<<<grid_for(d.E + d.hotCap, BLOCK), BLOCK, d.hotSmem, st>>>(
+                d, zeroStrain);
+            k_hot_build<<<1, 1024, 0, st>>>(d);
+            n += 2;
+        } else {
+            k_element_reduced<<<grid_for(d.E, BLOCK), BLOCK, 0, st>>>(d, zeroStrain);
+            n++;
+        }
     }
     S.mark(NF_GROUP_ELEMENT, false);
     if (d.K > 0) {

@@ -141,8 +141,10 @@ static __device__ __forceinline__ void prepare_node(const Dev &d, int i, double 
 // reducedIntegration, ExplicitSolver.java:1373-1504, for element e: B at the centroid, strain
 // increments, Cayley co-rotation, J2/Johnson-Cook return, FB hourglass, the eight force
 // terms into the element's contribution slots; folds its shortest edge into minEdge.
+// *cost (when given) receives the point's Johnson-Cook cost class (j2_update).
 static __device__ __forceinline__ void element_reduced(const Dev &d, int e, double strainDt,
-                                                       double hourglass, double &minEdge) {
+                                                       double hourglass, double &minEdge,
+                                                       int *cost = nullptr) {
     double *ef = d.contribution + 8 * (size_t)e;
     if (d.gone != nullptr && d.gone[e]) {
         for (int k = 0; k < 8; k++) ef[k] = 0.0;
@@ -225,10 +227,10 @@ static __device__ __forceinline__ void element_reduced(const Dev &d, int e, doub
             dr.fractureEnergy = d.dGf[e];
             dr.youngs = fl.youngs;
             j2_update(sg, bk, epsP, work, dEpsR, dEpsZ, dEpsT, dGamRZ, lambda, mu, fl,
-                      strainDt, &dr, d.dStrength[e], d.dSoft[e]);
+                      strainDt, &dr, d.dStrength[e], d.dSoft[e], cost);
         } else {
             j2_update(sg, bk, epsP, work, dEpsR, dEpsZ, dEpsT, dGamRZ, lambda, mu, fl,
-                      strainDt, (const DamageRef *)nullptr, 0.0, 0.0);
+                      strainDt, (const DamageRef *)nullptr, 0.0, 0.0, cost);
         }
         {
             double2 *ps = reinterpret_cast<double2 *>(d.sig + 4 * (size_t)e);

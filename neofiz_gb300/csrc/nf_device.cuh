@@ -130,10 +130,10 @@ __device__ __forceinline__ T jc_quasiStatic(const MatT<T> &f, T eps, T temperatu
     return jc_strainTerm(f, eps) * jc_thermalTerm(f, temperature);
 }
 
-// J2.solve, J2.java:332-375
+// J2.solve, J2.java:332-375. *iterations (when given) receives the iterations taken.
 template <typename T>
 static __device__ __noinline__ T j2_solve(T norm, T stiffness, T plasticStrain, T temperature,
-                                          T dt, const MatT<T> &jc) {
+                                          T dt, const MatT<T> &jc, int *iterations = nullptr) {
     const T thermal = jc_thermalTerm(jc, temperature);
     const T tolerance = Fn<T>::tolerance * jc.a;
     T lo = T(0);
@@ -147,7 +147,10 @@ static __device__ __noinline__ T j2_solve(T norm, T stiffness, T plasticStrain, 
         const T rateFactor = jc_rateTerm(jc, rate);
         const T g = norm - stiffness * dGamma - T(SQRT_2_3) * strain * rateFactor * thermal;
         if (g > T(0)) lo = dGamma; else hi = dGamma;
-        if (Fn<T>::abs(g) <= tolerance) return dGamma;
+        if (Fn<T>::abs(g) <= tolerance) {
+            if (iterations) *iterations = iteration + 1;
+            return dGamma;
+        }
         T slope = -stiffness
                   - T(TWO_THIRDS) * (jc.n * (strain - jc.a) / eps) * rateFactor * thermal;
         if (!(rate <= jc.refRate)) {
@@ -157,6 +160,7 @@ static __device__ __noinline__ T j2_solve(T norm, T stiffness, T plasticStrain, 
         if (!(next > lo && next < hi)) next = T(0.5) * (lo + hi);
         dGamma = next;
     }
+    if (iterations) *iterations = SOLVE_ITERATIONS;
     return dGamma;
 }
 
@@ -187,11 +191,14 @@ static __device__ __noinline__ void damage_begin(const DamageRefT<T> &d, T flowS
 
 // J2.update, J2.java:163-296. s[4] and bk[4] are the point's stress and back stress
 // ({rr, zz, tt, rz}); damage is null for a material that cannot fail, in which case
-// dStrength/dSoft are ignored. Returns the plastic multiplier.
+// dStrength/dSoft are ignored. Returns the plastic multiplier. *cost (when given) receives
+// the point's Johnson-Cook cost class: 0 none, 1 the quasi-static flow stress evaluated its
+// power laws, 1 + k a return-map solve of k iterations.
 template <typename T>
 __device__ __forceinline__ T j2_update(T *s, T *bk, T &epsP, T &work, T dRR, T dZZ, T dTT,
                                        T dGamRZ, T lambda, T mu, const MatT<T> &flow, T strainDt,
-                                       const DamageRefT<T> *damage, T dStrength, T dSoft) {
+                                       const DamageRefT<T> *damage, T dStrength, T dSoft,
+                                       int *cost = nullptr) {
     const T lt = lambda * (dRR + dZZ + dTT);
     const T tRR = s[0] + lt + T(2) * mu * dRR;
     const T tZZ = s[1] + lt + T(2) * mu * dZZ;
@@ -223,6 +230,7 @@ __device__ __forceinline__ T j2_update(T *s, T *bk, T &epsP, T &work, T dRR, T d
         hardening = flow.hIso;
     } else {
         flowStress = jc_quasiStatic(flow, epsP, temperature);
+        if (cost && (epsP > T(0) || work > T(0))) *cost = 1;
     }
     const T radius = T(SQRT_2_3) * flowStress;
 
@@ -242,7 +250,10 @@ __device__ __forceinline__ T j2_update(T *s, T *bk, T &epsP, T &work, T dRR, T d
             dGamma = norm / stiffness;
         }
     } else {
-        dGamma = j2_solve(norm, stiffness, epsP, temperature, strainDt, flow);
+        int iterations = 0;
+        dGamma = j2_solve(norm, stiffness, epsP, temperature, strainDt, flow,
+                          cost ? &iterations : nullptr);
+        if (cost) *cost = 1 + iterations;
     }
     const T inv = T(1) / norm;
     const T nRR = xRR * inv, nZZ = xZZ * inv, nTT = xTT * inv, nRZ = xRZ * inv;

@@ -68,6 +68,22 @@ struct DevScalars {
     int incOverflow;                         // a node's incident terms outgrew its fixed list
 };
 
+// The element pass's Johnson-Cook work list (FP64 reduced integration). Points whose return
+// map evaluated the Johnson-Cook power laws in one step are listed for the next, ordered by
+// cost class (solve iterations) from the most expensive down; the next element pass runs the
+// listed elements first, packed into warps of equal cost, then every other element. A warp
+// issues at most one FP64 instruction per 64 cycles and the SM's pipe takes one per 19, so a
+// long solve is a serial chain whose time grows with the warps sharing its SM: the pass runs
+// with two blocks per SM (eight warps) and the longest solves start first. The elements'
+// results do not depend on the order they are computed in.
+constexpr int HOT_CLASSES = 2 + 25;          // 0 none, 1 flow-stress powers, 1 + iterations
+struct HotList {
+    int count;                               // listed elements in this step's order
+    int nextCount;                           // entries appended by this step's pass
+    int epoch;                               // stamp of this step's listed elements
+    int pad;
+};
+
 struct Dev {
     // sizes and switches
     int N, E, K, ppe;
@@ -140,6 +156,12 @@ struct Dev {
     // scan workspace; the cooperative contact pass's grid and its per-block scan sums
     int32_t *scanTmp;
     int scanTmpSize;
+    // Johnson-Cook work list (null when no material is Johnson-Cook)
+    HotList *hot;
+    int32_t *hotList, *hotStamp;             // [hotCap] element order, [E] listing epoch
+    int2 *hotNext;                           // [hotCap] (element, cost class) appended
+    int hotCap;
+    int hotSmem;                             // the listed pass's occupancy-limiting request
     int coopBlocks;
     int32_t *coopSums;
     DevScalars *s;
@@ -351,6 +373,7 @@ int launch_contact(Solver &S, bool predicated);
 int scan_exclusive(const int32_t *in, int32_t *out, int n, int32_t *totalOut, int32_t *tmp,
                    cudaStream_t stream, const int *pred, const int *nDev);
 int contact_coop_blocks(int sms);
+int listed_pass_smem(int device);
 size_t scan_tmp_ints(int n);
 
 int grid_for(long long n, int block);
