@@ -269,7 +269,15 @@ __global__ void __launch_bounds__(1024) k_hot_build(Dev d) {
     const int epoch = h->epoch + 1;
     for (int k = threadIdx.x; k < HOT_CLASSES; k += blockDim.x) count[k] = 0;
     __syncthreads();
-    for (int i = threadIdx.x; i < n; i += blockDim.x) atomicAdd(&count[d.hotNext[i].y], 1);
+    // lanes of a warp holding the same class add to its counter once (few classes, many
+    // entries: per-entry atomics on a handful of shared words would serialise)
+    const int lane = threadIdx.x & 31;
+    for (int base = threadIdx.x - lane; base < n; base += blockDim.x) {
+        const int i = base + lane;
+        const int cls = i < n ? d.hotNext[i].y : -1;
+        const unsigned peers = __match_any_sync(0xffffffffu, cls);
+        if (cls >= 0 && lane == __ffs(peers) - 1) atomicAdd(&count[cls], __popc(peers));
+    }
     __syncthreads();
     if (threadIdx.x == 0) {
         int acc = 0;
@@ -279,11 +287,19 @@ __global__ void __launch_bounds__(1024) k_hot_build(Dev d) {
         }
     }
     __syncthreads();
-    for (int i = threadIdx.x; i < n; i += blockDim.x) {
-        const int2 it = d.hotNext[i];
-        const int pos = atomicAdd(&start[it.y], 1);
-        d.hotList[pos] = it.x;
-        d.hotStamp[it.x] = epoch;
+    for (int base = threadIdx.x - lane; base < n; base += blockDim.x) {
+        const int i = base + lane;
+        const int2 it = i < n ? d.hotNext[i] : make_int2(-1, -1);
+        const unsigned peers = __match_any_sync(0xffffffffu, it.y);
+        const int leader = __ffs(peers) - 1;
+        int first = 0;
+        if (it.y >= 0 && lane == leader) first = atomicAdd(&start[it.y], __popc(peers));
+        first = __shfl_sync(0xffffffffu, first, leader);
+        if (it.y >= 0) {
+            const int pos = first + __popc(peers & ((1u << lane) - 1u));
+            d.hotList[pos] = it.x;
+            d.hotStamp[it.x] = epoch;
+        }
     }
     __syncthreads();
     if (threadIdx.x == 0) {
@@ -462,32 +478,39 @@ __global__ void __launch_bounds__(BLOCK) k_gather(Dev d) {
 
 // ------------------------------------------------------------------------------------ end of step
 
-// Deterministic sum of n partials by one block: thread t adds partials t, t + B, t + 2B, ...
-// in that order, then the block's fixed tree adds the threads. Same inputs, same result.
-__device__ double fold(const double *p, int n, double *sh) {
-    double v = 0.0;
-    for (int k = threadIdx.x; k < n; k += blockDim.x) v += p[k];
-    return block_sum(v, sh);      // valid in thread 0
-}
+// Deterministic sums of the per-block partials: lane l of a warp adds partials l, l + 32, ...
+// in that order, then the warp's fixed tree adds the lanes. Same inputs, same result.
 
 // Folds the block partials, then the adaptive CFL step (:985-990).
 __global__ void __launch_bounds__(256) k_end(Dev d, int nodeBlocks, int elemBlocks,
                                             int slotBlocks, int updateDt) {
-    __shared__ double sh[256 / 32];
+    __shared__ double folded[6];
     DevScalars *s = d.s;
     if (!s->active) return;
-    double w0 = 0.0, w1 = 0.0, w2 = 0.0, er = 0.0, c0 = 0.0, c1 = 0.0;
-    if (updateDt && d.hasWall) {
-        w0 = fold(d.partials + (PARTIAL_WALL + 0) * d.maxBlocks, nodeBlocks, sh);
-        w1 = fold(d.partials + (PARTIAL_WALL + 1) * d.maxBlocks, nodeBlocks, sh);
-        w2 = fold(d.partials + (PARTIAL_WALL + 2) * d.maxBlocks, nodeBlocks, sh);
-    }
-    if (updateDt && d.hasErosion) er = fold(d.partials + PARTIAL_ERODE * d.maxBlocks, elemBlocks, sh);
-    if (d.hasContact) {
-        c0 = fold(d.partials + (PARTIAL_CONTACT + 0) * d.maxBlocks, slotBlocks, sh);
-        c1 = fold(d.partials + (PARTIAL_CONTACT + 1) * d.maxBlocks, slotBlocks, sh);
+    // the six per-block partial lists, one warp each: lane-strided sums, then a fixed tree
+    {
+        const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
+        const double *src = nullptr;
+        int count = 0;
+        if (warp < 3 && updateDt && d.hasWall) {
+            src = d.partials + (PARTIAL_WALL + warp) * d.maxBlocks;
+            count = nodeBlocks;
+        } else if (warp == 3 && updateDt && d.hasErosion) {
+            src = d.partials + PARTIAL_ERODE * d.maxBlocks;
+            count = elemBlocks;
+        } else if ((warp == 4 || warp == 5) && d.hasContact) {
+            src = d.partials + (PARTIAL_CONTACT + warp - 4) * d.maxBlocks;
+            count = slotBlocks;
+        }
+        double v = 0.0;
+        for (int k = lane; k < count; k += 32) v += src[k];
+        for (int o = 16; o > 0; o >>= 1) v += __shfl_down_sync(0xffffffffu, v, o);
+        if (lane == 0 && warp < 6) folded[warp] = v;
+        __syncthreads();
     }
     if (threadIdx.x != 0) return;
+    const double w0 = folded[0], w1 = folded[1], w2 = folded[2], er = folded[3];
+    const double c0 = folded[4], c1 = folded[5];
     if (updateDt && d.hasWall) {
         s->wImpulse += w0;
         s->wEnergyLoss += w1;
