@@ -30,9 +30,12 @@ sys.path.insert(0, HERE)
 CELL = 0.114e-3
 GAP = 0.5e-3
 L2_FLUSH_BYTES = 256 << 20
-# DRAM bytes (read + write) of one k_element_reduced launch of this workload after 300 steps,
-# from ncu (profiles/launches_perforation_200k_fp64.md; ncu cannot run inside the timed bench)
-ELEMENT_TRAFFIC_BYTES = {CELL: 39_627_008 + 108_032}
+# DRAM bytes (read + write) of one element-pass launch of this workload after 300 steps, and
+# its FP64 pipe use, from ncu (profiles/k_element_reduced_listed_perforation_200k_fp64.md;
+# ncu cannot run inside the timed bench)
+ELEMENT_TRAFFIC_BYTES = {CELL: 40_463_872 + 96_256}
+ELEMENT_FP64_PIPE = {CELL: {"active_pct": 76.6, "fp64_warp_instructions": 3_073_490,
+                            "all_warp_instructions": 18_741_510}}
 
 
 def parse():
@@ -284,7 +287,7 @@ def run_ours(args, world, rank, local):
                 "eroded_during_timing": eroded1 - eroded0,
             },
             "roofline": {
-                "bound": "hbm", "kernel": "k_element_reduced",
+                "bound": "hbm", "kernel": "k_element_reduced_listed",
                 "achieved": achieved, "peak": peaks.get("hbm_gbs"), "unit": "GB/s",
                 "frac": (achieved / peaks["hbm_gbs"]) if achieved else None,
                 "peak_source": peak_kind,
@@ -292,6 +295,7 @@ def run_ours(args, world, rank, local):
                 "traffic": ELEMENT_TRAFFIC_BYTES.get(args.cell),
                 "traffic_source": "ncu dram__bytes_read.sum + dram__bytes_write.sum, one launch",
                 "note": "FP64 arithmetic, not HBM, bounds this kernel on GB300",
+                "fp64_pipe_ncu": ELEMENT_FP64_PIPE.get(args.cell),
                 "group_ms_per_step": per_step, "top_group": top,
             },
             "cpu_baseline": cpu,

@@ -259,6 +259,8 @@ int listed_pass_smem(int device) {
     return smem;
 }
 
+constexpr int HOT_BATCH = 8;
+
 // The next step's work list from the entries the pass appended: a counting sort by cost class,
 // most expensive first; listed elements are stamped with the new epoch.
 __global__ void __launch_bounds__(1024) k_hot_build(Dev d) {
@@ -270,13 +272,22 @@ __global__ void __launch_bounds__(1024) k_hot_build(Dev d) {
     for (int k = threadIdx.x; k < HOT_CLASSES; k += blockDim.x) count[k] = 0;
     __syncthreads();
     // lanes of a warp holding the same class add to its counter once (few classes, many
-    // entries: per-entry atomics on a handful of shared words would serialise)
+    // entries: per-entry atomics on a handful of shared words would serialise); each thread
+    // loads HOT_BATCH entries before using them, so their loads overlap
     const int lane = threadIdx.x & 31;
-    for (int base = threadIdx.x - lane; base < n; base += blockDim.x) {
-        const int i = base + lane;
-        const int cls = i < n ? d.hotNext[i].y : -1;
-        const unsigned peers = __match_any_sync(0xffffffffu, cls);
-        if (cls >= 0 && lane == __ffs(peers) - 1) atomicAdd(&count[cls], __popc(peers));
+    const int stride = blockDim.x, span = HOT_BATCH * stride;
+    for (int base = threadIdx.x - lane; base < n; base += span) {
+        int cls[HOT_BATCH];
+#pragma unroll
+        for (int k = 0; k < HOT_BATCH; k++) {
+            const int i = base + k * stride + lane;
+            cls[k] = i < n ? d.hotNext[i].y : -1;
+        }
+#pragma unroll
+        for (int k = 0; k < HOT_BATCH; k++) {
+            const unsigned peers = __match_any_sync(0xffffffffu, cls[k]);
+            if (cls[k] >= 0 && lane == __ffs(peers) - 1) atomicAdd(&count[cls[k]], __popc(peers));
+        }
     }
     __syncthreads();
     if (threadIdx.x == 0) {
@@ -287,18 +298,25 @@ __global__ void __launch_bounds__(1024) k_hot_build(Dev d) {
         }
     }
     __syncthreads();
-    for (int base = threadIdx.x - lane; base < n; base += blockDim.x) {
-        const int i = base + lane;
-        const int2 it = i < n ? d.hotNext[i] : make_int2(-1, -1);
-        const unsigned peers = __match_any_sync(0xffffffffu, it.y);
-        const int leader = __ffs(peers) - 1;
-        int first = 0;
-        if (it.y >= 0 && lane == leader) first = atomicAdd(&start[it.y], __popc(peers));
-        first = __shfl_sync(0xffffffffu, first, leader);
-        if (it.y >= 0) {
-            const int pos = first + __popc(peers & ((1u << lane) - 1u));
-            d.hotList[pos] = it.x;
-            d.hotStamp[it.x] = epoch;
+    for (int base = threadIdx.x - lane; base < n; base += span) {
+        int2 it[HOT_BATCH];
+#pragma unroll
+        for (int k = 0; k < HOT_BATCH; k++) {
+            const int i = base + k * stride + lane;
+            it[k] = i < n ? d.hotNext[i] : make_int2(-1, -1);
+        }
+#pragma unroll
+        for (int k = 0; k < HOT_BATCH; k++) {
+            const unsigned peers = __match_any_sync(0xffffffffu, it[k].y);
+            const int leader = __ffs(peers) - 1;
+            int first = 0;
+            if (it[k].y >= 0 && lane == leader) first = atomicAdd(&start[it[k].y], __popc(peers));
+            first = __shfl_sync(0xffffffffu, first, leader);
+            if (it[k].y >= 0) {
+                const int pos = first + __popc(peers & ((1u << lane) - 1u));
+                d.hotList[pos] = it[k].x;
+                d.hotStamp[it[k].x] = epoch;
+            }
         }
     }
     __syncthreads();
