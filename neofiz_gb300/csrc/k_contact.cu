@@ -277,11 +277,14 @@ __device__ __forceinline__ bool excluded(const Dev &d, int i, int n, int s) {
 }
 
 // Contact.depth, Contact.java:642-652
+// The segment's unit tangent (cr[b] - cr[a]) / len, (cz[b] - cz[a]) / len is (-snz, snr) bit
+// for bit: the geometry phase formed snr = dz / len and snz = -dr / len from the same sums
+// (cr = x0 + u), and (-dr) / len is -(dr / len) exactly. Reading it saves two divisions.
 __device__ __forceinline__ double depth_of(const Dev &d, int n, int s) {
-    const int a = d.segA[s], b = d.segB[s];
+    const int a = d.segA[s];
     const double len = d.slen[s];
     if (len <= 0.0) return 0.0;
-    const double tr = (d.cr[b] - d.cr[a]) / len, tz = (d.cz[b] - d.cz[a]) / len;
+    const double tr = -d.snz[s], tz = d.snr[s];
     const double dr = d.cr[n] - d.cr[a], dz = d.cz[n] - d.cz[a];
     const double along = dr * tr + dz * tz;
     if (along < 0.0 || along > len) return 0.0;
@@ -307,8 +310,8 @@ __device__ void resolve_pair(const Dev &d, int i, int n, int s, double &energy, 
     const int a = d.segA[s], b = d.segB[s];
     const double depth = depth_of(d, n, s);
     const double len = d.slen[s];
-    const double tr = (d.cr[b] - d.cr[a]) / len;            // parameter, :655-661
-    const double tz = (d.cz[b] - d.cz[a]) / len;
+    const double tr = -d.snz[s];                            // parameter, :655-661 (the
+    const double tz = d.snr[s];                             // tangent as in depth_of)
     const double t = ((d.cr[n] - d.cr[a]) * tr + (d.cz[n] - d.cz[a]) * tz) / len;
     const double wa = 1.0 - t, wb = t;
     const double ma = d.mass[a], mb = d.mass[b];

@@ -8,6 +8,7 @@ determinism (ThreadingTest) and the published Taylor-impact table (README.md:306
 Citations are to src/test/java/org/neofiz/ in the reference.
 """
 import math
+import os
 
 import numpy as np
 import pytest
@@ -476,6 +477,20 @@ def test_threads_are_bit_identical():
 
 
 # ----------------------------------------------------------------------------- math layer
+
+def test_math_tables_match_their_generator():
+    """nf_math_tables.h is what gen_nf_math_tables.py computes (every entry an exact value
+    rounded to double)."""
+    pytest.importorskip("mpmath")
+    import subprocess
+    import sys
+    csrc = os.path.join(os.path.dirname(os.path.dirname(os.path.abspath(__file__))),
+                        "neofiz_gb300", "csrc")
+    out = subprocess.run([sys.executable, "gen_nf_math_tables.py"], cwd=csrc,
+                         capture_output=True, text=True, check=True).stdout
+    with open(os.path.join(csrc, "nf_math_tables.h")) as f:
+        assert out.strip() == f.read().strip()
+
 
 @pytest.mark.parametrize("name,gen", [
     ("log", lambda r: (math.exp(r.uniform(-700, 700)),)),
