@@ -108,13 +108,29 @@ class DefectField:
         wz = np.exp(-((gz[:, None] - (j0[:, None] + k)) ** 2) / two)
         norm = np.sqrt((wr * wr).sum(axis=1) * (wz * wz).sum(axis=1))
         out = np.empty(r.size)
+        if r.size == 0:
+            return out
+        # The noise of a lattice site is the same for every point whose window covers it: when
+        # the windows' lattice box is small (a mesh much finer than the lattice), evaluate each
+        # site once and gather; the sums below are the same either way.
+        ilo, jlo = int(i0.min()), int(j0.min())
+        ni, nj = int(i0.max()) - ilo + taps, int(j0.max()) - jlo + taps
+        grid = None
+        if ni * nj <= min(r.size * taps * taps, 1 << 26):
+            gi = np.arange(ilo, ilo + ni, dtype=np.int64)
+            gj = np.arange(jlo, jlo + nj, dtype=np.int64)
+            grid = self.white(np.broadcast_to(gi[None, :], (nj, ni)),
+                              np.broadcast_to(gj[:, None], (nj, ni)))
         chunk = 4096
         for s in range(0, r.size, chunk):
             e = min(r.size, s + chunk)
             ii = i0[s:e, None, None] + k[None, None, :]
             jj = j0[s:e, None, None] + k[None, :, None]
-            noise = self.white(np.broadcast_to(ii, (e - s, taps, taps)),
-                               np.broadcast_to(jj, (e - s, taps, taps)))
+            if grid is not None:
+                noise = grid[jj - jlo, ii - ilo]
+            else:
+                noise = self.white(np.broadcast_to(ii, (e - s, taps, taps)),
+                                   np.broadcast_to(jj, (e - s, taps, taps)))
             row = (noise * wr[s:e, None, :]).sum(axis=2)
             out[s:e] = (row * wz[s:e, :]).sum(axis=1)
         return out / norm
