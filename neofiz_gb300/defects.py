@@ -142,7 +142,11 @@ class DefectField:
         except ImportError:                       # pragma: no cover
             from math import erfc as _e
             erfc = np.vectorize(_e)
-        local_scale = self.base.scale * (np.asarray(volume) / self.referenceVolume) ** (
+        # one-dimensional arrays throughout: numpy evaluates a 0-d power by a different routine
+        # than an array's, and a point's value must not depend on how it was batched
+        volume = np.atleast_1d(np.asarray(volume, dtype=np.float64))
+        g = np.atleast_1d(np.asarray(g, dtype=np.float64))
+        local_scale = self.base.scale * (volume / self.referenceVolume) ** (
             -1.0 / self.base.modulus)
         c = np.clip(g, -self.CLAMP_SIGMA, self.CLAMP_SIGMA)
         cdf = 0.5 * erfc(-c / sqrt(2.0))
