@@ -464,8 +464,15 @@ nf_status nf_create(const nf_mesh *mesh, const nf_material *materials, int32_t m
     std::vector<int2> pe(K);
     for (int k = 0; k < K; k++)
         pe[k] = make_int2(mesh->pressure_edges[2 * k], mesh->pressure_edges[2 * k + 1]);
-    // partial-sum slots: the per-item grids (nodes, elements) and the fixed contact grid
-    d.maxBlocks = std::max(grid_for(std::max(std::max(N, E), 1), 128),
+    // the Johnson-Cook work list of the FP64 one-point element pass
+    bool anyJC = false;
+    for (int m = 0; m < material_count; m++) anyJC = anyJC || mats[m].jc != 0;
+    const bool listed = anyJC && !d.full && E > 0;
+    if (listed) d.hotCap = std::max(1024, (E / 4 + 127) & ~127);
+    // partial-sum slots: the per-item grids (nodes, elements, the listed element pass, which
+    // also erodes) and the fixed contact grid
+    d.maxBlocks = std::max(std::max(grid_for(std::max(std::max(N, E), 1), 128),
+                                    listed ? grid_for((long long)E + d.hotCap, 128) : 0),
                            std::max(d.coopBlocks, 8 * d.sms)) + 1;
     d.bucketCap = std::max(1 << 14, 2 * N);
     const size_t scanInts = scan_tmp_ints(std::max(std::max(4 * E, N + 1), d.bucketCap + 1)) + 16;
@@ -482,11 +489,7 @@ nf_status nf_create(const nf_mesh *mesh, const nf_material *materials, int32_t m
     A(d.partials, (size_t)PARTIAL_SLOTS * d.maxBlocks);
     A(d.edgeGroup, 4LL * E); A(d.groupStart, groupStart.size()); A(d.groupMember, 4LL * E);
     A(d.s, 1);
-    // the Johnson-Cook work list of the FP64 one-point element pass
-    bool anyJC = false;
-    for (int m = 0; m < material_count; m++) anyJC = anyJC || mats[m].jc != 0;
-    if (anyJC && !d.full && E > 0) {
-        d.hotCap = std::max(1024, (E / 4 + 127) & ~127);
+    if (listed) {
         d.hotSmem = listed_pass_smem(S->device);
         A(d.hot, 1); A(d.hotList, d.hotCap); A(d.hotNext, d.hotCap); A(d.hotStamp, E);
     }

@@ -149,13 +149,11 @@ int launch_point_volumes(Solver &S, double *out) {
 
 // ------------------------------------------------------------------------------------ erosion
 
-// erode, ExplicitSolver.java:663-691
-__global__ void __launch_bounds__(BLOCK) k_erode(Dev d) {
-    __shared__ double sh[BLOCK / 32];
-    if (!d.s->active) return;
-    double energy = 0.0;
-    for (int e = blockIdx.x * blockDim.x + threadIdx.x; e < d.E; e += gridDim.x * blockDim.x) {
-        if (d.gone[e]) continue;
+// erode, ExplicitSolver.java:663-691, for element e: its damage and signed current area
+// decide whether it goes; the strain energy it held is added to energy.
+__device__ __forceinline__ void erode_element(const Dev &d, int e, double &energy) {
+    if (d.gone[e]) return;
+    {
         bool failed = false;
         if (d.hasDamage) {                                  // elementDamage, :1764-1772
             double sum = 0.0;
@@ -185,6 +183,14 @@ __global__ void __launch_bounds__(BLOCK) k_erode(Dev d) {
             }
         }
     }
+}
+
+__global__ void __launch_bounds__(BLOCK) k_erode(Dev d) {
+    __shared__ double sh[BLOCK / 32];
+    if (!d.s->active) return;
+    double energy = 0.0;
+    for (int e = blockIdx.x * blockDim.x + threadIdx.x; e < d.E; e += gridDim.x * blockDim.x)
+        erode_element(d, e, energy);
     const double t = block_sum(energy, sh);
     if (threadIdx.x == 0) d.partials[PARTIAL_ERODE * d.maxBlocks + blockIdx.x] = t;
 }
@@ -212,8 +218,12 @@ __global__ void __launch_bounds__(BLOCK) k_element_reduced(Dev d, int zeroStrain
 // elements in list order (most expensive cost class first, so warps hold points of equal solve
 // length and the longest start first), threads [count, count + E) take every element not
 // listed; each element is computed once, by the same code as k_element_reduced. Each warp
-// appends its points' cost classes for the next step's list.
-__global__ void __launch_bounds__(BLOCK) k_element_reduced_listed(Dev d, int zeroStrain) {
+// appends its points' cost classes for the next step's list. With `erode` the pass first
+// decides each element's erosion (erode_element): an element's erosion reads only its own point
+// and nodes, which no other element's update writes, so deciding it just before the element's
+// own update is the same as a pass over all elements before any update.
+__global__ void __launch_bounds__(BLOCK) k_element_reduced_listed(Dev d, int zeroStrain, int erode) {
+    __shared__ double sh[BLOCK / 32];
     if (!d.s->active) return;
     const HotList *h = d.hot;
     const int listed = h->count;
@@ -225,8 +235,9 @@ __global__ void __launch_bounds__(BLOCK) k_element_reduced_listed(Dev d, int zer
         const int c = g - listed;
         if (d.hotStamp[c] != h->epoch) e = c;
     }
-    double minEdge = DMAX;
+    double minEdge = DMAX, energy = 0.0;
     int cost = 0;
+    if (erode && e >= 0) erode_element(d, e, energy);
     if (e >= 0) element_reduced(d, e, zeroStrain ? 0.0 : d.s->dt, d.hourglass, minEdge, &cost);
     const unsigned want = __ballot_sync(0xffffffffu, cost > 0);
     if (want) {
@@ -240,6 +251,10 @@ __global__ void __launch_bounds__(BLOCK) k_element_reduced_listed(Dev d, int zer
         }
     }
     min_edge_commit(d, minEdge);
+    if (erode) {
+        const double t = block_sum(energy, sh);
+        if (threadIdx.x == 0) d.partials[PARTIAL_ERODE * d.maxBlocks + blockIdx.x] = t;
+    }
 }
 
 // Dynamic shared memory (unused) that the listed pass requests so that at most two of its
@@ -572,7 +587,14 @@ __global__ void k_set_active(Dev d) {
 
 // ------------------------------------------------------------------------------------ launch
 
-static int assemble(Solver &S, int zeroStrain, bool prepared = false) {
+// The listed element pass erodes too (one pass instead of two over the elements) when the
+// step erodes and the pass is the FP64 one-point listed one.
+static bool erosion_fused(const Dev &d) { return d.hasErosion && d.E > 0 && d.hot && !d.mixed && !d.full; }
+static int eroding_blocks(const Solver &S) {
+    return erosion_fused(S.d) ? grid_for((long long)S.d.E + S.d.hotCap, BLOCK) : element_grid(S);
+}
+
+static int assemble(Solver &S, int zeroStrain, bool prepared = false, bool erode = false) {
     Dev &d = S.d;
     const cudaStream_t st = S.stream;
     int n = 0;
@@ -585,8 +607,8 @@ static int assemble(Solver &S, int zeroStrain, bool prepared = false) {
             k_element_full<<<grid_for(d.E, BLOCK), BLOCK, 0, st>>>(d, zeroStrain);
             n++;
         } else if (d.hot) {
-            k_element_reduced_listed<<<grid_for(d.E + d.hotCap, BLOCK), BLOCK, d.hotSmem, st>>>(
-                d, zeroStrain);
+            k_element_reduced_listed<<<grid_for((long long)d.E + d.hotCap, BLOCK), BLOCK,
+                                       d.hotSmem, st>>>(d, zeroStrain, erode ? 1 : 0);
             k_hot_build<<<1, 1024, 0, st>>>(d);
             n += 2;
         } else {
@@ -641,7 +663,8 @@ int launch_step(Solver &S, bool) {
         n++;
     }
     S.mark(NF_GROUP_NODAL, false);
-    if (d.hasErosion && d.E > 0) {
+    const bool fused = erosion_fused(d);
+    if (d.hasErosion && d.E > 0 && !fused) {
         S.mark(NF_GROUP_ERODE, true);
         if (d.mixed) n += launch_erode_mixed(S);
         else {
@@ -650,9 +673,9 @@ int launch_step(Solver &S, bool) {
         }
         S.mark(NF_GROUP_ERODE, false);
     }
-    n += assemble(S, 0, d.N > 0 && d.mixed);
+    n += assemble(S, 0, d.N > 0 && d.mixed, fused);
     S.mark(NF_GROUP_END, true);
-    k_end<<<1, 256, 0, st>>>(d, nodal_grid(S), element_grid(S), d.coopBlocks, 1);
+    k_end<<<1, 256, 0, st>>>(d, nodal_grid(S), eroding_blocks(S), d.coopBlocks, 1);
     n++;
     S.mark(NF_GROUP_END, false);
     return n;
