@@ -33,9 +33,9 @@ L2_FLUSH_BYTES = 256 << 20
 # DRAM bytes (read + write) of one element-pass launch of this workload after 300 steps, and
 # its FP64 pipe use, from ncu (profiles/k_element_reduced_listed_perforation_200k_fp64.md;
 # ncu cannot run inside the timed bench)
-ELEMENT_TRAFFIC_BYTES = {CELL: 40_463_872 + 96_256}
-ELEMENT_FP64_PIPE = {CELL: {"active_pct": 76.6, "fp64_warp_instructions": 3_073_490,
-                            "all_warp_instructions": 18_741_510}}
+ELEMENT_TRAFFIC_BYTES = {CELL: 40_489_984 + 62_976}
+ELEMENT_FP64_PIPE = {CELL: {"active_pct": 75.3, "fp64_warp_instructions": 3_307_977,
+                            "all_warp_instructions": 20_426_527}}
 
 
 def parse():
