@@ -516,7 +516,8 @@ nf_status nf_create(const nf_mesh *mesh, const nf_material *materials, int32_t m
     upload(*S, d.groupMember, groupMember.data(), groupMember.size());
     upload(*S, d.s, &s0, 1);
     if (d.hot) {
-        const HotList h0{0, 0, 1, 0};          // listing stamps start at 0: nothing listed
+        HotList h0{};                          // listing stamps start at 0: nothing listed
+        h0.epoch = 1;
         upload(*S, d.hot, &h0, 1);
     }
     d.scanTmpSize = (int)scanInts;

@@ -245,10 +245,14 @@ __global__ void __launch_bounds__(BLOCK) k_element_reduced_listed(Dev d, int zer
         int base = 0;
         if (lane == leader) base = atomicAdd(&d.hot->nextCount, __popc(want));
         base = __shfl_sync(0xffffffffu, base, leader);
-        if (cost > 0) {
-            const int pos = base + __popc(want & ((1u << lane) - 1u));
-            if (pos < d.hotCap) d.hotNext[pos] = make_int2(e, min(cost, HOT_CLASSES - 1));
-        }
+        const int cls = min(cost, HOT_CLASSES - 1);
+        const int pos = base + __popc(want & ((1u << lane) - 1u));
+        const bool kept = cost > 0 && pos < d.hotCap;
+        if (kept) d.hotNext[pos] = make_int2(e, cls);
+        // the kept entries per class, one atomic per class present in the warp
+        const int key = kept ? cls : -1;
+        const unsigned peers = __match_any_sync(0xffffffffu, key);
+        if (kept && lane == __ffs(peers) - 1) atomicAdd(&d.hot->classCount[cls], __popc(peers));
     }
     min_edge_commit(d, minEdge);
     if (erode) {
@@ -280,39 +284,23 @@ constexpr int HOT_BATCH = 8;
 // most expensive first; listed elements are stamped with the new epoch.
 __global__ void __launch_bounds__(1024) k_hot_build(Dev d) {
     if (!d.s->active) return;
-    __shared__ int count[HOT_CLASSES], start[HOT_CLASSES];
+    __shared__ int start[HOT_CLASSES];
     HotList *h = d.hot;
     const int n = min(h->nextCount, d.hotCap);
     const int epoch = h->epoch + 1;
-    for (int k = threadIdx.x; k < HOT_CLASSES; k += blockDim.x) count[k] = 0;
-    __syncthreads();
-    // lanes of a warp holding the same class add to its counter once (few classes, many
-    // entries: per-entry atomics on a handful of shared words would serialise); each thread
-    // loads HOT_BATCH entries before using them, so their loads overlap
-    const int lane = threadIdx.x & 31;
-    const int stride = blockDim.x, span = HOT_BATCH * stride;
-    for (int base = threadIdx.x - lane; base < n; base += span) {
-        int cls[HOT_BATCH];
-#pragma unroll
-        for (int k = 0; k < HOT_BATCH; k++) {
-            const int i = base + k * stride + lane;
-            cls[k] = i < n ? d.hotNext[i].y : -1;
-        }
-#pragma unroll
-        for (int k = 0; k < HOT_BATCH; k++) {
-            const unsigned peers = __match_any_sync(0xffffffffu, cls[k]);
-            if (cls[k] >= 0 && lane == __ffs(peers) - 1) atomicAdd(&count[cls[k]], __popc(peers));
-        }
-    }
-    __syncthreads();
-    if (threadIdx.x == 0) {
+    if (threadIdx.x == 0) {                  // the pass counted the classes as it appended
         int acc = 0;
         for (int k = HOT_CLASSES - 1; k >= 0; k--) {
             start[k] = acc;
-            acc += count[k];
+            acc += h->classCount[k];
         }
     }
     __syncthreads();
+    // lanes of a warp holding the same class take their positions with one atomic (few
+    // classes, many entries: per-entry atomics on a handful of shared words would serialise);
+    // each thread loads HOT_BATCH entries before using them, so their loads overlap
+    const int lane = threadIdx.x & 31;
+    const int stride = blockDim.x, span = HOT_BATCH * stride;
     for (int base = threadIdx.x - lane; base < n; base += span) {
         int2 it[HOT_BATCH];
 #pragma unroll
@@ -335,6 +323,7 @@ __global__ void __launch_bounds__(1024) k_hot_build(Dev d) {
         }
     }
     __syncthreads();
+    for (int k = threadIdx.x; k < HOT_CLASSES; k += blockDim.x) h->classCount[k] = 0;
     if (threadIdx.x == 0) {
         h->count = n;
         h->epoch = epoch;

@@ -82,6 +82,7 @@ struct HotList {
     int nextCount;                           // entries appended by this step's pass
     int epoch;                               // stamp of this step's listed elements
     int pad;
+    int classCount[HOT_CLASSES];             // the appended (and kept) entries per cost class
 };
 
 struct Dev {
