@@ -94,7 +94,7 @@ static __device__ __forceinline__ void nodal_node(const Dev &d, int i, const Nod
         d.flags[i] = (uint8_t)((fl & 3) | (onWall ? 4 : 0));
         d.wallState[i] = ws;
     }
-    if (!(isfinite(u.x) && isfinite(u.y) && isfinite(v.x) && isfinite(v.y)))
+    if (!(finite_bits(u.x) && finite_bits(u.y) && finite_bits(v.x) && finite_bits(v.y)))
         atomicOr(status, STATUS_NONFINITE);
     if (geo.pMid) {
         // the geometry of the coming assembly: mid-step and current positions as float

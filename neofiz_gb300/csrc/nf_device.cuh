@@ -108,6 +108,12 @@ __device__ __forceinline__ T jc_rateTerm(const MatT<T> &f, T rate) {
     // rate / 1 is rate exactly: the common reference rate of 1/s skips the division
     return T(1) + f.c * Fn<T>::log(f.refRate == T(1) ? rate : rate / f.refRate);
 }
+// isfinite by the exponent field (an integer test, off the FP64 pipe)
+__device__ __forceinline__ bool finite_bits(double x) {
+    return ((unsigned long long)__double_as_longlong(x) & 0x7ff0000000000000ULL) !=
+           0x7ff0000000000000ULL;
+}
+
 // x == +-0 by bit pattern for doubles (an integer test, off the FP64 pipe)
 __device__ __forceinline__ bool is_zero(double x) {
     return ((unsigned long long)__double_as_longlong(x) << 1) == 0ULL;
