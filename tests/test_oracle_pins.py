@@ -291,6 +291,59 @@ def test_hourglass_invisible_to_linear_fields(form):
     assert abs(on.hourglassEnergy()) <= on.strainEnergy() * 1e-12
 
 
+_UNIT = ([1.0, 2.0, 2.0, 1.0], [0.0, 0.0, 1.0, 1.0], [0, 1, 2, 3])
+
+
+def _hg_solver(mesh, q, integration=Integration.REDUCED):
+    s = OracleSolver(mesh, Material.STEEL_4340, Formulation.PLANE_STRAIN, integration, 1.0, 0.5)
+    s.setHourglassCoefficient(q)
+    return s
+
+
+def _hourglass(e):
+    return np.array([e, -e, e, -e])
+
+
+def test_the_hourglass_mode_is_free_without_control():
+    """HourglassTest.theModeIsFreeWithoutControl (:121-148)."""
+    mesh = QuadMesh(*_UNIT)
+    e = 1.0e-4
+    cheap = _impose(_hg_solver(mesh, 0.0), _hourglass(e), np.zeros(4))
+    expensive = _impose(_hg_solver(mesh, 0.0, Integration.FULL), _hourglass(e), np.zeros(4))
+    scale = np.linalg.norm(_impose(_hg_solver(mesh, 0.0), e * np.asarray(mesh.r), np.zeros(4)))
+    assert np.linalg.norm(cheap) < scale * 1e-12
+    assert np.linalg.norm(expensive) > scale * 0.1
+
+
+def test_hourglass_control_opposes_the_mode():
+    """HourglassTest.controlOpposesTheMode (:150-179): antiparallel force, linear in the
+    amplitude, energy quadratic."""
+    mesh = QuadMesh(*_UNIT)
+    e = 1.0e-4
+    s = _hg_solver(mesh, 0.05)
+    f = _impose(s, _hourglass(e), np.zeros(4))
+    energy = s.hourglassEnergy()
+    assert sum((1.0 if i % 2 == 0 else -1.0) * f[2 * i] for i in range(4)) < 0.0
+    assert energy > 0.0
+    twice = _hg_solver(mesh, 0.05)
+    f2 = _impose(twice, _hourglass(2.0 * e), np.zeros(4))
+    assert abs(np.linalg.norm(f2) / np.linalg.norm(f) - 2.0) <= 1e-9
+    assert abs(twice.hourglassEnergy() / energy - 4.0) <= 1e-9
+
+
+def test_hourglass_coefficient_scales_the_stiffness():
+    """HourglassTest.coefficientScalesStiffness (:180-204), on the distorted quad."""
+    mesh = QuadMesh([1.00, 2.10, 1.90, 0.85], [0.00, 0.15, 1.20, 0.95], [0, 1, 2, 3])
+    e = 1.0e-4
+    previous = None
+    for q in (0.02, 0.04, 0.08):
+        delta = (_impose(_hg_solver(mesh, q), _hourglass(e), np.zeros(4))
+                 - _impose(_hg_solver(mesh, 0.0), _hourglass(e), np.zeros(4)))
+        if previous is not None:
+            assert abs(np.linalg.norm(delta) / np.linalg.norm(previous) - 2.0) <= 1e-9
+        previous = delta
+
+
 def test_rigid_rotation_is_objective():
     """FiniteStrainTest.rigidRotationIsExactlyObjective (:59-110)."""
     mesh = QuadMesh([0.0, 1.0, 1.0, 0.0], [0.0, 0.0, 1.0, 1.0], [0, 1, 2, 3])
