@@ -395,6 +395,68 @@ def _approach(s, mesh, v):
     s.setVelocities(np.where(mesh.r < 10.0 * MM, v, -v), np.zeros(mesh.nodeCount))
 
 
+def _square_solver(material, kinematics, integration=Integration.REDUCED):
+    mesh = QuadMesh([0.0, 1.0, 1.0, 0.0], [0.0, 0.0, 1.0, 1.0], [0, 1, 2, 3])
+    return mesh, OracleSolver(mesh, material, Formulation.PLANE_STRAIN, integration, kinematics,
+                              1.0, 0.5)
+
+
+def _move_to(s, mesh, tr, tz):
+    """FiniteStrainTest.moveTo (:48-56)."""
+    dt = s.timestep()
+    ur, uz = s.radialDisplacement(), s.axialDisplacement()
+    for i in range(4):
+        s.setVelocity(i, (tr[i] - (mesh.r[i] + ur[i])) / dt, (tz[i] - (mesh.z[i] + uz[i])) / dt)
+    s.advance()
+
+
+def _mises(v):
+    p = (v[0] + v[1] + v[2]) / 3.0
+    return math.sqrt(1.5 * ((v[0] - p) ** 2 + (v[1] - p) ** 2 + (v[2] - p) ** 2 + 2 * v[3] ** 2))
+
+
+def test_isochoric_compression_hits_the_exact_yield_state():
+    """FiniteStrainTest.largeIsochoricDeformationHitsTheExactYieldState (:193-233)."""
+    sy = 800.0e6
+    mesh, s = _square_solver(Material.STEEL_4340.yielding(sy, 0.0), Kinematics.FINITE_STRAIN)
+    n = 4000
+    for i in range(1, n + 1):
+        c = 1.0 + (0.5 - 1.0) * i / n
+        _move_to(s, mesh, [0.0, 1.0 / c, 1.0 / c, 0.0], [0.0, 0.0, c, c])
+    sig = s.centroidStress(0)
+    assert s.plasticStrain()[0] > 0.3
+    assert abs(-(sig[0] + sig[1] + sig[2]) / 3.0) <= sy * 1e-3
+    assert abs(sig[1] + sy / math.sqrt(3.0)) <= sy * 5e-3
+    assert abs(_mises(sig) - sy) <= sy * 5e-3
+
+
+def _stress_after_stretch(kinematics, integration, stretch):
+    mesh, s = _square_solver(Material.STEEL_4340, kinematics, integration)
+    n = 500
+    for i in range(1, n + 1):
+        h = 1.0 + (stretch - 1.0) * i / n
+        _move_to(s, mesh, [0.0, 1.0, 1.0, 0.0], [0.0, 0.0, h, h])
+    return s.centroidStress(0)
+
+
+@pytest.mark.parametrize("integration", [Integration.REDUCED, Integration.FULL])
+def test_formulations_agree_at_small_strain(integration):
+    """FiniteStrainTest.formulationsAgreeAtSmallStrain (:235-253)."""
+    small = _stress_after_stretch(Kinematics.SMALL_STRAIN, integration, 1.0 + 2.0e-4)
+    finite = _stress_after_stretch(Kinematics.FINITE_STRAIN, integration, 1.0 + 2.0e-4)
+    scale = _mises(small)
+    assert scale > 0.0
+    assert np.all(np.abs(np.asarray(small) - np.asarray(finite)) <= scale * 1e-3)
+
+
+def test_formulations_diverge_at_large_strain():
+    """FiniteStrainTest.formulationsDivergeAtLargeStrain (:255-271)."""
+    small = _stress_after_stretch(Kinematics.SMALL_STRAIN, Integration.REDUCED, 1.20)
+    finite = _stress_after_stretch(Kinematics.FINITE_STRAIN, Integration.REDUCED, 1.20)
+    assert _mises(finite) < _mises(small)
+    assert abs(_mises(finite) - _mises(small)) > 0.05 * _mises(small)
+
+
 def test_collision_conserves_momentum():
     """ContactTest.momentumIsConserved (:85-103)."""
     mesh = _two_blocks()
