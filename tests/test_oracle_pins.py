@@ -482,6 +482,96 @@ def test_without_contact_blocks_interpenetrate():
     assert front > back
 
 
+def _contact_total(s):
+    return (s.centredKineticEnergy() + s.strainEnergy() + s.hourglassEnergy()
+            + s.contact().energy() + s.contact().dissipation())
+
+
+def test_elastic_collision_closes_the_energy_budget():
+    """ContactTest.elasticCollisionClosesTheEnergyBudget (:104-137): contact happens, nothing
+    tunnels, the budget closes within 4 %, and the left block turns around."""
+    mesh = _two_blocks()
+    s = _contact_solver(mesh)
+    s.setContact(Contact(mesh))
+    _approach(s, mesh, 60.0)
+    initial = _contact_total(s)
+    touched = False
+    for _ in range(400):
+        s.run(20)
+        touched = touched or s.contact().pairCount() > 0
+    assert touched
+    assert s.contact().escapedNodes() == 0
+    assert abs(_contact_total(s) / initial - 1.0) < 0.04
+    left = np.asarray(mesh.r) < 10.0 * MM
+    assert np.mean(np.asarray(s.velocityR())[left]) < 0.0
+
+
+def test_penetration_stays_a_small_fraction_of_a_cell():
+    """ContactTest.penetrationIsBounded (:139-157)."""
+    mesh = _two_blocks()
+    s = _contact_solver(mesh)
+    s.setContact(Contact(mesh))
+    _approach(s, mesh, 60.0)
+    worst = 0.0
+    for _ in range(400):
+        s.run(20)
+        worst = max(worst, s.contact().maxPenetration())
+    assert 0.0 < worst < 0.10 * MM
+
+
+def test_a_surface_at_rest_does_not_contact_itself():
+    """ContactTest.noSelfContactAtRest (:159-177): an L-shaped body (a re-entrant corner)."""
+    mesh = Outline.of(0.0, 0.0, 20.0 * MM, 0.0, 20.0 * MM, 6.0 * MM, 6.0 * MM, 6.0 * MM,
+                      6.0 * MM, 20.0 * MM, 0.0, 20.0 * MM).mesh(MM)
+    s = _contact_solver(mesh)
+    s.setContact(Contact(mesh))
+    s.run(200)
+    assert s.contact().pairCount() == 0
+    assert s.contact().escapedNodes() == 0
+    assert abs(s.kineticEnergy()) <= 1e-18
+
+
+def test_a_node_is_not_caught_by_a_surface_it_is_not_facing():
+    """ContactTest.facingIsRequired (:179-199): a block crushed against itself."""
+    mesh = Outline.rectangle(0.0, 0.0, 3.0 * MM, 3.0 * MM).mesh(MM)
+    s = _contact_solver(mesh)
+    s.setContact(Contact(mesh))
+    for i in range(mesh.nodeCount):
+        if mesh.r[i] == 0.0:
+            s.setVelocity(i, 120.0, 0.0)
+        if mesh.r[i] == 3.0 * MM:
+            s.setVelocity(i, -120.0, 0.0)
+    s.run(1500)
+    assert s.contact().pairCount() == 0
+
+
+def _slide_speed(mesh, mu):
+    s = _contact_solver(mesh)
+    c = Contact(mesh).withFriction(mu)
+    s.setContact(c)
+    for i in range(mesh.nodeCount):
+        if mesh.z[i] > 5.5 * MM:
+            s.setVelocity(i, 30.0, -40.0)
+        if mesh.z[i] == 0.0:
+            s.fixAxial(i)
+    initial = _contact_total(s)
+    for _ in range(30):
+        s.run(200)
+    assert s.contact().dissipation() >= 0.0
+    assert abs(_contact_total(s) / initial - 1.0) < 0.10
+    upper = np.asarray(mesh.z) > 5.5 * MM
+    return float(np.mean(np.asarray(s.velocityR())[upper]))
+
+
+def test_friction_opposes_sliding():
+    """ContactTest.frictionOpposesSliding (:201-244)."""
+    mesh = Outline.meshOf(MM, Outline.rectangle(0.0, 0.0, 20.0 * MM, 5.0 * MM),
+                          Outline.rectangle(5.0 * MM, 6.0 * MM, 13.0 * MM, 11.0 * MM))
+    free, rough = _slide_speed(mesh, 0.0), _slide_speed(mesh, 0.4)
+    assert rough < free
+    assert rough > 0.0
+
+
 def test_surface_covers_every_free_edge():
     """ContactTest.surfaceCoversEveryFreeEdge (:261-268): two 8x12 and 8x6 blocks have a
     perimeter of 40 + 28 cells."""
