@@ -90,6 +90,43 @@ def test_taylor_published_table(nr, integ, jc, mu, mush, ratio, eps, temp):
     assert s.hourglassEnergy() / k0 < 0.01
 
 
+def test_the_axis_holds():
+    """TaylorImpactTest.theAxisHolds (:75-97): axis nodes stay on the centreline exactly."""
+    nr, nz = 3, 8
+    mesh = QuadMesh.solidCylinder(0.5 * 7.595e-3, 8.0e-3, nr, nz)
+    s = OracleSolver(mesh, Material.STEEL_4340.withJohnsonCook(JohnsonCook.STEEL_4340),
+                     Formulation.AXISYMMETRIC, Integration.REDUCED, Kinematics.FINITE_STRAIN,
+                     1.0, 0.5)
+    for n in QuadMesh.axisNodes(nr, nz):
+        s.fixRadial(n)
+    s.setRigidWall(RigidWall.atZ(0.0))
+    s.setUniformVelocity(0.0, -181.0)
+    while s.time() < 20e-6:
+        s.step()
+    ur = s.radialDisplacement()
+    for n in QuadMesh.axisNodes(nr, nz):
+        assert ur[n] == 0.0, n
+    assert s.maxPlasticStrain() > 0.05
+
+
+def test_temperature_rise_and_johnson_cook_stiffening():
+    """TaylorImpactTest.temperatureRiseIsPhysical and johnsonCookStiffensTheResponse
+    (:164-197), on the n = 4 reference run: a rise of 100-400 K, the thermal term below 0.92,
+    and the Johnson-Cook rod shortening less and reaching less plastic strain than the
+    rate-independent surrogate."""
+    jc, _, info = scenes.taylor_reference(OracleSolver, 4)
+    surrogate, _, _ = scenes.taylor_reference(OracleSolver, 4, jc=False)
+    jc.runUntil(80e-6)
+    surrogate.runUntil(80e-6)
+    law = JohnsonCook.STEEL_4340
+    rise = jc.maxTemperature() - law.roomTemperature
+    assert 100.0 < rise < 400.0
+    homologous = rise / (law.meltTemperature - law.roomTemperature)
+    assert 1.0 - homologous ** law.m < 0.92
+    assert jc.measure().length / info["length"] > surrogate.measure().length / info["length"] + 0.015
+    assert jc.maxPlasticStrain() < surrogate.maxPlasticStrain()
+
+
 # ----------------------------------------------------------------------------- J2Test
 
 E, NU, SY = 205.0e9, 0.29, 800.0e6
