@@ -153,7 +153,6 @@ __device__ __forceinline__ double batch_step(const Dev &d, const BatchInst &in, 
         const double half = 0.5 * in.damping * dtAvg;
         co = NodalCoef{(1.0 - half) / (1.0 + half), dtAvg / (1.0 + half), dtAvg, dt};
     }
-    const double dtAvg = co.dtAvg;
     const WallRef w{in.hasWall, in.wallPlane, in.wallFriction, wallContact, wallStuck};
     if (COMP) {                                                  // requires bs
         for (int i = in.n0 + threadIdx.x; i < in.n1; i += T)
