@@ -38,6 +38,15 @@ def test_free_fall_is_exact():
     assert abs(s.axialMomentum() / total - (-9.81 * t)) <= 1e-9 * 9.81 * t
 
 
+def test_gravity_is_off_by_default():
+    """GravityTest.defaultIsNone (:81-92): an unforced body keeps exactly zero momentum."""
+    mesh = Outline.rectangle(0.0, 0.0, 6.0 * MM, 4.0 * MM).mesh(MM)
+    s = OracleSolver(mesh, Material.STEEL_4340, Formulation.PLANE_STRAIN, Integration.REDUCED,
+                     Kinematics.SMALL_STRAIN, 10.0 * MM, 0.5)
+    s.run(500)
+    assert s.axialMomentum() == 0.0
+
+
 def test_resting_body_does_not_sink():
     """GravityTest.restingBodyDoesNotSink (:61-80)."""
     mesh = Outline.rectangle(0.0, 0.0, 20.0 * MM, 5.0 * MM).mesh(MM)
