@@ -13,6 +13,8 @@ c_double_p = C.POINTER(C.c_double)
 c_int32_p = C.POINTER(C.c_int32)
 
 NF_OK, NF_EINVAL, NF_ESTATE, NF_EDEVICE, NF_ETIMEOUT, NF_ENOMEM = range(6)
+# bits of the device status word (nf_status_word)
+STATUS_NONFINITE, STATUS_BUCKET_OVERFLOW, STATUS_TIMEOUT = 1, 4, 8
 
 (FIELD_UR, FIELD_UZ, FIELD_VR, FIELD_VZ, FIELD_FR, FIELD_FZ, FIELD_MASS, FIELD_STRESS,
  FIELD_BACK_STRESS, FIELD_PLASTIC_STRAIN, FIELD_PLASTIC_WORK, FIELD_HOURGLASS_R,
@@ -135,6 +137,8 @@ _PROTOS = {
     "destroy": (None, [_H]),
     "last_error": (C.c_char_p, [_H]),
     "status_word": (_S, [_H, C.POINTER(C.c_uint32)]),
+    "check": (_S, [_H]),
+    "set_wait_limit": (_S, [_H, C.c_int64, C.c_int64]),
     "set_threads": (_S, [_H, C.c_int32]),
     "fix_radial": (_S, [_H, C.c_int32]),
     "fix_axial": (_S, [_H, C.c_int32]),

@@ -568,6 +568,50 @@ nf_status nf_destroy(nf_solver *h) {
     return NF_OK;
 }
 
+// A contact-pass barrier that gave up (STATUS_TIMEOUT) left that step's contact forces
+// incomplete, so the handle's state is no longer the reference's: the handle is marked failed,
+// and this call and every later run call report NF_ETIMEOUT.
+static const char *const TIMEOUT_MESSAGE =
+    "a grid barrier of the contact pass waited past its limit; that step's contact forces are "
+    "incomplete and this handle can no longer step";
+
+static nf_status note_status(Solver &S, uint32_t status) {
+    if (status & STATUS_TIMEOUT) S.failed = NF_ETIMEOUT;
+    if (S.failed) return fail(&S, S.failed, "%s", TIMEOUT_MESSAGE);
+    return NF_OK;
+}
+
+static nf_status read_status(Solver &S, uint32_t *out) {
+    CK(&S, cudaMemcpyAsync(out, &S.d.s->status, sizeof(uint32_t), cudaMemcpyDeviceToHost,
+                           S.stream));
+    return sync_check(S);
+}
+
+nf_status nf_check(nf_solver *h) {
+    Solver &S = *reinterpret_cast<Solver *>(h);
+    uint32_t w = 0;
+    nf_status st = read_status(S, &w);
+    if (st) return st;
+    st = note_status(S, w);
+    if (st) return st;
+    if (w & STATUS_NONFINITE)
+        return fail(&S, NF_EDEVICE, "a nodal velocity or displacement is not finite "
+                                    "(status word 0x%x)", w & ~(uint32_t)STATUS_GRID_HASHED);
+    if (w & STATUS_BUCKET_OVERFLOW)
+        return fail(&S, NF_EDEVICE, "a contact bucket exceeded its bound (status word 0x%x)",
+                    w & ~(uint32_t)STATUS_GRID_HASHED);
+    return NF_OK;
+}
+
+nf_status nf_set_wait_limit(nf_solver *h, int64_t polls, int64_t nanoseconds) {
+    Solver &S = *reinterpret_cast<Solver *>(h);
+    if (polls < 0 || nanoseconds < 0)
+        return fail(&S, NF_EINVAL, "wait limits must be >= 0 (0 restores the default)");
+    S.d.waitSpins = polls;
+    S.d.waitNs = nanoseconds;
+    return NF_OK;
+}
+
 nf_status nf_status_word(nf_solver *h, uint32_t *word) {
     Solver &S = *reinterpret_cast<Solver *>(h);
     DevScalars s;
@@ -897,6 +941,7 @@ static nf_status enqueue_steps(Solver &S, int64_t steps) {
 // run(int), ExplicitSolver.java:936-938. Enqueues the steps and returns; reads wait for them.
 nf_status nf_step(nf_solver *h, int64_t steps) {
     Solver &S = *reinterpret_cast<Solver *>(h);
+    if (S.failed) return note_status(S, 0);
     if (steps <= 0) return NF_OK;
     if (!S.unbounded) {
         k_set_run<<<1, 1, 0, S.stream>>>(S.d.s, INFINITY, (long long)9.0e18);
@@ -916,6 +961,7 @@ nf_status nf_step(nf_solver *h, int64_t steps) {
 
 nf_status nf_advance(nf_solver *h) {
     Solver &S = *reinterpret_cast<Solver *>(h);
+    if (S.failed) return note_status(S, 0);
     S.launches += launch_advance(S);
     return sync_check(S);
 }
@@ -925,6 +971,7 @@ nf_status nf_advance(nf_solver *h) {
 nf_status nf_run_until(nf_solver *h, double t_end, int64_t max_steps, int64_t *taken) {
     Solver &S = *reinterpret_cast<Solver *>(h);
     if (taken) *taken = 0;
+    if (S.failed) return note_status(S, 0);
     if (max_steps <= 0) return NF_OK;
     k_set_run<<<1, 1, 0, S.stream>>>(S.d.s, t_end, max_steps);
     S.launches++;
@@ -936,6 +983,11 @@ nf_status nf_run_until(nf_solver *h, double t_end, int64_t max_steps, int64_t *t
         if (st) return st;
         st = read_scalars(S, &s);
         if (st) return st;
+        if (s.status & STATUS_TIMEOUT) {
+            S.hostSteps += s.stepsTaken;
+            if (taken) *taken = s.stepsTaken;
+            return note_status(S, s.status);
+        }
         if (!s.active || s.stepsTaken >= max_steps || !(s.time < t_end)) break;
     }
     S.hostSteps += s.stepsTaken;
@@ -944,7 +996,11 @@ nf_status nf_run_until(nf_solver *h, double t_end, int64_t max_steps, int64_t *t
 }
 
 nf_status nf_synchronize(nf_solver *h) {
-    return sync_check(*reinterpret_cast<Solver *>(h));
+    Solver &S = *reinterpret_cast<Solver *>(h);
+    uint32_t w = 0;
+    nf_status st = read_status(S, &w);
+    if (st) return st;
+    return note_status(S, w);
 }
 
 nf_status nf_set_stream(nf_solver *h, void *stream) {

@@ -130,9 +130,14 @@ __device__ __forceinline__ void st_release(unsigned int *p, unsigned int v) {
 // block wrote, which the block barrier ordered before it) and waits with acquire loads for the
 // generation to move; the last arriver resets the counter and moves the generation with a
 // release store. Returns false when the wait ran out or another block gave up; the caller then
-// leaves the kernel.
-__device__ bool grid_sync(DevScalars *s) {
+// leaves the kernel. The wait polls at most d.waitSpins times and for at most d.waitNs
+// nanoseconds (defaults when zero).
+__device__ bool grid_sync(const Dev &d) {
     __shared__ int ok;
+    DevScalars *s = d.s;
+    const long long spinLimit = d.waitSpins > 0 ? d.waitSpins : WAIT_LIMIT_SPINS;
+    const unsigned long long nsLimit =
+        d.waitNs > 0 ? (unsigned long long)d.waitNs : WAIT_LIMIT_NS;
     __syncthreads();
     if (threadIdx.x == 0) {
         const unsigned int g = ld_relaxed(&s->barGen);
@@ -149,7 +154,7 @@ __device__ bool grid_sync(DevScalars *s) {
                     good = 0;
                     break;
                 }
-                if (++spins > WAIT_LIMIT_SPINS || global_ns() - t0 > WAIT_LIMIT_NS) {
+                if (++spins > spinLimit || global_ns() - t0 > nsLimit) {
                     atomicOr(&s->status, STATUS_TIMEOUT);
                     atomicExch(&s->barAbort, 1u);
                     good = 0;
@@ -178,7 +183,7 @@ __device__ bool grid_scan(const Dev &d, int32_t *in, int32_t *out, int32_t *out2
     int bsum;
     block_scan_incl(local, sh, &bsum);
     if (threadIdx.x == 0) d.coopSums[blockIdx.x] = bsum;
-    if (!grid_sync(d.s)) return false;
+    if (!grid_sync(d)) return false;
     // this block's offset: the sum over the earlier blocks' chunks
     int pre = 0;
     for (int j = threadIdx.x; j < (int)blockIdx.x; j += CB) pre += vload(&d.coopSums[j]);
@@ -211,7 +216,7 @@ __device__ bool grid_scan(const Dev &d, int32_t *in, int32_t *out, int32_t *out2
         }
         carry += tileTotal;
     }
-    return grid_sync(d.s);
+    return grid_sync(d);
 }
 
 // ---------------------------------------------------------------------------- contact geometry
@@ -517,7 +522,7 @@ __device__ void finish_slave(const Dev &d, int i, double best, int bestSeg, bool
 #define FOR_GRID(i, count)                                                                    \
     for (int i = ((threadIdx.x >> 5) * gridDim.x + blockIdx.x) * 32 + (threadIdx.x & 31);     \
          i < (count); i += gridDim.x * CB)
-#define SYNC() do { if (!grid_sync(s)) return; } while (0)
+#define SYNC() do { if (!grid_sync(d)) return; } while (0)
 
 // The per-step totals this pass accumulates into (Contact.begin, Contact.java:424-436) are
 // reset by the step's first kernel (contact_step_reset), so the pass needs no opening barrier.

@@ -29,10 +29,12 @@ namespace nf {
 
 // Status-word bits (nf_status_word).
 enum : uint32_t {
-    STATUS_NONFINITE = 1u,       // a nodal velocity or displacement stopped being finite
+    STATUS_NONFINITE = NF_STATUS_NONFINITE,          // a nodal velocity or displacement
+                                                     // stopped being finite
     STATUS_GRID_HASHED = 2u,     // informational: the contact grid outgrew direct indexing
-    STATUS_BUCKET_OVERFLOW = 4u, // a contact bucket exceeded the sort bound
-    STATUS_TIMEOUT = 8u,         // a grid barrier of the contact pass waited past its limit
+    STATUS_BUCKET_OVERFLOW = NF_STATUS_BUCKET_OVERFLOW,   // a contact bucket exceeded its bound
+    STATUS_TIMEOUT = NF_STATUS_TIMEOUT,              // a grid barrier of the contact pass
+                                                     // waited past its limit
 };
 
 struct DevScalars {
@@ -165,6 +167,9 @@ struct Dev {
     int hotSmem;                             // the listed pass's occupancy-limiting request
     int coopBlocks;
     int32_t *coopSums;
+    // limits of the contact pass's grid-barrier wait (0: the defaults, 2^27 polls or one
+    // second); nf_set_wait_limit lowers them so that tests can make a wait run out
+    long long waitSpins, waitNs;
     DevScalars *s;
 };
 
@@ -216,6 +221,8 @@ struct Solver {
     Dev graphDev{};
     bool graphValid = false;
     bool noGraphs = false;       // capture failed once: steps are enqueued directly
+    // a device-side wait that ran out leaves the state invalid: later run calls refuse
+    nf_status failed = NF_OK;
     void *arena = nullptr;       // nf_create's set-up arrays, one allocation
     size_t arenaBytes = 0;
     // per-group event profiling

@@ -31,6 +31,10 @@ class DeviceError(RuntimeError):
     pass
 
 
+class DeviceTimeout(DeviceError):
+    """A bounded device-side wait gave up (NF_ETIMEOUT); the handle can no longer step."""
+
+
 def _raise(api, handle, status: int):
     msg = api.last_error(handle)
     msg = msg.decode() if msg else f"status {status}"
@@ -38,6 +42,8 @@ def _raise(api, handle, status: int):
         raise ValueError(msg)
     if status == _abi.NF_ESTATE:
         raise RuntimeError(msg)
+    if status == _abi.NF_ETIMEOUT:
+        raise DeviceTimeout(msg)
     raise DeviceError(msg)
 
 
@@ -335,6 +341,16 @@ class ExplicitSolver:
 
     def synchronize(self):
         self._call(self._api.synchronize)
+
+    def check(self) -> None:
+        """Waits for the queued steps and raises if the device flagged a fault: DeviceTimeout
+        when a contact-pass barrier gave up, DeviceError when a nodal velocity or displacement
+        stopped being finite (the reference lets NaNs propagate silently)."""
+        self._call(self._api.check)
+
+    def setWaitLimit(self, polls: int, nanoseconds: int) -> None:
+        """Bounds of each contact-pass barrier wait (0, 0: the defaults); for tests."""
+        self._call(self._api.set_wait_limit, int(polls), int(nanoseconds))
 
     def setStream(self, stream_handle: int) -> None:
         """Runs this solver's kernels on a caller-owned cudaStream_t (0: its own)."""

@@ -1755,6 +1755,21 @@ API nf_status nfo_run_until(nfo_solver *h, double t_end, int64_t max_steps, int6
 }
 API nf_status nfo_synchronize(nfo_solver *h) { (void)h; return NF_OK; }
 API nf_status nfo_status_word(nfo_solver *h, uint32_t *w) { (void)h; *w = 0; return NF_OK; }
+/* The CPU twin of nf_check: nothing here waits, so only the finiteness of the nodal
+ * velocities and displacements is checked (the device's NF_STATUS_NONFINITE test). */
+API nf_status nfo_check(nfo_solver *h) {
+    for (int i = 0; i < h->N; i++)
+        if (!isfinite(h->ur[i]) || !isfinite(h->uz[i]) || !isfinite(h->vr[i]) ||
+            !isfinite(h->vz[i]))
+            return fail(h, NF_EDEVICE, "a nodal velocity or displacement is not finite "
+                                       "(status word 0x%x)", 1u);
+    return NF_OK;
+}
+API nf_status nfo_set_wait_limit(nfo_solver *h, int64_t polls, int64_t ns) {
+    if (polls < 0 || ns < 0)
+        return fail(h, NF_EINVAL, "wait limits must be >= 0 (0 restores the default)");
+    return NF_OK;
+}
 
 static nf_status field_desc(nfo_solver *h, int field, void **ptr, size_t *count, size_t *bytes) {
     const size_t N = (size_t)h->N, E = (size_t)h->E, P = (size_t)h->E * (size_t)h->ppe;
