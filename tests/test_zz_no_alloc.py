@@ -6,11 +6,13 @@ GPU memory belongs to its own pool allocator has none to spare). It stages throu
 device array instead. This test calls both entry points through the C ABI on the same inputs,
 twice in a row (the second call starting from the first call's results, so the shared array is
 reused with different contents), and requires bit-identical outputs -- the tolerance of every
-other parity test in this suite. It also checks that a request above the array's capacity is
-refused. This file sorts last so that a run stopping at the first failure has run everything
-else first.
+other parity test in this suite -- also at exactly the array's capacity with damage on (the
+top of the array in use). It checks that a request above the capacity is refused, and that a
+call neither waits for nor holds up work the caller has queued on another stream. This file
+sorts last so that a run stopping at the first failure has run everything else first.
 """
 import ctypes as C
+import time
 
 import numpy as np
 import pytest
@@ -51,13 +53,13 @@ def _call(fn, material, state, strain, damage):
     return dg
 
 
-@pytest.mark.parametrize("kind", ["linear", "jc-damage"])
-def test_static_entry_matches_allocating_entry(gpu_lib, kind):
+@pytest.mark.parametrize("kind,n", [("linear", 6000), ("jc-damage", 6000),
+                                    ("jc-damage", CAPACITY)])
+def test_static_entry_matches_allocating_entry(gpu_lib, kind, n):
     lib = gpu_lib.lib
     static = _bind(lib)
     allocating = gpu_lib.material_point_update
-    rng = np.random.default_rng(7 if kind == "linear" else 11)
-    n = 6000
+    rng = np.random.default_rng((7 if kind == "linear" else 11) + n)
     if kind == "linear":
         m = Material.STEEL_4340.yielding(800e6, 1e9, 2e9)
     else:
@@ -104,3 +106,28 @@ def test_static_entry_refuses_more_than_its_capacity(gpu_lib):
                 _dptr(z1.copy()))
     assert st == _abi.NF_EINVAL
     assert str(CAPACITY) in gpu_lib.last_error(None).decode()
+
+
+def test_static_entry_does_not_wait_for_the_callers_other_streams(gpu_lib):
+    """The caller keeps the legacy default stream (a blocking stream, which every blocking
+    stream waits for) busy with a bounded sleep of about a second; the call runs on the
+    library's own non-blocking stream and returns while that sleep is still running."""
+    torch = pytest.importorskip("torch")
+    static = _bind(gpu_lib.lib)
+    m = Material.STEEL_4340.yielding(800e6, 1e9, 2e9)
+    n = 256
+    rng = np.random.default_rng(3)
+    state = [rng.normal(0.0, 3e8, 4 * n), rng.normal(0.0, 5e7, 4 * n),
+             np.abs(rng.normal(0.0, 0.2, n)), np.abs(rng.normal(0.0, 2e8, n))]
+    strain = rng.normal(0.0, 2e-3, 4 * n)
+    _call(static, m, state, strain, None)            # the device's first call: set-up
+    torch.cuda.synchronize()
+    legacy = torch.cuda.default_stream()
+    with torch.cuda.stream(legacy):
+        torch.cuda._sleep(2_000_000_000)             # ~1 s of GPU clock cycles, bounded
+    t0 = time.perf_counter()
+    _call(static, m, state, strain, None)
+    elapsed = time.perf_counter() - t0
+    still_busy = not legacy.query()
+    torch.cuda.synchronize()
+    assert still_busy and elapsed < 0.5, f"the call waited {elapsed:.3f} s for another stream"
