@@ -64,18 +64,27 @@ def test_resting_body_does_not_sink():
 
 # README.md:306-312 (4340, 181 m/s, frictionless) and :344-352 (friction sweep, n = 8).
 PUBLISHED = [
-    # nr, integration, jc, friction, mushroom mm, L/L0, max eps_p, T max
-    (4, Integration.REDUCED, True, 0.0, 9.472, 0.9079, 0.50, 443),
-    (4, Integration.REDUCED, False, 0.0, 9.590, 0.8827, 0.54, None),
-    (8, Integration.REDUCED, True, 0.0, 9.776, 0.9081, 0.67, 495),
-    (8, Integration.REDUCED, True, 0.05, 9.476, 0.9085, None, None),
-    (8, Integration.REDUCED, True, math.inf, 8.928, 0.9106, None, None),
-    (8, Integration.FULL, True, 0.0, 9.448, 0.9076, 0.56, 459),
+    # the reference's Taylor-impact table (README.md:306-314) and its Coulomb friction sweep
+    # (README.md:344-352): nr, integration, jc, friction, mushroom mm, L/L0, max eps_p, T max,
+    # friction dissipation as a percentage of the impact energy
+    (4, Integration.REDUCED, True, 0.0, 9.472, 0.9079, 0.50, 443, None),
+    (4, Integration.REDUCED, False, 0.0, 9.590, 0.8827, 0.54, None, None),
+    (8, Integration.REDUCED, True, 0.0, 9.776, 0.9081, 0.67, 495, None),
+    (8, Integration.REDUCED, False, 0.0, 9.855, 0.8843, 0.72, None, None),
+    (16, Integration.REDUCED, True, 0.0, 9.965, 0.9080, 0.75, 517, None),
+    (16, Integration.REDUCED, False, 0.0, 10.005, 0.8845, 0.83, None, None),
+    (8, Integration.FULL, True, 0.0, 9.448, 0.9076, 0.56, 459, None),
+    (8, Integration.REDUCED, True, 0.02, 9.651, 0.9082, None, None, 0.46),
+    (8, Integration.REDUCED, True, 0.05, 9.476, 0.9085, None, None, 1.02),
+    (8, Integration.REDUCED, True, 0.10, 9.259, 0.9088, None, None, 1.67),
+    (8, Integration.REDUCED, True, 0.20, 8.987, 0.9093, None, None, 2.21),
+    (8, Integration.REDUCED, True, 0.50, 8.921, 0.9102, None, None, 1.48),
+    (8, Integration.REDUCED, True, math.inf, 8.928, 0.9106, None, None, 0.0),
 ]
 
 
-@pytest.mark.parametrize("nr,integ,jc,mu,mush,ratio,eps,temp", PUBLISHED)
-def test_taylor_published_table(nr, integ, jc, mu, mush, ratio, eps, temp):
+@pytest.mark.parametrize("nr,integ,jc,mu,mush,ratio,eps,temp,fric", PUBLISHED)
+def test_taylor_published_table(nr, integ, jc, mu, mush, ratio, eps, temp, fric):
     s, mesh, info = scenes.taylor_reference(OracleSolver, nr, integration=integ, friction=mu,
                                             jc=jc)
     wall = info["wall"]
@@ -88,6 +97,8 @@ def test_taylor_published_table(nr, integ, jc, mu, mush, ratio, eps, temp):
         assert round(s.maxPlasticStrain(), 2) == pytest.approx(eps, abs=1e-9)
     if temp is not None:
         assert round(s.maxTemperature()) == temp
+    if fric is not None:
+        assert round(100.0 * wall.frictionDissipation() / k0, 2) == pytest.approx(fric, abs=1e-9)
     # TaylorImpactTest.momentumBalance (:115-122): change in momentum = anvil impulse
     err = abs((s.axialMomentum() - p0) - wall.impulse()) / abs(p0)
     assert err < 1e-11
