@@ -9,6 +9,11 @@ Coulomb friction 0.2, Weibull (m = 10) failure strains with fracture-energy soft
 of the whole scene. Inputs are synthetic (the scene is generated); the state (~60 MB) fits
 in L2, so a 256 MB buffer is written between timed steps to flush it.
 
+The timed window is fixed by the scene, not by the flags: both arms first run the scene to
+step 400 (the slug strikes the blocks near step 73, so by then contact pairs, Johnson-Cook
+solves, damage and erosion are all active), then --warmup steps, then time --steps steps. The
+GPU arm and the reference arm therefore time the same steps of the same state.
+
   python bench.py [--gpus N] [--steps K] [--warmup W] [--impl ours|reference]
 
 --impl reference times the reference algorithm on the host cores: the C restatement of the
@@ -29,13 +34,14 @@ sys.path.insert(0, HERE)
 
 CELL = 0.114e-3
 GAP = 0.5e-3
+WINDOW_START = 400          # steps run before warm-up and timing, in both arms
 L2_FLUSH_BYTES = 256 << 20
-# DRAM bytes (read + write) of one element-pass launch of this workload after 300 steps, and
-# its FP64 pipe use, from ncu (profiles/k_element_reduced_listed_perforation_200k_fp64.md;
-# ncu cannot run inside the timed bench)
+# DRAM bytes (read + write) of one element-pass launch of this workload after 300 steps, from
+# ncu's dram__bytes_read.sum + dram__bytes_write.sum (ncu cannot run inside the timed bench)
 ELEMENT_TRAFFIC_BYTES = {CELL: 40_489_984 + 62_976}
-ELEMENT_FP64_PIPE = {CELL: {"active_pct": 75.3, "fp64_warp_instructions": 3_307_977,
-                            "all_warp_instructions": 20_426_527}}
+# FP64-pipe warp instructions of one element-pass launch in the window (ncu's
+# smsp__inst_executed_pipe_fp64.sum on the launch of step start + 1)
+ELEMENT_FP64_WARP_INST = {CELL: None}
 
 
 def parse():
@@ -45,6 +51,8 @@ def parse():
     p.add_argument("--warmup", type=int, default=20)
     p.add_argument("--impl", default="ours", choices=["ours", "reference"])
     p.add_argument("--cell", type=float, default=CELL)
+    p.add_argument("--start", type=int, default=WINDOW_START,
+                   help="steps run before the warm-up (the window's start)")
     p.add_argument("--no-cpu-baseline", action="store_true")
     p.add_argument("--no-e2e", action="store_true")
     p.add_argument("--no-mixed", action="store_true")
@@ -174,6 +182,29 @@ ELEMENT_BYTES = 16 + 2 * 96 + 24
 NODE_BYTES = 48
 
 
+WORKLOAD = ("plane-strain perforation: 10x20 mm steel slug at 700 m/s into 12 copper blocks "
+            "20x10 mm on a rigid floor, gravity, penalty contact mu 0.2, Weibull m=10 damage, "
+            "erosion")
+
+
+def bench_config(args, E, N):
+    """The workload of the line, the same dict in both arms."""
+    return {"workload": WORKLOAD, "elements": E, "nodes": N, "cell_mm": args.cell * 1e3,
+            "gap_mm": GAP * 1e3, "window": f"steps {args.start}+{args.warmup} .. "
+                                            f"{args.start}+{args.warmup}+{args.steps}",
+            "start_step": args.start,
+            "l2": f"GPU arm: flushed between timed steps ({L2_FLUSH_BYTES >> 20} MB write)"}
+
+
+def window_facts(s, info, t_start):
+    """What the window's first step starts from: the same in both arms (the device path is
+    bit-identical to the oracle)."""
+    a = s._auditC()
+    return {"t_start_us": t_start * 1e6, "contact_pairs": info["contact"].pairCount(),
+            "yielded_fraction": a.yielded_fraction, "eroded": s.erodedElements(),
+            "max_plastic_strain": a.max_plastic_strain}
+
+
 def run_ours(args, world, rank, local):
     import torch
     torch.cuda.set_device(local)
@@ -181,16 +212,26 @@ def run_ours(args, world, rank, local):
     nb.build()
     from neofiz_gb300 import ExplicitSolver, scenes
 
-    g, mesh, info = scenes.perforation(ExplicitSolver, cell=args.cell, gap=GAP)
+    inputs = scenes.perforation_inputs(cell=args.cell, gap=GAP)
+
+    def positioned():
+        """The scene run to the window: start + warm-up steps, on its own stream."""
+        g, mesh, info = scenes.perforation_build(ExplicitSolver, inputs)
+        if args.precision == "mixed":
+            from neofiz_gb300 import _abi
+            g.setPrecision(_abi.PRECISION_MIXED)
+        stream = torch.cuda.Stream()
+        g.setStream(stream.cuda_stream)
+        g.run(args.start)
+        g.synchronize()
+        facts = window_facts(g, info, g.time())
+        g.run(args.warmup)
+        g.synchronize()
+        return g, mesh, info, stream, facts
+
+    g, mesh, info, stream, facts = positioned()
     E, N = mesh.elementCount, mesh.nodeCount
-    if args.precision == "mixed":
-        from neofiz_gb300 import _abi
-        g.setPrecision(_abi.PRECISION_MIXED)
-    stream = torch.cuda.Stream()
-    g.setStream(stream.cuda_stream)
     flush = torch.empty(L2_FLUSH_BYTES, dtype=torch.uint8, device="cuda")
-    g.run(args.warmup)
-    g.synchronize()
     torch.cuda.synchronize()
     eroded0 = g.erodedElements()
     launches0 = g.launchCount()
@@ -220,24 +261,31 @@ def run_ours(args, world, rank, local):
     work = live_element_steps(E, eroded0, eroded1, args.steps)
     value = world * work / (ms_max * 1e-3)
     status = g.statusWord()
+    facts["eroded_during_timing"] = eroded1 - eroded0
+    facts["contact_pairs_at_end"] = info["contact"].pairCount()
+    end_state = (g.readField(1).tobytes(), g.time())
+    del g
 
-    # Roofline of the dominant kernel: the same kind of steps with every kernel group
-    # bracketed by events on the solver's stream.
-    prof_steps = min(args.steps, 100)
-    g.profile(True)
-    for _ in range(prof_steps):
-        with torch.cuda.stream(stream):
+    # Roofline of the dominant kernel, over the same steps: a second handle run to the same
+    # state (bit-identical), its timed steps bracketed group by group by events on its stream
+    p, _, _, pstream, _ = positioned()
+    p.profile(True)
+    for _ in range(args.steps):
+        with torch.cuda.stream(pstream):
             flush.zero_()
-        g.run(1)
-    groups, covered = g.profileRead()
-    g.profile(False)
+        p.run(1)
+    groups, covered = p.profileRead()
+    p.profile(False)
+    same_window = (p.readField(1).tobytes(), p.time()) == end_state
+    del p
     per_step = {k: v / max(covered, 1) for k, v in groups.items()}
     top = max(per_step, key=per_step.get)
     elem_ms = per_step["element"]
-    live = E - g.erodedElements()
+    live = E - 0.5 * (eroded0 + eroded1)
     elem_bytes = ELEMENT_BYTES * live + NODE_BYTES * N
     peaks, peak_kind = measured_peaks()
     achieved = elem_bytes / (elem_ms * 1e-3) / 1e9 if elem_ms > 0 else None
+    fp64 = fp64_roofline(elem_ms, args.cell)
 
     e2e = None
     if not args.no_e2e:
@@ -277,25 +325,21 @@ def run_ours(args, world, rank, local):
             "vs_baseline": None,
             "dtype": "f64" if args.precision == "fp64" else "f32 element arithmetic, f64 kinematics",
             "data": "synthetic (generated scene; no dataset)",
-            "config": {
-                "workload": "plane-strain perforation: 10x20 mm steel slug at 700 m/s into 12 "
-                            "copper blocks 20x10 mm on a rigid floor, gravity, penalty contact "
-                            "mu 0.2, Weibull m=10 damage, erosion",
-                "elements": E, "nodes": N, "cell_mm": args.cell * 1e3,
-                "parallelism": f"replicas x{world}" if world > 1 else "single scene",
-                "l2": f"flushed between timed steps ({L2_FLUSH_BYTES >> 20} MB write)",
-                "eroded_during_timing": eroded1 - eroded0,
-            },
+            "config": bench_config(args, E, N),
+            "parallelism": f"replicas x{world}" if world > 1 else "single scene",
+            "window_state": facts,
             "roofline": {
                 "bound": "hbm", "kernel": "k_element_reduced_listed",
                 "achieved": achieved, "peak": peaks.get("hbm_gbs"), "unit": "GB/s",
                 "frac": (achieved / peaks["hbm_gbs"]) if achieved else None,
                 "peak_source": peak_kind,
                 "bytes_per_launch": elem_bytes, "launch_ms": elem_ms,
+                "launch_ms_source": "CUDA events around the element group, same window, "
+                                    "second handle (same state: " + str(same_window) + ")",
                 "traffic": ELEMENT_TRAFFIC_BYTES.get(args.cell),
                 "traffic_source": "ncu dram__bytes_read.sum + dram__bytes_write.sum, one launch",
-                "note": "FP64 arithmetic, not HBM, bounds this kernel on GB300",
-                "fp64_pipe_ncu": ELEMENT_FP64_PIPE.get(args.cell),
+                "note": "FP64 arithmetic, not HBM, bounds this kernel on GB300: see fp64",
+                "fp64": fp64,
                 "group_ms_per_step": per_step, "top_group": top,
             },
             "cpu_baseline": cpu,
@@ -308,16 +352,73 @@ def run_ours(args, world, rank, local):
             "gpu_launches": launches,
             "status_word": status,
         }
+        line["summary"] = summary_of(line)
         print(json.dumps(line))
 
 
+def fp64_roofline(elem_ms, cell):
+    """The element pass against the device's measured FP64 pipe rate: its FP64 warp
+    instructions per launch (ncu, the same window) over its event-timed duration."""
+    from neofiz_gb300 import _native
+    rate, flops = _native.fp64_rate()
+    out = {"bound": "fp64", "unit": "FP64 warp instructions/s", "peak": rate,
+           "peak_tflops": flops / 1e12,
+           "peak_source": "measured in this run: nf_device_fp64_rate (DFMA chains, every SM)"}
+    count = ELEMENT_FP64_WARP_INST.get(cell)
+    if count and elem_ms > 0:
+        achieved = count / (elem_ms * 1e-3)
+        out.update({"achieved": achieved, "frac": achieved / rate,
+                    "fp64_warp_inst_per_launch": count,
+                    "count_source": "ncu smsp__inst_executed_pipe_fp64.sum, one launch of the "
+                                    "window"})
+    return out
+
+
+def summary_of(line):
+    """The headline figures of every leg, compact, as the line's last key."""
+    def g(d, *ks):
+        for k in ks:
+            if not isinstance(d, dict):
+                return None
+            d = d.get(k)
+        return d
+    r = line["roofline"]
+    out = {"value": line["value"], "e2e": g(line, "e2e", "value"),
+           "cpu": g(line, "cpu_baseline", "value"),
+           "hbm_frac": r.get("frac"), "fp64_frac": g(r, "fp64", "frac"),
+           "element_ms": r.get("launch_ms")}
+    if line.get("mixed"):
+        m = line["mixed"]
+        out["mixed"] = {"value": m["value"], "x_fp64": m["speedup_vs_fp64"],
+                        "slug_v_err": g(m, "errors_vs_fp64", "slug_residual_velocity_rel"),
+                        "eroded": g(m, "errors_vs_fp64", "eroded_count")}
+    if line.get("batched"):
+        b = line["batched"]
+        out["batched"] = {"value": b["value"], "x_plain": b.get("speedup_vs_plain_fp64_path"),
+                          "L_err_max": g(b, "L_over_L0_error_vs_fp64", "max"),
+                          "mixed": g(b, "mixed", "value"),
+                          "mixed_x_plain": g(b, "mixed", "speedup_vs_plain_fp64_path")}
+    if line.get("adjoint"):
+        a = line["adjoint"]
+        out["adjoint"] = {"cost_one": g(a, "cost_vs_forward", "one_objective"),
+                          "cost_both": g(a, "cost_vs_forward", "both_objectives"),
+                          "max_rel_error": g(a, "rod0", "max_rel_error"),
+                          "tube_cost": g(a, "tube", "cost_vs_forward"),
+                          "tube_max_rel_error": g(a, "tube", "max_rel_error")}
+    if line.get("burst"):
+        b = line["burst"]
+        out["burst"] = {"fp64": g(b, "fp64", "value"), "compensated": g(b, "compensated", "value")}
+    return out
+
+
 def run_e2e(args, torch):
-    """The same metric through the public API from host buffers: the scene's host inputs (mesh,
-    materials, velocities, failure strains) are generated first; the timed region then creates
-    the solver from them (every upload), sets it up, runs the steps, and reads the nodal
-    displacement and velocity fields back every 50 steps (a sampled frame) and at the end."""
+    """The same metric through the public API from host buffers, for the whole job up to the
+    window's end: the scene's host inputs (mesh, materials, velocities, failure strains) are
+    generated first; the timed region then creates the solver from them (every upload), sets
+    it up, runs start + warm-up + timed steps, and reads the nodal displacement and velocity
+    fields back every 50 steps (a sampled frame) and at the end."""
     from neofiz_gb300 import ExplicitSolver, scenes
-    steps = args.steps
+    steps = args.start + args.warmup + args.steps
     inputs = scenes.perforation_inputs(cell=args.cell, gap=GAP)
     mesh = inputs["mesh"]
     E, N = mesh.elementCount, mesh.nodeCount
@@ -340,8 +441,9 @@ def run_e2e(args, torch):
     work = live_element_steps(E, 0, eroded, steps)
     return {"value": work / elapsed, "unit": "element-cycles/s",
             "h2d_bytes_per_step": h2d / steps, "d2h_bytes_per_step": d2h / steps,
-            "seconds": elapsed, "frames": frames,
-            "note": "create + uploads + set-up + steps + frame read-backs, host wall clock"}
+            "seconds": elapsed, "frames": frames, "steps": steps,
+            "note": "create + uploads + set-up + steps 0 .. window end + frame read-backs, "
+                    "host wall clock"}
 
 
 def _slug_velocity(g, mesh, slug):
@@ -644,7 +746,7 @@ def run_adjoint(args):
 
 
 def run_burst(args):
-    """A burst sweep (SURVEY f4; BurstCase.run over a BarlowSweep-like grid): args.burst_count
+    """A burst sweep (BurstCase.run over a BarlowSweep-like grid): args.burst_count
     two-element wall slices, slenderness 15..60 and mean radius 10..40 mm drawn by SplitMix64,
     OFHC copper, ramp to 1.06 x the closed-form burst pressure, each run on the device until
     its capacity has turned over (BurstCase's sampling every 250 steps). FP64 (bit-identical to
@@ -753,15 +855,21 @@ def run_tube_adjoint(args):
             "max_rel_error": max(o["rel"] for o in out.values())}
 
 
-def cpu_baseline(args, budget_s=12.0):
-    """The reference algorithm on this host's cores (oracle, threaded as the reference's
-    Parallel pool), on the same scene; a bounded sample of steps."""
+def oracle_scene(args):
+    """The oracle's copy of the scene on every host core."""
     from neofiz_gb300 import scenes
     from oracle.oracle import OracleSolver
     cores = os.cpu_count() or 1
-    s, mesh, _ = scenes.perforation(OracleSolver, cell=args.cell, gap=GAP)
+    s, mesh, info = scenes.perforation(OracleSolver, cell=args.cell, gap=GAP)
     s.setThreads(cores)
-    s.run(2)
+    return s, mesh, info, cores
+
+
+def cpu_baseline(args, budget_s=12.0):
+    """The reference algorithm on this host's cores (oracle, threaded as the reference's
+    Parallel pool), on the same scene from the window's start; a bounded sample of steps."""
+    s, mesh, _, cores = oracle_scene(args)
+    s.run(args.start)
     done, t = 0, 0.0
     eroded0 = s.erodedElements()
     while t < budget_s and done < 2000:
@@ -771,26 +879,49 @@ def cpu_baseline(args, budget_s=12.0):
         done += 5
     work = live_element_steps(mesh.elementCount, eroded0, s.erodedElements(), done)
     return {"value": work / t, "unit": "element-cycles/s", "cores": cores, "kind": "port",
-            "sample": f"{done} steps of the {mesh.elementCount}-quad perforation from t=0, "
-                      f"{t:.1f} s, {cores} threads"}
+            "sample": f"steps {args.start} .. {args.start + done} of the "
+                      f"{mesh.elementCount}-quad perforation, {t:.1f} s, {cores} threads"}
 
 
 def run_reference(args, world, rank):
+    """The reference arm: the oracle (the C restatement of the Java path, threaded as its
+    Parallel pool) on every host core, timing exactly the GPU arm's window. Its e2e is the
+    whole job to the window's end (set-up and every step), as the GPU arm's e2e is."""
     if rank != 0:
         return
-    cpu = cpu_baseline(args, budget_s=max(10.0, 2.0 * args.steps / 100.0))
+    t_all = time.perf_counter()
+    s, mesh, info, cores = oracle_scene(args)
+    E, N = mesh.elementCount, mesh.nodeCount
+    s.run(args.start)
+    facts = window_facts(s, info, s.time())
+    s.run(args.warmup)
+    eroded0 = s.erodedElements()
+    t0 = time.perf_counter()
+    s.run(args.steps)
+    t1 = time.perf_counter()
+    eroded1 = s.erodedElements()
+    facts["eroded_during_timing"] = eroded1 - eroded0
+    facts["contact_pairs_at_end"] = info["contact"].pairCount()
+    value = live_element_steps(E, eroded0, eroded1, args.steps) / (t1 - t0)
+    all_steps = args.start + args.warmup + args.steps
+    e2e = live_element_steps(E, 0, eroded1, all_steps) / (t1 - t_all)
+    sample = (f"steps {args.start + args.warmup} .. {all_steps} of the {E}-quad perforation, "
+              f"{t1 - t0:.2f} s, {cores} threads")
     line = {
         "impl": "reference",
         "metric": "element-cycles/s, plain FP64 explicit timestep (live elements x steps / s)",
-        "value": cpu["value"], "unit": "element-cycles/s", "n_gpus": world,
-        "steps": args.steps, "warmup": args.warmup, "higher_is_better": True,
-        "scaling": "weak", "vs_baseline": None, "dtype": "f64",
+        "value": value, "unit": "element-cycles/s", "n_gpus": world,
+        "steps": args.steps, "warmup": args.warmup,
+        "ms_per_step": (t1 - t0) * 1e3 / args.steps,
+        "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "f64",
         "data": "synthetic (generated scene; no dataset)",
-        "config": {"workload": "plane-strain perforation, ~200k quads (as --impl ours)",
-                   "cell_mm": args.cell * 1e3},
-        "cpu_baseline": cpu,
-        "e2e": {"value": cpu["value"], "unit": "element-cycles/s", "h2d_bytes_per_step": 0,
-                "d2h_bytes_per_step": 0},
+        "config": bench_config(args, E, N),
+        "window_state": facts,
+        "cpu_baseline": {"value": value, "unit": "element-cycles/s", "cores": cores,
+                         "kind": "port", "sample": sample},
+        "e2e": {"value": e2e, "unit": "element-cycles/s", "h2d_bytes_per_step": 0,
+                "d2h_bytes_per_step": 0, "seconds": t1 - t_all, "steps": all_steps,
+                "note": "set-up + steps 0 .. window end, host wall clock"},
     }
     print(json.dumps(line))
 

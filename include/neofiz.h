@@ -195,8 +195,24 @@ nf_status nf_create(const nf_mesh *mesh, const nf_material *materials, int32_t m
 nf_status nf_destroy(nf_solver *h);
 /* Message of the last failure on this handle, or of the calling thread when h is NULL. */
 const char *nf_last_error(const nf_solver *h);
+/* Bits of the status word. */
+enum { NF_STATUS_NONFINITE = 1,        /* a nodal velocity or displacement stopped being finite */
+       NF_STATUS_BUCKET_OVERFLOW = 4,  /* a contact bucket exceeded its bound */
+       NF_STATUS_TIMEOUT = 8 };        /* a contact-pass grid barrier gave up waiting */
 /* Sticky device-side status bits (NaN seen, wait timed out); 0 when healthy. */
 nf_status nf_status_word(nf_solver *h, uint32_t *word);
+/* Waits for the handle's work, then turns the status word into a status: NF_ETIMEOUT when a
+ * contact-pass barrier gave up (that step's contact forces are incomplete; the handle refuses
+ * every later nf_step, nf_advance and nf_run_until with NF_ETIMEOUT, and nf_synchronize
+ * reports it too), NF_EDEVICE when a nodal velocity or displacement stopped being finite,
+ * NF_OK otherwise. The reference has no counterpart: its NaNs propagate silently, and
+ * nothing of it waits on another thread without end. A caller checks this on sampled
+ * frames. */
+nf_status nf_check(nf_solver *h);
+/* Limits of the contact pass's grid-barrier wait: at most `polls` polls and `nanoseconds` of
+ * the GPU's global timer per wait (0 restores the defaults, 2^27 polls and one second). For
+ * tests that make a wait run out; no reference counterpart. */
+nf_status nf_set_wait_limit(nf_solver *h, int64_t polls, int64_t nanoseconds);
 
 /* ------------------------------------------------------------------ setup (ExplicitSolver) */
 
@@ -236,7 +252,8 @@ nf_status nf_advance(nf_solver *h);                 /* advance(), :1069-1075 */
  * round trip is needed. */
 nf_status nf_run_until(nf_solver *h, double t_end, int64_t max_steps, int64_t *taken);
 /* Blocks until the handle's stream is idle. nf_step and nf_advance only enqueue work; reads,
- * audits and nf_synchronize wait for it. */
+ * audits and nf_synchronize wait for it. Returns NF_ETIMEOUT when a contact-pass barrier of
+ * the work waited for gave up (see nf_check). */
 nf_status nf_synchronize(nf_solver *h);
 /* Runs the handle's kernels on a caller-owned cudaStream_t (passed as void*), or on its own
  * stream again when stream is NULL. No reference counterpart: lets a host application order
@@ -267,6 +284,12 @@ nf_status nf_profile(nf_solver *h, int32_t enable);
 nf_status nf_profile_read(nf_solver *h, double *ms, int64_t *steps);
 /* Kernel launches issued so far by this handle (a replayed graph counts its kernels). */
 nf_status nf_launch_count(nf_solver *h, int64_t *launches);
+
+/* The current device's FP64 pipe rate, measured by a kernel of independent dependent DFMA
+ * chains on every SM (best of three launches): DFMA warp instructions per second and FP64
+ * FLOPs per second (two per lane per DFMA). The denominator of the element pass's FP64
+ * roofline; no reference counterpart. */
+nf_status nf_device_fp64_rate(double *warp_instructions_per_second, double *flops_per_second);
 
 /* ------------------------------------------------------------------ read-back */
 
@@ -311,9 +334,12 @@ nf_status nf_material_point_update(const nf_material *material, int32_t formulat
  * that cannot allocate device memory -- cudaMalloc/cudaFree synchronise the whole device, and
  * a process whose GPU memory is owned by its own pool allocator has none to spare. It stages
  * through a fixed device array of 8192 points held by the library (1.77 MB on each GPU that
- * loads it), so it calls no allocator; count > 8192 is rejected with NF_EINVAL. The array's
- * address is looked up on the first call on each device (make that call before any stream
- * capture); calls share the array, so calls that overlap on the GPU race. */
+ * loads it), so it calls no allocator; count > 8192 is rejected with NF_EINVAL. The first
+ * call on each device looks the array's address up and creates the library's own
+ * non-blocking stream for that device (make that first call before any stream capture
+ * begins); every call copies, computes and copies back on that stream and waits for it
+ * alone, so it neither waits for nor holds up the caller's other streams. Calls share the
+ * array, so calls made from several host threads at once race on it. */
 nf_status nf_material_point_update_static(const nf_material *material, int32_t formulation,
                                           int32_t count, double *sig, double *back,
                                           double *eps_p, double *work, const double *strain,

@@ -39,3 +39,17 @@ def api():
         if lib.nf_device_count() < 1:
             raise NativeUnavailable("libneofiz_gpu.so loaded but no CUDA device is visible")
     return _api
+
+
+def fp64_rate():
+    """(FP64 DFMA warp instructions per second, FP64 FLOPs per second) of the current device,
+    measured by nf_device_fp64_rate."""
+    a = api()
+    fn = a.lib.nf_device_fp64_rate
+    fn.restype = ctypes.c_int
+    fn.argtypes = [ctypes.POINTER(ctypes.c_double), ctypes.POINTER(ctypes.c_double)]
+    w, f = ctypes.c_double(), ctypes.c_double()
+    st = fn(ctypes.byref(w), ctypes.byref(f))
+    if st:
+        raise RuntimeError(f"nf_device_fp64_rate failed: {a.last_error(None)}")
+    return w.value, f.value

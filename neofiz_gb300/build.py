@@ -22,7 +22,8 @@ CSRC = os.path.join(HERE, "csrc")
 BUILD = os.path.join(HERE, "_build")
 LIBRARY = os.path.join(BUILD, "libneofiz_gpu.so")
 SOURCES = ["api.cu", "api_batch.cu", "k_step.cu", "k_contact.cu", "k_scan.cu", "k_mixed.cu",
-           "k_batch.cu", "k_batch_comp.cu", "k_adjoint.cu", "k_film.cu", "noalloc.cu"]
+           "k_batch.cu", "k_batch_comp.cu", "k_adjoint.cu", "k_film.cu", "noalloc.cu",
+           "k_peak.cu"]
 ARCH = ["-gencode", "arch=compute_103a,code=sm_103a"]
 NVCC_FLAGS = ["-O3", "-std=c++17", "-lineinfo", "--fmad=false", "-prec-div=true",
               "-prec-sqrt=true", "-Xcompiler", "-fPIC,-ffp-contract=off,-O2",

@@ -40,7 +40,7 @@ def test_library_exports_every_declared_symbol(library):
     assert r.returncode == 0, f"missing exports: {r.stdout} {r.stderr}"
 
 
-DEVICE_ONLY = {"nf_device_count", "nf_material_point_update_static"}
+DEVICE_ONLY = {"nf_device_count", "nf_material_point_update_static", "nf_device_fp64_rate"}
 # the device film has no CPU counterpart (it captures device memory)
 FILM = {"nf_film_create", "nf_film_destroy", "nf_film_capture", "nf_film_frames",
         "nf_film_read", "nf_film_clear", "nf_film_last_error"}
