@@ -548,7 +548,7 @@ nf_status nf_destroy(nf_solver *h) {
                     d.dFail, d.dGf, d.dGeom, d.dStrength, d.dSoft, d.dWidth, d.contribution,
                     d.nodeSlotStart, d.nodeSlot, d.pedges, d.partials, d.edgeGroup, d.groupStart,
                     d.groupMember, d.surfFlag, d.surfPos, d.nodeFlag, d.nodePos, d.segA, d.segB,
-                    d.segOwner, d.surfNodes, d.slotOf, d.segCount, d.segStart, d.segOf,
+                    d.segQ, d.surfWork, d.surfNodes, d.slotOf, d.segCount, d.segStart, d.segOf,
                     d.segCursor, d.cr, d.cz, d.snr, d.snz, d.slen, d.pnr, d.pnz, d.lastMaster,
                     d.master, d.dropped, d.bucketCount, d.bucketStart, d.bucketCursor,
                     d.bucketEntry, d.bucketCell, d.entryCell, d.pairNodes, d.pairVal,
@@ -706,7 +706,23 @@ nf_status nf_set_contact(nf_solver *h, double friction, double damping, double s
         A(d.dead, E);
         A(d.surfFlag, 4LL * E); A(d.surfPos, 4LL * E);
         A(d.nodeFlag, N); A(d.nodePos, N);
-        A(d.segA, 4LL * E); A(d.segB, 4LL * E); A(d.segOwner, 4LL * E);
+        A(d.segA, 4LL * E); A(d.segB, 4LL * E); A(d.segQ, 4LL * E);
+        // incremental rebuild: 1 + 4 + 16 + 12 ints per element, 1 + 1 + 5 + 1 per node
+        A(d.surfWork, 33LL * E + 8LL * N);
+        if (e_ == cudaSuccess) {
+            int32_t *w = d.surfWork;
+            auto take = [&w](long long n) { int32_t *p = w; w += n; return p; };
+            d.newDead = take(E);
+            d.nodeFree = take(N);
+            d.edgeStamp = take(4LL * E);
+            d.nodeStamp = take(N);
+            d.addE = take(4LL * E); d.remE = take(4LL * E);
+            d.addES = take(4LL * E); d.remES = take(4LL * E);
+            d.touched = take(N); d.addN = take(N); d.remN = take(N);
+            d.addNS = take(N); d.remNS = take(N);
+            d.tmpA = take(4LL * E); d.tmpB = take(4LL * E); d.tmpQ = take(4LL * E);
+            d.tmpNodes = take(N);
+        }
         A(d.surfNodes, N); A(d.slotOf, N);
         A(d.segCount, N + 1); A(d.segStart, N + 1); A(d.segOf, 8LL * E); A(d.segCursor, N + 1);
         A(d.cr, N); A(d.cz, N);
@@ -732,6 +748,9 @@ nf_status nf_set_contact(nf_solver *h, double friction, double damping, double s
     nf_status st = read_scalars(S, &s);
     if (st) return st;
     s.stale = 1;                       // new Contact(mesh): adopt() on the first begin
+    s.fullRebuild = 1;
+    s.newDeadCount = 0;
+    s.nAddE = s.nRemE = s.nTouched = s.nAddN = s.nRemN = 0;
     s.pairs = 0;
     s.escaped = 0;
     s.cEnergy = 0.0;

@@ -7,6 +7,13 @@
 // counting-sort grid, the search, the pair forces and their ordered accumulation. It replaces
 // some thirty launches of small kernels, whose launch gaps dominated the pass.
 //
+// The surface rebuild after erosion is incremental: only the edge groups of the elements
+// eroded since the last rebuild can change, so their members are re-flagged, the edges that
+// became free or stopped being free are ordered, and the segment and node lists are merged
+// (each kept entry moves by the changes before it) instead of recompacting all 4 E element
+// edges and all N nodes. The lists are the ones a full rebuild gives, entry for entry; the full
+// rebuild runs at set-up and when an unusually large number of elements erodes at once.
+//
 // The reference's result depends on three orders, and each is reproduced exactly:
 //   * the surface is listed in element order and its nodes ascending (ordered compactions,
 //     i.e. exclusive scans of per-edge and per-node flags);
@@ -517,6 +524,28 @@ __device__ void finish_slave(const Dev &d, int i, double best, int bestSeg, bool
 
 // ---------------------------------------------------------------------------- the pass
 
+// More erosions than this since the last rebuild take the full rebuild (the change lists are
+// ordered by counting, quadratic in their length).
+constexpr int INC_MAX_DEAD = 512;
+
+// Position of v in the ascending a[0, n): the number of entries below it.
+__device__ __forceinline__ int lower_bound_i(const int32_t *a, int n, int v) {
+    int lo = 0, hi = n;
+    while (lo < hi) {
+        const int mid = (lo + hi) >> 1;
+        if (a[mid] < v) lo = mid + 1;
+        else hi = mid;
+    }
+    return lo;
+}
+
+// Rank of v among the distinct a[0, n): the number of entries below it.
+__device__ __forceinline__ int rank_in(const int32_t *a, int n, int v) {
+    int r = 0;
+    for (int j = 0; j < n; j++) r += a[j] < v;
+    return r;
+}
+
 // Items are dealt to warps across the blocks first (warp w of block b takes the 32 items from
 // (w G + b) 32 on), so that a short list still spreads over every SM.
 #define FOR_GRID(i, count)                                                                    \
@@ -535,65 +564,183 @@ __global__ void __launch_bounds__(CB, 2) k_contact_pass(Dev d) {
 
     if (vload(&s->stale)) {
         // Contact.adopt, Contact.java:290-322: the free surface (QuadMesh.surface over the live
-        // elements), edges in element order, nodes ascending
-        FOR_GRID(q, 4 * d.E) {
-            const int e = q >> 2;
-            int flag = 0;
-            if (!d.dead[e]) {
-                const int g = d.edgeGroup[q];
+        // elements, QuadMesh.java:188-226), edges in element order, nodes ascending
+        const int oldEdges = vload(&s->surfEdges), oldNodes = vload(&s->surfNodes);
+        const int nDead = vload(&s->newDeadCount);
+        const int epoch = vload(&s->rebuildEpoch) + 1;
+        if (vload(&s->fullRebuild) || nDead > INC_MAX_DEAD) {
+            // every element edge: free when it is the only live member of its group
+            FOR_GRID(q, 4 * d.E) {
+                const int e = q >> 2;
+                int flag = 0;
+                if (!d.dead[e]) {
+                    const int g = d.edgeGroup[q];
+                    int live = 0;
+                    for (int m = d.groupStart[g]; m < d.groupStart[g + 1]; m++)
+                        if (!d.dead[d.groupMember[m] >> 2]) live++;
+                    flag = live == 1;
+                }
+                d.surfFlag[q] = flag;
+            }
+            FOR_GRID(n, d.N) {
+                d.nodeFlag[n] = 0;
+                d.nodeFree[n] = 0;
+            }
+            SYNC();
+            if (!grid_scan(d, d.surfFlag, d.surfPos, nullptr, 4 * d.E, &s->surfEdges, false))
+                return;
+            FOR_GRID(q, 4 * d.E) {
+                if (!d.surfFlag[q]) continue;
+                const int e = q >> 2, k = q & 3;
+                const int4 c = d.conn[e];
+                const int nn[4] = {c.x, c.y, c.z, c.w};
+                const int a = nn[k], b = nn[(k + 1) & 3];
+                const int p = d.surfPos[q];
+                d.segA[p] = a;
+                d.segB[p] = b;
+                d.segQ[p] = q;
+                d.nodeFlag[a] = 1;
+                d.nodeFlag[b] = 1;
+                atomicAdd(&d.nodeFree[a], 1);
+                atomicAdd(&d.nodeFree[b], 1);
+            }
+            SYNC();
+            if (!grid_scan(d, d.nodeFlag, d.nodePos, nullptr, d.N, &s->surfNodes, false)) return;
+            FOR_GRID(n, d.N) {
+                if (d.nodeFlag[n]) {
+                    const int slot = d.nodePos[n];
+                    d.surfNodes[slot] = n;
+                    d.slotOf[n] = slot;
+                    d.lastMaster[slot] = -1;             // :319-321
+                    d.master[slot] = -1;
+                    d.dropped[slot] = 0;
+                    d.segCount[slot] = d.nodeFree[n];    // its incident free edges
+                } else {
+                    d.slotOf[n] = -1;
+                }
+            }
+            if (gt == 0) d.segCount[vload(&s->surfNodes)] = 0;
+            SYNC();
+        } else {
+            // only the edge groups of the elements eroded since the last rebuild can change:
+            // re-flag their members (each once: the epoch stamp), list the edges that became
+            // free or stopped being free, keep each node's count of incident free edges, and
+            // note the nodes whose count changed
+            FOR_GRID(t, 4 * nDead) {
+                const int g = d.edgeGroup[4 * d.newDead[t >> 2] + (t & 3)];
+                const int g0 = d.groupStart[g], g1 = d.groupStart[g + 1];
                 int live = 0;
-                for (int m = d.groupStart[g]; m < d.groupStart[g + 1]; m++)
+                for (int m = g0; m < g1; m++)
                     if (!d.dead[d.groupMember[m] >> 2]) live++;
-                flag = live == 1;
+                for (int m = g0; m < g1; m++) {
+                    const int q = d.groupMember[m];
+                    if (atomicExch(&d.edgeStamp[q], epoch) == epoch) continue;
+                    const int now = !d.dead[q >> 2] && live == 1;
+                    if (now == d.surfFlag[q]) continue;
+                    d.surfFlag[q] = now;
+                    if (now) d.addE[atomicAdd(&s->nAddE, 1)] = q;
+                    else d.remE[atomicAdd(&s->nRemE, 1)] = q;
+                    const int4 c = d.conn[q >> 2];
+                    const int nn[4] = {c.x, c.y, c.z, c.w};
+                    const int ends[2] = {nn[q & 3], nn[(q + 1) & 3]};
+                    for (int k = 0; k < 2; k++) {
+                        atomicAdd(&d.nodeFree[ends[k]], now ? 1 : -1);
+                        if (atomicExch(&d.nodeStamp[ends[k]], epoch) != epoch)
+                            d.touched[atomicAdd(&s->nTouched, 1)] = ends[k];
+                    }
+                }
             }
-            d.surfFlag[q] = flag;
-        }
-        FOR_GRID(n, d.N) d.nodeFlag[n] = 0;
-        SYNC();
-        if (!grid_scan(d, d.surfFlag, d.surfPos, nullptr, 4 * d.E, &s->surfEdges, false)) return;
-        FOR_GRID(q, 4 * d.E) {
-            if (!d.surfFlag[q]) continue;
-            const int e = q >> 2, k = q & 3;
-            const int4 c = d.conn[e];
-            const int nn[4] = {c.x, c.y, c.z, c.w};
-            const int a = nn[k], b = nn[(k + 1) & 3];
-            const int p = d.surfPos[q];
-            d.segA[p] = a;
-            d.segB[p] = b;
-            d.segOwner[p] = e;
-            d.nodeFlag[a] = 1;
-            d.nodeFlag[b] = 1;
-        }
-        SYNC();
-        if (!grid_scan(d, d.nodeFlag, d.nodePos, nullptr, d.N, &s->surfNodes, false)) return;
-        FOR_GRID(n, d.N) {
-            if (d.nodeFlag[n]) {
-                const int slot = d.nodePos[n];
-                d.surfNodes[slot] = n;
-                d.slotOf[n] = slot;
-                d.lastMaster[slot] = -1;             // :319-321
-                d.master[slot] = -1;
-                d.dropped[slot] = 0;
-                d.segCount[slot] = 0;
-            } else {
-                d.slotOf[n] = -1;
+            SYNC();
+            const int nAddE = vload(&s->nAddE), nRemE = vload(&s->nRemE);
+            const int nTouched = vload(&s->nTouched);
+            // the changed edges in ascending order; the nodes that joined or left the surface
+            FOR_GRID(i, nAddE) {
+                const int q = d.addE[i];
+                d.addES[rank_in(d.addE, nAddE, q)] = q;
             }
+            FOR_GRID(i, nRemE) {
+                const int q = d.remE[i];
+                d.remES[rank_in(d.remE, nRemE, q)] = q;
+            }
+            FOR_GRID(i, nTouched) {
+                const int n = d.touched[i];
+                const bool was = d.slotOf[n] >= 0, is = d.nodeFree[n] > 0;
+                if (is && !was) d.addN[atomicAdd(&s->nAddN, 1)] = n;
+                else if (was && !is) d.remN[atomicAdd(&s->nRemN, 1)] = n;
+            }
+            SYNC();
+            const int nAddN = vload(&s->nAddN), nRemN = vload(&s->nRemN);
+            FOR_GRID(i, nAddN) {
+                const int n = d.addN[i];
+                d.addNS[rank_in(d.addN, nAddN, n)] = n;
+            }
+            FOR_GRID(i, nRemN) {
+                const int n = d.remN[i];
+                d.remNS[rank_in(d.remN, nRemN, n)] = n;
+            }
+            // the merged edge list: a kept edge moves back by the removed edges before it and
+            // on by the added ones; an added edge lands after the kept edges before it
+            FOR_GRID(p, oldEdges) {
+                const int q = d.segQ[p];
+                if (!d.surfFlag[q]) continue;
+                const int np = p - lower_bound_i(d.remES, nRemE, q) + lower_bound_i(d.addES, nAddE, q);
+                d.tmpA[np] = d.segA[p];
+                d.tmpB[np] = d.segB[p];
+                d.tmpQ[np] = q;
+            }
+            FOR_GRID(r, nAddE) {
+                const int q = d.addES[r];
+                const int np = lower_bound_i(d.segQ, oldEdges, q) - lower_bound_i(d.remES, nRemE, q) + r;
+                const int4 c = d.conn[q >> 2];
+                const int nn[4] = {c.x, c.y, c.z, c.w};
+                d.tmpA[np] = nn[q & 3];
+                d.tmpB[np] = nn[(q + 1) & 3];
+                d.tmpQ[np] = q;
+            }
+            SYNC();
+            const int newEdges = oldEdges - nRemE + nAddE, newNodes = oldNodes - nRemN + nAddN;
+            FOR_GRID(p, newEdges) {
+                d.segA[p] = d.tmpA[p];
+                d.segB[p] = d.tmpB[p];
+                d.segQ[p] = d.tmpQ[p];
+            }
+            // the merged node list, the same way
+            FOR_GRID(i, oldNodes) {
+                const int n = d.surfNodes[i];
+                if (d.nodeFree[n] == 0) continue;
+                d.tmpNodes[i - lower_bound_i(d.remNS, nRemN, n) + lower_bound_i(d.addNS, nAddN, n)] = n;
+            }
+            FOR_GRID(r, nAddN) {
+                const int n = d.addNS[r];
+                d.tmpNodes[lower_bound_i(d.surfNodes, oldNodes, n) - lower_bound_i(d.remNS, nRemN, n) + r] = n;
+            }
+            FOR_GRID(r, nRemN) d.slotOf[d.remNS[r]] = -1;
+            if (gt == 0) {
+                s->surfEdges = newEdges;
+                s->surfNodes = newNodes;
+            }
+            SYNC();
+            FOR_GRID(i, newNodes) {
+                const int n = d.tmpNodes[i];
+                d.surfNodes[i] = n;
+                d.slotOf[n] = i;
+                d.lastMaster[i] = -1;                    // :319-321
+                d.master[i] = -1;
+                d.dropped[i] = 0;
+                d.segCount[i] = d.nodeFree[n];
+            }
+            if (gt == 0) d.segCount[newNodes] = 0;
+            SYNC();
         }
-        if (gt == 0) d.segCount[vload(&s->surfNodes)] = 0;
-        SYNC();
+        // each surface node's segments, ascending (:298-313)
         const int edges = vload(&s->surfEdges), nodes = vload(&s->surfNodes);
-        FOR_GRID(e, edges) {
-            atomicAdd(&d.segCount[d.slotOf[d.segA[e]]], 1);
-            atomicAdd(&d.segCount[d.slotOf[d.segB[e]]], 1);
-        }
-        SYNC();
         if (!grid_scan(d, d.segCount, d.segStart, d.segCursor, nodes + 1, nullptr, false)) return;
         FOR_GRID(e, edges) {
             d.segOf[atomicAdd(&d.segCursor[d.slotOf[d.segA[e]]], 1)] = e;
             d.segOf[atomicAdd(&d.segCursor[d.slotOf[d.segB[e]]], 1)] = e;
         }
         SYNC();
-        FOR_GRID(i, nodes) {                         // ascending order per node, :306-313
+        FOR_GRID(i, nodes) {
             const int lo = d.segStart[i], hi = d.segStart[i + 1];
             for (int k = lo + 1; k < hi; k++) {
                 const int v = d.segOf[k];
@@ -605,7 +752,13 @@ __global__ void __launch_bounds__(CB, 2) k_contact_pass(Dev d) {
                 d.segOf[j + 1] = v;
             }
         }
-        if (gt == 0) s->stale = 0;
+        if (gt == 0) {
+            s->stale = 0;
+            s->fullRebuild = 0;
+            s->newDeadCount = 0;
+            s->rebuildEpoch = epoch;
+            s->nAddE = s->nRemE = s->nTouched = s->nAddN = s->nRemN = 0;
+        }
         SYNC();
     }
     const int nodes = vload(&s->surfNodes), edges = vload(&s->surfEdges);

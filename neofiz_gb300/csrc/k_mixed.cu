@@ -71,6 +71,7 @@ __global__ void __launch_bounds__(MB) k_erode_mixed(Dev d) {
             if (d.hasContact) {
                 d.dead[e] = 1;
                 d.s->stale = 1;
+                d.newDead[atomicAdd(&d.s->newDeadCount, 1)] = e;   // at most E, ever
             }
         }
     }

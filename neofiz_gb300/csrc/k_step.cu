@@ -180,6 +180,7 @@ __device__ __forceinline__ void erode_element(const Dev &d, int e, double &energ
             if (d.hasContact) {                              // Contact.forget, :329-332
                 d.dead[e] = 1;
                 d.s->stale = 1;
+                d.newDead[atomicAdd(&d.s->newDeadCount, 1)] = e;   // at most E, ever
             }
         }
     }
@@ -279,12 +280,21 @@ int listed_pass_smem(int device) {
 }
 
 constexpr int HOT_BATCH = 8;
+constexpr int HOT_BUILD_THREADS = 256;
+
+// Blocks of k_hot_build: HOT_BATCH entries per thread of the longest list, at most two per SM.
+static int hot_build_blocks(const Dev &d) {
+    const int per = HOT_BUILD_THREADS * HOT_BATCH;
+    const int want = (d.hotCap + per - 1) / per;
+    return want < 1 ? 1 : want > 2 * d.sms ? 2 * d.sms : want;
+}
 
 // The next step's work list from the entries the pass appended: a counting sort by cost class,
 // most expensive first; listed elements are stamped with the new epoch.
-__global__ void __launch_bounds__(1024) k_hot_build(Dev d) {
+__global__ void __launch_bounds__(HOT_BUILD_THREADS) k_hot_build(Dev d) {
     if (!d.s->active) return;
     __shared__ int start[HOT_CLASSES];
+    __shared__ int last;
     HotList *h = d.hot;
     const int n = min(h->nextCount, d.hotCap);
     const int epoch = h->epoch + 1;
@@ -296,12 +306,12 @@ __global__ void __launch_bounds__(1024) k_hot_build(Dev d) {
         }
     }
     __syncthreads();
-    // lanes of a warp holding the same class take their positions with one atomic (few
-    // classes, many entries: per-entry atomics on a handful of shared words would serialise);
-    // each thread loads HOT_BATCH entries before using them, so their loads overlap
+    // every block takes a run of entries; lanes of a warp holding the same class take their
+    // positions in that class with one atomic on its global fill count (few classes, many
+    // entries); each thread loads HOT_BATCH entries before using them, so their loads overlap
     const int lane = threadIdx.x & 31;
-    const int stride = blockDim.x, span = HOT_BATCH * stride;
-    for (int base = threadIdx.x - lane; base < n; base += span) {
+    const int stride = gridDim.x * blockDim.x, span = HOT_BATCH * stride;
+    for (int base = blockIdx.x * blockDim.x + threadIdx.x - lane; base < n; base += span) {
         int2 it[HOT_BATCH];
 #pragma unroll
         for (int k = 0; k < HOT_BATCH; k++) {
@@ -313,7 +323,8 @@ __global__ void __launch_bounds__(1024) k_hot_build(Dev d) {
             const unsigned peers = __match_any_sync(0xffffffffu, it[k].y);
             const int leader = __ffs(peers) - 1;
             int first = 0;
-            if (it[k].y >= 0 && lane == leader) first = atomicAdd(&start[it[k].y], __popc(peers));
+            if (it[k].y >= 0 && lane == leader)
+                first = start[it[k].y] + atomicAdd(&h->fill[it[k].y], __popc(peers));
             first = __shfl_sync(0xffffffffu, first, leader);
             if (it[k].y >= 0) {
                 const int pos = first + __popc(peers & ((1u << lane) - 1u));
@@ -322,12 +333,22 @@ __global__ void __launch_bounds__(1024) k_hot_build(Dev d) {
             }
         }
     }
+    // the last block to finish clears the counts for the pass that appends next
+    __threadfence();
     __syncthreads();
-    for (int k = threadIdx.x; k < HOT_CLASSES; k += blockDim.x) h->classCount[k] = 0;
+    if (threadIdx.x == 0) last = atomicAdd(&h->done, 1) == (int)gridDim.x - 1;
+    __syncthreads();
+    if (!last) return;
+    __threadfence();
+    for (int k = threadIdx.x; k < HOT_CLASSES; k += blockDim.x) {
+        h->classCount[k] = 0;
+        h->fill[k] = 0;
+    }
     if (threadIdx.x == 0) {
         h->count = n;
         h->epoch = epoch;
         h->nextCount = 0;
+        h->done = 0;
     }
 }
 
@@ -524,8 +545,18 @@ __global__ void __launch_bounds__(256) k_end(Dev d, int nodeBlocks, int elemBloc
             src = d.partials + (PARTIAL_CONTACT + warp - 4) * d.maxBlocks;
             count = slotBlocks;
         }
+        // lane l adds partials l, l + 32, ... in that order; the loads of eight terms are
+        // issued before they are added, so the warp waits for one round trip per eight
         double v = 0.0;
-        for (int k = lane; k < count; k += 32) v += src[k];
+        int k = lane;
+        for (; k + 7 * 32 < count; k += 8 * 32) {
+            double x[8];
+#pragma unroll
+            for (int j = 0; j < 8; j++) x[j] = src[k + 32 * j];
+#pragma unroll
+            for (int j = 0; j < 8; j++) v += x[j];
+        }
+        for (; k < count; k += 32) v += src[k];
         for (int o = 16; o > 0; o >>= 1) v += __shfl_down_sync(0xffffffffu, v, o);
         if (lane == 0 && warp < 6) folded[warp] = v;
         __syncthreads();
@@ -598,7 +629,7 @@ static int assemble(Solver &S, int zeroStrain, bool prepared = false, bool erode
         } else if (d.hot) {
             k_element_reduced_listed<<<grid_for((long long)d.E + d.hotCap, BLOCK), BLOCK,
                                        d.hotSmem, st>>>(d, zeroStrain, erode ? 1 : 0);
-            k_hot_build<<<1, 1024, 0, st>>>(d);
+            k_hot_build<<<hot_build_blocks(d), HOT_BUILD_THREADS, 0, st>>>(d);
             n += 2;
         } else {
             k_element_reduced<<<grid_for(d.E, BLOCK), BLOCK, 0, st>>>(d, zeroStrain);

@@ -68,6 +68,10 @@ struct DevScalars {
     uint32_t status;
     uint32_t barCount, barGen, barAbort;     // grid barrier of the cooperative contact pass
     int incOverflow;                         // a node's incident terms outgrew its fixed list
+    // the free-surface rebuild (Contact.adopt): a full rebuild at set-up, an incremental one
+    // after erosion (elements eroded since the last rebuild, changes this rebuild)
+    int fullRebuild, newDeadCount, rebuildEpoch;
+    int nAddE, nRemE, nTouched, nAddN, nRemN;
 };
 
 // The element pass's Johnson-Cook work list (FP64 reduced integration). Points whose return
@@ -85,6 +89,8 @@ struct HotList {
     int epoch;                               // stamp of this step's listed elements
     int pad;
     int classCount[HOT_CLASSES];             // the appended (and kept) entries per cost class
+    int fill[HOT_CLASSES];                   // entries placed so far per class (k_hot_build)
+    int done;                                // blocks of k_hot_build that have finished
 };
 
 struct Dev {
@@ -121,7 +127,20 @@ struct Dev {
     int32_t *edgeGroup, *groupStart, *groupMember;   // element-edge -> group of equal edges
     int32_t *surfFlag, *surfPos;             // [4E]
     int32_t *nodeFlag, *nodePos;             // [N]
-    int32_t *segA, *segB, *segOwner;         // [4E] current surface edges
+    int32_t *segA, *segB, *segQ;             // [4E] current surface edges: end nodes, and the
+                                             // element edge (4 e + corner) each one is
+    // incremental free-surface rebuild, carved from one allocation (surfWork): the elements
+    // eroded since the last rebuild, the free edges incident to each node, the rebuild epoch of
+    // each edge's and node's last visit, the changed edges and nodes (as found, and sorted),
+    // and the merged lists before they are copied back
+    int32_t *surfWork;
+    int32_t *newDead;                        // [E]
+    int32_t *nodeFree;                       // [N]
+    int32_t *edgeStamp, *nodeStamp;          // [4E], [N]
+    int32_t *addE, *remE, *addES, *remES;    // [4E] each
+    int32_t *touched, *addN, *remN, *addNS, *remNS;   // [N] each
+    int32_t *tmpA, *tmpB, *tmpQ;             // [4E] each
+    int32_t *tmpNodes;                       // [N]
     int32_t *surfNodes, *slotOf;             // [N]
     int32_t *segCount, *segStart, *segOf, *segCursor;   // per surface node
     double *cr, *cz;                         // [N]
