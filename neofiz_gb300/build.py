@@ -43,6 +43,35 @@ def flags_for(src: str):
     return [f for f in NVCC_FLAGS if f not in strict] + FAST_FLOAT_FLAGS
 
 
+# The host-side set-up library (the defect field's deterministic arithmetic), plain C.
+HOST_LIBRARY = os.path.join(BUILD, "libneofiz_host.so")
+HOST_SOURCES = ["defect_field.c"]
+HOST_FLAGS = ["-O2", "-std=gnu11", "-ffp-contract=off", "-fno-fast-math", "-fPIC", "-shared",
+              "-pthread", "-fvisibility=hidden"]
+
+
+def build_host(force: bool = False) -> str:
+    """Compiles libneofiz_host.so with contraction off (no fused multiply-add contraction, so
+    the field is the same on every host)."""
+    os.makedirs(BUILD, exist_ok=True)
+    deps = [os.path.join(CSRC, f) for f in HOST_SOURCES]
+    deps += [os.path.join(CSRC, "nf_math.h"), os.path.join(CSRC, "nf_math_tables.h")]
+    if not force and os.path.exists(HOST_LIBRARY):
+        t = os.path.getmtime(HOST_LIBRARY)
+        if all(os.path.getmtime(d) <= t for d in deps):
+            return HOST_LIBRARY
+    cc = shutil.which("gcc") or shutil.which("cc")
+    if cc is None:
+        raise RuntimeError("no C compiler (gcc) found for libneofiz_host.so")
+    tmp = f"{HOST_LIBRARY}.{os.getpid()}.tmp"
+    cmd = [cc, *HOST_FLAGS, *[os.path.join(CSRC, f) for f in HOST_SOURCES], "-o", tmp, "-lm"]
+    r = subprocess.run(cmd, capture_output=True, text=True)
+    if r.returncode != 0:
+        raise RuntimeError(f"gcc failed on the host library:\n{r.stderr}")
+    os.replace(tmp, HOST_LIBRARY)
+    return HOST_LIBRARY
+
+
 def nvcc() -> str:
     cand = shutil.which("nvcc") or "/usr/local/cuda/bin/nvcc"
     if not os.path.exists(cand):
@@ -58,6 +87,7 @@ def _deps():
 
 def build(force: bool = False, verbose: bool = False, extra=()) -> str:
     os.makedirs(BUILD, exist_ok=True)
+    build_host(force)
     if not force and os.path.exists(LIBRARY):
         t = os.path.getmtime(LIBRARY)
         if all(os.path.getmtime(d) <= t for d in _deps()):

@@ -1,34 +1,71 @@
 """Host-side Weibull defect field: per-element failure strains for the damage model.
 
-Restates core/DefectField.java (smoothed hash-seeded white noise, :239-347) and
-core/Weibull.java (quantiles, size scaling, :114-164) in numpy. The field is a function of
-position only, so the same seed gives the same failure strain at the same place on any mesh
-(DefectFieldTest.java:112). The noise hash is the reference's SplitMix64-style mix
-(DefectField.java:325-347); the Box-Muller transform and the normal cdf use numpy/scipy
-rather than the reference's Cody erfc, so values agree with the reference to rounding, not
-bit for bit. The failure strains are set-up data handed to ExplicitSolver.setDamage.
+Restates core/DefectField.java (smoothed hash-seeded white noise, :239-347), core/Normal.java
+(Cody's erfc, :50-129) and core/Weibull.java (quantiles, size scaling, :114-164). The
+arithmetic runs in libneofiz_host.so (csrc/defect_field.c, built by neofiz_gb300.build) in the
+reference's operation order -- the window's sums row by row, Cody's rational erfc, log1p on the
+weak side -- over the deterministic elementary functions the kernels and the oracle share, so a
+field is bit-identical on every host rather than dependent on a platform's libm. The field is a
+function of position only, so the same seed gives the same failure strain at the same place on
+any mesh (DefectFieldTest.java:112). The failure strains are set-up data handed to
+ExplicitSolver.setDamage.
 """
 from __future__ import annotations
 
+import ctypes as C
 import math
 
 import numpy as np
 
-_M1 = np.uint64(0xBF58476D1CE4E5B9)
-_M2 = np.uint64(0x94D049BB133111EB)
-_GOLD = np.uint64(0x9E3779B97F4A7C15)
-_SALT = np.uint64(0xD6E8FEB86659FD93)
+_lib = None
 
 
-def _mix(z: np.ndarray) -> np.ndarray:
-    with np.errstate(over="ignore"):
-        z = (z ^ (z >> np.uint64(30))) * _M1
-        z = (z ^ (z >> np.uint64(27))) * _M2
-        return z ^ (z >> np.uint64(31))
+def _host():
+    """libneofiz_host.so, built on first use."""
+    global _lib
+    if _lib is None:
+        from . import build
+        lib = C.CDLL(build.build_host())
+        d, i64, u64 = C.c_double, C.c_int64, C.c_uint64
+        dp, lp = C.POINTER(C.c_double), C.POINTER(C.c_int64)
+        lib.nf_field_gaussian.argtypes = [d, u64, i64, dp, dp, dp]
+        lib.nf_field_gaussian.restype = C.c_int
+        lib.nf_field_failure_strain.argtypes = [d, d, d, d, u64, i64, dp, dp, dp, dp]
+        lib.nf_field_failure_strain.restype = C.c_int
+        lib.nf_field_white.argtypes = [u64, i64, lp, lp, dp]
+        lib.nf_field_white.restype = None
+        lib.nf_normal.argtypes = [i64, dp, dp, dp]
+        lib.nf_normal.restype = None
+        lib.nf_weibull_quantile.argtypes = [d, d, C.c_int, i64, dp, dp]
+        lib.nf_weibull_quantile.restype = None
+        lib.nf_weibull_size_factor.argtypes = [d, d]
+        lib.nf_weibull_size_factor.restype = d
+        _lib = lib
+    return _lib
 
 
-def _unit_open(bits: np.ndarray) -> np.ndarray:
-    return ((bits >> np.uint64(11)).astype(np.float64) + 0.5) * 2.0 ** -53
+def _arr(x) -> np.ndarray:
+    return np.ascontiguousarray(np.atleast_1d(np.asarray(x, dtype=np.float64)))
+
+
+def _p(a: np.ndarray):
+    return a.ctypes.data_as(C.POINTER(C.c_double))
+
+
+def normal_cdf(x) -> np.ndarray:
+    """Normal.cdf, core/Normal.java:33-35."""
+    x = _arr(x)
+    out = np.empty_like(x)
+    _host().nf_normal(x.size, _p(x), _p(out), None)
+    return out
+
+
+def normal_survival(x) -> np.ndarray:
+    """Normal.survival, core/Normal.java:43-45."""
+    x = _arr(x)
+    out = np.empty_like(x)
+    _host().nf_normal(x.size, _p(x), None, _p(out))
+    return out
 
 
 class Weibull:
@@ -42,16 +79,28 @@ class Weibull:
         self.scale = float(scale)
         self.modulus = float(modulus)
 
+    def _quantile(self, p, survival: int):
+        p = _arr(p)
+        bad = ~((p >= 0.0) & (p <= 1.0))
+        if np.any(bad):
+            raise ValueError(f"probability must lie in [0, 1], was {p[bad][0]}")
+        out = np.empty_like(p)
+        _host().nf_weibull_quantile(self.scale, self.modulus, survival, p.size, _p(p), _p(out))
+        return out
+
     def quantile(self, p):
-        return self.scale * np.power(-np.log1p(-np.asarray(p)), 1.0 / self.modulus)
+        """Weibull.quantile, :114-119: scale (-log1p(-p))^(1/m)."""
+        return self._quantile(p, 0)
 
     def quantileFromSurvival(self, s):
-        return self.scale * np.power(-np.log(np.asarray(s)), 1.0 / self.modulus)
+        """Weibull.quantileFromSurvival, :126-131: scale (-log s)^(1/m)."""
+        return self._quantile(s, 1)
 
     def minimumOf(self, n: float) -> "Weibull":
         if not (n > 0.0):
             raise ValueError(f"sample count must be positive, was {n}")
-        return Weibull(self.scale * n ** (-1.0 / self.modulus), self.modulus)
+        return Weibull(self.scale * _host().nf_weibull_size_factor(float(n), self.modulus),
+                       self.modulus)
 
     def forVolume(self, volume: float, referenceVolume: float) -> "Weibull":
         if not (volume > 0.0):
@@ -76,88 +125,44 @@ class DefectField:
         self.base = base
         self.referenceVolume = referenceVolume
         self.correlationLength = correlationLength
-        self.seed = np.uint64(seed & 0xFFFFFFFFFFFFFFFF)
+        self.seed = seed & 0xFFFFFFFFFFFFFFFF
         self.cell = correlationLength / self.CELLS_PER_LENGTH
         self.sigmaCells = (correlationLength / math.sqrt(2.0)) / self.cell
         self.radius = int(math.ceil(self.KERNEL_RADII * self.sigmaCells))
 
-    def white(self, i: np.ndarray, j: np.ndarray) -> np.ndarray:
+    def white(self, i, j) -> np.ndarray:
         """Unit normal deviate per lattice site (DefectField.java:325-332)."""
-        i = np.asarray(i, dtype=np.int64).astype(np.uint64)
-        j = np.asarray(j, dtype=np.int64).astype(np.uint64)
-        with np.errstate(over="ignore"):
-            h = _mix(np.full(i.shape, self.seed, dtype=np.uint64) + _GOLD)
-            h = _mix(h ^ (i * _M1))
-            h = _mix(h ^ (j * _M2))
-        u1 = _unit_open(h)
-        u2 = _unit_open(_mix(h ^ _SALT))
-        return np.sqrt(-2.0 * np.log(u1)) * np.cos(2.0 * math.pi * u2)
+        i = np.ascontiguousarray(np.atleast_1d(np.asarray(i, dtype=np.int64)))
+        j = np.ascontiguousarray(np.broadcast_to(np.asarray(j, dtype=np.int64), i.shape))
+        out = np.empty(i.shape)
+        lp = C.POINTER(C.c_int64)
+        _host().nf_field_white(int(self.seed), i.size, i.ctypes.data_as(lp),
+                               j.ctypes.data_as(lp), _p(out))
+        return out
 
     def gaussianAt(self, r, z) -> np.ndarray:
         """Separable Gaussian window over the lattice noise (DefectField.java:289-319)."""
-        r = np.atleast_1d(np.asarray(r, dtype=np.float64))
-        z = np.atleast_1d(np.asarray(z, dtype=np.float64))
-        gr = r / self.cell
-        gz = z / self.cell
-        i0 = np.floor(gr).astype(np.int64) - self.radius
-        j0 = np.floor(gz).astype(np.int64) - self.radius
-        taps = 2 * self.radius + 2
-        two = 2.0 * self.sigmaCells * self.sigmaCells
-        k = np.arange(taps)
-        wr = np.exp(-((gr[:, None] - (i0[:, None] + k)) ** 2) / two)
-        wz = np.exp(-((gz[:, None] - (j0[:, None] + k)) ** 2) / two)
-        norm = np.sqrt((wr * wr).sum(axis=1) * (wz * wz).sum(axis=1))
+        r, z = _arr(r), _arr(z)
         out = np.empty(r.size)
-        if r.size == 0:
-            return out
-        # The noise of a lattice site is the same for every point whose window covers it: when
-        # the windows' lattice box is small (a mesh much finer than the lattice), evaluate each
-        # site once and gather; the sums below are the same either way.
-        ilo, jlo = int(i0.min()), int(j0.min())
-        ni, nj = int(i0.max()) - ilo + taps, int(j0.max()) - jlo + taps
-        grid = None
-        if ni * nj <= min(r.size * taps * taps, 1 << 26):
-            gi = np.arange(ilo, ilo + ni, dtype=np.int64)
-            gj = np.arange(jlo, jlo + nj, dtype=np.int64)
-            grid = self.white(np.broadcast_to(gi[None, :], (nj, ni)),
-                              np.broadcast_to(gj[:, None], (nj, ni)))
-        chunk = 4096
-        for s in range(0, r.size, chunk):
-            e = min(r.size, s + chunk)
-            ii = i0[s:e, None, None] + k[None, None, :]
-            jj = j0[s:e, None, None] + k[None, :, None]
-            if grid is not None:
-                noise = grid[jj - jlo, ii - ilo]
-            else:
-                noise = self.white(np.broadcast_to(ii, (e - s, taps, taps)),
-                                   np.broadcast_to(jj, (e - s, taps, taps)))
-            row = (noise * wr[s:e, None, :]).sum(axis=2)
-            out[s:e] = (row * wz[s:e, :]).sum(axis=1)
-        return out / norm
-
-    def _transform(self, g: np.ndarray, volume) -> np.ndarray:
-        from math import sqrt
-        try:
-            from scipy.special import erfc
-        except ImportError:                       # pragma: no cover
-            from math import erfc as _e
-            erfc = np.vectorize(_e)
-        # one-dimensional arrays throughout: numpy evaluates a 0-d power by a different routine
-        # than an array's, and a point's value must not depend on how it was batched
-        volume = np.atleast_1d(np.asarray(volume, dtype=np.float64))
-        g = np.atleast_1d(np.asarray(g, dtype=np.float64))
-        local_scale = self.base.scale * (volume / self.referenceVolume) ** (
-            -1.0 / self.base.modulus)
-        c = np.clip(g, -self.CLAMP_SIGMA, self.CLAMP_SIGMA)
-        cdf = 0.5 * erfc(-c / sqrt(2.0))
-        surv = 0.5 * erfc(c / sqrt(2.0))
-        weak = local_scale * np.power(-np.log1p(-cdf), 1.0 / self.base.modulus)
-        strong = local_scale * np.power(-np.log(surv), 1.0 / self.base.modulus)
-        return np.where(c <= 0.0, weak, strong)
+        st = _host().nf_field_gaussian(self.correlationLength, int(self.seed), r.size, _p(r),
+                                       _p(z), _p(out))
+        if st:
+            raise MemoryError("the defect field's lattice does not fit in host memory")
+        return out
 
     def failureStrainForVolume(self, r, z, volume) -> np.ndarray:
-        """DefectField.java:233-236: the field at (r, z) for a given volume."""
-        return self._transform(self.gaussianAt(r, z), volume)
+        """DefectField.java:233-236: the field at (r, z) for a given volume, through the
+        copula (:262-274) to the volume's Weibull law."""
+        r, z = _arr(r), _arr(z)
+        volume = np.ascontiguousarray(np.broadcast_to(_arr(volume), r.shape))
+        out = np.empty(r.size)
+        st = _host().nf_field_failure_strain(self.base.scale, self.base.modulus,
+                                             self.referenceVolume, self.correlationLength,
+                                             int(self.seed), r.size, _p(r), _p(z), _p(volume),
+                                             _p(out))
+        if st:
+            raise MemoryError("the defect field's lattice does not fit in host memory")
+        return out
 
     def effectiveVolume(self, centroidRadius, crossSectionArea):
         """DefectField.java:204-208 (axisymmetric rings)."""
@@ -170,5 +175,4 @@ class DefectField:
         """DefectField.sampleOnto, DefectField.java:239-248 (axisymmetric size effect)."""
         rc = mesh.centroidRadii()
         zc = mesh.centroidZs()
-        g = self.gaussianAt(rc, zc)
-        return self._transform(g, self.effectiveVolume(rc, mesh.signedAreas()))
+        return self.failureStrainForVolume(rc, zc, self.effectiveVolume(rc, mesh.signedAreas()))
