@@ -29,8 +29,16 @@ enum { NF_ADJ_P_A = 0, NF_ADJ_P_B, NF_ADJ_P_N, NF_ADJ_P_C, NF_ADJ_P_M, NF_ADJ_P_
 
 #define NF_ADJ_SQRT_2_3 0x1.a20bd700c2c3ep-1
 #define NF_ADJ_TWO_THIRDS (2.0 / 3.0)
-#define NF_ADJ_TOLERANCE 1.0e-10
-#define NF_ADJ_ITERATIONS 25
+/* The reverse differentiates the Johnson-Cook return through its root (implicit function
+ * theorem), so the root it evaluates the derivative at is converged further than the forward
+ * pass converges it (J2.solve's 1e-10 A, J2.java:332-375, which the forward keeps for parity):
+ * at 1e-10 A a solve can stop short of the root -- a bracket closing on the rate term's kink,
+ * the iteration cap -- and over a long run the derivatives evaluated there drift from those of
+ * the map (0.3 % in d(L/L0)/d(friction) over the 80 us rod). Solved to 1e-14 A the reverse
+ * agrees with central differences of the forward map itself. The forward trajectory and the
+ * objective values are untouched: the plain step code produces them. */
+#define NF_ADJ_TOLERANCE 1.0e-14
+#define NF_ADJ_ITERATIONS 80
 
 /* The material constants one point reads (ExplicitSolver.java:289-299, J2.Flow.of). */
 typedef struct {
@@ -55,7 +63,7 @@ NF_HD double nf_adj_thermal_term(const nf_adj_mat *f, double temperature) {
     return 1.0 - nf_pow(homologous, f->m);
 }
 
-/* J2.solve, J2.java:332-375, in the forward kernels' order. */
+/* J2.solve, J2.java:332-375, in the forward kernels' order, to the reverse's tolerance. */
 NF_HD double nf_adj_solve(double norm, double stiffness, double plasticStrain,
                           double temperature, double dt, const nf_adj_mat *jc) {
     const double thermal = nf_adj_thermal_term(jc, temperature);

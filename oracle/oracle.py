@@ -24,8 +24,10 @@ CFLAGS = ["-O2", "-std=gnu11", "-ffp-contract=off", "-fno-fast-math", "-fPIC", "
 def build(force: bool = False) -> str:
     """Compiles refcpu.c with contraction off (bitwise Java evaluation order)."""
     os.makedirs(BUILD, exist_ok=True)
+    csrc = os.path.join(HERE, "..", "neofiz_gb300", "csrc")
     deps = SOURCES + [os.path.join(HERE, "..", "include", "neofiz.h"),
-                      os.path.join(HERE, "..", "neofiz_gb300", "csrc", "nf_math.h")]
+                      os.path.join(csrc, "nf_math.h"), os.path.join(csrc, "nf_math_tables.h"),
+                      os.path.join(csrc, "nf_adjoint.h")]
     if not force and os.path.exists(LIBRARY):
         t = os.path.getmtime(LIBRARY)
         if all(os.path.getmtime(d) <= t for d in deps):

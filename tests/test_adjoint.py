@@ -223,3 +223,30 @@ def test_yield_and_isotropic_hardening_gradients_match_central_differences():
     rod = _rod()
     _, jc = _gradients(rod, every=20)
     assert jc[0][1][_abi.PARAM_YIELD] == 0.0 and jc[0][1][_abi.PARAM_ISOTROPIC] == 0.0
+
+
+def test_full_run_gradients_match_central_differences_on_the_oracle():
+    """The reference adjoint over the 10 x 60 rod's whole 80 us run (about 3800 steps, every
+    kind of frozen decision switching many times): d(L/L0) and d(mushroom) with respect to
+    the wall friction, n and C against central differences (h = 1e-6 relative) within 1e-4.
+    The reverse solves the return map to its converged root; at the forward's tolerance the
+    friction gradient of L/L0 was off by 3.4e-3 over this run."""
+    import importlib.util
+    import os
+    spec = importlib.util.spec_from_file_location(
+        "adjoint_gpu_helpers", os.path.join(os.path.dirname(__file__), "test_adjoint_gpu.py"))
+    helpers = importlib.util.module_from_spec(spec)
+    spec.loader.exec_module(helpers)
+    rod = scenes.adjoint_rods(1)[0]
+    b = OracleBatch(scenes.sweep_instances([rod]), scenes.Formulation.AXISYMMETRIC, cfl=0.6)
+    b.adjointForward(200)
+    steps = int(b.state()["steps"][0])
+    grads = {obj: b.adjointBackward(obj)[1][0] for obj in (0, 1)}
+    b.close()
+    names = ("friction", "n", "C")
+    fd = helpers._fd_full_run(OracleBatch, rod, steps, names)
+    for name in names:
+        k = _abi.PARAM_NAMES.index(name)
+        for obj in (0, 1):
+            ad, ref = grads[obj][k], fd[name][obj]
+            assert abs(ad - ref) <= 1e-4 * abs(ref), (name, obj, ad, ref)

@@ -123,3 +123,56 @@ def test_linear_hardening_gradients_match_the_reference_adjoint(gpu_lib):
         assert np.array_equal(g[0], o[0])
         np.testing.assert_allclose(g[1], o[1], rtol=1e-9, atol=0.0)
         assert np.all(g[1][:, _abi.PARAM_YIELD] != 0.0)
+
+
+def _fd_full_run(cls, rod, steps, names, h=1.0e-6):
+    """Central differences of L/L0 and the mushroom diameter after `steps` steps of the plain
+    path, one parameter at a time, the perturbed rods run as one batch."""
+    import dataclasses
+    jc0 = scenes._rod_jc(rod)
+    mat0 = scenes.rod_material_with(jc0)
+    p0 = {"A": jc0.a, "B": jc0.b, "n": jc0.n, "C": jc0.c, "m": jc0.m,
+          "kinematic": mat0.kinematicHardening, "friction": rod["mu"]}
+    insts = []
+    for name in names:
+        for sgn in (1.0, -1.0):
+            inst = scenes.sweep_instances([rod])[0]
+            val = p0[name] * (1.0 + sgn * h)
+            if name in ("A", "B", "n", "C", "m"):
+                f = {"A": "a", "B": "b", "n": "n", "C": "c", "m": "m"}[name]
+                inst.material = scenes.rod_material_with(
+                    dataclasses.replace(jc0, **{f: val})).withKinematicHardening(
+                        mat0.kinematicHardening)
+            elif name == "kinematic":
+                inst.material = mat0.withKinematicHardening(val)
+            else:
+                inst.wall = (0.0, val)
+            inst.t_end = 1.0
+            insts.append(inst)
+    b = cls(insts, scenes.Formulation.AXISYMMETRIC, cfl=0.6)
+    b.run(max_steps=steps)
+    m = b.measure()
+    b.close()
+    return {name: ((m[2 * k].length - m[2 * k + 1].length) / 25.0e-3 / (2.0 * p0[name] * h),
+                   (m[2 * k].mushroom_diameter - m[2 * k + 1].mushroom_diameter)
+                   / (2.0 * p0[name] * h)) for k, name in enumerate(names)}
+
+
+def test_full_run_gradients_match_central_differences(gpu_lib):
+    """The 10 x 60 rod of the gradient batch over its whole 80 us (about 3800 steps): the
+    kernel's gradients of L/L0 and of the mushroom diameter with respect to A, B, n, C, m, the
+    kinematic modulus and the wall friction against central differences of the plain path
+    (h = 1e-6 relative), within 1e-4 (the bar for gradients is 1e-3)."""
+    rod = scenes.adjoint_rods(1)[0]
+    b = BatchSolver(scenes.sweep_instances([rod]), scenes.Formulation.AXISYMMETRIC, cfl=0.6)
+    b.adjointForward(200)
+    steps = int(b.state()["steps"][0])
+    grads = {obj: b.adjointBackward(obj)[1][0] for obj in (0, 1)}
+    b.close()
+    assert steps > 3000
+    names = ("A", "B", "n", "C", "m", "kinematic", "friction")
+    fd = _fd_full_run(BatchSolver, rod, steps, names)
+    for k, name in enumerate(names):
+        for obj in (0, 1):
+            ad, ref = grads[obj][k], fd[name][obj]
+            assert abs(ad - ref) <= 1e-4 * abs(ref), (name, obj, ad, ref)
