@@ -38,10 +38,10 @@ WINDOW_START = 400          # steps run before warm-up and timing, in both arms
 L2_FLUSH_BYTES = 256 << 20
 # DRAM bytes (read + write) of one element-pass launch of this workload after 300 steps, from
 # ncu's dram__bytes_read.sum + dram__bytes_write.sum (ncu cannot run inside the timed bench)
-ELEMENT_TRAFFIC_BYTES = {CELL: 40_489_984 + 62_976}
-# FP64-pipe warp instructions of one element-pass launch in the window (ncu's
-# smsp__inst_executed_pipe_fp64.sum on the launch of step start + 1)
-ELEMENT_FP64_WARP_INST = {CELL: None}
+ELEMENT_TRAFFIC_BYTES = {CELL: 40_560_000 + 40_000}
+# FP64-pipe warp instructions of one element-pass launch in the window: the mean of ncu's
+# smsp__inst_executed_pipe_fp64.sum over the launches of steps start + 6 and start + 7
+ELEMENT_FP64_WARP_INST = {CELL: (3_784_456 + 3_675_685) // 2}
 
 
 def parse():
