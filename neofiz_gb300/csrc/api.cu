@@ -555,7 +555,7 @@ nf_status nf_destroy(nf_solver *h) {
                     d.pairEnergy, d.pairDiss, d.incCount, d.incStart, d.incCursor, d.incEntry,
                     d.scanTmp, d.s, d.matsF, d.sigF, d.backF, d.epsPF, d.wPF, d.hgKF,
                     d.contribF, d.hgF, d.dStrF, d.dSoftF, d.dWidthF, d.dFailF, d.dGfF, d.dGeomF,
-                    d.pMid, d.pCur, d.vdt, d.gaussVol, d.coopSums, d.incSlots, d.bucketA, d.bucketN, d.slaveXY,
+                    d.pMid, d.pCur, d.vdt, d.gaussVol, d.coopSums, d.incSlots, d.bucketA, d.bucketN, d.bucketL, d.slaveXY,
                     d.hot, d.hotList, d.hotNext, d.hotStamp};
     const char *a0 = static_cast<const char *>(S->arena), *a1 = a0 + S->arenaBytes;
     for (void *p : ptrs) {
@@ -732,6 +732,7 @@ nf_status nf_set_contact(nf_solver *h, double friction, double damping, double s
         A(d.bucketCount, d.bucketCap + 1); A(d.bucketStart, d.bucketCap + 1);
         A(d.bucketCursor, d.bucketCap + 1);
         A(d.bucketEntry, 8LL * E); A(d.bucketA, 8LL * E); A(d.bucketN, 8LL * E);
+        A(d.bucketL, 8LL * E);
         A(d.slaveXY, N); A(d.bucketCell, 8LL * E); A(d.entryCell, 8LL * E);
         A(d.pairNodes, N); A(d.pairVal, 12LL * N); A(d.pairEnergy, N); A(d.pairDiss, N);
         A(d.incCount, N + 1); A(d.incStart, N + 1); A(d.incCursor, N + 1); A(d.incEntry, 3LL * N);

@@ -473,14 +473,23 @@ __device__ void search_group(const Dev &d, const Grid &g, int slot, int nodes, d
         const long long kc = d.bucketCell[k];
         const int entry = d.bucketEntry[k];
         const double2 pa = d.bucketA[k], nrm = d.bucketN[k];
+        const double len = d.bucketL[k];
         if (kc != cc) continue;
-        const double gap = (xn.x - pa.x) * nrm.x + (xn.y - pa.y) * nrm.y;
-        if (!(gap < 0.0)) continue;             // depth_of would return zero
+        // depth_of from what the filing staged beside the entry (the segment's first node,
+        // normal and length: the same values, the same expressions): zero unless the slave is
+        // behind the segment and projects onto it
+        const double dr = xn.x - pa.x, dz = xn.y - pa.y;
+        const double gap = dr * nrm.x + dz * nrm.y;
+        if (!(gap < 0.0)) continue;
+        if (len <= 0.0) continue;
+        const double along = dr * -nrm.y + dz * nrm.x;
+        if (along < 0.0 || along > len) continue;
+        const double depth = -gap;
+        // the exclusions read the slave's own rings (dependent loads); a candidate that fails
+        // them is skipped whatever its depth, so testing them after the depth changes nothing
         const int sg = entry >> 1;
         if (excluded(d, slot, n, sg)) continue;
-        const double depth = depth_of(d, n, sg);
-        if (depth <= 0.0) continue;
-        if (depth > MAX_DEPTH * d.slen[sg]) {
+        if (depth > MAX_DEPTH * len) {
             if (sg == last) fell = true;
             continue;
         }
@@ -865,6 +874,7 @@ __global__ void __launch_bounds__(CB, 2) k_contact_pass(Dev d) {
         d.bucketCell[pos] = cell;
         d.bucketA[pos] = make_double2(d.cr[a], d.cz[a]);
         d.bucketN[pos] = make_double2(d.snr[e], d.snz[e]);
+        d.bucketL[pos] = d.slen[e];
     }
     SYNC();
 

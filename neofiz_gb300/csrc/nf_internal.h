@@ -151,6 +151,7 @@ struct Dev {
     int32_t *bucketCount, *bucketStart, *bucketCursor;   // [bucketCap + 1]
     int32_t *bucketEntry;                    // [8E] entries (2 s + end)
     double2 *bucketA, *bucketN;              // [8E] by position: the segment's first node, normal
+    double *bucketL;                         // [8E] by position: the segment's length
     long long *bucketCell;                   // [8E] cell of each filed entry, by position
     long long *entryCell;                    // [8E] cell of each entry, by entry
     int bucketCap;
