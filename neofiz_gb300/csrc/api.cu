@@ -547,15 +547,15 @@ nf_status nf_destroy(nf_solver *h) {
                     d.emat, d.mats, d.sig, d.back, d.epsP, d.wP, d.hg, d.hgK, d.gone, d.dead,
                     d.dFail, d.dGf, d.dGeom, d.dStrength, d.dSoft, d.dWidth, d.contribution,
                     d.nodeSlotStart, d.nodeSlot, d.pedges, d.partials, d.edgeGroup, d.groupStart,
-                    d.groupMember, d.surfFlag, d.surfPos, d.nodeFlag, d.nodePos, d.segA, d.segB,
-                    d.segQ, d.surfWork, d.surfNodes, d.slotOf, d.segCount, d.segStart, d.segOf,
-                    d.segCursor, d.cr, d.cz, d.snr, d.snz, d.slen, d.pnr, d.pnz, d.lastMaster,
+                    d.groupMember, d.surfFlag, d.segA, d.segB, d.edgeList, d.edgePos, d.nodeList,
+                    d.nodePos, d.nodeFree, d.nodeSeg, d.edgeStamp, d.nodeStamp, d.touched,
+                    d.newDead, d.cr, d.cz, d.snr, d.snz, d.slen, d.pnr, d.pnz, d.lastMaster,
                     d.master, d.dropped, d.bucketCount, d.bucketStart, d.bucketCursor,
                     d.bucketEntry, d.bucketCell, d.entryCell, d.pairNodes, d.pairVal,
                     d.pairEnergy, d.pairDiss, d.incCount, d.incStart, d.incCursor, d.incEntry,
                     d.scanTmp, d.s, d.matsF, d.sigF, d.backF, d.epsPF, d.wPF, d.hgKF,
                     d.contribF, d.hgF, d.dStrF, d.dSoftF, d.dWidthF, d.dFailF, d.dGfF, d.dGeomF,
-                    d.pMid, d.pCur, d.vdt, d.gaussVol, d.coopSums, d.incSlots, d.bucketA, d.bucketN, d.bucketL, d.slaveXY,
+                    d.pMid, d.pCur, d.vdt, d.gaussVol, d.coopSums, d.incSlots, d.bucketA, d.bucketN, d.bucketL,
                     d.hot, d.hotList, d.hotNext, d.hotStamp};
     const char *a0 = static_cast<const char *>(S->arena), *a1 = a0 + S->arenaBytes;
     for (void *p : ptrs) {
@@ -700,31 +700,23 @@ nf_status nf_set_contact(nf_solver *h, double friction, double damping, double s
                     "frequency exceeds what central difference can integrate, was %.17g", scale);
     Dev &d = S.d;
     const int N = S.N, E = S.E;
+    // a node's free edges are at most two per element around it
+    std::vector<int32_t> valence(N, 0);
+    for (long long k = 0; k < 4LL * E; k++) valence[S.hostConn[k]]++;
+    int segCap = 2;
+    for (int n = 0; n < N; n++) segCap = std::max(segCap, 2 * valence[n]);
     if (!d.dead) {
         cudaError_t e_ = cudaSuccess;
 #define A(ptr, n) if (e_ == cudaSuccess) e_ = dalloc(S, &(ptr), (n))
         A(d.dead, E);
-        A(d.surfFlag, 4LL * E); A(d.surfPos, 4LL * E);
-        A(d.nodeFlag, N); A(d.nodePos, N);
-        A(d.segA, 4LL * E); A(d.segB, 4LL * E); A(d.segQ, 4LL * E);
-        // incremental rebuild: 1 + 4 + 16 + 12 ints per element, 1 + 1 + 5 + 1 per node
-        A(d.surfWork, 33LL * E + 8LL * N);
-        if (e_ == cudaSuccess) {
-            int32_t *w = d.surfWork;
-            auto take = [&w](long long n) { int32_t *p = w; w += n; return p; };
-            d.newDead = take(E);
-            d.nodeFree = take(N);
-            d.edgeStamp = take(4LL * E);
-            d.nodeStamp = take(N);
-            d.addE = take(4LL * E); d.remE = take(4LL * E);
-            d.addES = take(4LL * E); d.remES = take(4LL * E);
-            d.touched = take(N); d.addN = take(N); d.remN = take(N);
-            d.addNS = take(N); d.remNS = take(N);
-            d.tmpA = take(4LL * E); d.tmpB = take(4LL * E); d.tmpQ = take(4LL * E);
-            d.tmpNodes = take(N);
-        }
-        A(d.surfNodes, N); A(d.slotOf, N);
-        A(d.segCount, N + 1); A(d.segStart, N + 1); A(d.segOf, 8LL * E); A(d.segCursor, N + 1);
+        A(d.surfFlag, 4LL * E);
+        A(d.segA, 4LL * E); A(d.segB, 4LL * E);
+        A(d.edgeList, 4LL * E); A(d.edgePos, 4LL * E);
+        A(d.nodeList, N); A(d.nodePos, N);
+        A(d.nodeFree, N);
+        A(d.nodeSeg, (size_t)N * (size_t)segCap);
+        A(d.edgeStamp, 4LL * E); A(d.nodeStamp, N); A(d.touched, N);
+        A(d.newDead, E);
         A(d.cr, N); A(d.cz, N);
         A(d.snr, 4LL * E); A(d.snz, 4LL * E); A(d.slen, 4LL * E);
         A(d.pnr, N); A(d.pnz, N);
@@ -733,7 +725,7 @@ nf_status nf_set_contact(nf_solver *h, double friction, double damping, double s
         A(d.bucketCursor, d.bucketCap + 1);
         A(d.bucketEntry, 8LL * E); A(d.bucketA, 8LL * E); A(d.bucketN, 8LL * E);
         A(d.bucketL, 8LL * E);
-        A(d.slaveXY, N); A(d.bucketCell, 8LL * E); A(d.entryCell, 8LL * E);
+        A(d.bucketCell, 8LL * E); A(d.entryCell, 8LL * E);
         A(d.pairNodes, N); A(d.pairVal, 12LL * N); A(d.pairEnergy, N); A(d.pairDiss, N);
         A(d.incCount, N + 1); A(d.incStart, N + 1); A(d.incCursor, N + 1); A(d.incEntry, 3LL * N);
         A(d.incSlots, (size_t)NF_INC_CAP * N);
@@ -742,6 +734,18 @@ nf_status nf_set_contact(nf_solver *h, double friction, double damping, double s
 #undef A
         if (e_ != cudaSuccess)
             return fail(&S, NF_ENOMEM, "contact allocation failed: %s", cudaGetErrorString(e_));
+        d.segCap = segCap;
+        // the end nodes of every element edge (QuadMesh.surface's edge k of element e runs
+        // from corner k to corner k + 1)
+        std::vector<int32_t> a(4LL * E), b(4LL * E);
+        for (long long q = 0; q < 4LL * E; q++) {
+            a[q] = S.hostConn[q];
+            b[q] = S.hostConn[(q & ~3LL) + ((q + 1) & 3)];
+        }
+        CK(&S, upload(S, d.segA, a.data(), a.size()));
+        CK(&S, upload(S, d.segB, b.data(), b.size()));
+        const nf_status up = sync_check(S);             // a and b are about to go
+        if (up) return up;
     } else {
         CK(&S, cudaMemsetAsync(d.dead, 0, E, S.stream));
     }
@@ -751,7 +755,8 @@ nf_status nf_set_contact(nf_solver *h, double friction, double damping, double s
     s.stale = 1;                       // new Contact(mesh): adopt() on the first begin
     s.fullRebuild = 1;
     s.newDeadCount = 0;
-    s.nAddE = s.nRemE = s.nTouched = s.nAddN = s.nRemN = 0;
+    s.nTouched = 0;
+    s.edgeListLen = s.nodeListLen = 0;
     s.pairs = 0;
     s.escaped = 0;
     s.cEnergy = 0.0;
@@ -1187,27 +1192,44 @@ nf_status nf_read_field(nf_solver *h, int32_t field, void *dst, size_t nbytes) {
             return NF_OK;
         }
         case NF_FIELD_CONTACT_MASTER: {
+            // the device keeps masters as element edges; the reference numbers a segment by
+            // its rank among the free edges in element order (QuadMesh.surface)
             int32_t *o = (int32_t *)dst;
             for (size_t i = 0; i < count; i++) o[i] = -1;
             if (!S.contactSet) return NF_OK;
-            DevScalars s;
-            st = read_scalars(S, &s);
-            if (st) return st;
-            std::vector<int32_t> nodes(s.surfNodes), master(s.surfNodes);
-            if (s.surfNodes) {
-                CK(&S, cudaMemcpy(nodes.data(), d.surfNodes, 4 * (size_t)s.surfNodes, cudaMemcpyDeviceToHost));
-                CK(&S, cudaMemcpy(master.data(), d.master, 4 * (size_t)s.surfNodes, cudaMemcpyDeviceToHost));
+            std::vector<int32_t> flag(4LL * S.E), pos(S.N), master(S.N);
+            CK(&S, cudaMemcpy(flag.data(), d.surfFlag, 4 * flag.size(), cudaMemcpyDeviceToHost));
+            CK(&S, cudaMemcpy(pos.data(), d.nodePos, 4 * pos.size(), cudaMemcpyDeviceToHost));
+            CK(&S, cudaMemcpy(master.data(), d.master, 4 * master.size(), cudaMemcpyDeviceToHost));
+            std::vector<int32_t> rank(flag.size());
+            int32_t r = 0;
+            for (size_t q = 0; q < flag.size(); q++) {
+                rank[q] = r;
+                r += flag[q] ? 1 : 0;
             }
-            for (int i = 0; i < s.surfNodes; i++) o[nodes[i]] = master[i];
+            for (int n = 0; n < S.N; n++)
+                if (pos[n] >= 0 && master[n] >= 0) o[n] = rank[master[n]];
             return NF_OK;
         }
-        case NF_FIELD_SURFACE_NODES: return copy(d.surfNodes);
-        case NF_FIELD_SURFACE_EDGES: {
-            std::vector<int32_t> a(count / 2), b(count / 2);
-            CK(&S, cudaMemcpy(a.data(), d.segA, 4 * a.size(), cudaMemcpyDeviceToHost));
-            CK(&S, cudaMemcpy(b.data(), d.segB, 4 * b.size(), cudaMemcpyDeviceToHost));
+        case NF_FIELD_SURFACE_NODES: {              // the surface nodes, ascending
+            std::vector<int32_t> free(S.N);
+            CK(&S, cudaMemcpy(free.data(), d.nodeFree, 4 * free.size(), cudaMemcpyDeviceToHost));
             int32_t *o = (int32_t *)dst;
-            for (size_t i = 0; i < a.size(); i++) { o[2 * i] = a[i]; o[2 * i + 1] = b[i]; }
+            size_t k = 0;
+            for (int n = 0; n < S.N && k < count; n++)
+                if (free[n] > 0) o[k++] = n;
+            return NF_OK;
+        }
+        case NF_FIELD_SURFACE_EDGES: {              // the free edges in element order
+            std::vector<int32_t> flag(4LL * S.E);
+            CK(&S, cudaMemcpy(flag.data(), d.surfFlag, 4 * flag.size(), cudaMemcpyDeviceToHost));
+            int32_t *o = (int32_t *)dst;
+            size_t k = 0;
+            for (size_t q = 0; q < flag.size() && k + 1 < count + 1; q++) {
+                if (!flag[q]) continue;
+                o[k++] = S.hostConn[q];
+                o[k++] = S.hostConn[(q & ~(size_t)3) + ((q + 1) & 3)];
+            }
             return NF_OK;
         }
         default: return fail(&S, NF_EINVAL, "unknown field %d", field);

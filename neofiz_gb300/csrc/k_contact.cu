@@ -7,27 +7,33 @@
 // counting-sort grid, the search, the pair forces and their ordered accumulation. It replaces
 // some thirty launches of small kernels, whose launch gaps dominated the pass.
 //
-// The surface rebuild after erosion is incremental: only the edge groups of the elements
-// eroded since the last rebuild can change, so their members are re-flagged, the edges that
-// became free or stopped being free are ordered, and the segment and node lists are merged
-// (each kept entry moves by the changes before it) instead of recompacting all 4 E element
-// edges and all N nodes. The lists are the ones a full rebuild gives, entry for entry; the full
-// rebuild runs at set-up and when an unusually large number of elements erodes at once.
+// A segment is named by its element edge q = 4 e + corner and a surface node by its node
+// number, and all per-segment and per-node state is indexed by them. The reference numbers
+// its segments by their rank among the free edges in element order and its surface nodes by
+// rank in ascending node order; ranks are monotone in q and in the node number, so wherever
+// the reference's answer depends on an order, ordering by q or by node number gives the same
+// answer, and the surface needs no ordered lists at all: the free edges and the surface nodes
+// are kept as lists in any order, appended to and struck out as erosion changes them, and
+// each node keeps its own free edges in ascending q. After erosion only the edge groups of the
+// eroded elements are re-flagged and only the nodes they touch are revisited (two phases);
+// the first rebuild flags every element edge. Segment numbers are formed only when a caller
+// reads them (the host ranks the free edges).
 //
 // The reference's result depends on three orders, and each is reproduced exactly:
-//   * the surface is listed in element order and its nodes ascending (ordered compactions,
-//     i.e. exclusive scans of per-edge and per-node flags);
+//   * each node's segments, for its normal and its exclusion rings, in ascending segment
+//     order (ascending q);
 //   * the search visits the nine cells in (dj, di) order and, within a cell, the segments in
 //     the order the counting sort filed them -- ascending segment, first endpoint before the
 //     second (Contact.java:530-545, :578-603). Buckets are filled with atomics in any order;
-//     each candidate carries its visit key (cell in the nine, 2 s + endpoint) instead, and
+//     each candidate carries its visit key (cell in the nine, 2 q + endpoint) instead, and
 //     ties in depth go to the smallest key, the candidate the serial loop keeps;
 //   * every node's force receives its contact terms in slave order, normal before tangent
 //     (Contact.java:446-462, :717-754). Each pair's twelve terms are computed in parallel and
-//     filed in fixed per-node lists; each node then sorts its list and adds in that order.
-// The running totals (spring energy, dissipation) are audits; they are reduced in a fixed
-// order per block over a fixed grid, so they are deterministic but not summed in the
-// reference's serial order.
+//     filed in fixed per-node lists of entries (slave node << 2 | role); each node then sorts
+//     its list and adds in that order.
+// The running totals (spring energy, dissipation) are audits: each slave's terms are kept per
+// node and summed over a fixed grid of node numbers in a fixed order, so they are deterministic
+// but not summed in the reference's serial order.
 //
 // The grid barrier is a counter and a generation word in device memory. The launch is
 // cooperative, so every block is resident and the barrier cannot deadlock; its wait is bounded
@@ -275,15 +281,17 @@ __device__ __forceinline__ int bucket_of(const Dev &d, const Grid &g, long long 
     return g.hashed ? (int)(cell % d.bucketCap) : (int)cell;
 }
 
-// Contact.excluded, Contact.java:620-639
-__device__ __forceinline__ bool excluded(const Dev &d, int i, int n, int s) {
-    const int a = d.segA[s], b = d.segB[s];
-    if (d.pnr[i] * d.snr[s] + d.pnz[i] * d.snz[s] > -FACING) return true;
+// Contact.excluded, Contact.java:620-639, for slave node n and segment q: facing, an end of
+// its own, or sharing a node with one of the slave's own segments.
+__device__ __forceinline__ bool excluded(const Dev &d, int n, int q) {
+    const int a = d.segA[q], b = d.segB[q];
+    if (d.pnr[n] * d.snr[q] + d.pnz[n] * d.snz[q] > -FACING) return true;
     if (a == n || b == n) return true;
-    for (int k = d.segStart[i]; k < d.segStart[i + 1]; k++) {
-        const int own = d.segOf[k];
-        const int p = d.segA[own], q = d.segB[own];
-        if (p == a || p == b || q == a || q == b) return true;
+    const int32_t *own = d.nodeSeg + (size_t)n * d.segCap;
+    const int count = d.nodeFree[n];
+    for (int k = 0; k < count; k++) {
+        const int p = d.segA[own[k]], r = d.segB[own[k]];
+        if (p == a || p == b || r == a || r == b) return true;
     }
     return false;
 }
@@ -292,38 +300,38 @@ __device__ __forceinline__ bool excluded(const Dev &d, int i, int n, int s) {
 // The segment's unit tangent (cr[b] - cr[a]) / len, (cz[b] - cz[a]) / len is (-snz, snr) bit
 // for bit: the geometry phase formed snr = dz / len and snz = -dr / len from the same sums
 // (cr = x0 + u), and (-dr) / len is -(dr / len) exactly. Reading it saves two divisions.
-__device__ __forceinline__ double depth_of(const Dev &d, int n, int s) {
-    const int a = d.segA[s];
-    const double len = d.slen[s];
+__device__ __forceinline__ double depth_of(const Dev &d, int n, int q) {
+    const int a = d.segA[q];
+    const double len = d.slen[q];
     if (len <= 0.0) return 0.0;
-    const double tr = -d.snz[s], tz = d.snr[s];
+    const double tr = -d.snz[q], tz = d.snr[q];
     const double dr = d.cr[n] - d.cr[a], dz = d.cz[n] - d.cz[a];
     const double along = dr * tr + dz * tz;
     if (along < 0.0 || along > len) return 0.0;
-    const double gap = dr * d.snr[s] + dz * d.snz[s];
+    const double gap = dr * d.snr[q] + dz * d.snz[q];
     return gap < 0.0 ? -gap : 0.0;
 }
 
-// Files one incident term (pair i, role r as i << 2 | r) in node slot j's fixed list; a list
-// that overflows switches the step to the general path (a scan over the counts).
+// Files one incident term (the pair of slave node m, role r, as m << 2 | r) in node j's fixed
+// list; a list that overflows switches the step to the general path (a scan over the counts).
 __device__ __forceinline__ void inc_push(const Dev &d, int j, int entry) {
     const int pos = atomicAdd(&d.incCount[j], 1);
     if (pos < INC_CAP) d.incSlots[(size_t)j * INC_CAP + pos] = entry;
     else d.s->incOverflow = 1;
 }
 
-// Contact.accumulate + resolve, Contact.java:446-462, :663-762, for slave i (node n) and its
-// master segment s: writes the pair's twelve force terms as values to ADD (x - y is computed
-// as x + (-y), the same IEEE result) and files them at the pair's three nodes. Adds the
-// pair's spring energy and dissipation.
-__device__ void resolve_pair(const Dev &d, int i, int n, int s, double &energy, double &diss) {
+// Contact.accumulate + resolve, Contact.java:446-462, :663-762, for slave node n and its
+// master segment q: writes the pair's twelve force terms as values to ADD (x - y is computed
+// as x + (-y), the same IEEE result) and files them at the pair's three nodes; keeps the
+// pair's spring energy and dissipation at the slave.
+__device__ void resolve_pair(const Dev &d, int n, int q) {
     const double dt = d.s->dt;
     const double reference = d.dt0;
-    const int a = d.segA[s], b = d.segB[s];
-    const double depth = depth_of(d, n, s);
-    const double len = d.slen[s];
-    const double tr = -d.snz[s];                            // parameter, :655-661 (the
-    const double tz = d.snr[s];                             // tangent as in depth_of)
+    const int a = d.segA[q], b = d.segB[q];
+    const double depth = depth_of(d, n, q);
+    const double len = d.slen[q];
+    const double tr = -d.snz[q];                            // parameter, :655-661 (the
+    const double tz = d.snr[q];                             // tangent as in depth_of)
     const double t = ((d.cr[n] - d.cr[a]) * tr + (d.cz[n] - d.cz[a]) * tz) / len;
     const double wa = 1.0 - t, wb = t;
     const double ma = d.mass[a], mb = d.mass[b];
@@ -333,7 +341,7 @@ __device__ void resolve_pair(const Dev &d, int i, int n, int s, double &energy, 
     const double mSlave = d.mass[n];
     const double mStar = mSlave * mMaster / (mSlave + mMaster);
     const double k = d.cScale * mStar / (reference * reference);
-    const double nR = d.snr[s], nZ = d.snz[s];
+    const double nR = d.snr[q], nZ = d.snz[q];
     const double mTrue = 1.0 / (wa * wa / ma + wb * wb / mb);
     const double mTangent = mSlave * mTrue / (mSlave + mTrue);
     const double2 vn = d.V[n], va = d.V[a], vb = d.V[b];
@@ -341,7 +349,7 @@ __device__ void resolve_pair(const Dev &d, int i, int n, int s, double &energy, 
                            + (vn.y - wa * va.y - wb * vb.y) * nZ;
     const double damper = 2.0 * d.cDamping * mStar * sqrt(d.cScale) / reference;
     const double normal = jmax(0.0, k * depth - damper * closing);
-    double *pv = d.pairVal + 12 * (size_t)i;
+    double *pv = d.pairVal + 12 * (size_t)n;
     pv[0] = normal * nR;
     pv[1] = normal * nZ;
     pv[4] = -(wa * normal * nR);
@@ -349,7 +357,7 @@ __device__ void resolve_pair(const Dev &d, int i, int n, int s, double &energy, 
     pv[8] = -(wb * normal * nR);
     pv[9] = -(wb * normal * nZ);
     atomicAdd(&d.s->pairs, 1);
-    energy += 0.5 * k * depth * depth;
+    d.pairEnergy[n] = 0.5 * k * depth * depth;
     atomicMax(&d.s->maxPenBits, (unsigned long long)__double_as_longlong(depth));
     double dthis = 0.0;
     const double damperForce = normal - k * depth;
@@ -377,39 +385,32 @@ __device__ void resolve_pair(const Dev &d, int i, int n, int s, double &energy, 
         dthis += -tangent * 0.5 * (slide + after) * dt;
         state |= slipped ? NF_CONTACT_SLIP : NF_CONTACT_STICK;
     }
-    diss += dthis;
+    d.pairDiss[n] = dthis;
     d.contactState[n] = state;
-    d.pairNodes[i] = make_int4(n, a, b, 1);
-    inc_push(d, i, (i << 2) | 0);              // the slave's slot is i
-    inc_push(d, d.slotOf[a], (i << 2) | 1);
-    inc_push(d, d.slotOf[b], (i << 2) | 2);
+    d.pairNodes[n] = make_int4(n, a, b, 1);
+    inc_push(d, n, (n << 2) | 0);
+    inc_push(d, a, (n << 2) | 1);
+    inc_push(d, b, (n << 2) | 2);
 }
 
-// Contact.nearestPenetrated, Contact.java:570-606, then the pair, for slave i, by one whole
-// warp. The reference visits the nine cells in (dj, di) order and each cell's entries in the
-// order its counting sort filed them, ascending entry (2 s + endpoint), and keeps the first
-// candidate of greatest depth. Here the nine bucket ranges are concatenated, the lanes take
-// the candidates round-robin, and each candidate carries its visit key (cell in the nine,
-// entry): the warp keeps the greatest depth with the smallest key, which is the candidate the
-// serial loop keeps, so the buckets need no order. A candidate's depth is zero unless its gap
-// is negative; that test is exact and reads only what the fill staged beside the entry, so it
-// runs first, before the exclusions and the divisions.
-// Contact.nearestPenetrated (Contact.java:570-606) for four surface slots per warp, eight lanes
-// (a group) each: the deepest admissible segment and whether the last step's master was seen
-// too deep. Every candidate carries its visit key (cell in the nine, then the bucket entry),
-// and ties in depth go to the smallest key, the candidate the serial loop keeps. All 32 lanes
-// run every shuffle; a lane's group answer is valid when slot < nodes.
+// Contact.nearestPenetrated (Contact.java:570-606) for four slaves per warp, eight lanes (a
+// group) each: the deepest admissible segment and whether the last step's master was seen too
+// deep. Entry idx of the surface-node list is the group's slave (none when idx is past the
+// list or struck out). The nine bucket ranges are concatenated, the lanes take the candidates
+// round-robin, and every candidate carries its visit key (cell in the nine, then the bucket
+// entry 2 q + end): ties in depth go to the smallest key, the candidate the serial loop keeps,
+// so the buckets need no order. All 32 lanes run every shuffle.
 constexpr int SG = 8;                          // lanes per slave
-__device__ void search_group(const Dev &d, const Grid &g, int slot, int nodes, double &bestOut,
+__device__ void search_group(const Dev &d, const Grid &g, int idx, int listLen, double &bestOut,
                              int &segOut, bool &fellOut) {
     const int lane = threadIdx.x & 31, gl = lane & (SG - 1);
-    const bool live = slot < nodes;
+    int n = idx < listLen ? d.nodeList[idx] : -1;
+    const bool live = n >= 0;
     double2 xn = make_double2(0.0, 0.0);
-    int n = -1, last = -1, ci = 0, cj = 0;
+    int last = -1, ci = 0, cj = 0;
     if (live) {
-        xn = d.slaveXY[slot];
-        n = d.surfNodes[slot];
-        last = d.lastMaster[slot];
+        xn = make_double2(d.cr[n], d.cz[n]);
+        last = d.lastMaster[n];
         ci = iclamp(jd2i((xn.x - g.r0) / g.cellSize), g.cols);
         cj = iclamp(jd2i((xn.y - g.z0) / g.cellSize), g.rows);
     }
@@ -457,9 +458,9 @@ __device__ void search_group(const Dev &d, const Grid &g, int slot, int nodes, d
         const int t = base + gl;
         int c = 0;                              // which of the nine ranges holds position t
 #pragma unroll
-        for (int q = 1; q < SG; q++) {
-            const int oq = __shfl_sync(0xffffffffu, off, q, SG);
-            if (t >= oq) c = q;
+        for (int qq = 1; qq < SG; qq++) {
+            const int oq = __shfl_sync(0xffffffffu, off, qq, SG);
+            if (t >= oq) c = qq;
         }
         if (t >= off8) c = 8;
         const int src = c < SG ? c : 0;
@@ -473,7 +474,7 @@ __device__ void search_group(const Dev &d, const Grid &g, int slot, int nodes, d
         const long long kc = d.bucketCell[k];
         const int entry = d.bucketEntry[k];
         const double2 pa = d.bucketA[k], nrm = d.bucketN[k];
-        const double len = d.bucketL[k];
+        const double slen = d.bucketL[k];
         if (kc != cc) continue;
         // depth_of from what the filing staged beside the entry (the segment's first node,
         // normal and length: the same values, the same expressions): zero unless the slave is
@@ -481,15 +482,15 @@ __device__ void search_group(const Dev &d, const Grid &g, int slot, int nodes, d
         const double dr = xn.x - pa.x, dz = xn.y - pa.y;
         const double gap = dr * nrm.x + dz * nrm.y;
         if (!(gap < 0.0)) continue;
-        if (len <= 0.0) continue;
+        if (slen <= 0.0) continue;
         const double along = dr * -nrm.y + dz * nrm.x;
-        if (along < 0.0 || along > len) continue;
+        if (along < 0.0 || along > slen) continue;
         const double depth = -gap;
         // the exclusions read the slave's own rings (dependent loads); a candidate that fails
         // them is skipped whatever its depth, so testing them after the depth changes nothing
         const int sg = entry >> 1;
-        if (excluded(d, slot, n, sg)) continue;
-        if (depth > MAX_DEPTH * len) {
+        if (excluded(d, n, sg)) continue;
+        if (depth > MAX_DEPTH * slen) {
             if (sg == last) fell = true;
             continue;
         }
@@ -516,44 +517,46 @@ __device__ void search_group(const Dev &d, const Grid &g, int slot, int nodes, d
     segOut = __shfl_sync(0xffffffffu, bestSeg, 0, SG);
 }
 
-// The pair of surface slot i from its search (Contact.java:446-462): master, last master,
-// the escape count and the pair forces; one lane.
-__device__ void finish_slave(const Dev &d, int i, double best, int bestSeg, bool anyFell,
-                             double &energy, double &diss) {
-    const int last = d.lastMaster[i];
-    d.master[i] = best > 0.0 ? bestSeg : -1;
+// The pair of slave node n from its search (Contact.java:446-462): master, last master, the
+// escape count and the pair forces; one lane.
+__device__ void finish_slave(const Dev &d, int n, double best, int bestSeg, bool anyFell) {
+    const int last = d.lastMaster[n];
+    d.master[n] = best > 0.0 ? bestSeg : -1;
     if (!(best > 0.0)) {                      // no pair: Contact.java:446-452
         if (last >= 0 && anyFell) atomicAdd(&d.s->escaped, 1);
-        d.lastMaster[i] = -1;
+        d.lastMaster[n] = -1;
         return;
     }
-    d.lastMaster[i] = bestSeg;
-    resolve_pair(d, i, d.surfNodes[i], bestSeg, energy, diss);
+    d.lastMaster[n] = bestSeg;
+    resolve_pair(d, n, bestSeg);
+}
+
+// Node n's free edges in ascending q, from the corners of its elements (the node slots of the
+// force gather): at corner c of element e the edges 4 e + c (leaving it) and 4 e + (c + 3) % 4
+// (arriving at it).
+__device__ void build_node_segs(const Dev &d, int n) {
+    int32_t *out = d.nodeSeg + (size_t)n * d.segCap;
+    int count = 0;
+    for (int k = d.nodeSlotStart[n]; k < d.nodeSlotStart[n + 1]; k++) {
+        const int v = d.nodeSlot[k];
+        if (v >= 8 * d.E) continue;                  // a pressure edge's slot
+        const int e = v >> 3, c = v & 7;
+        const int q1 = 4 * e + c, q0 = 4 * e + ((c + 3) & 3);
+        if (d.surfFlag[q1] && count < d.segCap) out[count++] = q1;
+        if (d.surfFlag[q0] && count < d.segCap) out[count++] = q0;
+    }
+    for (int i = 1; i < count; i++) {
+        const int v = out[i];
+        int j = i - 1;
+        while (j >= 0 && out[j] > v) {
+            out[j + 1] = out[j];
+            j--;
+        }
+        out[j + 1] = v;
+    }
 }
 
 // ---------------------------------------------------------------------------- the pass
-
-// More erosions than this since the last rebuild take the full rebuild (the change lists are
-// ordered by counting, quadratic in their length).
-constexpr int INC_MAX_DEAD = 512;
-
-// Position of v in the ascending a[0, n): the number of entries below it.
-__device__ __forceinline__ int lower_bound_i(const int32_t *a, int n, int v) {
-    int lo = 0, hi = n;
-    while (lo < hi) {
-        const int mid = (lo + hi) >> 1;
-        if (a[mid] < v) lo = mid + 1;
-        else hi = mid;
-    }
-    return lo;
-}
-
-// Rank of v among the distinct a[0, n): the number of entries below it.
-__device__ __forceinline__ int rank_in(const int32_t *a, int n, int v) {
-    int r = 0;
-    for (int j = 0; j < n; j++) r += a[j] < v;
-    return r;
-}
 
 // Items are dealt to warps across the blocks first (warp w of block b takes the 32 items from
 // (w G + b) 32 on), so that a short list still spreads over every SM.
@@ -570,15 +573,14 @@ __global__ void __launch_bounds__(CB, 2) k_contact_pass(Dev d) {
     DevScalars *s = d.s;
     if (!vload(&s->active)) return;
     const int gt = blockIdx.x * CB + threadIdx.x;
+    const bool rebuilt = vload(&s->stale) != 0;
 
-    if (vload(&s->stale)) {
-        // Contact.adopt, Contact.java:290-322: the free surface (QuadMesh.surface over the live
-        // elements, QuadMesh.java:188-226), edges in element order, nodes ascending
-        const int oldEdges = vload(&s->surfEdges), oldNodes = vload(&s->surfNodes);
-        const int nDead = vload(&s->newDeadCount);
+    if (rebuilt) {
+        // Contact.adopt, Contact.java:290-322: the free surface, QuadMesh.surface over the
+        // live elements (QuadMesh.java:188-226): an element edge is free when it is the only
+        // live member of its group of equal edges
         const int epoch = vload(&s->rebuildEpoch) + 1;
-        if (vload(&s->fullRebuild) || nDead > INC_MAX_DEAD) {
-            // every element edge: free when it is the only live member of its group
+        if (vload(&s->fullRebuild)) {
             FOR_GRID(q, 4 * d.E) {
                 const int e = q >> 2;
                 int flag = 0;
@@ -592,49 +594,44 @@ __global__ void __launch_bounds__(CB, 2) k_contact_pass(Dev d) {
                 d.surfFlag[q] = flag;
             }
             FOR_GRID(n, d.N) {
-                d.nodeFlag[n] = 0;
                 d.nodeFree[n] = 0;
+                d.nodePos[n] = -1;
+                d.pairNodes[n] = make_int4(-1, -1, -1, 0);
+                d.incCount[n] = 0;
+            }
+            if (gt == 0) {
+                s->edgeListLen = 0;
+                s->nodeListLen = 0;
             }
             SYNC();
-            if (!grid_scan(d, d.surfFlag, d.surfPos, nullptr, 4 * d.E, &s->surfEdges, false))
-                return;
             FOR_GRID(q, 4 * d.E) {
-                if (!d.surfFlag[q]) continue;
-                const int e = q >> 2, k = q & 3;
-                const int4 c = d.conn[e];
-                const int nn[4] = {c.x, c.y, c.z, c.w};
-                const int a = nn[k], b = nn[(k + 1) & 3];
-                const int p = d.surfPos[q];
-                d.segA[p] = a;
-                d.segB[p] = b;
-                d.segQ[p] = q;
-                d.nodeFlag[a] = 1;
-                d.nodeFlag[b] = 1;
-                atomicAdd(&d.nodeFree[a], 1);
-                atomicAdd(&d.nodeFree[b], 1);
-            }
-            SYNC();
-            if (!grid_scan(d, d.nodeFlag, d.nodePos, nullptr, d.N, &s->surfNodes, false)) return;
-            FOR_GRID(n, d.N) {
-                if (d.nodeFlag[n]) {
-                    const int slot = d.nodePos[n];
-                    d.surfNodes[slot] = n;
-                    d.slotOf[n] = slot;
-                    d.lastMaster[slot] = -1;             // :319-321
-                    d.master[slot] = -1;
-                    d.dropped[slot] = 0;
-                    d.segCount[slot] = d.nodeFree[n];    // its incident free edges
-                } else {
-                    d.slotOf[n] = -1;
+                if (!d.surfFlag[q]) {
+                    d.edgePos[q] = -1;
+                    continue;
                 }
+                const int pos = atomicAdd(&s->edgeListLen, 1);
+                d.edgeList[pos] = q;
+                d.edgePos[q] = pos;
+                atomicAdd(&d.nodeFree[d.segA[q]], 1);
+                atomicAdd(&d.nodeFree[d.segB[q]], 1);
             }
-            if (gt == 0) d.segCount[vload(&s->surfNodes)] = 0;
             SYNC();
+            FOR_GRID(n, d.N) {
+                if (d.nodeFree[n] == 0) continue;
+                const int pos = atomicAdd(&s->nodeListLen, 1);
+                d.nodeList[pos] = n;
+                d.nodePos[n] = pos;
+                build_node_segs(d, n);
+            }
+            if (gt == 0) {
+                s->surfEdges = vload(&s->edgeListLen);
+            }
         } else {
             // only the edge groups of the elements eroded since the last rebuild can change:
-            // re-flag their members (each once: the epoch stamp), list the edges that became
-            // free or stopped being free, keep each node's count of incident free edges, and
-            // note the nodes whose count changed
+            // re-flag their members (each once: the epoch stamp), append the edges that became
+            // free to the list and strike out those that stopped being free, keep each node's
+            // count of free edges, and note the nodes touched
+            const int nDead = vload(&s->newDeadCount);
             FOR_GRID(t, 4 * nDead) {
                 const int g = d.edgeGroup[4 * d.newDead[t >> 2] + (t & 3)];
                 const int g0 = d.groupStart[g], g1 = d.groupStart[g + 1];
@@ -647,11 +644,16 @@ __global__ void __launch_bounds__(CB, 2) k_contact_pass(Dev d) {
                     const int now = !d.dead[q >> 2] && live == 1;
                     if (now == d.surfFlag[q]) continue;
                     d.surfFlag[q] = now;
-                    if (now) d.addE[atomicAdd(&s->nAddE, 1)] = q;
-                    else d.remE[atomicAdd(&s->nRemE, 1)] = q;
-                    const int4 c = d.conn[q >> 2];
-                    const int nn[4] = {c.x, c.y, c.z, c.w};
-                    const int ends[2] = {nn[q & 3], nn[(q + 1) & 3]};
+                    if (now) {
+                        const int pos = atomicAdd(&s->edgeListLen, 1);
+                        d.edgeList[pos] = q;
+                        d.edgePos[q] = pos;
+                    } else {
+                        d.edgeList[d.edgePos[q]] = -1;
+                        d.edgePos[q] = -1;
+                    }
+                    atomicAdd(&s->surfEdges, now ? 1 : -1);
+                    const int ends[2] = {d.segA[q], d.segB[q]};
                     for (int k = 0; k < 2; k++) {
                         atomicAdd(&d.nodeFree[ends[k]], now ? 1 : -1);
                         if (atomicExch(&d.nodeStamp[ends[k]], epoch) != epoch)
@@ -660,149 +662,83 @@ __global__ void __launch_bounds__(CB, 2) k_contact_pass(Dev d) {
                 }
             }
             SYNC();
-            const int nAddE = vload(&s->nAddE), nRemE = vload(&s->nRemE);
+            // the touched nodes: join or leave the surface, and list their free edges again
             const int nTouched = vload(&s->nTouched);
-            // the changed edges in ascending order; the nodes that joined or left the surface
-            FOR_GRID(i, nAddE) {
-                const int q = d.addE[i];
-                d.addES[rank_in(d.addE, nAddE, q)] = q;
-            }
-            FOR_GRID(i, nRemE) {
-                const int q = d.remE[i];
-                d.remES[rank_in(d.remE, nRemE, q)] = q;
-            }
             FOR_GRID(i, nTouched) {
                 const int n = d.touched[i];
-                const bool was = d.slotOf[n] >= 0, is = d.nodeFree[n] > 0;
-                if (is && !was) d.addN[atomicAdd(&s->nAddN, 1)] = n;
-                else if (was && !is) d.remN[atomicAdd(&s->nRemN, 1)] = n;
-            }
-            SYNC();
-            const int nAddN = vload(&s->nAddN), nRemN = vload(&s->nRemN);
-            FOR_GRID(i, nAddN) {
-                const int n = d.addN[i];
-                d.addNS[rank_in(d.addN, nAddN, n)] = n;
-            }
-            FOR_GRID(i, nRemN) {
-                const int n = d.remN[i];
-                d.remNS[rank_in(d.remN, nRemN, n)] = n;
-            }
-            // the merged edge list: a kept edge moves back by the removed edges before it and
-            // on by the added ones; an added edge lands after the kept edges before it
-            FOR_GRID(p, oldEdges) {
-                const int q = d.segQ[p];
-                if (!d.surfFlag[q]) continue;
-                const int np = p - lower_bound_i(d.remES, nRemE, q) + lower_bound_i(d.addES, nAddE, q);
-                d.tmpA[np] = d.segA[p];
-                d.tmpB[np] = d.segB[p];
-                d.tmpQ[np] = q;
-            }
-            FOR_GRID(r, nAddE) {
-                const int q = d.addES[r];
-                const int np = lower_bound_i(d.segQ, oldEdges, q) - lower_bound_i(d.remES, nRemE, q) + r;
-                const int4 c = d.conn[q >> 2];
-                const int nn[4] = {c.x, c.y, c.z, c.w};
-                d.tmpA[np] = nn[q & 3];
-                d.tmpB[np] = nn[(q + 1) & 3];
-                d.tmpQ[np] = q;
-            }
-            SYNC();
-            const int newEdges = oldEdges - nRemE + nAddE, newNodes = oldNodes - nRemN + nAddN;
-            FOR_GRID(p, newEdges) {
-                d.segA[p] = d.tmpA[p];
-                d.segB[p] = d.tmpB[p];
-                d.segQ[p] = d.tmpQ[p];
-            }
-            // the merged node list, the same way
-            FOR_GRID(i, oldNodes) {
-                const int n = d.surfNodes[i];
-                if (d.nodeFree[n] == 0) continue;
-                d.tmpNodes[i - lower_bound_i(d.remNS, nRemN, n) + lower_bound_i(d.addNS, nAddN, n)] = n;
-            }
-            FOR_GRID(r, nAddN) {
-                const int n = d.addNS[r];
-                d.tmpNodes[lower_bound_i(d.surfNodes, oldNodes, n) - lower_bound_i(d.remNS, nRemN, n) + r] = n;
-            }
-            FOR_GRID(r, nRemN) d.slotOf[d.remNS[r]] = -1;
-            if (gt == 0) {
-                s->surfEdges = newEdges;
-                s->surfNodes = newNodes;
-            }
-            SYNC();
-            FOR_GRID(i, newNodes) {
-                const int n = d.tmpNodes[i];
-                d.surfNodes[i] = n;
-                d.slotOf[n] = i;
-                d.lastMaster[i] = -1;                    // :319-321
-                d.master[i] = -1;
-                d.dropped[i] = 0;
-                d.segCount[i] = d.nodeFree[n];
-            }
-            if (gt == 0) d.segCount[newNodes] = 0;
-            SYNC();
-        }
-        // each surface node's segments, ascending (:298-313)
-        const int edges = vload(&s->surfEdges), nodes = vload(&s->surfNodes);
-        if (!grid_scan(d, d.segCount, d.segStart, d.segCursor, nodes + 1, nullptr, false)) return;
-        FOR_GRID(e, edges) {
-            d.segOf[atomicAdd(&d.segCursor[d.slotOf[d.segA[e]]], 1)] = e;
-            d.segOf[atomicAdd(&d.segCursor[d.slotOf[d.segB[e]]], 1)] = e;
-        }
-        SYNC();
-        FOR_GRID(i, nodes) {
-            const int lo = d.segStart[i], hi = d.segStart[i + 1];
-            for (int k = lo + 1; k < hi; k++) {
-                const int v = d.segOf[k];
-                int j = k - 1;
-                while (j >= lo && d.segOf[j] > v) {
-                    d.segOf[j + 1] = d.segOf[j];
-                    j--;
+                const bool was = d.nodePos[n] >= 0, is = d.nodeFree[n] > 0;
+                if (is && !was) {
+                    const int pos = atomicAdd(&s->nodeListLen, 1);
+                    d.nodeList[pos] = n;
+                    d.nodePos[n] = pos;
+                    atomicAdd(&s->surfNodes, 1);
+                } else if (was && !is) {
+                    d.nodeList[d.nodePos[n]] = -1;
+                    d.nodePos[n] = -1;
+                    atomicAdd(&s->surfNodes, -1);
+                    d.pairNodes[n] = make_int4(-1, -1, -1, 0);
+                    d.incCount[n] = 0;
                 }
-                d.segOf[j + 1] = v;
+                if (is) build_node_segs(d, n);
             }
         }
         if (gt == 0) {
             s->stale = 0;
-            s->fullRebuild = 0;
             s->newDeadCount = 0;
             s->rebuildEpoch = epoch;
-            s->nAddE = s->nRemE = s->nTouched = s->nAddN = s->nRemN = 0;
         }
+        const bool full = vload(&s->fullRebuild) != 0;
         SYNC();
+        // after a full rebuild the list has no struck-out entries: its length is the count
+        if (gt == 0) {
+            if (full) {
+                s->surfNodes = vload(&s->nodeListLen);
+                s->fullRebuild = 0;
+            }
+            s->nTouched = 0;
+        }
     }
-    const int nodes = vload(&s->surfNodes), edges = vload(&s->surfEdges);
+    const int nodeLen = vload(&s->nodeListLen), edgeLen = vload(&s->edgeListLen);
 
     // Contact.geometry, Contact.java:467-500: current coordinates, the bounding box, segment
-    // lengths and normals (from X0 + U directly, the same sums the coordinates hold)
+    // lengths and normals (from X0 + U directly, the same sums the coordinates hold). After a
+    // rebuild every surface node forgets its last master (Contact.adopt, :319-321).
     {
         unsigned long long kr0 = ~0ULL, kz0 = ~0ULL, kr1 = 0ULL, kz1 = 0ULL, lb = 0ULL;
-        FOR_GRID(i, nodes) {
-            const int n = d.surfNodes[i];
+        FOR_GRID(i, nodeLen) {
+            const int n = d.nodeList[i];
+            if (n < 0) continue;
             const double2 x = d.X0[n], u = d.U[n];
             const double cr = x.x + u.x, cz = x.y + u.y;
             d.cr[n] = cr;
             d.cz[n] = cz;
-            d.slaveXY[i] = make_double2(cr, cz);
-            d.incCount[i] = 0;
-            d.pairNodes[i] = make_int4(-1, -1, -1, 0);
+            d.incCount[n] = 0;
+            d.pairNodes[n] = make_int4(-1, -1, -1, 0);
+            if (rebuilt) {
+                d.lastMaster[n] = -1;
+                d.master[n] = -1;
+                d.dropped[n] = 0;
+            }
             const unsigned long long kr = okey(cr), kz = okey(cz);
             kr0 = min(kr0, kr); kr1 = max(kr1, kr);
             kz0 = min(kz0, kz); kz1 = max(kz1, kz);
         }
-        if (gt == 0) d.incCount[nodes] = 0;
-        FOR_GRID(e, edges) {
-            const int a = d.segA[e], b = d.segB[e];
+        if (gt == 0) d.incCount[d.N] = 0;
+        FOR_GRID(i, edgeLen) {
+            const int q = d.edgeList[i];
+            if (q < 0) continue;
+            const int a = d.segA[q], b = d.segB[q];
             const double2 xa = d.X0[a], ua = d.U[a], xb = d.X0[b], ub = d.U[b];
             const double dr = (xb.x + ub.x) - (xa.x + ua.x);
             const double dz = (xb.y + ub.y) - (xa.y + ua.y);
             const double len = sqrt(dr * dr + dz * dz);
-            d.slen[e] = len;
+            d.slen[q] = len;
             if (len > 0.0) {
-                d.snr[e] = dz / len;
-                d.snz[e] = -dr / len;
+                d.snr[q] = dz / len;
+                d.snz[q] = -dr / len;
             } else {
-                d.snr[e] = 0.0;
-                d.snz[e] = 0.0;
+                d.snr[q] = 0.0;
+                d.snz[q] = 0.0;
             }
             lb = max(lb, (unsigned long long)__double_as_longlong(len));
         }
@@ -828,6 +764,7 @@ __global__ void __launch_bounds__(CB, 2) k_contact_pass(Dev d) {
 
     // the grid, in every block; node normals; the counting sort's counts (:530-545).
     // bucketCount is all zero on entry and is left all zero.
+    const int nodes = vload(&s->surfNodes);
     if (threadIdx.x == 0) {
         grid_from_box(d, nodes, grid);
         if (blockIdx.x == 0) {
@@ -844,57 +781,76 @@ __global__ void __launch_bounds__(CB, 2) k_contact_pass(Dev d) {
     }
     __syncthreads();
     const Grid g = grid;
-    FOR_GRID(i, nodes) {
+    FOR_GRID(i, nodeLen) {                       // each node's segments in ascending order
+        const int n = d.nodeList[i];
+        if (n < 0) continue;
+        const int32_t *own = d.nodeSeg + (size_t)n * d.segCap;
+        const int count = d.nodeFree[n];
         double sr = 0.0, sz = 0.0;
-        for (int k = d.segStart[i]; k < d.segStart[i + 1]; k++) {
-            sr += d.snr[d.segOf[k]];
-            sz += d.snz[d.segOf[k]];
+        for (int k = 0; k < count; k++) {
+            sr += d.snr[own[k]];
+            sz += d.snz[own[k]];
         }
         const double len = sqrt(sr * sr + sz * sz);
-        d.pnr[i] = len > 0.0 ? sr / len : 0.0;
-        d.pnz[i] = len > 0.0 ? sz / len : 0.0;
+        d.pnr[n] = len > 0.0 ? sr / len : 0.0;
+        d.pnz[n] = len > 0.0 ? sz / len : 0.0;
     }
-    FOR_GRID(q, 2 * edges) {
-        const int e = q >> 1;
-        const int node = (q & 1) ? d.segB[e] : d.segA[e];
+    FOR_GRID(t, 2 * edgeLen) {
+        const int q = d.edgeList[t >> 1];
+        if (q < 0) continue;
+        const int node = (t & 1) ? d.segB[q] : d.segA[q];
         const long long cell = cell_of(g, d.cr[node], d.cz[node]);
-        d.entryCell[q] = cell;
+        d.entryCell[2 * q + (t & 1)] = cell;
         atomicAdd(&d.bucketCount[bucket_of(d, g, cell)], 1);
     }
     SYNC();
     if (!grid_scan(d, d.bucketCount, d.bucketStart, d.bucketCursor, g.bucketN, nullptr, true))
         return;
-    // file the entries; stage beside each what the search's gap test reads
-    FOR_GRID(q, 2 * edges) {
-        const long long cell = d.entryCell[q];
-        const int e = q >> 1;
-        const int a = d.segA[e];
+    // file the entries; stage beside each what the search's depth test reads
+    FOR_GRID(t, 2 * edgeLen) {
+        const int q = d.edgeList[t >> 1];
+        if (q < 0) continue;
+        const int entry = 2 * q + (t & 1);
+        const long long cell = d.entryCell[entry];
+        const int a = d.segA[q];
         const int pos = atomicAdd(&d.bucketCursor[bucket_of(d, g, cell)], 1);
-        d.bucketEntry[pos] = q;
+        d.bucketEntry[pos] = entry;
         d.bucketCell[pos] = cell;
         d.bucketA[pos] = make_double2(d.cr[a], d.cz[a]);
-        d.bucketN[pos] = make_double2(d.snr[e], d.snz[e]);
-        d.bucketL[pos] = d.slen[e];
+        d.bucketN[pos] = make_double2(d.snr[q], d.snz[q]);
+        d.bucketL[pos] = d.slen[q];
     }
     SYNC();
 
     // the search and the pair forces: each warp searches four slaves at a time, eight lanes
     // each, and the groups' first lanes then compute the four pairs' forces side by side (long
-    // dependent chains of divisions). The totals are per-block partials, folded in a fixed
-    // order at the step's end.
+    // dependent chains of divisions)
     {
-        double energy = 0.0, diss = 0.0;
         const int warpsTotal = gridDim.x * CB_WARPS;
         const int group = (threadIdx.x & 31) / SG;
-        for (int w = (threadIdx.x >> 5) * gridDim.x + blockIdx.x; w * (32 / SG) < nodes;
+        for (int w = (threadIdx.x >> 5) * gridDim.x + blockIdx.x; w * (32 / SG) < nodeLen;
              w += warpsTotal) {
-            const int slot = w * (32 / SG) + group;
+            const int idx = w * (32 / SG) + group;
             double best;
             int seg;
             bool fell;
-            search_group(d, g, slot, nodes, best, seg, fell);
-            if ((threadIdx.x & (SG - 1)) == 0 && slot < nodes)
-                finish_slave(d, slot, best, seg, fell, energy, diss);
+            search_group(d, g, idx, nodeLen, best, seg, fell);
+            if ((threadIdx.x & (SG - 1)) == 0 && idx < nodeLen) {
+                const int n = d.nodeList[idx];
+                if (n >= 0) finish_slave(d, n, best, seg, fell);
+            }
+        }
+    }
+    SYNC();
+    const bool friction = d.cFriction > 0.0;
+    // the pairs' spring energy and dissipation, summed over a fixed grid of node numbers
+    {
+        double energy = 0.0, diss = 0.0;
+        FOR_GRID(n, d.N) {
+            if (d.pairNodes[n].w) {
+                energy += d.pairEnergy[n];
+                diss += d.pairDiss[n];
+            }
         }
         const double e1 = block_sum_c(energy, shd);
         const double e2 = block_sum_c(diss, shd);
@@ -903,18 +859,18 @@ __global__ void __launch_bounds__(CB, 2) k_contact_pass(Dev d) {
             d.partials[(PARTIAL_CONTACT + 1) * d.maxBlocks + blockIdx.x] = e2;
         }
     }
-    SYNC();
-    const bool friction = d.cFriction > 0.0;
     if (!vload(&s->incOverflow)) {
         // each node adds its terms in slave order, normal then tangent (:717-754): the fixed
         // list, sorted in registers by an odd-even transposition network
-        FOR_GRID(j, nodes) {
-            const int c = d.incCount[j];
+        FOR_GRID(i, nodeLen) {
+            const int node = d.nodeList[i];
+            if (node < 0) continue;
+            const int c = d.incCount[node];
             if (c == 0) continue;
             int e[INC_CAP];
 #pragma unroll
             for (int k = 0; k < INC_CAP; k++)
-                e[k] = k < c ? d.incSlots[(size_t)j * INC_CAP + k] : 0x7fffffff;
+                e[k] = k < c ? d.incSlots[(size_t)node * INC_CAP + k] : 0x7fffffff;
 #pragma unroll
             for (int r = 0; r < INC_CAP; r++) {
 #pragma unroll
@@ -924,7 +880,6 @@ __global__ void __launch_bounds__(CB, 2) k_contact_pass(Dev d) {
                     e[k + 1] = y;
                 }
             }
-            const int node = d.surfNodes[j];
             double2 f = d.F[node];
 #pragma unroll
             for (int k = 0; k < INC_CAP; k++) {
@@ -942,18 +897,22 @@ __global__ void __launch_bounds__(CB, 2) k_contact_pass(Dev d) {
         }
         return;
     }
-    // the general path: incidence lists by a scan over the counts
-    if (!grid_scan(d, d.incCount, d.incStart, d.incCursor, nodes + 1, nullptr, false)) return;
-    FOR_GRID(i, nodes) {
-        const int4 p = d.pairNodes[i];
+    // the general path: incidence lists by a scan over every node's count
+    if (!grid_scan(d, d.incCount, d.incStart, d.incCursor, d.N + 1, nullptr, false)) return;
+    FOR_GRID(i, nodeLen) {
+        const int m = d.nodeList[i];
+        if (m < 0) continue;
+        const int4 p = d.pairNodes[m];
         if (!p.w) continue;
-        d.incEntry[atomicAdd(&d.incCursor[d.slotOf[p.x]], 1)] = (i << 2) | 0;
-        d.incEntry[atomicAdd(&d.incCursor[d.slotOf[p.y]], 1)] = (i << 2) | 1;
-        d.incEntry[atomicAdd(&d.incCursor[d.slotOf[p.z]], 1)] = (i << 2) | 2;
+        d.incEntry[atomicAdd(&d.incCursor[p.x], 1)] = (m << 2) | 0;
+        d.incEntry[atomicAdd(&d.incCursor[p.y], 1)] = (m << 2) | 1;
+        d.incEntry[atomicAdd(&d.incCursor[p.z], 1)] = (m << 2) | 2;
     }
     SYNC();
-    FOR_GRID(j, nodes) {
-        const int lo = d.incStart[j], hi = d.incStart[j + 1];
+    FOR_GRID(i, nodeLen) {
+        const int node = d.nodeList[i];
+        if (node < 0) continue;
+        const int lo = d.incStart[node], hi = d.incStart[node + 1];
         if (lo == hi) continue;
         for (int k = lo + 1; k < hi; k++) {
             const int v = d.incEntry[k];
@@ -964,7 +923,6 @@ __global__ void __launch_bounds__(CB, 2) k_contact_pass(Dev d) {
             }
             d.incEntry[q + 1] = v;
         }
-        const int node = d.surfNodes[j];
         double2 f = d.F[node];
         for (int k = lo; k < hi; k++) {
             const int ent = d.incEntry[k];

@@ -55,7 +55,9 @@ struct DevScalars {
     int erodedCount, invertedCount;
     double erodedEnergy;
     // contact (Contact.java:236-250)
-    int stale, surfEdges, surfNodes, pairs, escaped, rebuild;
+    int stale, surfEdges, surfNodes, pairs, escaped, rebuild;   // surfEdges/surfNodes: how
+                                             // many free edges and surface nodes there are
+    int edgeListLen, nodeListLen;            // lengths of the lists, removed entries included
     double cEnergy, cDissipation;
     unsigned long long maxPenBits;
     unsigned long long bbox[4];              // order-preserving bits of rlo, zlo, -rhi, -zhi
@@ -70,8 +72,7 @@ struct DevScalars {
     int incOverflow;                         // a node's incident terms outgrew its fixed list
     // the free-surface rebuild (Contact.adopt): a full rebuild at set-up, an incremental one
     // after erosion (elements eroded since the last rebuild, changes this rebuild)
-    int fullRebuild, newDeadCount, rebuildEpoch;
-    int nAddE, nRemE, nTouched, nAddN, nRemN;
+    int fullRebuild, newDeadCount, rebuildEpoch, nTouched;
 };
 
 // The element pass's Johnson-Cook work list (FP64 reduced integration). Points whose return
@@ -123,45 +124,41 @@ struct Dev {
     // partial sums (deterministic reductions)
     double *partials;                        // [PARTIAL_SLOTS * maxBlocks]
     int maxBlocks;
-    // surface / contact
+    // surface / contact. Segments are identified by their element edge q = 4 e + corner and
+    // surface nodes by their node number: ascending q is the reference's segment order
+    // (QuadMesh.surface lists free edges in element order) and ascending node number its
+    // surface-node order, so every order-dependent result keys on these.
     int32_t *edgeGroup, *groupStart, *groupMember;   // element-edge -> group of equal edges
-    int32_t *surfFlag, *surfPos;             // [4E]
-    int32_t *nodeFlag, *nodePos;             // [N]
-    int32_t *segA, *segB, *segQ;             // [4E] current surface edges: end nodes, and the
-                                             // element edge (4 e + corner) each one is
-    // incremental free-surface rebuild, carved from one allocation (surfWork): the elements
-    // eroded since the last rebuild, the free edges incident to each node, the rebuild epoch of
-    // each edge's and node's last visit, the changed edges and nodes (as found, and sorted),
-    // and the merged lists before they are copied back
-    int32_t *surfWork;
-    int32_t *newDead;                        // [E]
-    int32_t *nodeFree;                       // [N]
-    int32_t *edgeStamp, *nodeStamp;          // [4E], [N]
-    int32_t *addE, *remE, *addES, *remES;    // [4E] each
-    int32_t *touched, *addN, *remN, *addNS, *remNS;   // [N] each
-    int32_t *tmpA, *tmpB, *tmpQ;             // [4E] each
-    int32_t *tmpNodes;                       // [N]
-    int32_t *surfNodes, *slotOf;             // [N]
-    int32_t *segCount, *segStart, *segOf, *segCursor;   // per surface node
+    int32_t *surfFlag;                       // [4E] 1 while the element edge is free
+    int32_t *segA, *segB;                    // [4E] end nodes of each element edge
+    int32_t *edgeList, *edgePos;             // [4E] the free edges in any order (-1: no longer
+                                             // free), and each edge's place in it
+    int32_t *nodeList, *nodePos;             // [N] the surface nodes in any order (-1: left the
+                                             // surface), and each node's place (-1: none)
+    int32_t *nodeFree;                       // [N] free edges incident to each node
+    int32_t *nodeSeg;                        // [N x segCap] each surface node's free edges,
+    int segCap;                              // ascending (2 x the largest node valence)
+    int32_t *edgeStamp, *nodeStamp;          // [4E], [N] rebuild epoch of the last visit
+    int32_t *touched;                        // [N] nodes whose free edges changed
+    int32_t *newDead;                        // [E] elements eroded since the last rebuild
     double *cr, *cz;                         // [N]
-    double *snr, *snz, *slen;                // [4E]
+    double *snr, *snz, *slen;                // [4E] by element edge
     double *pnr, *pnz;                       // [N]
-    int32_t *lastMaster, *master;            // [N]
+    int32_t *lastMaster, *master;            // [N] by node: the master element edge, or -1
     uint8_t *dropped;                        // [N]
     int32_t *bucketCount, *bucketStart, *bucketCursor;   // [bucketCap + 1]
-    int32_t *bucketEntry;                    // [8E] entries (2 s + end)
+    int32_t *bucketEntry;                    // [8E] entries (2 q + end)
     double2 *bucketA, *bucketN;              // [8E] by position: the segment's first node, normal
     double *bucketL;                         // [8E] by position: the segment's length
     long long *bucketCell;                   // [8E] cell of each filed entry, by position
     long long *entryCell;                    // [8E] cell of each entry, by entry
     int bucketCap;
-    // pair records, per surface slot
-    int4 *pairNodes;                         // (n, a, b, valid)
-    double2 *slaveXY;                        // [N] current coordinates by surface slot
-    double *pairVal;                         // [12 per slot]: role-major (n,a,b) x (normal r,z, tangent r,z)
-    double *pairEnergy, *pairDiss;           // per slot
-    int32_t *incCount, *incStart, *incCursor, *incEntry;   // per surface slot, entries (i<<2 | role)
-    int32_t *incSlots;                       // [NF_INC_CAP per surface slot] fixed lists
+    // pair records, per node
+    int4 *pairNodes;                         // [N] (n, a, b, valid)
+    double *pairVal;                         // [12 per node]: role-major (n,a,b) x (normal r,z, tangent r,z)
+    double *pairEnergy, *pairDiss;           // [N]
+    int32_t *incCount, *incStart, *incCursor, *incEntry;   // [N + 1] per node, entries (n<<2 | role)
+    int32_t *incSlots;                       // [NF_INC_CAP per node] fixed lists
     // mixed precision: FP32 element state, float contributions, per-node float positions
     int mixed;
     MatF *matsF;
