@@ -525,40 +525,53 @@ __global__ void __launch_bounds__(BLOCK) k_gather(Dev d) {
 // in that order, then the warp's fixed tree adds the lanes. Same inputs, same result.
 
 // Folds the block partials, then the adaptive CFL step (:985-990).
-__global__ void __launch_bounds__(256) k_end(Dev d, int nodeBlocks, int elemBlocks,
-                                            int slotBlocks, int updateDt) {
+constexpr int END_WARPS_PER_LIST = 5;         // k_end: 6 lists x 5 warps of its 32
+__global__ void __launch_bounds__(1024) k_end(Dev d, int nodeBlocks, int elemBlocks,
+                                             int slotBlocks, int updateDt) {
+    __shared__ double part[6][END_WARPS_PER_LIST];
     __shared__ double folded[6];
     DevScalars *s = d.s;
     if (!s->active) return;
-    // the six per-block partial lists, one warp each: lane-strided sums, then a fixed tree
+    // the six per-block partial lists, five warps each: warp w of a list takes the w-th of five
+    // contiguous runs of it, each lane adds its terms lane-strided in order, the warp's fixed
+    // tree adds the lanes, and the five runs are added in order -- a fixed order, so the totals
+    // are deterministic
     {
         const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
+        const int list = warp / END_WARPS_PER_LIST, run = warp % END_WARPS_PER_LIST;
         const double *src = nullptr;
         int count = 0;
-        if (warp < 3 && updateDt && d.hasWall) {
-            src = d.partials + (PARTIAL_WALL + warp) * d.maxBlocks;
+        if (list < 3 && updateDt && d.hasWall) {
+            src = d.partials + (PARTIAL_WALL + list) * d.maxBlocks;
             count = nodeBlocks;
-        } else if (warp == 3 && updateDt && d.hasErosion) {
+        } else if (list == 3 && updateDt && d.hasErosion) {
             src = d.partials + PARTIAL_ERODE * d.maxBlocks;
             count = elemBlocks;
-        } else if ((warp == 4 || warp == 5) && d.hasContact) {
-            src = d.partials + (PARTIAL_CONTACT + warp - 4) * d.maxBlocks;
+        } else if ((list == 4 || list == 5) && d.hasContact) {
+            src = d.partials + (PARTIAL_CONTACT + list - 4) * d.maxBlocks;
             count = slotBlocks;
         }
-        // lane l adds partials l, l + 32, ... in that order; the loads of eight terms are
-        // issued before they are added, so the warp waits for one round trip per eight
+        const int chunk = (count + END_WARPS_PER_LIST - 1) / END_WARPS_PER_LIST;
+        const int lo = min(count, run * chunk), hi = min(count, lo + chunk);
+        // the loads of eight terms are issued before they are added
         double v = 0.0;
-        int k = lane;
-        for (; k + 7 * 32 < count; k += 8 * 32) {
+        int k = lo + lane;
+        for (; k + 7 * 32 < hi; k += 8 * 32) {
             double x[8];
 #pragma unroll
             for (int j = 0; j < 8; j++) x[j] = src[k + 32 * j];
 #pragma unroll
             for (int j = 0; j < 8; j++) v += x[j];
         }
-        for (; k < count; k += 32) v += src[k];
+        for (; k < hi; k += 32) v += src[k];
         for (int o = 16; o > 0; o >>= 1) v += __shfl_down_sync(0xffffffffu, v, o);
-        if (lane == 0 && warp < 6) folded[warp] = v;
+        if (lane == 0 && list < 6) part[list][run] = v;
+        __syncthreads();
+        if (threadIdx.x < 6) {
+            double t = 0.0;
+            for (int r = 0; r < END_WARPS_PER_LIST; r++) t += part[threadIdx.x][r];
+            folded[threadIdx.x] = t;
+        }
         __syncthreads();
     }
     if (threadIdx.x != 0) return;
@@ -667,7 +680,7 @@ int launch_initial_assembly(Solver &S) {
     Dev &d = S.d;
     k_begin<<<1, 1, 0, S.stream>>>(d, 1);
     int n = 1 + assemble(S, 1);
-    k_end<<<1, 256, 0, S.stream>>>(d, nodal_grid(S), element_grid(S), d.coopBlocks, 0);
+    k_end<<<1, 1024, 0, S.stream>>>(d, nodal_grid(S), element_grid(S), d.coopBlocks, 0);
     return n + 1;
 }
 
@@ -695,7 +708,7 @@ int launch_step(Solver &S, bool) {
     }
     n += assemble(S, 0, d.N > 0 && d.mixed, fused);
     S.mark(NF_GROUP_END, true);
-    k_end<<<1, 256, 0, st>>>(d, nodal_grid(S), eroding_blocks(S), d.coopBlocks, 1);
+    k_end<<<1, 1024, 0, st>>>(d, nodal_grid(S), eroding_blocks(S), d.coopBlocks, 1);
     n++;
     S.mark(NF_GROUP_END, false);
     return n;
@@ -710,7 +723,7 @@ int launch_advance(Solver &S) {
         n++;
     }
     n += assemble(S, 0);
-    k_end<<<1, 256, 0, S.stream>>>(d, nodal_grid(S), element_grid(S), d.coopBlocks, 0);
+    k_end<<<1, 1024, 0, S.stream>>>(d, nodal_grid(S), element_grid(S), d.coopBlocks, 0);
     return n + 1;
 }
 
