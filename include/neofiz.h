@@ -213,6 +213,11 @@ nf_status nf_check(nf_solver *h);
  * the GPU's global timer per wait (0 restores the defaults, 2^27 polls and one second). For
  * tests that make a wait run out; no reference counterpart. */
 nf_status nf_set_wait_limit(nf_solver *h, int64_t polls, int64_t nanoseconds);
+/* Slots per cell of the contact pass's direct-indexed grid, 0..64 (default 64): a step whose
+ * busiest cell holds more entries than this files through the counting sort instead; 0 sends
+ * every step there. Both layouts give the same bits; for tests of the fallback and tuning. No
+ * reference counterpart. */
+nf_status nf_set_grid_slots(nf_solver *h, int32_t slots);
 
 /* ------------------------------------------------------------------ setup (ExplicitSolver) */
 

@@ -139,6 +139,7 @@ _PROTOS = {
     "status_word": (_S, [_H, C.POINTER(C.c_uint32)]),
     "check": (_S, [_H]),
     "set_wait_limit": (_S, [_H, C.c_int64, C.c_int64]),
+    "set_grid_slots": (_S, [_H, C.c_int32]),
     "set_threads": (_S, [_H, C.c_int32]),
     "fix_radial": (_S, [_H, C.c_int32]),
     "fix_axial": (_S, [_H, C.c_int32]),

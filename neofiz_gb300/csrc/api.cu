@@ -555,7 +555,8 @@ nf_status nf_destroy(nf_solver *h) {
                     d.pairEnergy, d.pairDiss, d.incCount, d.incStart, d.incCursor, d.incEntry,
                     d.scanTmp, d.s, d.matsF, d.sigF, d.backF, d.epsPF, d.wPF, d.hgKF,
                     d.contribF, d.hgF, d.dStrF, d.dSoftF, d.dWidthF, d.dFailF, d.dGfF, d.dGeomF,
-                    d.pMid, d.pCur, d.vdt, d.gaussVol, d.coopSums, d.incSlots, d.bucketA, d.bucketN, d.bucketL,
+                    d.pMid, d.pCur, d.vdt, d.gaussVol, d.coopSums, d.incSlots, d.bucketA, d.bucketN, d.bucketL, d.fastCount, d.fastEntry,
+                    d.fastA, d.fastN, d.fastL,
                     d.hot, d.hotList, d.hotNext, d.hotStamp};
     const char *a0 = static_cast<const char *>(S->arena), *a1 = a0 + S->arenaBytes;
     for (void *p : ptrs) {
@@ -609,6 +610,15 @@ nf_status nf_set_wait_limit(nf_solver *h, int64_t polls, int64_t nanoseconds) {
         return fail(&S, NF_EINVAL, "wait limits must be >= 0 (0 restores the default)");
     S.d.waitSpins = polls;
     S.d.waitNs = nanoseconds;
+    return NF_OK;
+}
+
+nf_status nf_set_grid_slots(nf_solver *h, int32_t slots) {
+    Solver &S = *reinterpret_cast<Solver *>(h);
+    if (slots < 0 || slots > NF_GRID_SLOTS)
+        return fail(&S, NF_EINVAL, "grid slots must be in [0, 64]");
+    S.gridSlots = slots;
+    if (S.d.fastCount) S.d.fastLimit = slots;
     return NF_OK;
 }
 
@@ -726,6 +736,13 @@ nf_status nf_set_contact(nf_solver *h, double friction, double damping, double s
         A(d.bucketEntry, 8LL * E); A(d.bucketA, 8LL * E); A(d.bucketN, 8LL * E);
         A(d.bucketL, 8LL * E);
         A(d.bucketCell, 8LL * E); A(d.entryCell, 8LL * E);
+        d.fastCells = std::min(d.bucketCap + 1, 1 << 16);
+        d.fastCap = NF_GRID_SLOTS;
+        d.fastLimit = S.gridSlots;
+        A(d.fastCount, d.fastCells);
+        A(d.fastEntry, (size_t)d.fastCells * d.fastCap);
+        A(d.fastA, (size_t)d.fastCells * d.fastCap); A(d.fastN, (size_t)d.fastCells * d.fastCap);
+        A(d.fastL, (size_t)d.fastCells * d.fastCap);
         A(d.pairNodes, N); A(d.pairVal, 12LL * N); A(d.pairEnergy, N); A(d.pairDiss, N);
         A(d.incCount, N + 1); A(d.incStart, N + 1); A(d.incCursor, N + 1); A(d.incEntry, 3LL * N);
         A(d.incSlots, (size_t)NF_INC_CAP * N);

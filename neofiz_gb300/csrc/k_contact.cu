@@ -393,16 +393,37 @@ __device__ void resolve_pair(const Dev &d, int n, int q) {
     inc_push(d, b, (n << 2) | 2);
 }
 
-// Contact.nearestPenetrated (Contact.java:570-606) for four slaves per warp, eight lanes (a
+// Contact.nearestPenetrated (Contact.java:570-606) for 32 / SG slaves per warp, SG lanes (a
 // group) each: the deepest admissible segment and whether the last step's master was seen too
 // deep. Entry idx of the surface-node list is the group's slave (none when idx is past the
 // list or struck out). The nine bucket ranges are concatenated, the lanes take the candidates
 // round-robin, and every candidate carries its visit key (cell in the nine, then the bucket
 // entry 2 q + end): ties in depth go to the smallest key, the candidate the serial loop keeps,
 // so the buckets need no order. All 32 lanes run every shuffle.
+// The grid's buckets as the search reads them: the counting-sort layout (bucket b's entries at
+// [start[b], start[b + 1]), each with its cell) or the direct-indexed one (cell c's entries at
+// [c cap, c cap + count[c]), every entry in its own cell).
+struct BucketView {
+    const int32_t *start, *count;
+    const long long *cell;                     // null in the direct-indexed layout
+    const int32_t *entry;
+    const double2 *a, *n;
+    const double *l;
+    int cap;                                   // 0: the counting-sort layout
+};
+__device__ __forceinline__ void bucket_range(const BucketView &v, int b, int &lo, int &len) {
+    if (v.cap) {
+        lo = b * v.cap;
+        len = v.count[b];
+    } else {
+        lo = v.start[b];
+        len = v.start[b + 1] - lo;
+    }
+}
+
 constexpr int SG = 8;                          // lanes per slave
-__device__ void search_group(const Dev &d, const Grid &g, int idx, int listLen, double &bestOut,
-                             int &segOut, bool &fellOut) {
+__device__ void search_group(const Dev &d, const Grid &g, const BucketView &v, int idx,
+                             int listLen, double &bestOut, int &segOut, bool &fellOut) {
     const int lane = threadIdx.x & 31, gl = lane & (SG - 1);
     int n = idx < listLen ? d.nodeList[idx] : -1;
     const bool live = n >= 0;
@@ -418,22 +439,18 @@ __device__ void search_group(const Dev &d, const Grid &g, int idx, int listLen, 
     int lo = 0, len = 0, lo8 = 0, len8 = 0;
     long long myCell = -1, cell8 = -1;
     if (live) {
-        {
+        if (gl < 8) {                           // lanes from 8 on take no cell
             const int j = cj + gl / 3 - 1, ii = ci + gl % 3 - 1;
             if (j >= 0 && j < g.rows && ii >= 0 && ii < g.cols) {
                 myCell = (long long)j * g.cols + ii;
-                const int bkt = bucket_of(d, g, myCell);
-                lo = d.bucketStart[bkt];
-                len = d.bucketStart[bkt + 1] - lo;
+                bucket_range(v, bucket_of(d, g, myCell), lo, len);
             }
         }
         if (gl == 0) {
             const int j = cj + 1, ii = ci + 1;
             if (j < g.rows && ii < g.cols) {
                 cell8 = (long long)j * g.cols + ii;
-                const int bkt = bucket_of(d, g, cell8);
-                lo8 = d.bucketStart[bkt];
-                len8 = d.bucketStart[bkt + 1] - lo8;
+                bucket_range(v, bucket_of(d, g, cell8), lo8, len8);
             }
         }
     }
@@ -458,24 +475,23 @@ __device__ void search_group(const Dev &d, const Grid &g, int idx, int listLen, 
         const int t = base + gl;
         int c = 0;                              // which of the nine ranges holds position t
 #pragma unroll
-        for (int qq = 1; qq < SG; qq++) {
+        for (int qq = 1; qq < 8; qq++) {
             const int oq = __shfl_sync(0xffffffffu, off, qq, SG);
             if (t >= oq) c = qq;
         }
         if (t >= off8) c = 8;
-        const int src = c < SG ? c : 0;
+        const int src = c < 8 ? c : 0;
         const int oc0 = __shfl_sync(0xffffffffu, off, src, SG);
         const int lc0 = __shfl_sync(0xffffffffu, lo, src, SG);
         const long long cc0 = __shfl_sync(0xffffffffu, myCell, src, SG);
         if (t >= total) continue;
-        const int oc = c < SG ? oc0 : off8, lc = c < SG ? lc0 : lo8;
-        const long long cc = c < SG ? cc0 : cell8;
+        const int oc = c < 8 ? oc0 : off8, lc = c < 8 ? lc0 : lo8;
+        const long long cc = c < 8 ? cc0 : cell8;
         const int k = lc + (t - oc);
-        const long long kc = d.bucketCell[k];
-        const int entry = d.bucketEntry[k];
-        const double2 pa = d.bucketA[k], nrm = d.bucketN[k];
-        const double slen = d.bucketL[k];
-        if (kc != cc) continue;
+        const int entry = v.entry[k];
+        const double2 pa = v.a[k], nrm = v.n[k];
+        const double slen = v.l[k];
+        if (v.cell && v.cell[k] != cc) continue;        // a hashed bucket shares cells
         // depth_of from what the filing staged beside the entry (the segment's first node,
         // normal and length: the same values, the same expressions): zero unless the slave is
         // behind the segment and projects onto it
@@ -795,35 +811,66 @@ __global__ void __launch_bounds__(CB, 2) k_contact_pass(Dev d) {
         d.pnr[n] = len > 0.0 ? sr / len : 0.0;
         d.pnz[n] = len > 0.0 ? sz / len : 0.0;
     }
-    FOR_GRID(t, 2 * edgeLen) {
-        const int q = d.edgeList[t >> 1];
-        if (q < 0) continue;
-        const int node = (t & 1) ? d.segB[q] : d.segA[q];
-        const long long cell = cell_of(g, d.cr[node], d.cz[node]);
-        d.entryCell[2 * q + (t & 1)] = cell;
-        atomicAdd(&d.bucketCount[bucket_of(d, g, cell)], 1);
-    }
-    SYNC();
-    if (!grid_scan(d, d.bucketCount, d.bucketStart, d.bucketCursor, g.bucketN, nullptr, true))
-        return;
-    // file the entries; stage beside each what the search's depth test reads
+    // A grid of at most fastCells - 1 cells is indexed directly: each entry takes the next of
+    // its cell's slots (fastLimit of the fastCap reserved) and is filed there at once, staging
+    // beside it what the search's depth test reads. A larger (or hashed) grid, or a cell that
+    // outgrows its slots, takes the counting sort: the counts, an exclusive scan, the filing.
+    const bool fast = !g.hashed && g.cells < d.fastCells;
     FOR_GRID(t, 2 * edgeLen) {
         const int q = d.edgeList[t >> 1];
         if (q < 0) continue;
         const int entry = 2 * q + (t & 1);
-        const long long cell = d.entryCell[entry];
-        const int a = d.segA[q];
-        const int pos = atomicAdd(&d.bucketCursor[bucket_of(d, g, cell)], 1);
-        d.bucketEntry[pos] = entry;
-        d.bucketCell[pos] = cell;
-        d.bucketA[pos] = make_double2(d.cr[a], d.cz[a]);
-        d.bucketN[pos] = make_double2(d.snr[q], d.snz[q]);
-        d.bucketL[pos] = d.slen[q];
+        const int node = (t & 1) ? d.segB[q] : d.segA[q];
+        const long long cell = cell_of(g, d.cr[node], d.cz[node]);
+        d.entryCell[entry] = cell;
+        if (fast) {
+            const int pos = atomicAdd(&d.fastCount[cell], 1);
+            if (pos < d.fastLimit) {
+                const size_t slot = (size_t)cell * d.fastCap + pos;
+                const int a = d.segA[q];
+                d.fastEntry[slot] = entry;
+                d.fastA[slot] = make_double2(d.cr[a], d.cz[a]);
+                d.fastN[slot] = make_double2(d.snr[q], d.snz[q]);
+                d.fastL[slot] = d.slen[q];
+            } else {
+                s->fastOverflow = 1;
+            }
+        } else {
+            atomicAdd(&d.bucketCount[bucket_of(d, g, cell)], 1);
+        }
     }
     SYNC();
+    const bool direct = fast && !vload(&s->fastOverflow);
+    if (!direct) {
+        if (!grid_scan(d, fast ? d.fastCount : d.bucketCount, d.bucketStart, d.bucketCursor,
+                       g.bucketN, nullptr, true))
+            return;
+        FOR_GRID(t, 2 * edgeLen) {
+            const int q = d.edgeList[t >> 1];
+            if (q < 0) continue;
+            const int entry = 2 * q + (t & 1);
+            const long long cell = d.entryCell[entry];
+            const int a = d.segA[q];
+            const int pos = atomicAdd(&d.bucketCursor[bucket_of(d, g, cell)], 1);
+            d.bucketEntry[pos] = entry;
+            d.bucketCell[pos] = cell;
+            d.bucketA[pos] = make_double2(d.cr[a], d.cz[a]);
+            d.bucketN[pos] = make_double2(d.snr[q], d.snz[q]);
+            d.bucketL[pos] = d.slen[q];
+        }
+        SYNC();
+    }
+    BucketView view;
+    if (direct) {
+        view = BucketView{nullptr, d.fastCount, nullptr, d.fastEntry, d.fastA, d.fastN, d.fastL,
+                          d.fastCap};
+    } else {
+        view = BucketView{d.bucketStart, nullptr, d.bucketCell, d.bucketEntry, d.bucketA,
+                          d.bucketN, d.bucketL, 0};
+    }
 
-    // the search and the pair forces: each warp searches four slaves at a time, eight lanes
-    // each, and the groups' first lanes then compute the four pairs' forces side by side (long
+    // the search and the pair forces: each warp searches 32 / SG slaves at a time, SG lanes
+    // each, and the groups' first lanes then compute the pairs' forces side by side (long
     // dependent chains of divisions)
     {
         const int warpsTotal = gridDim.x * CB_WARPS;
@@ -834,7 +881,7 @@ __global__ void __launch_bounds__(CB, 2) k_contact_pass(Dev d) {
             double best;
             int seg;
             bool fell;
-            search_group(d, g, idx, nodeLen, best, seg, fell);
+            search_group(d, g, view, idx, nodeLen, best, seg, fell);
             if ((threadIdx.x & (SG - 1)) == 0 && idx < nodeLen) {
                 const int n = d.nodeList[idx];
                 if (n >= 0) finish_slave(d, n, best, seg, fell);
@@ -842,6 +889,7 @@ __global__ void __launch_bounds__(CB, 2) k_contact_pass(Dev d) {
         }
     }
     SYNC();
+    if (direct) FOR_GRID(c, (int)g.cells) d.fastCount[c] = 0;   // all zero again for the next step
     const bool friction = d.cFriction > 0.0;
     // the pairs' spring energy and dissipation, summed over a fixed grid of node numbers
     {

@@ -70,6 +70,7 @@ struct DevScalars {
     uint32_t status;
     uint32_t barCount, barGen, barAbort;     // grid barrier of the cooperative contact pass
     int incOverflow;                         // a node's incident terms outgrew its fixed list
+    int fastOverflow;                        // a cell of the direct-indexed grid overflowed
     // the free-surface rebuild (Contact.adopt): a full rebuild at set-up, an incremental one
     // after erosion (elements eroded since the last rebuild, changes this rebuild)
     int fullRebuild, newDeadCount, rebuildEpoch, nTouched;
@@ -152,6 +153,14 @@ struct Dev {
     double *bucketL;                         // [8E] by position: the segment's length
     long long *bucketCell;                   // [8E] cell of each filed entry, by position
     long long *entryCell;                    // [8E] cell of each entry, by entry
+    // the direct-indexed grid: cell c's entries in slots [c fastCap, c fastCap + fastCount[c])
+    // when the grid has at most fastCells cells and none holds more than fastCap entries
+    int32_t *fastCount;                      // [fastCells]
+    int32_t *fastEntry;                      // [fastCells x fastCap]
+    double2 *fastA, *fastN;                  // [fastCells x fastCap]
+    double *fastL;                           // [fastCells x fastCap]
+    int fastCells, fastCap;                  // cells indexed directly, slots per cell
+    int fastLimit;                           // slots a step may use, <= fastCap (nf_set_grid_slots)
     int bucketCap;
     // pair records, per node
     int4 *pairNodes;                         // [N] (n, a, b, valid)
@@ -191,6 +200,7 @@ struct Dev {
 };
 
 constexpr int NF_INC_CAP = 8;
+constexpr int NF_GRID_SLOTS = 64;            // slots per cell of the direct-indexed contact grid
 
 // Contact.begin, Contact.java:424-436: the per-step totals and extrema the contact pass
 // accumulates into; run by the step's first kernel, before the pass.
@@ -203,6 +213,7 @@ __device__ inline void contact_step_reset(DevScalars *s) {
     s->bbox[3] = 0ULL;    // max z
     s->longestBits = 0ULL;
     s->incOverflow = 0;
+    s->fastOverflow = 0;
     s->barCount = 0;      // a fresh grid barrier
     s->barAbort = 0;
 }
@@ -228,6 +239,7 @@ struct Solver {
     double massScale = 1.0;
     double hourglass = 0.05;
     bool contactSet = false, damageSet = false, erosionSet = false;
+    int gridSlots = NF_GRID_SLOTS;   // nf_set_grid_slots, applied when the contact data exists
     // launch bookkeeping
     cudaStream_t ownStream = nullptr;
     long long launches = 0;

@@ -352,6 +352,12 @@ class ExplicitSolver:
         """Bounds of each contact-pass barrier wait (0, 0: the defaults); for tests."""
         self._call(self._api.set_wait_limit, int(polls), int(nanoseconds))
 
+    def setGridSlots(self, slots: int) -> None:
+        """Slots per cell of the contact pass's direct-indexed grid, 0..64 (default 64); a step
+        whose busiest cell holds more takes the counting sort, and 0 sends every step there.
+        Both give the same bits; for tests and tuning."""
+        self._call(self._api.set_grid_slots, int(slots))
+
     def setStream(self, stream_handle: int) -> None:
         """Runs this solver's kernels on a caller-owned cudaStream_t (0: its own)."""
         self._call(self._api.set_stream, C.c_void_p(stream_handle or None))

@@ -1771,6 +1771,12 @@ API nf_status nfo_set_wait_limit(nfo_solver *h, int64_t polls, int64_t ns) {
     return NF_OK;
 }
 
+API nf_status nfo_set_grid_slots(nfo_solver *h, int32_t slots) {
+    /* the oracle files its buckets by a counting sort only; the setting is validated */
+    if (slots < 0 || slots > 64) return fail(h, NF_EINVAL, "grid slots must be in [0, 64]");
+    return NF_OK;
+}
+
 static nf_status field_desc(nfo_solver *h, int field, void **ptr, size_t *count, size_t *bytes) {
     const size_t N = (size_t)h->N, E = (size_t)h->E, P = (size_t)h->E * (size_t)h->ppe;
     *ptr = NULL; *count = 0; *bytes = 8;

@@ -25,3 +25,11 @@ def test_oracle_wait_limit_validation():
     o.setWaitLimit(0, 0)
     with pytest.raises(ValueError, match=">= 0"):
         o.setWaitLimit(0, -5)
+
+
+def test_oracle_grid_slots_validation():
+    o, _, _ = scenes.taylor_rod(OracleSolver, nr=2, nz=8)
+    o.setGridSlots(0)
+    o.setGridSlots(64)
+    with pytest.raises(ValueError, match=r"\[0, 64\]"):
+        o.setGridSlots(65)

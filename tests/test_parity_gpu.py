@@ -147,6 +147,30 @@ def test_perforation_coarse_erosion_and_contact(gpu_lib):
     assert info["contact"].pairCount() > 0
 
 
+@pytest.mark.parametrize("slots", [0, 3])
+def test_perforation_coarse_grid_layouts(gpu_lib, slots):
+    """The contact grid's two layouts give the same bits. With 0 slots per cell every step
+    files its buckets by the counting sort; with 3, a step whose busiest cell holds more than
+    three segment ends falls back to it, so the run mixes both layouts."""
+    g, o, _, info = pair(scenes.perforation, cell=1.0e-3)
+    g.setGridSlots(slots)
+    o.setGridSlots(slots)
+    for chunk in (200, 400):
+        g.run(chunk)
+        o.run(chunk)
+        assert_bitwise(g, o, f"perforation, {slots} grid slots")
+    assert_totals(g, o, "perforation")
+    assert info["contact"].pairCount() > 0
+
+
+def test_grid_slots_are_validated(gpu_lib):
+    g, _, _ = scenes.two_blocks(ExplicitSolver)
+    for bad in (-1, 65):
+        with pytest.raises(ValueError, match=r"\[0, 64\]"):
+            g.setGridSlots(bad)
+    g.setGridSlots(64)
+
+
 def run_both(g, o, marks, label):
     """Steps both solvers to each mark in turn and compares them there, bit for bit."""
     done = 0
