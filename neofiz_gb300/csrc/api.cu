@@ -492,6 +492,7 @@ nf_status nf_create(const nf_mesh *mesh, const nf_material *materials, int32_t m
     if (listed) {
         d.hotSmem = listed_pass_smem(S->device);
         A(d.hot, 1); A(d.hotList, d.hotCap); A(d.hotNext, d.hotCap); A(d.hotStamp, E);
+        A(d.jcYield, E);
     }
 #undef A
     const cudaError_t e_ = arena.commit(*S);
@@ -520,6 +521,7 @@ nf_status nf_create(const nf_mesh *mesh, const nf_material *materials, int32_t m
         h0.epoch = 1;
         upload(*S, d.hot, &h0, 1);
     }
+    if (d.jcYield) launch_jc_yield(d, S->stream);
     d.scanTmpSize = (int)scanInts;
     d.scanTmp = nullptr;
     nf_status st = sync_check(*S);
@@ -557,7 +559,7 @@ nf_status nf_destroy(nf_solver *h) {
                     d.contribF, d.hgF, d.dStrF, d.dSoftF, d.dWidthF, d.dFailF, d.dGfF, d.dGeomF,
                     d.pMid, d.pCur, d.vdt, d.gaussVol, d.coopSums, d.incSlots, d.bucketA, d.bucketN, d.bucketL, d.fastCount, d.fastEntry,
                     d.fastA, d.fastN, d.fastL,
-                    d.hot, d.hotList, d.hotNext, d.hotStamp};
+                    d.hot, d.hotList, d.hotNext, d.hotStamp, d.jcYield};
     const char *a0 = static_cast<const char *>(S->arena), *a1 = a0 + S->arenaBytes;
     for (void *p : ptrs) {
         const char *c = static_cast<const char *>(p);
@@ -1294,8 +1296,14 @@ nf_status nf_write_field(nf_solver *h, int32_t field, const void *src, size_t nb
         case NF_FIELD_VZ: return pair(d.V, 1);
         case NF_FIELD_STRESS: CK(&S, cudaMemcpy(d.sig, src, nbytes, cudaMemcpyHostToDevice)); return NF_OK;
         case NF_FIELD_BACK_STRESS: CK(&S, cudaMemcpy(d.back, src, nbytes, cudaMemcpyHostToDevice)); return NF_OK;
-        case NF_FIELD_PLASTIC_STRAIN: CK(&S, cudaMemcpy(d.epsP, src, nbytes, cudaMemcpyHostToDevice)); return NF_OK;
-        case NF_FIELD_PLASTIC_WORK: CK(&S, cudaMemcpy(d.wP, src, nbytes, cudaMemcpyHostToDevice)); return NF_OK;
+        case NF_FIELD_PLASTIC_STRAIN: case NF_FIELD_PLASTIC_WORK:
+            CK(&S, cudaMemcpy(field == NF_FIELD_PLASTIC_STRAIN ? d.epsP : d.wP, src, nbytes,
+                              cudaMemcpyHostToDevice));
+            if (d.jcYield) {                   // the kept yield radii follow the new state
+                launch_jc_yield(d, S.stream);
+                return sync_check(S);
+            }
+            return NF_OK;
         default: return NF_EINVAL;
     }
 }

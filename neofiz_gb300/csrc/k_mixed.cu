@@ -230,6 +230,10 @@ __global__ void k_convert_state(Dev d, int toFloat, size_t points, int what) {
         } else {
             d.epsP[p] = d.epsPF[p];
             d.wP[p] = d.wPF[p];
+            if (d.jcYield) {                   // the kept yield radii follow the new state
+                const MatDev &f = d.mats[d.emat[p]];
+                if (f.jc) d.jcYield[p] = jc_yield(f, d.epsP[p], d.wP[p]);
+            }
         }
     }
     if (p < points && (what & 2)) {

@@ -151,7 +151,9 @@ int launch_point_volumes(Solver &S, double *out) {
 
 // erode, ExplicitSolver.java:663-691, for element e: its damage and signed current area
 // decide whether it goes; the strain energy it held is added to energy.
-__device__ __forceinline__ void erode_element(const Dev &d, int e, double &energy) {
+// cur (when given) holds element_current(d, e).
+__device__ __forceinline__ void erode_element(const Dev &d, int e, double &energy,
+                                              const double2 *cur = nullptr) {
     if (d.gone[e]) return;
     {
         bool failed = false;
@@ -163,15 +165,21 @@ __device__ __forceinline__ void erode_element(const Dev &d, int e, double &energ
             }
             failed = (d.ppe == 1 ? sum : sum / d.ppe) >= d.erosionDamage;   // x / 1 is x
         }
-        const int4 c = d.conn[e];                            // currentArea, :681-691
-        const int nn[4] = {c.x, c.y, c.z, c.w};
+        double2 p[4];                                        // currentArea, :681-691
+        if (cur) {
+            for (int k = 0; k < 4; k++) p[k] = cur[k];
+        } else {
+            element_current(d, e, p);
+        }
         double a = 0.0;
         for (int k = 0; k < 4; k++) {
-            const int i = nn[k], j = nn[(k + 1) & 3];
-            const double2 xi = d.X0[i], xj = d.X0[j], ui = d.U[i], uj = d.U[j];
-            a += (xi.x + ui.x) * (xj.y + uj.y) - (xj.x + uj.x) * (xi.y + ui.y);
+            const double2 pi = p[k], pj = p[(k + 1) & 3];
+            a += pi.x * pj.y - pj.x * pi.y;
         }
-        const bool inverted = 0.5 * a <= 0.0;
+        // 0.5 a <= 0 by a's bits: a <= 0 (either zero, a negative number or -inf), or a the
+        // least subnormal, whose half rounds to +0; NaN is neither
+        const uint64_t ua = (uint64_t)__double_as_longlong(a);
+        const bool inverted = (ua << 1) <= 2u || ((ua >> 63) && (ua << 1) <= 0xffe0000000000000ULL);
         if (failed || inverted) {
             d.gone[e] = 1;
             atomicAdd(&d.s->erodedCount, 1);
@@ -238,8 +246,12 @@ __global__ void __launch_bounds__(BLOCK) k_element_reduced_listed(Dev d, int zer
     }
     double minEdge = DMAX, energy = 0.0;
     int cost = 0;
-    if (erode && e >= 0) erode_element(d, e, energy);
-    if (e >= 0) element_reduced(d, e, zeroStrain ? 0.0 : d.s->dt, d.hourglass, minEdge, &cost);
+    if (e >= 0) {
+        double2 cur[4];                  // x + u of the nodes, for the erosion test and cr/cz
+        element_current(d, e, cur);
+        if (erode) erode_element(d, e, energy, cur);
+        element_reduced(d, e, zeroStrain ? 0.0 : d.s->dt, d.hourglass, minEdge, &cost, cur);
+    }
     const unsigned want = __ballot_sync(0xffffffffu, cost > 0);
     if (want) {
         const int lane = threadIdx.x & 31, leader = __ffs(want) - 1;
@@ -266,6 +278,17 @@ __global__ void __launch_bounds__(BLOCK) k_element_reduced_listed(Dev d, int zer
 // blocks share an SM: eight warps per SM keep the FP64 pipe busy, and a listed warp with a long
 // Johnson-Cook solve competes with seven others for it instead of eleven. Needs the device
 // current; sets the kernel's attribute.
+__global__ void k_jc_yield(Dev d) {
+    for (int e = blockIdx.x * blockDim.x + threadIdx.x; e < d.E; e += gridDim.x * blockDim.x) {
+        const MatDev &f = d.mats[d.emat[e]];
+        if (f.jc) d.jcYield[e] = jc_yield(f, d.epsP[e], d.wP[e]);
+    }
+}
+
+void launch_jc_yield(const Dev &d, cudaStream_t st) {
+    if (d.jcYield && d.E > 0) k_jc_yield<<<grid_for(d.E, BLOCK), BLOCK, 0, st>>>(d);
+}
+
 int listed_pass_smem(int device) {
     int perSm = 0, optin = 0;
     if (cudaDeviceGetAttribute(&perSm, cudaDevAttrMaxSharedMemoryPerMultiprocessor, device) != cudaSuccess ||

@@ -142,9 +142,23 @@ static __device__ __forceinline__ void prepare_node(const Dev &d, int i, double 
 // increments, Cayley co-rotation, J2/Johnson-Cook return, FB hourglass, the eight force
 // terms into the element's contribution slots; folds its shortest edge into minEdge.
 // *cost (when given) receives the point's Johnson-Cook cost class (j2_update).
+// The current positions x + u of element e's four nodes (the sums cr/cz and currentArea both
+// start from).
+static __device__ __forceinline__ void element_current(const Dev &d, int e, double2 *cur) {
+    const int4 c = d.conn[e];
+    const int n[4] = {c.x, c.y, c.z, c.w};
+#pragma unroll
+    for (int k = 0; k < 4; k++) {
+        const double2 x = d.X0[n[k]], u = d.U[n[k]];
+        cur[k] = make_double2(x.x + u.x, x.y + u.y);
+    }
+}
+
+// cur (when given) holds element_current(d, e), already formed for the erosion test.
 static __device__ __forceinline__ void element_reduced(const Dev &d, int e, double strainDt,
                                                        double hourglass, double &minEdge,
-                                                       int *cost = nullptr) {
+                                                       int *cost = nullptr,
+                                                       const double2 *cur = nullptr) {
     double *ef = d.contribution + 8 * (size_t)e;
     if (d.gone != nullptr && d.gone[e]) {
         for (int k = 0; k < 8; k++) ef[k] = 0.0;
@@ -153,16 +167,21 @@ static __device__ __forceinline__ void element_reduced(const Dev &d, int e, doub
         const double lambda = fl.lambda, mu = fl.mu;
         const int4 c = d.conn[e];
         const double mid = -0.5 * strainDt;
-        const double2 x0 = d.X0[c.x], x1 = d.X0[c.y], x2 = d.X0[c.z], x3 = d.X0[c.w];
-        const double2 u0 = d.U[c.x], u1 = d.U[c.y], u2 = d.U[c.z], u3 = d.U[c.w];
         const double2 v0 = d.V[c.x], v1 = d.V[c.y], v2 = d.V[c.z], v3 = d.V[c.w];
         double r0, r1, r2, r3, z0, z1, z2, z3;
         if (d.finite) {                                  // cr/cz, :1176-1182
-            r0 = x0.x + u0.x + mid * v0.x; r1 = x1.x + u1.x + mid * v1.x;
-            r2 = x2.x + u2.x + mid * v2.x; r3 = x3.x + u3.x + mid * v3.x;
-            z0 = x0.y + u0.y + mid * v0.y; z1 = x1.y + u1.y + mid * v1.y;
-            z2 = x2.y + u2.y + mid * v2.y; z3 = x3.y + u3.y + mid * v3.y;
+            double2 p[4];
+            if (cur) {
+                for (int k = 0; k < 4; k++) p[k] = cur[k];
+            } else {
+                element_current(d, e, p);
+            }
+            r0 = p[0].x + mid * v0.x; r1 = p[1].x + mid * v1.x;
+            r2 = p[2].x + mid * v2.x; r3 = p[3].x + mid * v3.x;
+            z0 = p[0].y + mid * v0.y; z1 = p[1].y + mid * v1.y;
+            z2 = p[2].y + mid * v2.y; z3 = p[3].y + mid * v3.y;
         } else {
+            const double2 x0 = d.X0[c.x], x1 = d.X0[c.y], x2 = d.X0[c.z], x3 = d.X0[c.w];
             r0 = x0.x; r1 = x1.x; r2 = x2.x; r3 = x3.x;
             z0 = x0.y; z1 = x1.y; z2 = x2.y; z3 = x3.y;
         }
@@ -173,19 +192,35 @@ static __device__ __forceinline__ void element_reduced(const Dev &d, int e, doub
 
         if (d.finite) minEdge = shortestEdge(minEdge, r0, r1, r2, r3, z0, z1, z2, z3);
 
-        const double J00 = 0.25 * (-r0 + r1 + r2 - r3);
-        const double J01 = 0.25 * (-z0 + z1 + z2 - z3);
-        const double J10 = 0.25 * (-r0 - r1 + r2 + r3);
-        const double J11 = 0.25 * (-z0 - z1 + z2 + z3);
-        const double det = J00 * J11 - J01 * J10;
-        const double inv = 1.0 / det;
-
-        const double d0r = 0.25 * (J01 - J11) * inv;
-        const double d1r = 0.25 * (J01 + J11) * inv;
+        // J = S / 4 with S the corner sums, det = D / 16 with D = S00 S11 - S01 S10, and so
+        // 0.25 (J01 - J11) / det = (S01 - S11) / D: the powers of two cancel exactly (rounding
+        // commutes with them) as long as every scaled value stays normal, which bounding the
+        // S and D exponents guarantees; otherwise the reference's own sequence runs
+        const double S00 = -r0 + r1 + r2 - r3;
+        const double S01 = -z0 + z1 + z2 - z3;
+        const double S10 = -r0 - r1 + r2 + r3;
+        const double S11 = -z0 - z1 + z2 + z3;
+        const double D = S00 * S11 - S01 * S10;
+        double det, d0r, d1r, d0z, d1z;
+        if (moderate_or_zero(S00) && moderate_or_zero(S01) && moderate_or_zero(S10) &&
+            moderate_or_zero(S11) && moderate_or_zero(D)) {
+            const double invD = 1.0 / D;
+            det = 0.0625 * D;
+            d0r = (S01 - S11) * invD;
+            d1r = (S01 + S11) * invD;
+            d0z = (S10 - S00) * invD;
+            d1z = -((S10 + S00) * invD);
+        } else {
+            const double J00 = 0.25 * S00, J01 = 0.25 * S01, J10 = 0.25 * S10, J11 = 0.25 * S11;
+            det = J00 * J11 - J01 * J10;
+            const double inv = 1.0 / det;
+            d0r = 0.25 * (J01 - J11) * inv;
+            d1r = 0.25 * (J01 + J11) * inv;
+            d0z = 0.25 * (J10 - J00) * inv;
+            d1z = -0.25 * (J10 + J00) * inv;
+        }
         const double d2r = -d0r;
         const double d3r = -d1r;
-        const double d0z = 0.25 * (J10 - J00) * inv;
-        const double d1z = -0.25 * (J10 + J00) * inv;
         const double d2z = -d0z;
         const double d3z = -d1z;
 
@@ -213,10 +248,13 @@ static __device__ __forceinline__ void element_reduced(const Dev &d, int e, doub
             if (!is_zero(spinDt)) {
                 const double cs = corot_cos(spinDt), sn = corot_sin(spinDt);
                 corot_rotate(sg, cs, sn);
-                corot_rotate(bk, cs, sn);
+                // a back stress of +0s (no kinematic hardening) rotates to itself
+                if (!(all_plus_zero(bk[0], bk[1], bk[2], bk[3]) && corot_keeps_zero(cs, sn)))
+                    corot_rotate(bk, cs, sn);
             }
         }
         double epsP = d.epsP[e], work = d.wP[e];
+        double2 *const jcYield = d.jcYield && fl.jc ? d.jcYield + e : nullptr;
         if (d.hasDamage) {
             DamageRef dr;
             dr.failureStrain = d.dFail[e];
@@ -227,10 +265,10 @@ static __device__ __forceinline__ void element_reduced(const Dev &d, int e, doub
             dr.fractureEnergy = d.dGf[e];
             dr.youngs = fl.youngs;
             j2_update(sg, bk, epsP, work, dEpsR, dEpsZ, dEpsT, dGamRZ, lambda, mu, fl,
-                      strainDt, &dr, d.dStrength[e], d.dSoft[e], cost);
+                      strainDt, &dr, d.dStrength[e], d.dSoft[e], cost, jcYield);
         } else {
             j2_update(sg, bk, epsP, work, dEpsR, dEpsZ, dEpsT, dGamRZ, lambda, mu, fl,
-                      strainDt, (const DamageRef *)nullptr, 0.0, 0.0, cost);
+                      strainDt, (const DamageRef *)nullptr, 0.0, 0.0, cost, jcYield);
         }
         {
             double2 *ps = reinterpret_cast<double2 *>(d.sig + 4 * (size_t)e);

@@ -47,6 +47,7 @@ template <> struct Fn<double> {
     static __device__ __forceinline__ double sin(double a) { return nf_sin(a); }
     static __device__ __forceinline__ double cos(double a) { return nf_cos(a); }
     static __device__ __forceinline__ double abs(double a) { return ::fabs(a); }
+    static __device__ __forceinline__ double div3(double a);
     static constexpr double tolerance = SOLVE_TOLERANCE;
 };
 // The FP32 forms run well inside their error budget with CUDA's fast pow and log (a few ulp
@@ -61,9 +62,27 @@ template <> struct Fn<float> {
     static __device__ __forceinline__ float sin(float a) { return ::sinf(a); }
     static __device__ __forceinline__ float cos(float a) { return ::cosf(a); }
     static __device__ __forceinline__ float abs(float a) { return ::fabsf(a); }
+    static __device__ __forceinline__ float div3(float a) { return a / 3.0f; }
     // 1e-10 A is below FP32 resolution of the residual; 1e-5 A is a few ulp of it.
     static constexpr float tolerance = 1.0e-5f;
 };
+
+// x / 3 correctly rounded, without a division. z = RN(1/3) satisfies 3 z = 1 - 2^-54, so
+// q0 = RN(x z) lies within one ulp of x / 3; the remainder x - 3 q0 is then exact (one fused
+// multiply-add), and one correction q0 + r z rounded once is RN(x / 3) (Markstein, "Computation
+// of elementary functions on the IBM RISC System/6000 processor", IBM J. Res. Dev. 34(1),
+// 1990: a faithful quotient corrected with the correctly rounded reciprocal). The argument
+// needs x and the quotient far from underflow and overflow: 2^-1000 <= |x| < 2^1001 takes this
+// path, +-0 gives q0 = +-0 (which is x / 3), and anything else is divided.
+__device__ __forceinline__ double Fn<double>::div3(double x) {
+    const double z = 0x1.5555555555555p-2;
+    const uint64_t u = (uint64_t)__double_as_longlong(x);
+    const unsigned e = (unsigned)(u >> 52) & 0x7ffu;
+    const double q0 = x * z;
+    if (e - 23u < 2002u) return fma(fma(-q0, 3.0, x), z, q0);
+    if ((u << 1) == 0) return q0;
+    return x / 3.0;
+}
 
 // Damage state of one point (Damage.java:166-200), accessed through pointers so the
 // element kernel can leave the rarely-touched geometry in global memory.
@@ -136,11 +155,20 @@ __device__ __forceinline__ T jc_quasiStatic(const MatT<T> &f, T eps, T temperatu
     return jc_strainTerm(f, eps) * jc_thermalTerm(f, temperature);
 }
 
-// J2.solve, J2.java:332-375. *iterations (when given) receives the iterations taken.
+// What J2.solve returns, and what it knew of its answer: the iterations taken and, when it
+// converged, the strain term at the returned increment (the new state's, which the caller
+// would otherwise evaluate again).
 template <typename T>
-static __device__ __noinline__ T j2_solve(T norm, T stiffness, T plasticStrain, T temperature,
-                                          T dt, const MatT<T> &jc, int *iterations = nullptr) {
-    const T thermal = jc_thermalTerm(jc, temperature);
+struct SolveOut {
+    T dGamma, strain;
+    int iterations, converged;
+};
+
+// J2.solve, J2.java:332-375, given the thermal term jc_thermalTerm(jc, temperature) of the
+// point's temperature (the reference evaluates it first thing, from the same argument).
+template <typename T>
+static __device__ __noinline__ SolveOut<T> j2_solve(T norm, T stiffness, T plasticStrain,
+                                                    T thermal, T dt, const MatT<T> &jc) {
     const T tolerance = Fn<T>::tolerance * jc.a;
     T lo = T(0);
     T hi = norm / stiffness;
@@ -153,10 +181,7 @@ static __device__ __noinline__ T j2_solve(T norm, T stiffness, T plasticStrain, 
         const T rateFactor = jc_rateTerm(jc, rate);
         const T g = norm - stiffness * dGamma - T(SQRT_2_3) * strain * rateFactor * thermal;
         if (g > T(0)) lo = dGamma; else hi = dGamma;
-        if (Fn<T>::abs(g) <= tolerance) {
-            if (iterations) *iterations = iteration + 1;
-            return dGamma;
-        }
+        if (Fn<T>::abs(g) <= tolerance) return SolveOut<T>{dGamma, strain, iteration + 1, 1};
         T slope = -stiffness
                   - T(TWO_THIRDS) * (jc.n * (strain - jc.a) / eps) * rateFactor * thermal;
         if (!(rate <= jc.refRate)) {
@@ -166,8 +191,7 @@ static __device__ __noinline__ T j2_solve(T norm, T stiffness, T plasticStrain, 
         if (!(next > lo && next < hi)) next = T(0.5) * (lo + hi);
         dGamma = next;
     }
-    if (iterations) *iterations = SOLVE_ITERATIONS;
-    return dGamma;
+    return SolveOut<T>{dGamma, T(0), SOLVE_ITERATIONS, 0};
 }
 
 // Damage.begin, Damage.java:306-336
@@ -195,23 +219,33 @@ static __device__ __noinline__ void damage_begin(const DamageRefT<T> &d, T flowS
     *d.softening = slope < floor_ ? floor_ : slope;
 }
 
+// The Johnson-Cook yield radius sqrt(2/3) A(eps) T(work) of a point's state and its thermal
+// term T: the quasi-static flow stress J2.update evaluates (JohnsonCook.java:138-209), in the
+// same operations, so a point whose state is unchanged since may use the kept pair instead.
+__device__ __forceinline__ double2 jc_yield(const MatDev &f, double epsP, double work) {
+    const double thermal = jc_thermalTerm(f, f.room + f.thermalCoefficient * work);
+    return make_double2(SQRT_2_3 * (jc_strainTerm(f, epsP) * thermal), thermal);
+}
+
 // J2.update, J2.java:163-296. s[4] and bk[4] are the point's stress and back stress
 // ({rr, zz, tt, rz}); damage is null for a material that cannot fail, in which case
 // dStrength/dSoft are ignored. Returns the plastic multiplier. *cost (when given) receives
 // the point's Johnson-Cook cost class: 0 none, 1 the quasi-static flow stress evaluated its
-// power laws, 1 + k a return-map solve of k iterations.
+// power laws, 1 + k a return-map solve of k iterations. jcYield (FP64 only, when given) holds
+// jc_yield of the point's current plastic strain and work for a Johnson-Cook material; it is
+// read in place of the power laws and kept up to date whenever they change.
 template <typename T>
 __device__ __forceinline__ T j2_update(T *s, T *bk, T &epsP, T &work, T dRR, T dZZ, T dTT,
                                        T dGamRZ, T lambda, T mu, const MatT<T> &flow, T strainDt,
                                        const DamageRefT<T> *damage, T dStrength, T dSoft,
-                                       int *cost = nullptr) {
+                                       int *cost = nullptr, double2 *jcYield = nullptr) {
     const T lt = lambda * (dRR + dZZ + dTT);
     const T tRR = s[0] + lt + T(2) * mu * dRR;
     const T tZZ = s[1] + lt + T(2) * mu * dZZ;
     const T tTT = s[2] + lt + T(2) * mu * dTT;
     const T tRZ = s[3] + mu * dGamRZ;
 
-    const T p = (tRR + tZZ + tTT) / T(3);
+    const T p = Fn<T>::div3(tRR + tZZ + tTT);
     const T xRR = tRR - p - bk[0];
     const T xZZ = tZZ - p - bk[1];
     const T xTT = tTT - p - bk[2];
@@ -219,11 +253,9 @@ __device__ __forceinline__ T j2_update(T *s, T *bk, T &epsP, T &work, T dRR, T d
     const T norm = Fn<T>::sqrt(xRR * xRR + xZZ * xZZ + xTT * xTT + T(2) * xRZ * xRZ);
 
     const bool jc = flow.jc != 0;
-    const T temperature = !jc ? T(0) : flow.room + flow.thermalCoefficient * work;
-
     const bool softening = damage != nullptr && dStrength > T(0);
     T hardening = T(0);
-    T flowStress;
+    T flowStress = T(0), radius, thermal = T(1);
     if (softening) {
         flowStress = dStrength + dSoft * (epsP - damage->failureStrain);
         if (flowStress > T(0)) {
@@ -231,14 +263,23 @@ __device__ __forceinline__ T j2_update(T *s, T *bk, T &epsP, T &work, T dRR, T d
         } else {
             flowStress = T(0);
         }
+        radius = T(SQRT_2_3) * flowStress;
     } else if (!jc) {
         flowStress = flow.sy0 + flow.hIso * epsP;
         hardening = flow.hIso;
+        radius = T(SQRT_2_3) * flowStress;
     } else {
-        flowStress = jc_quasiStatic(flow, epsP, temperature);
+        if (jcYield) {
+            const double2 y = *jcYield;
+            radius = T(y.x);
+            thermal = T(y.y);
+        } else {                          // jc_quasiStatic, its thermal term kept for the solve
+            thermal = jc_thermalTerm(flow, flow.room + flow.thermalCoefficient * work);
+            flowStress = jc_strainTerm(flow, epsP) * thermal;
+            radius = T(SQRT_2_3) * flowStress;
+        }
         if (cost && (epsP > T(0) || work > T(0))) *cost = 1;
     }
-    const T radius = T(SQRT_2_3) * flowStress;
 
     if (!(norm > radius)) {
         s[0] = tRR;
@@ -250,16 +291,21 @@ __device__ __forceinline__ T j2_update(T *s, T *bk, T &epsP, T &work, T dRR, T d
 
     const T stiffness = T(2) * mu + T(TWO_THIRDS) * flow.hKin;
     T dGamma;
+    T strainNew = T(0);                   // the strain term at the new plastic strain, if known
+    bool haveStrain = false;
     if (!jc || softening) {
         dGamma = (norm - radius) / (stiffness + T(TWO_THIRDS) * hardening);
         if (softening && flowStress + hardening * T(SQRT_2_3) * dGamma < T(0)) {
             dGamma = norm / stiffness;
         }
     } else {
-        int iterations = 0;
-        dGamma = j2_solve(norm, stiffness, epsP, temperature, strainDt, flow,
-                          cost ? &iterations : nullptr);
-        if (cost) *cost = 1 + iterations;
+        const SolveOut<T> r = j2_solve(norm, stiffness, epsP, thermal, strainDt, flow);
+        dGamma = r.dGamma;
+        // the solve's last strain term was taken at plasticStrain + sqrt(2/3) dGamma, the same
+        // sum that forms the new plastic strain below
+        strainNew = r.strain;
+        haveStrain = r.converged != 0;
+        if (cost) *cost = 1 + r.iterations;
     }
     const T inv = T(1) / norm;
     const T nRR = xRR * inv, nZZ = xZZ * inv, nTT = xTT * inv, nRZ = xRZ * inv;
@@ -281,10 +327,19 @@ __device__ __forceinline__ T j2_update(T *s, T *bk, T &epsP, T &work, T dRR, T d
 
     epsP += T(SQRT_2_3) * dGamma;
 
-    if (damage != nullptr && !softening && epsP >= damage->failureStrain) {
-        damage_begin(*damage,
-                     !jc ? flow.sy0 + flow.hIso * epsP : jc_quasiStatic(flow, epsP, temperature),
+    const bool onset = damage != nullptr && !softening && epsP >= damage->failureStrain;
+    if (jc && !haveStrain && (onset || jcYield)) {
+        strainNew = jc_strainTerm(flow, epsP);
+        haveStrain = true;
+    }
+    if (onset) {
+        // jc_quasiStatic(flow, epsP, temperature): the new strain, the step's own temperature
+        damage_begin(*damage, !jc ? flow.sy0 + flow.hIso * epsP : strainNew * thermal,
                      nRR, nZZ, nRZ);
+    }
+    if (jc && jcYield) {
+        const double th = jc_thermalTerm(flow, flow.room + flow.thermalCoefficient * work);
+        *jcYield = make_double2(SQRT_2_3 * ((double)strainNew * th), th);
     }
     return dGamma;
 }
@@ -307,6 +362,30 @@ template <typename T>
 __device__ __forceinline__ T corot_sin(T spinDt) {
     const T h = T(0.5) * spinDt;
     return T(2) * h / (T(1) + h * h);
+}
+
+// corot_rotate of a tensor whose rr, zz and rz are +0 gives +0 in all three when c and sn are
+// finite (|c|, |sn| <= 1, so no product overflows) and the rz component's two terms,
+// (c sn)(+0) and (c^2 - sn^2)(+0), are not both -0: a product's sign is its factors' sign
+// bits xor-ed, and +0 + -0 = +0.
+__device__ __forceinline__ bool corot_keeps_zero(double c, double sn) {
+    const uint64_t uc = (uint64_t)__double_as_longlong(c), us = (uint64_t)__double_as_longlong(sn);
+    const uint64_t ud = (uint64_t)__double_as_longlong(c * c - sn * sn);
+    return finite_bits(c) && finite_bits(sn) && !(((uc ^ us) & ud) >> 63);
+}
+
+// x is +-0 or 2^-400 <= |x| < 2^400 (the exponent field alone): scaling such values by a
+// power of two between 2^-8 and 2^8, and their products and differences, stay normal.
+__device__ __forceinline__ bool moderate_or_zero(double x) {
+    const uint64_t u = (uint64_t)__double_as_longlong(x);
+    const unsigned e = (unsigned)(u >> 52) & 0x7ffu;
+    return e - 623u < 800u || (u << 1) == 0;
+}
+
+// Bits of four values all zero: every value is +0.
+__device__ __forceinline__ bool all_plus_zero(double a, double b, double c, double d) {
+    return (__double_as_longlong(a) | __double_as_longlong(b) | __double_as_longlong(c) |
+            __double_as_longlong(d)) == 0;
 }
 
 template <typename T>

@@ -114,6 +114,9 @@ struct Dev {
     int32_t *emat;
     MatDev *mats;
     double *sig, *back, *epsP, *wP;
+    // [E] jc_yield of each Johnson-Cook point's plastic strain and work (one-point FP64 pass
+    // with a Johnson-Cook material; null otherwise), kept current with them
+    double2 *jcYield;
     double2 *hg;
     double *hgK;
     uint8_t *gone, *dead;
@@ -391,6 +394,8 @@ void solver_state_to_double(Solver &S);
 nf_status solver_fail(Solver &S, nf_status st, const char *message);
 nf_status solver_sync(Solver &S);
 void launch_measure(Solver &S, nf_measure *out);
+// jc_yield of every Johnson-Cook point's current state into d.jcYield (enqueued on st).
+void launch_jc_yield(const Dev &d, cudaStream_t st);
 void launch_material_points(const MatDev &m, int count, double *sig, double *back, double *epsP,
                             double *work, const double *strain, double strainDt,
                             const double *fail, const double *gf, const double *youngs,
