@@ -240,6 +240,7 @@ struct Grid {
     double cellSize, r0, z0;
     int cols, rows, hashed, bucketN;
     long long cells;
+    float screen;                // the FP32 screen's margin (search_group)
 };
 
 __device__ void grid_from_box(const Dev &d, int nodes, Grid &g) {
@@ -251,6 +252,7 @@ __device__ void grid_from_box(const Dev &d, int nodes, Grid &g) {
         g.cells = 1;
         g.hashed = 0;
         g.bucketN = 2;
+        g.screen = 0.0f;
         return;
     }
     const double rlo = unokey(vload(&s->bbox[0])), zlo = unokey(vload(&s->bbox[1]));
@@ -267,6 +269,10 @@ __device__ void grid_from_box(const Dev &d, int nodes, Grid &g) {
     g.cells = (long long)g.cols * (long long)g.rows;
     g.hashed = g.cells > d.bucketCap;
     g.bucketN = (int)((g.hashed ? (long long)d.bucketCap : g.cells) + 1);
+    // every surface node lies within W = max(rhi - rlo, zhi - zlo) of the origin in each
+    // coordinate; 2^-18 W bounds the FP32 screen's error twice over
+    const double w = rhi - rlo > zhi - zlo ? rhi - rlo : zhi - zlo;
+    g.screen = (float)(w * 0x1p-18);
 }
 
 __device__ __forceinline__ int iclamp(int v, int n) { return v < 0 ? 0 : v >= n ? n - 1 : v; }
@@ -320,6 +326,12 @@ __device__ __forceinline__ void inc_push(const Dev &d, int j, int entry) {
     else d.s->incOverflow = 1;
 }
 
+// x is a normal number below 2^1000 in size (the exponent field alone).
+__device__ __forceinline__ bool normal_below_2p1000(double x) {
+    const unsigned e = (unsigned)((unsigned long long)__double_as_longlong(x) >> 52) & 0x7ffu;
+    return e - 1u < 2022u;
+}
+
 // Contact.accumulate + resolve, Contact.java:446-462, :663-762, for slave node n and its
 // master segment q: writes the pair's twelve force terms as values to ADD (x - y is computed
 // as x + (-y), the same IEEE result) and files them at the pair's three nodes; keeps the
@@ -335,7 +347,11 @@ __device__ void resolve_pair(const Dev &d, int n, int q) {
     const double t = ((d.cr[n] - d.cr[a]) * tr + (d.cz[n] - d.cz[a]) * tz) / len;
     const double wa = 1.0 - t, wb = t;
     const double ma = d.mass[a], mb = d.mass[b];
-    const double invMaster = 0.25 / ma + 0.25 / mb;
+    // 0.25 / m is 0.25 (1 / m) exactly for a normal mass below 2^1000 (a power of two scales
+    // a rounded quotient without rounding again), and 1 / m is the kept invMass
+    const double qa = normal_below_2p1000(ma) ? 0.25 * d.invMass[a] : 0.25 / ma;
+    const double qb = normal_below_2p1000(mb) ? 0.25 * d.invMass[b] : 0.25 / mb;
+    const double invMaster = qa + qb;
     if (!(invMaster > 0.0)) return;
     const double mMaster = 1.0 / invMaster;
     const double mSlave = d.mass[n];
@@ -347,7 +363,7 @@ __device__ void resolve_pair(const Dev &d, int n, int q) {
     const double2 vn = d.V[n], va = d.V[a], vb = d.V[b];
     const double closing = (vn.x - wa * va.x - wb * vb.x) * nR
                            + (vn.y - wa * va.y - wb * vb.y) * nZ;
-    const double damper = 2.0 * d.cDamping * mStar * sqrt(d.cScale) / reference;
+    const double damper = 2.0 * d.cDamping * mStar * d.cSqrtScale / reference;
     const double normal = jmax(0.0, k * depth - damper * closing);
     double *pv = d.pairVal + 12 * (size_t)n;
     pv[0] = normal * nR;
@@ -396,19 +412,25 @@ __device__ void resolve_pair(const Dev &d, int n, int q) {
 // Contact.nearestPenetrated (Contact.java:570-606) for 32 / SG slaves per warp, SG lanes (a
 // group) each: the deepest admissible segment and whether the last step's master was seen too
 // deep. Entry idx of the surface-node list is the group's slave (none when idx is past the
-// list or struck out). The nine bucket ranges are concatenated, the lanes take the candidates
-// round-robin, and every candidate carries its visit key (cell in the nine, then the bucket
-// entry 2 q + end): ties in depth go to the smallest key, the candidate the serial loop keeps,
-// so the buckets need no order. All 32 lanes run every shuffle.
-// The grid's buckets as the search reads them: the counting-sort layout (bucket b's entries at
+// list or struck out). The nine bucket ranges are concatenated and the lanes take the
+// candidates round-robin; every candidate carries its visit key (cell in the nine, then the
+// bucket entry 2 q + end): ties in depth go to the smallest key, the candidate the serial loop
+// keeps, so neither the buckets nor the order the lanes test in matter.
+//
+// An FP32 screen first drops every candidate the exact test would reject for lying in front of
+// the segment or beyond its ends: positions relative to the grid origin are below W (the
+// larger box side) in size, so the FP32 gap and projection differ from the FP64 ones by less
+// than 2^-19 W, and a candidate is dropped only when its FP32 value clears the bound by
+// 2^-18 W (g.screen). The few that pass take the exact FP64 test, each lane its own. The
+// grid's buckets as the search reads them: the counting-sort layout (bucket b's entries at
 // [start[b], start[b + 1]), each with its cell) or the direct-indexed one (cell c's entries at
 // [c cap, c cap + count[c]), every entry in its own cell).
 struct BucketView {
     const int32_t *start, *count;
     const long long *cell;                     // null in the direct-indexed layout
     const int32_t *entry;
-    const double2 *a, *n;
-    const double *l;
+    const float4 *f;                           // first node - grid origin, normal (FP32)
+    const float *fl;                           // length (FP32)
     int cap;                                   // 0: the counting-sort layout
 };
 __device__ __forceinline__ void bucket_range(const BucketView &v, int b, int &lo, int &len) {
@@ -422,34 +444,37 @@ __device__ __forceinline__ void bucket_range(const BucketView &v, int b, int &lo
 }
 
 constexpr int SG = 8;                          // lanes per slave
+constexpr int KEPT = 4;                        // screened candidates a lane keeps for later
 __device__ void search_group(const Dev &d, const Grid &g, const BucketView &v, int idx,
                              int listLen, double &bestOut, int &segOut, bool &fellOut) {
     const int lane = threadIdx.x & 31, gl = lane & (SG - 1);
     int n = idx < listLen ? d.nodeList[idx] : -1;
     const bool live = n >= 0;
     double2 xn = make_double2(0.0, 0.0);
+    float xs = 0.0f, ys = 0.0f;
     int last = -1, ci = 0, cj = 0;
     if (live) {
         xn = make_double2(d.cr[n], d.cz[n]);
         last = d.lastMaster[n];
-        ci = iclamp(jd2i((xn.x - g.r0) / g.cellSize), g.cols);
-        cj = iclamp(jd2i((xn.y - g.z0) / g.cellSize), g.rows);
+        const int2 cell = d.nodeCell[n];
+        ci = cell.x;
+        cj = cell.y;
+        xs = (float)(xn.x - g.r0);
+        ys = (float)(xn.y - g.z0);
     }
     // the nine cells in visit order: lane gl takes cell gl, lane 0 also cell 8
     int lo = 0, len = 0, lo8 = 0, len8 = 0;
     long long myCell = -1, cell8 = -1;
     if (live) {
-        if (gl < 8) {                           // lanes from 8 on take no cell
-            const int j = cj + gl / 3 - 1, ii = ci + gl % 3 - 1;
-            if (j >= 0 && j < g.rows && ii >= 0 && ii < g.cols) {
-                myCell = (long long)j * g.cols + ii;
-                bucket_range(v, bucket_of(d, g, myCell), lo, len);
-            }
+        const int j = cj + gl / 3 - 1, ii = ci + gl % 3 - 1;
+        if (j >= 0 && j < g.rows && ii >= 0 && ii < g.cols) {
+            myCell = (long long)j * g.cols + ii;
+            bucket_range(v, bucket_of(d, g, myCell), lo, len);
         }
         if (gl == 0) {
-            const int j = cj + 1, ii = ci + 1;
-            if (j < g.rows && ii < g.cols) {
-                cell8 = (long long)j * g.cols + ii;
+            const int j8 = cj + 1, i8 = ci + 1;
+            if (j8 < g.rows && i8 < g.cols) {
+                cell8 = (long long)j8 * g.cols + i8;
                 bucket_range(v, bucket_of(d, g, cell8), lo8, len8);
             }
         }
@@ -465,50 +490,66 @@ __device__ void search_group(const Dev &d, const Grid &g, const BucketView &v, i
     len8 = __shfl_sync(0xffffffffu, len8, 0, SG);
     cell8 = __shfl_sync(0xffffffffu, cell8, 0, SG);
     const int total = off8 + len8;
-    int rounds = total;                         // the longest group's candidates, warp-wide
-    for (int o = 16; o > 0; o >>= 1) rounds = max(rounds, __shfl_xor_sync(0xffffffffu, rounds, o));
+    // every lane keeps the group's nine ranges (start in the concatenation, first slot, cell)
+    int offs[8], los[8];
+    long long cellq[8];
+#pragma unroll
+    for (int qq = 0; qq < 8; qq++) {
+        offs[qq] = __shfl_sync(0xffffffffu, off, qq, SG);
+        los[qq] = __shfl_sync(0xffffffffu, lo, qq, SG);
+        cellq[qq] = __shfl_sync(0xffffffffu, myCell, qq, SG);
+    }
+    // position t of the concatenation: its range c (0..8), its slot k and the range's cell
+    auto locate = [&](int t, int &c, int &k, long long &cc) {
+        c = 0;
+        int oc = offs[0], lc = los[0];
+        cc = cellq[0];
+#pragma unroll
+        for (int qq = 1; qq < 8; qq++) {
+            if (t >= offs[qq]) {
+                c = qq;
+                oc = offs[qq];
+                lc = los[qq];
+                cc = cellq[qq];
+            }
+        }
+        if (t >= off8) {
+            c = 8;
+            oc = off8;
+            lc = lo8;
+            cc = cell8;
+        }
+        k = lc + (t - oc);
+    };
     double best = 0.0;
     unsigned long long bestKey = ~0ULL;
     int bestSeg = -1;
     bool fell = false;
-    for (int base = 0; base < rounds; base += SG) {
-        const int t = base + gl;
-        int c = 0;                              // which of the nine ranges holds position t
-#pragma unroll
-        for (int qq = 1; qq < 8; qq++) {
-            const int oq = __shfl_sync(0xffffffffu, off, qq, SG);
-            if (t >= oq) c = qq;
-        }
-        if (t >= off8) c = 8;
-        const int src = c < 8 ? c : 0;
-        const int oc0 = __shfl_sync(0xffffffffu, off, src, SG);
-        const int lc0 = __shfl_sync(0xffffffffu, lo, src, SG);
-        const long long cc0 = __shfl_sync(0xffffffffu, myCell, src, SG);
-        if (t >= total) continue;
-        const int oc = c < 8 ? oc0 : off8, lc = c < 8 ? lc0 : lo8;
-        const long long cc = c < 8 ? cc0 : cell8;
-        const int k = lc + (t - oc);
+    // the exact test of position t (Contact.depth, Contact.java:642-652, and the exclusions):
+    // the segment's first node, normal and length as the geometry phase left them
+    auto exact = [&](int t) {
+        int c, k;
+        long long cc;
+        locate(t, c, k, cc);
+        if (v.cell && v.cell[k] != cc) return;          // a hashed bucket shares cells
         const int entry = v.entry[k];
-        const double2 pa = v.a[k], nrm = v.n[k];
-        const double slen = v.l[k];
-        if (v.cell && v.cell[k] != cc) continue;        // a hashed bucket shares cells
-        // depth_of from what the filing staged beside the entry (the segment's first node,
-        // normal and length: the same values, the same expressions): zero unless the slave is
-        // behind the segment and projects onto it
-        const double dr = xn.x - pa.x, dz = xn.y - pa.y;
-        const double gap = dr * nrm.x + dz * nrm.y;
-        if (!(gap < 0.0)) continue;
-        if (slen <= 0.0) continue;
-        const double along = dr * -nrm.y + dz * nrm.x;
-        if (along < 0.0 || along > slen) continue;
+        const int sg = entry >> 1;
+        const int a = d.segA[sg];
+        const double dr = xn.x - d.cr[a], dz = xn.y - d.cz[a];
+        const double nr = d.snr[sg], nz = d.snz[sg];
+        const double gap = dr * nr + dz * nz;
+        if (!(gap < 0.0)) return;
+        const double slen = d.slen[sg];
+        if (slen <= 0.0) return;
+        const double along = dr * -nz + dz * nr;
+        if (along < 0.0 || along > slen) return;
         const double depth = -gap;
         // the exclusions read the slave's own rings (dependent loads); a candidate that fails
         // them is skipped whatever its depth, so testing them after the depth changes nothing
-        const int sg = entry >> 1;
-        if (excluded(d, n, sg)) continue;
+        if (excluded(d, n, sg)) return;
         if (depth > MAX_DEPTH * slen) {
             if (sg == last) fell = true;
-            continue;
+            return;
         }
         const unsigned long long key = ((unsigned long long)c << 32) | (unsigned int)entry;
         if (depth > best || (depth == best && key < bestKey)) {
@@ -516,7 +557,32 @@ __device__ void search_group(const Dev &d, const Grid &g, const BucketView &v, i
             bestKey = key;
             bestSeg = sg;
         }
+    };
+    int kept[KEPT];
+#pragma unroll
+    for (int j = 0; j < KEPT; j++) kept[j] = -1;
+    for (int t = gl; t < total; t += SG) {
+        int c, k;
+        long long cc;
+        locate(t, c, k, cc);
+        const float4 f = v.f[k];
+        const float dr = xs - f.x, dz = ys - f.y;
+        if (dr * f.z + dz * f.w > g.screen) continue;
+        const float along = dr * -f.w + dz * f.z;
+        if (along < -g.screen || along > v.fl[k] + g.screen) continue;
+        bool placed = false;
+#pragma unroll
+        for (int j = 0; j < KEPT; j++) {
+            if (!placed && kept[j] < 0) {
+                kept[j] = t;
+                placed = true;
+            }
+        }
+        if (!placed) exact(t);
     }
+#pragma unroll
+    for (int j = 0; j < KEPT; j++)
+        if (kept[j] >= 0) exact(kept[j]);
     for (int o = SG / 2; o > 0; o >>= 1) {
         const double ob = __shfl_down_sync(0xffffffffu, best, o, SG);
         const unsigned long long ok = __shfl_down_sync(0xffffffffu, bestKey, o, SG);
@@ -797,7 +863,15 @@ __global__ void __launch_bounds__(CB, 2) k_contact_pass(Dev d) {
     }
     __syncthreads();
     const Grid g = grid;
-    FOR_GRID(i, nodeLen) {                       // each node's segments in ascending order
+    // Per surface node: its normal from its segments in ascending order; its grid cell, once
+    // (the search reads it for the node as a slave); and the filing of every segment end at the
+    // node under that cell. A grid of at most fastCells - 1 cells is indexed directly: each
+    // entry takes the next of its cell's slots (fastLimit of the fastCap reserved) and is filed
+    // there at once, with the FP32 values the search's screen reads. A larger (or hashed) grid,
+    // or a cell that outgrows its slots, takes the counting sort: the counts, an exclusive
+    // scan, the filing.
+    const bool fast = !g.hashed && g.cells < d.fastCells;
+    FOR_GRID(i, nodeLen) {
         const int n = d.nodeList[i];
         if (n < 0) continue;
         const int32_t *own = d.nodeSeg + (size_t)n * d.segCap;
@@ -810,33 +884,29 @@ __global__ void __launch_bounds__(CB, 2) k_contact_pass(Dev d) {
         const double len = sqrt(sr * sr + sz * sz);
         d.pnr[n] = len > 0.0 ? sr / len : 0.0;
         d.pnz[n] = len > 0.0 ? sz / len : 0.0;
-    }
-    // A grid of at most fastCells - 1 cells is indexed directly: each entry takes the next of
-    // its cell's slots (fastLimit of the fastCap reserved) and is filed there at once, staging
-    // beside it what the search's depth test reads. A larger (or hashed) grid, or a cell that
-    // outgrows its slots, takes the counting sort: the counts, an exclusive scan, the filing.
-    const bool fast = !g.hashed && g.cells < d.fastCells;
-    FOR_GRID(t, 2 * edgeLen) {
-        const int q = d.edgeList[t >> 1];
-        if (q < 0) continue;
-        const int entry = 2 * q + (t & 1);
-        const int node = (t & 1) ? d.segB[q] : d.segA[q];
-        const long long cell = cell_of(g, d.cr[node], d.cz[node]);
-        d.entryCell[entry] = cell;
-        if (fast) {
-            const int pos = atomicAdd(&d.fastCount[cell], 1);
-            if (pos < d.fastLimit) {
-                const size_t slot = (size_t)cell * d.fastCap + pos;
-                const int a = d.segA[q];
-                d.fastEntry[slot] = entry;
-                d.fastA[slot] = make_double2(d.cr[a], d.cz[a]);
-                d.fastN[slot] = make_double2(d.snr[q], d.snz[q]);
-                d.fastL[slot] = d.slen[q];
+        const int ci = iclamp(jd2i((d.cr[n] - g.r0) / g.cellSize), g.cols);   // cell_of
+        const int cj = iclamp(jd2i((d.cz[n] - g.z0) / g.cellSize), g.rows);
+        d.nodeCell[n] = make_int2(ci, cj);
+        const long long cell = (long long)cj * g.cols + ci;
+        for (int k = 0; k < count; k++) {
+            const int q = own[k];
+            const int a = d.segA[q];
+            const int entry = 2 * q + (a == n ? 0 : 1);
+            d.entryCell[entry] = cell;
+            if (fast) {
+                const int pos = atomicAdd(&d.fastCount[cell], 1);
+                if (pos < d.fastLimit) {
+                    const size_t slot = (size_t)cell * d.fastCap + pos;
+                    d.fastEntry[slot] = entry;
+                    d.fastF[slot] = make_float4((float)(d.cr[a] - g.r0), (float)(d.cz[a] - g.z0),
+                                                (float)d.snr[q], (float)d.snz[q]);
+                    d.fastFL[slot] = (float)d.slen[q];
+                } else {
+                    s->fastOverflow = 1;
+                }
             } else {
-                s->fastOverflow = 1;
+                atomicAdd(&d.bucketCount[bucket_of(d, g, cell)], 1);
             }
-        } else {
-            atomicAdd(&d.bucketCount[bucket_of(d, g, cell)], 1);
         }
     }
     SYNC();
@@ -854,19 +924,18 @@ __global__ void __launch_bounds__(CB, 2) k_contact_pass(Dev d) {
             const int pos = atomicAdd(&d.bucketCursor[bucket_of(d, g, cell)], 1);
             d.bucketEntry[pos] = entry;
             d.bucketCell[pos] = cell;
-            d.bucketA[pos] = make_double2(d.cr[a], d.cz[a]);
-            d.bucketN[pos] = make_double2(d.snr[q], d.snz[q]);
-            d.bucketL[pos] = d.slen[q];
+            d.bucketF[pos] = make_float4((float)(d.cr[a] - g.r0), (float)(d.cz[a] - g.z0),
+                                         (float)d.snr[q], (float)d.snz[q]);
+            d.bucketFL[pos] = (float)d.slen[q];
         }
         SYNC();
     }
     BucketView view;
     if (direct) {
-        view = BucketView{nullptr, d.fastCount, nullptr, d.fastEntry, d.fastA, d.fastN, d.fastL,
-                          d.fastCap};
+        view = BucketView{nullptr, d.fastCount, nullptr, d.fastEntry, d.fastF, d.fastFL, d.fastCap};
     } else {
-        view = BucketView{d.bucketStart, nullptr, d.bucketCell, d.bucketEntry, d.bucketA,
-                          d.bucketN, d.bucketL, 0};
+        view = BucketView{d.bucketStart, nullptr, d.bucketCell, d.bucketEntry, d.bucketF,
+                          d.bucketFL, 0};
     }
 
     // the search and the pair forces: each warp searches 32 / SG slaves at a time, SG lanes

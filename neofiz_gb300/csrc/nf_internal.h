@@ -103,6 +103,7 @@ struct Dev {
     double gravR, gravZ, targetPressure, rampDuration, erosionDamage;
     double wallPlane, wallFriction;
     double cFriction, cScale, cDamping, dt0;
+    double cSqrtScale;                       // sqrt(cScale), rounded once
     int nmat;
     int sms;                                 // multiprocessors on the device
     // nodes
@@ -140,6 +141,7 @@ struct Dev {
     int32_t *nodeList, *nodePos;             // [N] the surface nodes in any order (-1: left the
                                              // surface), and each node's place (-1: none)
     int32_t *nodeFree;                       // [N] free edges incident to each node
+    int2 *nodeCell;                          // [N] a surface node's grid cell (column, row)
     int32_t *nodeSeg;                        // [N x segCap] each surface node's free edges,
     int segCap;                              // ascending (2 x the largest node valence)
     int32_t *edgeStamp, *nodeStamp;          // [4E], [N] rebuild epoch of the last visit
@@ -152,16 +154,18 @@ struct Dev {
     uint8_t *dropped;                        // [N]
     int32_t *bucketCount, *bucketStart, *bucketCursor;   // [bucketCap + 1]
     int32_t *bucketEntry;                    // [8E] entries (2 q + end)
-    double2 *bucketA, *bucketN;              // [8E] by position: the segment's first node, normal
-    double *bucketL;                         // [8E] by position: the segment's length
+    // [8E] by position, for the search's FP32 screen: the segment's first node relative to the
+    // grid origin and its normal (float4), and its length (float)
+    float4 *bucketF;
+    float *bucketFL;
     long long *bucketCell;                   // [8E] cell of each filed entry, by position
     long long *entryCell;                    // [8E] cell of each entry, by entry
     // the direct-indexed grid: cell c's entries in slots [c fastCap, c fastCap + fastCount[c])
     // when the grid has at most fastCells cells and none holds more than fastCap entries
     int32_t *fastCount;                      // [fastCells]
     int32_t *fastEntry;                      // [fastCells x fastCap]
-    double2 *fastA, *fastN;                  // [fastCells x fastCap]
-    double *fastL;                           // [fastCells x fastCap]
+    float4 *fastF;                           // [fastCells x fastCap] as bucketF
+    float *fastFL;                           // [fastCells x fastCap] as bucketFL
     int fastCells, fastCap;                  // cells indexed directly, slots per cell
     int fastLimit;                           // slots a step may use, <= fastCap (nf_set_grid_slots)
     int bucketCap;
