@@ -21,6 +21,7 @@ constexpr double SQRT_2_3 = 0x1.a20bd700c2c3ep-1;     // Math.sqrt(2.0 / 3.0)
 constexpr double TWO_THIRDS = 2.0 / 3.0;
 constexpr double SOLVE_TOLERANCE = 1.0e-10;
 constexpr int SOLVE_ITERATIONS = 25;
+constexpr int COST_NEAR_YIELD = SOLVE_ITERATIONS + 2;   // cost class of an elastic point near yield
 constexpr double ISOTROPIC = 1.0e-9;
 constexpr double DMAX = 1.7976931348623157e308;        // Double.MAX_VALUE
 
@@ -164,6 +165,13 @@ struct SolveOut {
     int iterations, converged;
 };
 
+// An ordering hint only (never part of a result): norm / radius above about 0.81, for
+// non-negative norm and positive radius, from their bit patterns.
+__device__ __forceinline__ bool near_yield(double norm, double radius) {
+    return __double_as_longlong(norm) - __double_as_longlong(radius) > -(1351079888211148LL);
+}
+__device__ __forceinline__ bool near_yield(float norm, float radius) { return norm > 0.81f * radius; }
+
 // J2.solve, J2.java:332-375, given the thermal term jc_thermalTerm(jc, temperature) of the
 // point's temperature (the reference evaluates it first thing, from the same argument).
 template <typename T>
@@ -286,6 +294,10 @@ __device__ __forceinline__ T j2_update(T *s, T *bk, T &epsP, T &work, T dRR, T d
         s[1] = tZZ;
         s[2] = tTT;
         s[3] = tRZ;
+        // a Johnson-Cook point within about 20 % of its yield radius is likely to yield soon:
+        // the bit patterns of two positive doubles differ by about 2^52 log2 of their ratio,
+        // so an integer difference above -0.3 2^52 is a ratio above about 0.81
+        if (cost && jc && !softening && near_yield(norm, radius)) *cost = COST_NEAR_YIELD;
         return T(0);
     }
 

@@ -82,9 +82,13 @@ struct DevScalars {
 // listed elements first, packed into warps of equal cost, then every other element. A warp
 // issues at most one FP64 instruction per 64 cycles and the SM's pipe takes one per 19, so a
 // long solve is a serial chain whose time grows with the warps sharing its SM: the pass runs
-// with two blocks per SM (eight warps) and the longest solves start first. The elements'
+// with two blocks per SM (eight warps) and the longest solves start first. A point that stayed
+// elastic close to its yield surface (COST_NEAR_YIELD) is listed too, ahead of every solve
+// class: yielding again after unloading, or for the first time, takes the longest solves, and
+// such a point in a warp of elastic points makes the whole warp run its solve. The elements'
 // results do not depend on the order they are computed in.
-constexpr int HOT_CLASSES = 2 + 25;          // 0 none, 1 flow-stress powers, 1 + iterations
+constexpr int HOT_CLASSES = COST_NEAR_YIELD + 1;   // 0 none, 1 flow-stress powers,
+                                                   // 1 + iterations, near yield
 struct HotList {
     int count;                               // listed elements in this step's order
     int nextCount;                           // entries appended by this step's pass
