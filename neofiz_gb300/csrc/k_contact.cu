@@ -74,9 +74,11 @@ __device__ __forceinline__ T vload(const T *p) { return *(const volatile T *)p; 
 
 // ---------------------------------------------------------------------------- block helpers
 
-// Fixed-order block sum; the result is valid in thread 0. Leaves sh free for reuse.
+// Fixed-order block sum; the result is valid in thread 0. Leaves sh free for reuse. A warp of
+// +0s skips its tree (its sum is +0 either way).
 __device__ double block_sum_c(double v, double *sh) {
-    for (int o = 16; o > 0; o >>= 1) v += __shfl_down_sync(0xffffffffu, v, o);
+    if (__any_sync(0xffffffffu, __double_as_longlong(v) != 0))
+        for (int o = 16; o > 0; o >>= 1) v += __shfl_down_sync(0xffffffffu, v, o);
     const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
     __syncthreads();
     if (lane == 0) sh[warp] = v;

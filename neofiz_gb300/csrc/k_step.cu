@@ -27,8 +27,12 @@ __device__ __forceinline__ double bitsd(unsigned long long u) {
 }
 
 // Fixed-shape block sum: the same inputs in the same threads always add in the same order.
+// A warp whose 32 values are all +0 skips its tree (its sum is +0 either way), which most warps
+// of the per-step totals are (wall terms, eroded energy): an FP64 warp instruction costs the
+// same with any number of lanes, so the tree is not free.
 __device__ double block_sum(double v, double *sh) {
-    for (int o = 16; o > 0; o >>= 1) v += __shfl_down_sync(0xffffffffu, v, o);
+    if (__any_sync(0xffffffffu, __double_as_longlong(v) != 0))
+        for (int o = 16; o > 0; o >>= 1) v += __shfl_down_sync(0xffffffffu, v, o);
     const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
     __syncthreads();
     if (lane == 0) sh[warp] = v;
@@ -576,18 +580,29 @@ __global__ void __launch_bounds__(1024) k_end(Dev d, int nodeBlocks, int elemBlo
         }
         const int chunk = (count + END_WARPS_PER_LIST - 1) / END_WARPS_PER_LIST;
         const int lo = min(count, run * chunk), hi = min(count, lo + chunk);
-        // the loads of eight terms are issued before they are added
+        // each lane adds the terms lo + lane, + 32, + 64, ... in that order, eight loads at a
+        // time. The loop runs the same number of times in every lane of the warp (positions at
+        // or past hi read as +0), so the warp vote inside it is taken by all 32 lanes. A batch
+        // of +0s in every lane is skipped: v starts at +0 and a sum of doubles only reaches -0
+        // from -0 terms, so adding +0 never changes it (most blocks' wall and erosion terms
+        // are +0)
         double v = 0.0;
-        int k = lo + lane;
-        for (; k + 7 * 32 < hi; k += 8 * 32) {
+        for (int base = lo; base < hi; base += 8 * 32) {
             double x[8];
+            long long any = 0;
 #pragma unroll
-            for (int j = 0; j < 8; j++) x[j] = src[k + 32 * j];
+            for (int j = 0; j < 8; j++) {
+                const int k = base + lane + 32 * j;
+                x[j] = k < hi ? src[k] : 0.0;
+                any |= __double_as_longlong(x[j]);
+            }
+            if (__any_sync(0xffffffffu, any != 0)) {
 #pragma unroll
-            for (int j = 0; j < 8; j++) v += x[j];
+                for (int j = 0; j < 8; j++) v += x[j];
+            }
         }
-        for (; k < hi; k += 32) v += src[k];
-        for (int o = 16; o > 0; o >>= 1) v += __shfl_down_sync(0xffffffffu, v, o);
+        if (__any_sync(0xffffffffu, __double_as_longlong(v) != 0))
+            for (int o = 16; o > 0; o >>= 1) v += __shfl_down_sync(0xffffffffu, v, o);
         if (lane == 0 && list < 6) part[list][run] = v;
         __syncthreads();
         if (threadIdx.x < 6) {

@@ -427,10 +427,11 @@ int listed_pass_smem(int device);
 size_t scan_tmp_ints(int n);
 
 int grid_for(long long n, int block);
-// Fixed grids of the node and element kernels that reduce per block: a few blocks per SM,
-// striding over the items, so the number of partial sums stays small.
+// Fixed grids of the node and element kernels that reduce per block, striding over the items.
+// The nodal update takes one node per thread up to sixteen blocks per SM (every block resident
+// at once, no second pass over the nodes); the element kernels stop at eight.
 inline int nodal_grid(const Solver &S) {
-    const int g = grid_for(S.d.N, 128), cap = 8 * S.d.sms;
+    const int g = grid_for(S.d.N, 128), cap = 16 * S.d.sms;
     return g < cap ? g : cap;
 }
 inline int element_grid(const Solver &S) {
