@@ -36,12 +36,13 @@ CELL = 0.114e-3
 GAP = 0.5e-3
 WINDOW_START = 400          # steps run before warm-up and timing, in both arms
 L2_FLUSH_BYTES = 256 << 20
-# DRAM bytes (read + write) of one element-pass launch of this workload after 300 steps, from
-# ncu's dram__bytes_read.sum + dram__bytes_write.sum (ncu cannot run inside the timed bench)
-ELEMENT_TRAFFIC_BYTES = {CELL: 40_560_000 + 40_000}
+# DRAM bytes (read + write) of one element-pass launch of this workload in the window, from
+# ncu's dram__bytes_read.sum + dram__bytes_write.sum, the mean over the launches of steps
+# start + 6 and start + 7 (ncu cannot run inside the timed bench)
+ELEMENT_TRAFFIC_BYTES = {CELL: (43_484_160 + 177_408 + 43_474_688 + 37_888) // 2}
 # FP64-pipe warp instructions of one element-pass launch in the window: the mean of ncu's
-# smsp__inst_executed_pipe_fp64.sum over the launches of steps start + 6 and start + 7
-ELEMENT_FP64_WARP_INST = {CELL: (3_784_456 + 3_675_685) // 2}
+# smsp__inst_executed_pipe_fp64.sum over the same two launches
+ELEMENT_FP64_WARP_INST = {CELL: (3_066_238 + 3_058_495) // 2}
 
 
 def parse():

@@ -177,10 +177,13 @@ __global__ void k_scale_mass(double *mass, double *invMass, int n, double factor
         invMass[i] = 1.0 / mass[i];
     }
 }
+// The bounds of a run; the next step's run predicate follows from them (each step's end sets
+// it for the step after).
 __global__ void k_set_run(DevScalars *s, double tEnd, long long maxSteps) {
     s->tEnd = tEnd;
     s->maxSteps = maxSteps;
     s->stepsTaken = 0;
+    s->active = s->time < tEnd && 0 < maxSteps ? 1 : 0;
 }
 
 nf_status sync_check(Solver &S) {
@@ -686,6 +689,7 @@ nf_status nf_set_rigid_wall(nf_solver *h, double plane, double friction) {
     if (st) return st;
     s.wImpulse = s.wEnergyLoss = s.wFriction = 0.0;
     s.wContact = s.wStuck = 0;
+    s.wContactAcc = s.wStuckAcc = 0;
     CK(&S, cudaMemcpyAsync(S.d.s, &s, sizeof s, cudaMemcpyHostToDevice, S.stream));
     S.d.hasWall = 1;
     S.d.wallPlane = plane;

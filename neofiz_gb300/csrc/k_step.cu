@@ -1,15 +1,17 @@
 // k_step.cu -- the kernels of one explicit central-difference timestep
 // (ExplicitSolver.step, src/main/java/org/neofiz/solver/ExplicitSolver.java:940-991):
 //
-//   k_begin            dtAvg, decay, gain; the run predicate                       :947-956
-//   k_nodal            velocity/position update, fixed DOFs, rigid wall            :998-1062
+//   k_nodal            dtAvg, decay, gain; velocity/position update, fixed DOFs,   :947-956,
+//                      rigid wall                                                  :998-1062
 //   k_erode            deletion of failed or inverted elements                      :663-691
 //   k_element_reduced  one-point quadrature + Flanagan-Belytschko hourglass        :1373-1504
 //   k_element_full     2x2 Gauss quadrature                                         :1219-1339
 //   k_pressure         follower pressure on the bore edges                          :1511-1556
 //   k_gather           per-node sum of its sources in CSR order, plus m g           :1147-1165
 //   (contact kernels, k_contact.cu)                                                :1099-1109
-//   k_end              running totals, adaptive CFL step                            :985-990
+//   k_end              running totals, adaptive CFL step, the next step's run      :985-990
+//                      predicate
+//   (k_begin starts the initial assembly only)
 //
 // Every kernel reads the solver's scalars (dt, time, ...) from device memory, so a sequence
 // of steps is a fixed sequence of launches with no host decision between them.
@@ -47,21 +49,12 @@ __device__ double block_sum(double v, double *sh) {
 
 // ------------------------------------------------------------------------------------ begin
 
-__global__ void k_begin(Dev d, int initial) {
+// The initial assembly's start: the run predicate and the contact pass's per-step scalars.
+// A step proper starts inside k_nodal.
+__global__ void k_begin(Dev d) {
     DevScalars *s = d.s;
-    const bool active = s->time < s->tEnd && s->stepsTaken < s->maxSteps;
-    s->active = active ? 1 : 0;
+    s->active = s->time < s->tEnd && s->stepsTaken < s->maxSteps ? 1 : 0;
     contact_step_reset(s);
-    if (!active || initial) return;
-    const double dtAvg = 0.5 * (s->dtPrevious + s->dt);
-    const double half = 0.5 * d.damping * dtAvg;
-    s->decay = (1.0 - half) / (1.0 + half);
-    s->gain = dtAvg / (1.0 + half);
-    s->dtAvg = dtAvg;
-    if (d.hasWall) {                 // RigidWall.beginStep, RigidWall.java:153-156
-        s->wContact = 0;
-        s->wStuck = 0;
-    }
 }
 
 // ------------------------------------------------------------------------------------ nodal
@@ -71,15 +64,40 @@ __global__ void k_begin(Dev d, int initial) {
 // wall terms in node order and the block adds its threads in a fixed tree, so the totals are
 // deterministic. 1/m comes from the invMass array (the same division, done once). In the
 // mixed form the kernel also writes the FP32 geometry the element kernel reads.
+//
+// The step starts here (ExplicitSolver.java:944-952): the run predicate was set by the last
+// step's end (or by the run's bounds); each block's first thread forms the damping
+// coefficients from dt and dtPrevious, which nothing in this kernel writes (the same values in
+// every block; one thread, as FP64 costs a whole warp's issue whatever the lanes), and block 0
+// resets the contact pass's per-step scalars, which nothing in this kernel reads. The wall
+// counts add into their own accumulators, which the step's end publishes and clears
+// (RigidWall.beginStep, RigidWall.java:153-156).
 __global__ void __launch_bounds__(BLOCK) k_nodal(Dev d) {
     __shared__ double sh[BLOCK / 32];
-    const DevScalars *s = d.s;
+    __shared__ double coef[3];
+    DevScalars *s = d.s;
     if (!s->active) return;
-    const double decay = s->decay, gain = s->gain, dtAvg = s->dtAvg, dt = s->dt;
+    const double dt = s->dt;
+    if (threadIdx.x == 0) {
+        const double avg = 0.5 * (s->dtPrevious + dt);
+        const double half = 0.5 * d.damping * avg;
+        coef[0] = (1.0 - half) / (1.0 + half);
+        coef[1] = avg / (1.0 + half);
+        coef[2] = avg;
+        if (blockIdx.x == 0) {
+            s->decay = coef[0];
+            s->gain = coef[1];
+            s->dtAvg = avg;
+            contact_step_reset(s);
+        }
+    }
+    __syncthreads();
+    const double decay = coef[0], gain = coef[1], dtAvg = coef[2];
     double impulse = 0.0, loss = 0.0, fric = 0.0;
     for (int i = blockIdx.x * blockDim.x + threadIdx.x; i < d.N; i += gridDim.x * blockDim.x) {
         nodal_node(d, i, NodalCoef{decay, gain, dtAvg, dt},
-                   WallRef{d.hasWall, d.wallPlane, d.wallFriction, &d.s->wContact, &d.s->wStuck},
+                   WallRef{d.hasWall, d.wallPlane, d.wallFriction, &d.s->wContactAcc,
+                           &d.s->wStuckAcc},
                    d.mixed ? MixedGeo{d.pMid, d.pCur, d.vdt, 0} : MixedGeo{nullptr, nullptr, nullptr, 0},
                    &d.s->status, impulse, loss, fric);
     }
@@ -619,6 +637,10 @@ __global__ void __launch_bounds__(1024) k_end(Dev d, int nodeBlocks, int elemBlo
         s->wImpulse += w0;
         s->wEnergyLoss += w1;
         s->wFriction += w2;
+        s->wContact = s->wContactAcc;
+        s->wStuck = s->wStuckAcc;
+        s->wContactAcc = 0;
+        s->wStuckAcc = 0;
     }
     if (updateDt && d.hasErosion) s->erodedEnergy += er;
     if (d.hasContact) {
@@ -635,6 +657,8 @@ __global__ void __launch_bounds__(1024) k_end(Dev d, int nodeBlocks, int elemBlo
         }
         s->stepsTaken += 1;
     }
+    // the next step's run predicate (its kernels all read it)
+    s->active = s->time < s->tEnd && s->stepsTaken < s->maxSteps ? 1 : 0;
 }
 
 // advance(), ExplicitSolver.java:1069-1075: displacement from the current velocity, no
@@ -716,7 +740,7 @@ static int assemble(Solver &S, int zeroStrain, bool prepared = false, bool erode
 
 int launch_initial_assembly(Solver &S) {
     Dev &d = S.d;
-    k_begin<<<1, 1, 0, S.stream>>>(d, 1);
+    k_begin<<<1, 1, 0, S.stream>>>(d);
     int n = 1 + assemble(S, 1);
     k_end<<<1, 1024, 0, S.stream>>>(d, nodal_grid(S), element_grid(S), d.coopBlocks, 0);
     return n + 1;
@@ -727,8 +751,6 @@ int launch_step(Solver &S, bool) {
     const cudaStream_t st = S.stream;
     int n = 0;
     S.mark(NF_GROUP_NODAL, true);
-    k_begin<<<1, 1, 0, st>>>(d, 0);
-    n++;
     if (d.N > 0) {
         k_nodal<<<nodal_grid(S), BLOCK, 0, st>>>(d);    // in the mixed form it also prepares
         n++;

@@ -50,7 +50,8 @@ struct DevScalars {
     int pad0;
     // rigid wall (RigidWall.java:103-107)
     double wImpulse, wEnergyLoss, wFriction;
-    int wContact, wStuck;
+    int wContact, wStuck;                    // the last step's counts
+    int wContactAcc, wStuckAcc;              // this step's counts as the nodal update adds them
     // erosion (ExplicitSolver.java:228-234)
     int erodedCount, invertedCount;
     double erodedEnergy;
