@@ -561,8 +561,9 @@ nf_status nf_destroy(nf_solver *h) {
                     d.pairEnergy, d.pairDiss, d.incCount, d.incStart, d.incCursor, d.incEntry,
                     d.scanTmp, d.s, d.matsF, d.sigF, d.backF, d.epsPF, d.wPF, d.hgKF,
                     d.contribF, d.hgF, d.dStrF, d.dSoftF, d.dWidthF, d.dFailF, d.dGfF, d.dGeomF,
-                    d.pMid, d.pCur, d.vdt, d.gaussVol, d.coopSums, d.incSlots, d.bucketF, d.bucketFL, d.fastCount, d.fastEntry,
-                    d.fastF, d.fastFL, d.nodeCell,
+                    d.pMid, d.pCur, d.vdt, d.gaussVol, d.coopSums, d.incSlots, d.bucketF, d.bucketFL, d.bucketAB, d.bucketA, d.bucketN, d.bucketL,
+                    d.fastCount, d.fastEntry, d.fastF, d.fastFL, d.fastAB, d.fastA, d.fastN,
+                    d.fastL, d.nodeCell,
                     d.hot, d.hotList, d.hotNext, d.hotStamp, d.jcYield};
     const char *a0 = static_cast<const char *>(S->arena), *a1 = a0 + S->arenaBytes;
     for (void *p : ptrs) {
@@ -741,6 +742,7 @@ nf_status nf_set_contact(nf_solver *h, double friction, double damping, double s
         A(d.bucketCount, d.bucketCap + 1); A(d.bucketStart, d.bucketCap + 1);
         A(d.bucketCursor, d.bucketCap + 1);
         A(d.bucketEntry, 8LL * E); A(d.bucketF, 8LL * E); A(d.bucketFL, 8LL * E);
+        A(d.bucketAB, 8LL * E); A(d.bucketA, 8LL * E); A(d.bucketN, 8LL * E); A(d.bucketL, 8LL * E);
         A(d.bucketCell, 8LL * E); A(d.entryCell, 8LL * E);
         d.fastCells = std::min(d.bucketCap + 1, 1 << 16);
         d.fastCap = NF_GRID_SLOTS;
@@ -748,6 +750,9 @@ nf_status nf_set_contact(nf_solver *h, double friction, double damping, double s
         A(d.fastCount, d.fastCells);
         A(d.fastEntry, (size_t)d.fastCells * d.fastCap);
         A(d.fastF, (size_t)d.fastCells * d.fastCap); A(d.fastFL, (size_t)d.fastCells * d.fastCap);
+        A(d.fastAB, (size_t)d.fastCells * d.fastCap);
+        A(d.fastA, (size_t)d.fastCells * d.fastCap); A(d.fastN, (size_t)d.fastCells * d.fastCap);
+        A(d.fastL, (size_t)d.fastCells * d.fastCap);
         A(d.nodeCell, N);
         A(d.pairNodes, N); A(d.pairVal, 12LL * N); A(d.pairEnergy, N); A(d.pairDiss, N);
         A(d.incCount, N + 1); A(d.incStart, N + 1); A(d.incCursor, N + 1); A(d.incEntry, 3LL * N);

@@ -289,21 +289,6 @@ __device__ __forceinline__ int bucket_of(const Dev &d, const Grid &g, long long 
     return g.hashed ? (int)(cell % d.bucketCap) : (int)cell;
 }
 
-// Contact.excluded, Contact.java:620-639, for slave node n and segment q: facing, an end of
-// its own, or sharing a node with one of the slave's own segments.
-__device__ __forceinline__ bool excluded(const Dev &d, int n, int q) {
-    const int a = d.segA[q], b = d.segB[q];
-    if (d.pnr[n] * d.snr[q] + d.pnz[n] * d.snz[q] > -FACING) return true;
-    if (a == n || b == n) return true;
-    const int32_t *own = d.nodeSeg + (size_t)n * d.segCap;
-    const int count = d.nodeFree[n];
-    for (int k = 0; k < count; k++) {
-        const int p = d.segA[own[k]], r = d.segB[own[k]];
-        if (p == a || p == b || r == a || r == b) return true;
-    }
-    return false;
-}
-
 // Contact.depth, Contact.java:642-652
 // The segment's unit tangent (cr[b] - cr[a]) / len, (cz[b] - cz[a]) / len is (-snz, snr) bit
 // for bit: the geometry phase formed snr = dz / len and snz = -dr / len from the same sums
@@ -433,6 +418,9 @@ struct BucketView {
     const int32_t *entry;
     const float4 *f;                           // first node - grid origin, normal (FP32)
     const float *fl;                           // length (FP32)
+    const int2 *ab;                            // the segment's ends
+    const double2 *a, *n;                      // its first node and normal
+    const double *l;                           // its length
     int cap;                                   // 0: the counting-sort layout
 };
 __device__ __forceinline__ void bucket_range(const BucketView &v, int b, int &lo, int &len) {
@@ -447,22 +435,39 @@ __device__ __forceinline__ void bucket_range(const BucketView &v, int b, int &lo
 
 constexpr int SG = 8;                          // lanes per slave
 constexpr int KEPT = 4;                        // screened candidates a lane keeps for later
+constexpr int OWN_KEPT = 4;                    // a slave's own segments held in registers
 __device__ void search_group(const Dev &d, const Grid &g, const BucketView &v, int idx,
                              int listLen, double &bestOut, int &segOut, bool &fellOut) {
     const int lane = threadIdx.x & 31, gl = lane & (SG - 1);
     int n = idx < listLen ? d.nodeList[idx] : -1;
     const bool live = n >= 0;
-    double2 xn = make_double2(0.0, 0.0);
+    double2 xn = make_double2(0.0, 0.0), pn = make_double2(0.0, 0.0);
     float xs = 0.0f, ys = 0.0f;
     int last = -1, ci = 0, cj = 0;
+    // the slave's own ring (Contact.excluded's second half): its free edges' ends, the first
+    // OWN_KEPT in registers
+    int ownCount = 0, ownP[OWN_KEPT], ownR[OWN_KEPT];
+#pragma unroll
+    for (int k = 0; k < OWN_KEPT; k++) ownP[k] = ownR[k] = -1;
     if (live) {
         xn = make_double2(d.cr[n], d.cz[n]);
+        pn = make_double2(d.pnr[n], d.pnz[n]);
         last = d.lastMaster[n];
         const int2 cell = d.nodeCell[n];
         ci = cell.x;
         cj = cell.y;
         xs = (float)(xn.x - g.r0);
         ys = (float)(xn.y - g.z0);
+        ownCount = d.nodeFree[n];
+        const int32_t *own = d.nodeSeg + (size_t)n * d.segCap;
+#pragma unroll
+        for (int k = 0; k < OWN_KEPT; k++) {
+            if (k < ownCount) {
+                const int q = own[k];
+                ownP[k] = d.segA[q];
+                ownR[k] = d.segB[q];
+            }
+        }
     }
     // the nine cells in visit order: lane gl takes cell gl, lane 0 also cell 8
     int lo = 0, len = 0, lo8 = 0, len8 = 0;
@@ -528,7 +533,8 @@ __device__ void search_group(const Dev &d, const Grid &g, const BucketView &v, i
     int bestSeg = -1;
     bool fell = false;
     // the exact test of position t (Contact.depth, Contact.java:642-652, and the exclusions):
-    // the segment's first node, normal and length as the geometry phase left them
+    // the segment's ends, first node, normal and length as the filing staged them beside the
+    // entry (the values the geometry phase left)
     auto exact = [&](int t) {
         int c, k;
         long long cc;
@@ -536,19 +542,34 @@ __device__ void search_group(const Dev &d, const Grid &g, const BucketView &v, i
         if (v.cell && v.cell[k] != cc) return;          // a hashed bucket shares cells
         const int entry = v.entry[k];
         const int sg = entry >> 1;
-        const int a = d.segA[sg];
-        const double dr = xn.x - d.cr[a], dz = xn.y - d.cz[a];
-        const double nr = d.snr[sg], nz = d.snz[sg];
-        const double gap = dr * nr + dz * nz;
+        const double2 pa = v.a[k], nq = v.n[k];
+        const double dr = xn.x - pa.x, dz = xn.y - pa.y;
+        const double gap = dr * nq.x + dz * nq.y;
         if (!(gap < 0.0)) return;
-        const double slen = d.slen[sg];
+        const double slen = v.l[k];
         if (slen <= 0.0) return;
-        const double along = dr * -nz + dz * nr;
+        const double along = dr * -nq.y + dz * nq.x;
         if (along < 0.0 || along > slen) return;
         const double depth = -gap;
-        // the exclusions read the slave's own rings (dependent loads); a candidate that fails
-        // them is skipped whatever its depth, so testing them after the depth changes nothing
-        if (excluded(d, n, sg)) return;
+        // Contact.excluded (Contact.java:620-639): facing, an end of its own, or sharing a node
+        // with one of the slave's own segments; a candidate that fails it is skipped whatever
+        // its depth, so testing it after the depth changes nothing
+        if (pn.x * nq.x + pn.y * nq.y > -FACING) return;
+        const int2 ab = v.ab[k];
+        if (ab.x == n || ab.y == n) return;
+        bool ring = false;
+#pragma unroll
+        for (int j = 0; j < OWN_KEPT; j++)
+            ring = ring || (j < ownCount && (ownP[j] == ab.x || ownP[j] == ab.y ||
+                                             ownR[j] == ab.x || ownR[j] == ab.y));
+        if (!ring && ownCount > OWN_KEPT) {
+            const int32_t *own = d.nodeSeg + (size_t)n * d.segCap;
+            for (int j = OWN_KEPT; j < ownCount && !ring; j++) {
+                const int p = d.segA[own[j]], r = d.segB[own[j]];
+                ring = p == ab.x || p == ab.y || r == ab.x || r == ab.y;
+            }
+        }
+        if (ring) return;
         if (depth > MAX_DEPTH * slen) {
             if (sg == last) fell = true;
             return;
@@ -899,10 +920,17 @@ __global__ void __launch_bounds__(CB, 2) k_contact_pass(Dev d) {
                 const int pos = atomicAdd(&d.fastCount[cell], 1);
                 if (pos < d.fastLimit) {
                     const size_t slot = (size_t)cell * d.fastCap + pos;
+                    const double2 pa = make_double2(d.cr[a], d.cz[a]);
+                    const double2 nq = make_double2(d.snr[q], d.snz[q]);
+                    const double lq = d.slen[q];
                     d.fastEntry[slot] = entry;
-                    d.fastF[slot] = make_float4((float)(d.cr[a] - g.r0), (float)(d.cz[a] - g.z0),
-                                                (float)d.snr[q], (float)d.snz[q]);
-                    d.fastFL[slot] = (float)d.slen[q];
+                    d.fastF[slot] = make_float4((float)(pa.x - g.r0), (float)(pa.y - g.z0),
+                                                (float)nq.x, (float)nq.y);
+                    d.fastFL[slot] = (float)lq;
+                    d.fastAB[slot] = make_int2(a, d.segB[q]);
+                    d.fastA[slot] = pa;
+                    d.fastN[slot] = nq;
+                    d.fastL[slot] = lq;
                 } else {
                     s->fastOverflow = 1;
                 }
@@ -924,20 +952,28 @@ __global__ void __launch_bounds__(CB, 2) k_contact_pass(Dev d) {
             const long long cell = d.entryCell[entry];
             const int a = d.segA[q];
             const int pos = atomicAdd(&d.bucketCursor[bucket_of(d, g, cell)], 1);
+            const double2 pa = make_double2(d.cr[a], d.cz[a]);
+            const double2 nq = make_double2(d.snr[q], d.snz[q]);
+            const double lq = d.slen[q];
             d.bucketEntry[pos] = entry;
             d.bucketCell[pos] = cell;
-            d.bucketF[pos] = make_float4((float)(d.cr[a] - g.r0), (float)(d.cz[a] - g.z0),
-                                         (float)d.snr[q], (float)d.snz[q]);
-            d.bucketFL[pos] = (float)d.slen[q];
+            d.bucketF[pos] = make_float4((float)(pa.x - g.r0), (float)(pa.y - g.z0),
+                                         (float)nq.x, (float)nq.y);
+            d.bucketFL[pos] = (float)lq;
+            d.bucketAB[pos] = make_int2(a, d.segB[q]);
+            d.bucketA[pos] = pa;
+            d.bucketN[pos] = nq;
+            d.bucketL[pos] = lq;
         }
         SYNC();
     }
     BucketView view;
     if (direct) {
-        view = BucketView{nullptr, d.fastCount, nullptr, d.fastEntry, d.fastF, d.fastFL, d.fastCap};
+        view = BucketView{nullptr, d.fastCount, nullptr, d.fastEntry, d.fastF, d.fastFL,
+                          d.fastAB, d.fastA, d.fastN, d.fastL, d.fastCap};
     } else {
         view = BucketView{d.bucketStart, nullptr, d.bucketCell, d.bucketEntry, d.bucketF,
-                          d.bucketFL, 0};
+                          d.bucketFL, d.bucketAB, d.bucketA, d.bucketN, d.bucketL, 0};
     }
 
     // the search and the pair forces: each warp searches 32 / SG slaves at a time, SG lanes

@@ -8,6 +8,7 @@
 //   k_element_full     2x2 Gauss quadrature                                         :1219-1339
 //   k_pressure         follower pressure on the bore edges                          :1511-1556
 //   k_gather           per-node sum of its sources in CSR order, plus m g           :1147-1165
+//                      (its first blocks sort the next step's work list)
 //   (contact kernels, k_contact.cu)                                                :1099-1109
 //   k_end              running totals, adaptive CFL step, the next step's run      :985-990
 //                      predicate
@@ -325,19 +326,19 @@ int listed_pass_smem(int device) {
 }
 
 constexpr int HOT_BATCH = 8;
-constexpr int HOT_BUILD_THREADS = 256;
 
-// Blocks of k_hot_build: HOT_BATCH entries per thread of the longest list, at most two per SM.
+// Blocks that build the work list: HOT_BATCH entries per thread of the longest list, at most
+// two per SM.
 static int hot_build_blocks(const Dev &d) {
-    const int per = HOT_BUILD_THREADS * HOT_BATCH;
+    const int per = BLOCK * HOT_BATCH;
     const int want = (d.hotCap + per - 1) / per;
     return want < 1 ? 1 : want > 2 * d.sms ? 2 * d.sms : want;
 }
 
 // The next step's work list from the entries the pass appended: a counting sort by cost class,
-// most expensive first; listed elements are stamped with the new epoch.
-__global__ void __launch_bounds__(HOT_BUILD_THREADS) k_hot_build(Dev d) {
-    if (!d.s->active) return;
+// most expensive first; listed elements are stamped with the new epoch. Run by `blocks` blocks
+// of the launch, this one being `block` of them.
+__device__ void hot_build(const Dev &d, int block, int blocks) {
     __shared__ int start[HOT_CLASSES];
     __shared__ int last;
     HotList *h = d.hot;
@@ -355,8 +356,8 @@ __global__ void __launch_bounds__(HOT_BUILD_THREADS) k_hot_build(Dev d) {
     // positions in that class with one atomic on its global fill count (few classes, many
     // entries); each thread loads HOT_BATCH entries before using them, so their loads overlap
     const int lane = threadIdx.x & 31;
-    const int stride = gridDim.x * blockDim.x, span = HOT_BATCH * stride;
-    for (int base = blockIdx.x * blockDim.x + threadIdx.x - lane; base < n; base += span) {
+    const int stride = blocks * blockDim.x, span = HOT_BATCH * stride;
+    for (int base = block * blockDim.x + threadIdx.x - lane; base < n; base += span) {
         int2 it[HOT_BATCH];
 #pragma unroll
         for (int k = 0; k < HOT_BATCH; k++) {
@@ -381,7 +382,7 @@ __global__ void __launch_bounds__(HOT_BUILD_THREADS) k_hot_build(Dev d) {
     // the last block to finish clears the counts for the pass that appends next
     __threadfence();
     __syncthreads();
-    if (threadIdx.x == 0) last = atomicAdd(&h->done, 1) == (int)gridDim.x - 1;
+    if (threadIdx.x == 0) last = atomicAdd(&h->done, 1) == blocks - 1;
     __syncthreads();
     if (!last) return;
     __threadfence();
@@ -555,10 +556,16 @@ __global__ void k_pressure(Dev d) {
 
 // ------------------------------------------------------------------------------------ gather
 
-// gather, ExplicitSolver.java:1147-1165: ascending source order, then gravity.
-__global__ void __launch_bounds__(BLOCK) k_gather(Dev d) {
+// gather, ExplicitSolver.java:1147-1165: ascending source order, then gravity. With a work
+// list, the launch's first listBlocks blocks build the next step's list instead (the two read
+// and write disjoint data, and one launch saves a kernel boundary per step).
+__global__ void __launch_bounds__(BLOCK) k_gather(Dev d, int listBlocks) {
     if (!d.s->active) return;
-    const int n = blockIdx.x * blockDim.x + threadIdx.x;
+    if ((int)blockIdx.x < listBlocks) {
+        hot_build(d, blockIdx.x, listBlocks);
+        return;
+    }
+    const int n = (blockIdx.x - listBlocks) * blockDim.x + threadIdx.x;
     if (n >= d.N) return;
     d.F[n] = gather_node(d, n);
     if (d.hasContact) d.contactState[n] = 0;
@@ -704,8 +711,7 @@ static int assemble(Solver &S, int zeroStrain, bool prepared = false, bool erode
         } else if (d.hot) {
             k_element_reduced_listed<<<grid_for((long long)d.E + d.hotCap, BLOCK), BLOCK,
                                        d.hotSmem, st>>>(d, zeroStrain, erode ? 1 : 0);
-            k_hot_build<<<hot_build_blocks(d), HOT_BUILD_THREADS, 0, st>>>(d);
-            n += 2;
+            n++;
         } else {
             k_element_reduced<<<grid_for(d.E, BLOCK), BLOCK, 0, st>>>(d, zeroStrain);
             n++;
@@ -722,10 +728,15 @@ static int assemble(Solver &S, int zeroStrain, bool prepared = false, bool erode
         S.mark(NF_GROUP_PRESSURE, false);
     }
     S.mark(NF_GROUP_GATHER, true);
-    if (d.N > 0) {
-        if (d.mixed) n += launch_gather_mixed(S);
-        else {
-            k_gather<<<grid_for(d.N, BLOCK), BLOCK, 0, st>>>(d);
+    // the listed element pass's work list is built by the gather's launch (or alone)
+    const int listBlocks = !d.mixed && d.E > 0 && !d.full && d.hot ? hot_build_blocks(d) : 0;
+    if (d.N > 0 && !d.mixed) {
+        k_gather<<<listBlocks + grid_for(d.N, BLOCK), BLOCK, 0, st>>>(d, listBlocks);
+        n++;
+    } else {
+        if (d.N > 0) n += launch_gather_mixed(S);
+        if (listBlocks) {
+            k_gather<<<listBlocks, BLOCK, 0, st>>>(d, listBlocks);
             n++;
         }
     }

@@ -96,8 +96,8 @@ struct HotList {
     int epoch;                               // stamp of this step's listed elements
     int pad;
     int classCount[HOT_CLASSES];             // the appended (and kept) entries per cost class
-    int fill[HOT_CLASSES];                   // entries placed so far per class (k_hot_build)
-    int done;                                // blocks of k_hot_build that have finished
+    int fill[HOT_CLASSES];                   // entries placed so far per class (hot_build)
+    int done;                                // blocks of hot_build that have finished
 };
 
 struct Dev {
@@ -160,9 +160,13 @@ struct Dev {
     int32_t *bucketCount, *bucketStart, *bucketCursor;   // [bucketCap + 1]
     int32_t *bucketEntry;                    // [8E] entries (2 q + end)
     // [8E] by position, for the search's FP32 screen: the segment's first node relative to the
-    // grid origin and its normal (float4), and its length (float)
+    // grid origin and its normal (float4), and its length (float); for the exact test: the
+    // segment's ends (int2), first node and normal (double2) and length
     float4 *bucketF;
     float *bucketFL;
+    int2 *bucketAB;
+    double2 *bucketA, *bucketN;
+    double *bucketL;
     long long *bucketCell;                   // [8E] cell of each filed entry, by position
     long long *entryCell;                    // [8E] cell of each entry, by entry
     // the direct-indexed grid: cell c's entries in slots [c fastCap, c fastCap + fastCount[c])
@@ -171,6 +175,9 @@ struct Dev {
     int32_t *fastEntry;                      // [fastCells x fastCap]
     float4 *fastF;                           // [fastCells x fastCap] as bucketF
     float *fastFL;                           // [fastCells x fastCap] as bucketFL
+    int2 *fastAB;                            // [fastCells x fastCap] as bucketAB
+    double2 *fastA, *fastN;                  // [fastCells x fastCap] as bucketA, bucketN
+    double *fastL;                           // [fastCells x fastCap] as bucketL
     int fastCells, fastCap;                  // cells indexed directly, slots per cell
     int fastLimit;                           // slots a step may use, <= fastCap (nf_set_grid_slots)
     int bucketCap;
