@@ -40,6 +40,7 @@
 // all the same: a block that waits longer than a second sets STATUS_TIMEOUT and an abort word
 // that releases the others, and the kernel returns.
 #include "nf_internal.h"
+#include "nf_surface.cuh"
 
 namespace nf {
 
@@ -636,31 +637,6 @@ __device__ void finish_slave(const Dev &d, int n, double best, int bestSeg, bool
     resolve_pair(d, n, bestSeg);
 }
 
-// Node n's free edges in ascending q, from the corners of its elements (the node slots of the
-// force gather): at corner c of element e the edges 4 e + c (leaving it) and 4 e + (c + 3) % 4
-// (arriving at it).
-__device__ void build_node_segs(const Dev &d, int n) {
-    int32_t *out = d.nodeSeg + (size_t)n * d.segCap;
-    int count = 0;
-    for (int k = d.nodeSlotStart[n]; k < d.nodeSlotStart[n + 1]; k++) {
-        const int v = d.nodeSlot[k];
-        if (v >= 8 * d.E) continue;                  // a pressure edge's slot
-        const int e = v >> 3, c = v & 7;
-        const int q1 = 4 * e + c, q0 = 4 * e + ((c + 3) & 3);
-        if (d.surfFlag[q1] && count < d.segCap) out[count++] = q1;
-        if (d.surfFlag[q0] && count < d.segCap) out[count++] = q0;
-    }
-    for (int i = 1; i < count; i++) {
-        const int v = out[i];
-        int j = i - 1;
-        while (j >= 0 && out[j] > v) {
-            out[j + 1] = out[j];
-            j--;
-        }
-        out[j + 1] = v;
-    }
-}
-
 // ---------------------------------------------------------------------------- the pass
 
 // Items are dealt to warps across the blocks first (warp w of block b takes the 32 items from
@@ -679,6 +655,8 @@ __global__ void __launch_bounds__(CB, 2) k_contact_pass(Dev d) {
     if (!vload(&s->active)) return;
     const int gt = blockIdx.x * CB + threadIdx.x;
     const bool rebuilt = vload(&s->stale) != 0;
+    // the surface changed this step, here or in the gather's launch (surface_rebuild_block)
+    const bool changed = rebuilt || vload(&s->rebuiltNow) != 0;
 
     if (rebuilt) {
         // Contact.adopt, Contact.java:290-322: the free surface, QuadMesh.surface over the
@@ -737,55 +715,11 @@ __global__ void __launch_bounds__(CB, 2) k_contact_pass(Dev d) {
             // free to the list and strike out those that stopped being free, keep each node's
             // count of free edges, and note the nodes touched
             const int nDead = vload(&s->newDeadCount);
-            FOR_GRID(t, 4 * nDead) {
-                const int g = d.edgeGroup[4 * d.newDead[t >> 2] + (t & 3)];
-                const int g0 = d.groupStart[g], g1 = d.groupStart[g + 1];
-                int live = 0;
-                for (int m = g0; m < g1; m++)
-                    if (!d.dead[d.groupMember[m] >> 2]) live++;
-                for (int m = g0; m < g1; m++) {
-                    const int q = d.groupMember[m];
-                    if (atomicExch(&d.edgeStamp[q], epoch) == epoch) continue;
-                    const int now = !d.dead[q >> 2] && live == 1;
-                    if (now == d.surfFlag[q]) continue;
-                    d.surfFlag[q] = now;
-                    if (now) {
-                        const int pos = atomicAdd(&s->edgeListLen, 1);
-                        d.edgeList[pos] = q;
-                        d.edgePos[q] = pos;
-                    } else {
-                        d.edgeList[d.edgePos[q]] = -1;
-                        d.edgePos[q] = -1;
-                    }
-                    atomicAdd(&s->surfEdges, now ? 1 : -1);
-                    const int ends[2] = {d.segA[q], d.segB[q]};
-                    for (int k = 0; k < 2; k++) {
-                        atomicAdd(&d.nodeFree[ends[k]], now ? 1 : -1);
-                        if (atomicExch(&d.nodeStamp[ends[k]], epoch) != epoch)
-                            d.touched[atomicAdd(&s->nTouched, 1)] = ends[k];
-                    }
-                }
-            }
+            FOR_GRID(t, 4 * nDead) surface_reflag(d, t, epoch);
             SYNC();
             // the touched nodes: join or leave the surface, and list their free edges again
             const int nTouched = vload(&s->nTouched);
-            FOR_GRID(i, nTouched) {
-                const int n = d.touched[i];
-                const bool was = d.nodePos[n] >= 0, is = d.nodeFree[n] > 0;
-                if (is && !was) {
-                    const int pos = atomicAdd(&s->nodeListLen, 1);
-                    d.nodeList[pos] = n;
-                    d.nodePos[n] = pos;
-                    atomicAdd(&s->surfNodes, 1);
-                } else if (was && !is) {
-                    d.nodeList[d.nodePos[n]] = -1;
-                    d.nodePos[n] = -1;
-                    atomicAdd(&s->surfNodes, -1);
-                    d.pairNodes[n] = make_int4(-1, -1, -1, 0);
-                    d.incCount[n] = 0;
-                }
-                if (is) build_node_segs(d, n);
-            }
+            FOR_GRID(i, nTouched) surface_touched(d, i);
         }
         if (gt == 0) {
             s->stale = 0;
@@ -819,7 +753,7 @@ __global__ void __launch_bounds__(CB, 2) k_contact_pass(Dev d) {
             d.cz[n] = cz;
             d.incCount[n] = 0;
             d.pairNodes[n] = make_int4(-1, -1, -1, 0);
-            if (rebuilt) {
+            if (changed) {
                 d.lastMaster[n] = -1;
                 d.master[n] = -1;
                 d.dropped[n] = 0;
@@ -866,6 +800,7 @@ __global__ void __launch_bounds__(CB, 2) k_contact_pass(Dev d) {
         }
     }
     SYNC();
+    if (gt == 0) s->rebuiltNow = 0;             // every block has read it
 
     // the grid, in every block; node normals; the counting sort's counts (:530-545).
     // bucketCount is all zero on entry and is left all zero.

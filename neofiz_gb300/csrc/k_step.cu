@@ -17,6 +17,7 @@
 // Every kernel reads the solver's scalars (dt, time, ...) from device memory, so a sequence
 // of steps is a fixed sequence of launches with no host decision between them.
 #include "nf_bodies.cuh"
+#include "nf_surface.cuh"
 
 namespace nf {
 
@@ -557,15 +558,24 @@ __global__ void k_pressure(Dev d) {
 // ------------------------------------------------------------------------------------ gather
 
 // gather, ExplicitSolver.java:1147-1165: ascending source order, then gravity. With a work
-// list, the launch's first listBlocks blocks build the next step's list instead (the two read
-// and write disjoint data, and one launch saves a kernel boundary per step).
-__global__ void __launch_bounds__(BLOCK) k_gather(Dev d, int listBlocks) {
-    if (!d.s->active) return;
+// list, the launch's first listBlocks blocks build the next step's list instead, and with
+// contact the next block rebuilds the surface after this step's erosion when few elements
+// eroded (the three read and write disjoint data; the contact pass, next on the stream, reads
+// the surface). One launch saves kernel boundaries, and the rebuild runs beside the gather
+// instead of as two barrier-separated phases of the contact pass.
+__global__ void __launch_bounds__(BLOCK) k_gather(Dev d, int listBlocks, int surfaceBlock) {
+    DevScalars *s = d.s;
+    if (!s->active) return;
     if ((int)blockIdx.x < listBlocks) {
         hot_build(d, blockIdx.x, listBlocks);
         return;
     }
-    const int n = (blockIdx.x - listBlocks) * blockDim.x + threadIdx.x;
+    if (surfaceBlock && (int)blockIdx.x == listBlocks) {
+        if (s->stale && !s->fullRebuild && s->newDeadCount <= SURFACE_BLOCK_DEAD)
+            surface_rebuild_block(d);
+        return;
+    }
+    const int n = (blockIdx.x - listBlocks - surfaceBlock) * blockDim.x + threadIdx.x;
     if (n >= d.N) return;
     d.F[n] = gather_node(d, n);
     if (d.hasContact) d.contactState[n] = 0;
@@ -731,12 +741,14 @@ static int assemble(Solver &S, int zeroStrain, bool prepared = false, bool erode
     // the listed element pass's work list is built by the gather's launch (or alone)
     const int listBlocks = !d.mixed && d.E > 0 && !d.full && d.hot ? hot_build_blocks(d) : 0;
     if (d.N > 0 && !d.mixed) {
-        k_gather<<<listBlocks + grid_for(d.N, BLOCK), BLOCK, 0, st>>>(d, listBlocks);
+        const int surfaceBlock = d.hasContact ? 1 : 0;
+        k_gather<<<listBlocks + surfaceBlock + grid_for(d.N, BLOCK), BLOCK, 0, st>>>(
+            d, listBlocks, surfaceBlock);
         n++;
     } else {
         if (d.N > 0) n += launch_gather_mixed(S);
         if (listBlocks) {
-            k_gather<<<listBlocks, BLOCK, 0, st>>>(d, listBlocks);
+            k_gather<<<listBlocks, BLOCK, 0, st>>>(d, listBlocks, 0);
             n++;
         }
     }

@@ -72,6 +72,7 @@ struct DevScalars {
     uint32_t barCount, barGen, barAbort;     // grid barrier of the cooperative contact pass
     int incOverflow;                         // a node's incident terms outgrew its fixed list
     int fastOverflow;                        // a cell of the direct-indexed grid overflowed
+    int rebuiltNow;                          // the gather's launch rebuilt the surface this step
     // the free-surface rebuild (Contact.adopt): a full rebuild at set-up, an incremental one
     // after erosion (elements eroded since the last rebuild, changes this rebuild)
     int fullRebuild, newDeadCount, rebuildEpoch, nTouched;

@@ -1,0 +1,119 @@
+// nf_surface.cuh -- the contact surface's incremental rebuild after erosion (Contact.adopt,
+// Contact.java:290-332, over QuadMesh.surface, QuadMesh.java:188-226), shared by the contact
+// pass (many blocks, separated by a grid barrier) and by one block of the gather's launch (the
+// usual few eroded elements a step).
+//
+// The surface is kept as unordered lists keyed by element edge q = 4 e + corner and node
+// number: an element edge is free when it is the only live member of its group of equal edges.
+#pragma once
+
+#include "nf_internal.h"
+
+namespace nf {
+
+template <typename T>
+__device__ __forceinline__ T vload_s(const T *p) { return *(const volatile T *)p; }
+
+// Node n's free edges in ascending q, from the corners of its elements (the node slots of the
+// force gather): at corner c of element e the edges 4 e + c (leaving it) and 4 e + (c + 3) % 4
+// (arriving at it).
+static __device__ void build_node_segs(const Dev &d, int n) {
+    int32_t *out = d.nodeSeg + (size_t)n * d.segCap;
+    int count = 0;
+    for (int k = d.nodeSlotStart[n]; k < d.nodeSlotStart[n + 1]; k++) {
+        const int v = d.nodeSlot[k];
+        if (v >= 8 * d.E) continue;                  // a pressure edge's slot
+        const int e = v >> 3, c = v & 7;
+        const int q1 = 4 * e + c, q0 = 4 * e + ((c + 3) & 3);
+        if (d.surfFlag[q1] && count < d.segCap) out[count++] = q1;
+        if (d.surfFlag[q0] && count < d.segCap) out[count++] = q0;
+    }
+    for (int i = 1; i < count; i++) {
+        const int v = out[i];
+        int j = i - 1;
+        while (j >= 0 && out[j] > v) {
+            out[j + 1] = out[j];
+            j--;
+        }
+        out[j + 1] = v;
+    }
+}
+
+// Item t of the re-flagging: edge t & 3 of the element newDead[t >> 2]. Its group's members are
+// re-flagged (each once a rebuild: the epoch stamp); an edge that became free is appended to the
+// edge list and one that stopped being free is struck out; each node keeps its count of free
+// edges, and the nodes touched are noted.
+__device__ __forceinline__ void surface_reflag(const Dev &d, int t, int epoch) {
+    DevScalars *s = d.s;
+    const int g = d.edgeGroup[4 * d.newDead[t >> 2] + (t & 3)];
+    const int g0 = d.groupStart[g], g1 = d.groupStart[g + 1];
+    int live = 0;
+    for (int m = g0; m < g1; m++)
+        if (!d.dead[d.groupMember[m] >> 2]) live++;
+    for (int m = g0; m < g1; m++) {
+        const int q = d.groupMember[m];
+        if (atomicExch(&d.edgeStamp[q], epoch) == epoch) continue;
+        const int now = !d.dead[q >> 2] && live == 1;
+        if (now == d.surfFlag[q]) continue;
+        d.surfFlag[q] = now;
+        if (now) {
+            const int pos = atomicAdd(&s->edgeListLen, 1);
+            d.edgeList[pos] = q;
+            d.edgePos[q] = pos;
+        } else {
+            d.edgeList[d.edgePos[q]] = -1;
+            d.edgePos[q] = -1;
+        }
+        atomicAdd(&s->surfEdges, now ? 1 : -1);
+        const int ends[2] = {d.segA[q], d.segB[q]};
+        for (int k = 0; k < 2; k++) {
+            atomicAdd(&d.nodeFree[ends[k]], now ? 1 : -1);
+            if (atomicExch(&d.nodeStamp[ends[k]], epoch) != epoch)
+                d.touched[atomicAdd(&s->nTouched, 1)] = ends[k];
+        }
+    }
+}
+
+// Item i of the touched nodes: join or leave the surface, and list the node's free edges again.
+__device__ __forceinline__ void surface_touched(const Dev &d, int i) {
+    DevScalars *s = d.s;
+    const int n = d.touched[i];
+    const bool was = d.nodePos[n] >= 0, is = d.nodeFree[n] > 0;
+    if (is && !was) {
+        const int pos = atomicAdd(&s->nodeListLen, 1);
+        d.nodeList[pos] = n;
+        d.nodePos[n] = pos;
+        atomicAdd(&s->surfNodes, 1);
+    } else if (was && !is) {
+        d.nodeList[d.nodePos[n]] = -1;
+        d.nodePos[n] = -1;
+        atomicAdd(&s->surfNodes, -1);
+        d.pairNodes[n] = make_int4(-1, -1, -1, 0);
+        d.incCount[n] = 0;
+    }
+    if (is) build_node_segs(d, n);
+}
+
+// The incremental rebuild in one block: the re-flagging, a block barrier, the touched nodes.
+// Leaves the rebuild's marks as the contact pass's own rebuild does, and rebuiltNow set, so
+// the pass's geometry phase still makes every surface node forget its last master.
+constexpr int SURFACE_BLOCK_DEAD = 256;   // most eroded elements one block rebuilds for
+static __device__ void surface_rebuild_block(const Dev &d) {
+    DevScalars *s = d.s;
+    const int epoch = s->rebuildEpoch + 1;
+    const int nDead = s->newDeadCount;
+    for (int t = threadIdx.x; t < 4 * nDead; t += blockDim.x) surface_reflag(d, t, epoch);
+    __syncthreads();
+    const int nTouched = vload_s(&s->nTouched);
+    for (int i = threadIdx.x; i < nTouched; i += blockDim.x) surface_touched(d, i);
+    __syncthreads();
+    if (threadIdx.x == 0) {
+        s->stale = 0;
+        s->newDeadCount = 0;
+        s->rebuildEpoch = epoch;
+        s->nTouched = 0;
+        s->rebuiltNow = 1;
+    }
+}
+
+}  // namespace nf
