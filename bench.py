@@ -39,10 +39,10 @@ L2_FLUSH_BYTES = 256 << 20
 # DRAM bytes (read + write) of one element-pass launch of this workload in the window, from
 # ncu's dram__bytes_read.sum + dram__bytes_write.sum, the mean over the launches of steps
 # start + 6 and start + 7 (ncu cannot run inside the timed bench)
-ELEMENT_TRAFFIC_BYTES = {CELL: (43_484_160 + 177_408 + 43_474_688 + 37_888) // 2}
+ELEMENT_TRAFFIC_BYTES = {CELL: (43_483_904 + 173_568 + 43_474_176 + 36_864) // 2}
 # FP64-pipe warp instructions of one element-pass launch in the window: the mean of ncu's
 # smsp__inst_executed_pipe_fp64.sum over the same two launches
-ELEMENT_FP64_WARP_INST = {CELL: (3_066_238 + 3_058_495) // 2}
+ELEMENT_FP64_WARP_INST = {CELL: (3_078_533 + 3_061_133) // 2}
 
 
 def parse():

@@ -714,12 +714,14 @@ __global__ void __launch_bounds__(CB, 2) k_contact_pass(Dev d) {
             // re-flag their members (each once: the epoch stamp), append the edges that became
             // free to the list and strike out those that stopped being free, keep each node's
             // count of free edges, and note the nodes touched
+            const SurfaceCounters k{&s->edgeListLen, &s->surfEdges, &s->nTouched,
+                                    &s->nodeListLen, &s->surfNodes};
             const int nDead = vload(&s->newDeadCount);
-            FOR_GRID(t, 4 * nDead) surface_reflag(d, t, epoch);
+            FOR_GRID(t, 4 * nDead) surface_reflag(d, t, epoch, k);
             SYNC();
             // the touched nodes: join or leave the surface, and list their free edges again
             const int nTouched = vload(&s->nTouched);
-            FOR_GRID(i, nTouched) surface_touched(d, i);
+            FOR_GRID(i, nTouched) surface_touched(d, i, k);
         }
         if (gt == 0) {
             s->stale = 0;
