@@ -280,12 +280,6 @@ __device__ void grid_from_box(const Dev &d, int nodes, Grid &g) {
 
 __device__ __forceinline__ int iclamp(int v, int n) { return v < 0 ? 0 : v >= n ? n - 1 : v; }
 
-__device__ __forceinline__ long long cell_of(const Grid &g, double r, double z) {
-    const int i = iclamp(jd2i((r - g.r0) / g.cellSize), g.cols);
-    const int j = iclamp(jd2i((z - g.z0) / g.cellSize), g.rows);
-    return (long long)j * g.cols + i;
-}
-
 __device__ __forceinline__ int bucket_of(const Dev &d, const Grid &g, long long cell) {
     return g.hashed ? (int)(cell % d.bucketCap) : (int)cell;
 }
@@ -844,7 +838,8 @@ __global__ void __launch_bounds__(CB, 2) k_contact_pass(Dev d) {
         const double len = sqrt(sr * sr + sz * sz);
         d.pnr[n] = len > 0.0 ? sr / len : 0.0;
         d.pnz[n] = len > 0.0 ? sz / len : 0.0;
-        const int ci = iclamp(jd2i((d.cr[n] - g.r0) / g.cellSize), g.cols);   // cell_of
+        // Contact.cellOf, Contact.java:553-557
+        const int ci = iclamp(jd2i((d.cr[n] - g.r0) / g.cellSize), g.cols);
         const int cj = iclamp(jd2i((d.cz[n] - g.z0) / g.cellSize), g.rows);
         d.nodeCell[n] = make_int2(ci, cj);
         const long long cell = (long long)cj * g.cols + ci;
