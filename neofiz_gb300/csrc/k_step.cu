@@ -80,6 +80,18 @@ __global__ void __launch_bounds__(BLOCK) k_nodal(Dev d) {
     DevScalars *s = d.s;
     if (!s->active) return;
     const double dt = s->dt;
+    {
+        // the thread's first node is fetched into L1 while the coefficients are formed
+        const int i = blockIdx.x * blockDim.x + threadIdx.x;
+        if (i < d.N) {
+            asm volatile("prefetch.global.L1 [%0];" ::"l"(d.U + i));
+            asm volatile("prefetch.global.L1 [%0];" ::"l"(d.V + i));
+            asm volatile("prefetch.global.L1 [%0];" ::"l"(d.F + i));
+            asm volatile("prefetch.global.L1 [%0];" ::"l"(d.X0 + i));
+            asm volatile("prefetch.global.L1 [%0];" ::"l"(d.mass + i));
+            asm volatile("prefetch.global.L1 [%0];" ::"l"(d.invMass + i));
+        }
+    }
     if (threadIdx.x == 0) {
         const double avg = 0.5 * (s->dtPrevious + dt);
         const double half = 0.5 * d.damping * avg;
@@ -104,9 +116,16 @@ __global__ void __launch_bounds__(BLOCK) k_nodal(Dev d) {
                    &d.s->status, impulse, loss, fric);
     }
     if (d.hasWall) {
-        const double a = block_sum(impulse, sh);
-        const double b = block_sum(loss, sh);
-        const double c = block_sum(fric, sh);
+        // a block whose terms are all +0 (no node on the wall) has sums of +0: one vote
+        // instead of three trees
+        const bool any = (__double_as_longlong(impulse) | __double_as_longlong(loss) |
+                          __double_as_longlong(fric)) != 0;
+        double a = 0.0, b = 0.0, c = 0.0;
+        if (__syncthreads_or(any)) {
+            a = block_sum(impulse, sh);
+            b = block_sum(loss, sh);
+            c = block_sum(fric, sh);
+        }
         if (threadIdx.x == 0) {
             d.partials[(PARTIAL_WALL + 0) * d.maxBlocks + blockIdx.x] = a;
             d.partials[(PARTIAL_WALL + 1) * d.maxBlocks + blockIdx.x] = b;

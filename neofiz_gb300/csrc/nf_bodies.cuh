@@ -735,15 +735,31 @@ static __device__ __forceinline__ float2 gather_node_comp(const Dev &d, int n, f
 }
 
 // gather, ExplicitSolver.java:1147-1165: node n's sources in ascending order, then m g.
+// Four slots at a time: their indices, then their values, are loaded before any is added, so
+// the loads overlap; the sums still take the slots in order.
 static __device__ __forceinline__ double2 gather_node(const Dev &d, int n) {
     double sr = 0.0, sz = 0.0;
     const int end = d.nodeSlotStart[n + 1];
-    for (int k = d.nodeSlotStart[n]; k < end; k++) {
-        const int slot = d.nodeSlot[k];
-        sr += d.contribution[slot];
-        sz += d.contribution[slot + 4];
-    }
     const double m = d.mass[n];
+    for (int k = d.nodeSlotStart[n]; k < end; k += 4) {
+        const int cnt = end - k < 4 ? end - k : 4;
+        int slot[4];
+        double vr[4], vz[4];
+#pragma unroll
+        for (int j = 0; j < 4; j++) slot[j] = j < cnt ? d.nodeSlot[k + j] : 0;
+#pragma unroll
+        for (int j = 0; j < 4; j++) {
+            vr[j] = j < cnt ? d.contribution[slot[j]] : 0.0;
+            vz[j] = j < cnt ? d.contribution[slot[j] + 4] : 0.0;
+        }
+#pragma unroll
+        for (int j = 0; j < 4; j++) {
+            if (j < cnt) {
+                sr += vr[j];
+                sz += vz[j];
+            }
+        }
+    }
     return make_double2(sr + m * d.gravR, sz + m * d.gravZ);
 }
 
