@@ -843,31 +843,42 @@ __global__ void __launch_bounds__(CB, 2) k_contact_pass(Dev d) {
         const int cj = iclamp(jd2i((d.cz[n] - g.z0) / g.cellSize), g.rows);
         d.nodeCell[n] = make_int2(ci, cj);
         const long long cell = (long long)cj * g.cols + ci;
-        for (int k = 0; k < count; k++) {
-            const int q = own[k];
-            const int a = d.segA[q];
-            const int entry = 2 * q + (a == n ? 0 : 1);
-            d.entryCell[entry] = cell;
-            if (fast) {
-                const int pos = atomicAdd(&d.fastCount[cell], 1);
-                if (pos < d.fastLimit) {
-                    const size_t slot = (size_t)cell * d.fastCap + pos;
-                    const double2 pa = make_double2(d.cr[a], d.cz[a]);
-                    const double2 nq = make_double2(d.snr[q], d.snz[q]);
-                    const double lq = d.slen[q];
-                    d.fastEntry[slot] = entry;
-                    d.fastF[slot] = make_float4((float)(pa.x - g.r0), (float)(pa.y - g.z0),
-                                                (float)nq.x, (float)nq.y);
-                    d.fastFL[slot] = (float)lq;
-                    d.fastAB[slot] = make_int2(a, d.segB[q]);
-                    d.fastA[slot] = pa;
-                    d.fastN[slot] = nq;
-                    d.fastL[slot] = lq;
+        // the node's ends, two at a time: both slots are claimed before either is written, so
+        // the atomics' round trips overlap
+        for (int k0 = 0; k0 < count; k0 += 2) {
+            int qs[2], as[2], pos[2];
+#pragma unroll
+            for (int j = 0; j < 2; j++) {
+                qs[j] = k0 + j < count ? own[k0 + j] : -1;
+                as[j] = qs[j] >= 0 ? d.segA[qs[j]] : -1;
+                pos[j] = fast && qs[j] >= 0 ? atomicAdd(&d.fastCount[cell], 1) : 0;
+            }
+#pragma unroll
+            for (int j = 0; j < 2; j++) {
+                if (qs[j] < 0) continue;
+                const int q = qs[j], a = as[j];
+                const int entry = 2 * q + (a == n ? 0 : 1);
+                d.entryCell[entry] = cell;
+                if (fast) {
+                    if (pos[j] < d.fastLimit) {
+                        const size_t slot = (size_t)cell * d.fastCap + pos[j];
+                        const double2 pa = make_double2(d.cr[a], d.cz[a]);
+                        const double2 nq = make_double2(d.snr[q], d.snz[q]);
+                        const double lq = d.slen[q];
+                        d.fastEntry[slot] = entry;
+                        d.fastF[slot] = make_float4((float)(pa.x - g.r0), (float)(pa.y - g.z0),
+                                                    (float)nq.x, (float)nq.y);
+                        d.fastFL[slot] = (float)lq;
+                        d.fastAB[slot] = make_int2(a, d.segB[q]);
+                        d.fastA[slot] = pa;
+                        d.fastN[slot] = nq;
+                        d.fastL[slot] = lq;
+                    } else {
+                        s->fastOverflow = 1;
+                    }
                 } else {
-                    s->fastOverflow = 1;
+                    atomicAdd(&d.bucketCount[bucket_of(d, g, cell)], 1);
                 }
-            } else {
-                atomicAdd(&d.bucketCount[bucket_of(d, g, cell)], 1);
             }
         }
     }

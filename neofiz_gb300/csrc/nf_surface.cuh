@@ -14,16 +14,32 @@ namespace nf {
 // Node n's free edges in ascending q, from the corners of its elements (the node slots of the
 // force gather): at corner c of element e the edges 4 e + c (leaving it) and 4 e + (c + 3) % 4
 // (arriving at it).
+// Four slots at a time: their indices, then the eight edges' flags, are loaded before any is
+// used, so the loads overlap instead of chaining; the edges are taken in the slots' order.
 static __device__ void build_node_segs(const Dev &d, int n) {
     int32_t *out = d.nodeSeg + (size_t)n * d.segCap;
     int count = 0;
-    for (int k = d.nodeSlotStart[n]; k < d.nodeSlotStart[n + 1]; k++) {
-        const int v = d.nodeSlot[k];
-        if (v >= 8 * d.E) continue;                  // a pressure edge's slot
-        const int e = v >> 3, c = v & 7;
-        const int q1 = 4 * e + c, q0 = 4 * e + ((c + 3) & 3);
-        if (d.surfFlag[q1] && count < d.segCap) out[count++] = q1;
-        if (d.surfFlag[q0] && count < d.segCap) out[count++] = q0;
+    const int k1 = d.nodeSlotStart[n + 1];
+    for (int k = d.nodeSlotStart[n]; k < k1; k += 4) {
+        int q1[4], q0[4], f1[4], f0[4];
+#pragma unroll
+        for (int j = 0; j < 4; j++) {
+            const int v = k + j < k1 ? d.nodeSlot[k + j] : 8 * d.E;
+            const bool edge = v < 8 * d.E;           // not a pressure edge's slot
+            const int e = v >> 3, c = v & 7;
+            q1[j] = edge ? 4 * e + c : -1;
+            q0[j] = edge ? 4 * e + ((c + 3) & 3) : -1;
+        }
+#pragma unroll
+        for (int j = 0; j < 4; j++) {
+            f1[j] = q1[j] >= 0 ? d.surfFlag[q1[j]] : 0;
+            f0[j] = q0[j] >= 0 ? d.surfFlag[q0[j]] : 0;
+        }
+#pragma unroll
+        for (int j = 0; j < 4; j++) {
+            if (f1[j] && count < d.segCap) out[count++] = q1[j];
+            if (f0[j] && count < d.segCap) out[count++] = q0[j];
+        }
     }
     for (int i = 1; i < count; i++) {
         const int v = out[i];

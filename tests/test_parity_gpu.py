@@ -304,6 +304,20 @@ def test_run_until_matches_step_loop(gpu_lib):
     assert_bitwise(a, b, "run_until")
 
 
+def test_run_until_keeps_the_last_steps_totals(gpu_lib):
+    """runUntil replays predicated steps in chunks of sixteen. The steps past the bound do
+    nothing, and the totals still describe the last step taken: contact pairs, penetration
+    and wall counts equal the oracle's after the same run."""
+    g, o, _, _ = pair(scenes.two_blocks, speed=400.0)
+    t_end = 2.0e-6                     # 21 steps: pairs and wall contacts are both active
+    n = g.runUntil(t_end)
+    assert n % 16 != 0, "the bound should fall inside a chunk of sixteen"
+    assert o.runUntil(t_end) == n
+    assert g._contactInfo().pair_count > 0 and g._wallInfo().contact_count > 0
+    assert_bitwise(g, o, "run_until")
+    assert_totals(g, o, "run_until")
+
+
 def test_repeat_runs_are_identical(gpu_lib):
     """ThreadingTest's property on the device: the answer does not depend on the schedule."""
     a, _, _ = scenes.perforation(ExplicitSolver, cell=1.0e-3)
