@@ -2,9 +2,9 @@
 
 FP32 element arithmetic changes every step's rounding, so the two runs agree to a relative
 error rather than bit for bit. The bars: L/L0 of the 10 x 60 Taylor rod within 1e-4 relative
-of the FP64 run (the benchmark spec's batched mixed-precision bar), its mushroom diameter within
-1e-3; on the coarse perforation, the slug's residual velocity within 1 %, the eroded count
-within a few per cent, and the energy balance to within 1 % of the FP64 run's.
+of the FP64 run (the error bar the mixed-precision forms are held to), its mushroom diameter
+within 1e-3; on the coarse perforation, the slug's residual velocity within 1 %, the eroded
+count within a few per cent, and the energy balance to within 1 % of the FP64 run's.
 """
 import numpy as np
 import pytest
