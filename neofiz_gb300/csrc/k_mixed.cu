@@ -30,62 +30,71 @@ __global__ void k_prepare_mixed(Dev d, int zeroStrain) {
     prepare_node(d, i, zeroStrain ? 0.0 : d.s->dt, MixedGeo{d.pMid, d.pCur, d.vdt, 0});
 }
 
-// Element damage (mean over points) and signed current area, FP32 (:663-691).
-__global__ void __launch_bounds__(MB) k_erode_mixed(Dev d) {
+// Element damage (mean over points) and signed current area, FP32 (:663-691): whether live
+// element e goes, adding the strain energy it held to energy.
+__device__ __forceinline__ void erode_element_mixed(const Dev &d, int e, double &energy) {
+    if (d.gone[e]) return;
+    bool failed = false;
+    if (d.hasDamage) {
+        float sum = 0.0f;
+        for (int g = 0; g < d.ppe; g++) {
+            const int p = e * d.ppe + g;
+            sum += damage_at(d.dStrF[p], d.dSoftF[p], d.dFailF[e], d.epsPF[p]);
+        }
+        failed = sum / d.ppe >= (float)d.erosionDamage;
+    }
+    const int4 c = d.conn[e];
+    const float4 p0 = d.pCur[c.x], p1 = d.pCur[c.y], p2 = d.pCur[c.z], p3 = d.pCur[c.w];
+    const float r1 = diff_hl(p1, p0, 0), r2 = diff_hl(p2, p0, 0), r3 = diff_hl(p3, p0, 0);
+    const float z1 = diff_hl(p1, p0, 1), z2 = diff_hl(p2, p0, 1), z3 = diff_hl(p3, p0, 1);
+    // shoelace with node 0 at the origin
+    const float a = (r1 * z2 - r2 * z1) + (r2 * z3 - r3 * z2);
+    const bool inverted = 0.5f * a <= 0.0f;
+    if (failed || inverted) {
+        d.gone[e] = 1;
+        atomicAdd(&d.s->erodedCount, 1);
+        if (inverted && !failed) atomicAdd(&d.s->invertedCount, 1);
+        const MatF &m = d.matsF[d.emat[e]];
+        for (int g = 0; g < d.ppe; g++) {
+            const int p = e * d.ppe + g;
+            const float4 s = reinterpret_cast<const float4 *>(d.sigF)[p];
+            const double s0 = s.x, s1 = s.y, s2 = s.z, s3 = s.w;
+            const double press = (s0 + s1 + s2) / 3.0;
+            const double aa = s0 - press, bb = s1 - press, cc = s2 - press;
+            const double density = (aa * aa + bb * bb + cc * cc + 2.0 * s3 * s3) / (4.0 * (double)m.mu)
+                                   + press * press / (2.0 * (double)m.bulk);
+            energy += density * d.gaussVol[p];
+        }
+        if (d.hasContact) {
+            d.dead[e] = 1;
+            d.s->stale = 1;
+            d.newDead[atomicAdd(&d.s->newDeadCount, 1)] = e;   // at most E, ever
+        }
+    }
+}
+
+// The block's eroded energy into its partial, in a fixed order (deterministic). A block whose
+// terms are all +0 has a sum of +0: one vote instead of the tree.
+__device__ __forceinline__ void erode_partial_mixed(const Dev &d, double energy) {
     __shared__ double sh[MB / 32];
+    double t = 0.0;
+    if (__syncthreads_or(__double_as_longlong(energy) != 0)) {
+        for (int o = 16; o > 0; o >>= 1) energy += __shfl_down_sync(0xffffffffu, energy, o);
+        const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
+        if (lane == 0) sh[warp] = energy;
+        __syncthreads();
+        for (int w = 0; w < MB / 32; w++) t += sh[w];
+    }
+    if (threadIdx.x == 0) d.partials[PARTIAL_ERODE * d.maxBlocks + blockIdx.x] = t;
+}
+
+// The erosion pass on its own (the full-integration mixed form).
+__global__ void __launch_bounds__(MB) k_erode_mixed(Dev d) {
     if (!d.s->active) return;
     double energy = 0.0;
-    for (int e = blockIdx.x * blockDim.x + threadIdx.x; e < d.E; e += gridDim.x * blockDim.x) {
-        if (d.gone[e]) continue;
-        bool failed = false;
-        if (d.hasDamage) {
-            float sum = 0.0f;
-            for (int g = 0; g < d.ppe; g++) {
-                const int p = e * d.ppe + g;
-                sum += damage_at(d.dStrF[p], d.dSoftF[p], d.dFailF[e], d.epsPF[p]);
-            }
-            failed = sum / d.ppe >= (float)d.erosionDamage;
-        }
-        const int4 c = d.conn[e];
-        const float4 p0 = d.pCur[c.x], p1 = d.pCur[c.y], p2 = d.pCur[c.z], p3 = d.pCur[c.w];
-        const float r1 = diff_hl(p1, p0, 0), r2 = diff_hl(p2, p0, 0), r3 = diff_hl(p3, p0, 0);
-        const float z1 = diff_hl(p1, p0, 1), z2 = diff_hl(p2, p0, 1), z3 = diff_hl(p3, p0, 1);
-        // shoelace with node 0 at the origin
-        const float a = (r1 * z2 - r2 * z1) + (r2 * z3 - r3 * z2);
-        const bool inverted = 0.5f * a <= 0.0f;
-        if (failed || inverted) {
-            d.gone[e] = 1;
-            atomicAdd(&d.s->erodedCount, 1);
-            if (inverted && !failed) atomicAdd(&d.s->invertedCount, 1);
-            const MatF &m = d.matsF[d.emat[e]];
-            for (int g = 0; g < d.ppe; g++) {
-                const int p = e * d.ppe + g;
-                const float4 s = reinterpret_cast<const float4 *>(d.sigF)[p];
-                const double s0 = s.x, s1 = s.y, s2 = s.z, s3 = s.w;
-                const double press = (s0 + s1 + s2) / 3.0;
-                const double aa = s0 - press, bb = s1 - press, cc = s2 - press;
-                const double density = (aa * aa + bb * bb + cc * cc + 2.0 * s3 * s3) / (4.0 * (double)m.mu)
-                                       + press * press / (2.0 * (double)m.bulk);
-                energy += density * d.gaussVol[p];
-            }
-            if (d.hasContact) {
-                d.dead[e] = 1;
-                d.s->stale = 1;
-                d.newDead[atomicAdd(&d.s->newDeadCount, 1)] = e;   // at most E, ever
-            }
-        }
-    }
-    // deterministic block sum, as the FP64 path
-    for (int o = 16; o > 0; o >>= 1) energy += __shfl_down_sync(0xffffffffu, energy, o);
-    const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
-    __syncthreads();
-    if (lane == 0) sh[warp] = energy;
-    __syncthreads();
-    if (threadIdx.x == 0) {
-        double t = 0.0;
-        for (int w = 0; w < MB / 32; w++) t += sh[w];
-        d.partials[PARTIAL_ERODE * d.maxBlocks + blockIdx.x] = t;
-    }
+    for (int e = blockIdx.x * blockDim.x + threadIdx.x; e < d.E; e += gridDim.x * blockDim.x)
+        erode_element_mixed(d, e, energy);
+    erode_partial_mixed(d, energy);
 }
 
 __device__ __forceinline__ void min_edge_commit_f(Dev &d, float minEdge) {
@@ -93,16 +102,21 @@ __device__ __forceinline__ void min_edge_commit_f(Dev &d, float minEdge) {
     if ((threadIdx.x & 31) == 0) atomicMin(&d.s->minEdgeBits, dbits_m((double)minEdge));
 }
 
-// reducedIntegration (ExplicitSolver.java:1373-1504) in FP32.
-__global__ void __launch_bounds__(MB) k_element_reduced_mixed(Dev d, int zeroStrain) {
+// reducedIntegration (ExplicitSolver.java:1373-1504) in FP32. With `erode` each element first
+// decides its own erosion: that reads only its own points and nodes, which no other element's
+// update writes, so it is the same as an erosion pass over all elements before any update.
+__global__ void __launch_bounds__(MB) k_element_reduced_mixed(Dev d, int zeroStrain, int erode) {
     if (!d.s->active) return;
     const int e = blockIdx.x * blockDim.x + threadIdx.x;
     float minEdge = 3.4028235e38f;
+    double energy = 0.0;
     if (e < d.E) {
+        if (erode) erode_element_mixed(d, e, energy);
         element_reduced_f32(d, e, zeroStrain ? 0.0f : (float)d.s->dt, (float)d.hourglass, d.pMid,
                             d.vdt, 0, minEdge);
     }
     min_edge_commit_f(d, minEdge);
+    if (erode) erode_partial_mixed(d, energy);
 }
 
 // fullIntegration (ExplicitSolver.java:1219-1339) in FP32.
@@ -274,10 +288,10 @@ int launch_erode_mixed(Solver &S) {
     k_erode_mixed<<<element_grid(S), MB, 0, S.stream>>>(S.d);
     return 1;
 }
-int launch_element_mixed(Solver &S, int zeroStrain) {
+int launch_element_mixed(Solver &S, int zeroStrain, bool erode) {
     if (S.d.E <= 0) return 0;
     if (S.d.full) k_element_full_mixed<<<grid_for(S.d.E, MB), MB, 0, S.stream>>>(S.d, zeroStrain);
-    else k_element_reduced_mixed<<<grid_for(S.d.E, MB), MB, 0, S.stream>>>(S.d, zeroStrain);
+    else k_element_reduced_mixed<<<grid_for(S.d.E, MB), MB, 0, S.stream>>>(S.d, zeroStrain, erode ? 1 : 0);
     return 1;
 }
 int launch_pressure_mixed(Solver &S) {

@@ -718,11 +718,15 @@ __global__ void k_set_active(Dev d) {
 
 // ------------------------------------------------------------------------------------ launch
 
-// The listed element pass erodes too (one pass instead of two over the elements) when the
-// step erodes and the pass is the FP64 one-point listed one.
-static bool erosion_fused(const Dev &d) { return d.hasErosion && d.E > 0 && d.hot && !d.mixed && !d.full; }
+// The one-point element pass erodes too (one pass instead of two over the elements) when the
+// step erodes and the pass is the FP64 listed one or the mixed one; its blocks then hold the
+// eroded-energy partials.
+static bool erosion_fused(const Dev &d) {
+    return d.hasErosion && d.E > 0 && !d.full && (d.mixed || d.hot);
+}
 static int eroding_blocks(const Solver &S) {
-    return erosion_fused(S.d) ? grid_for((long long)S.d.E + S.d.hotCap, BLOCK) : element_grid(S);
+    if (!erosion_fused(S.d)) return element_grid(S);
+    return S.d.mixed ? grid_for(S.d.E, 128) : grid_for((long long)S.d.E + S.d.hotCap, BLOCK);
 }
 
 static int assemble(Solver &S, int zeroStrain, bool prepared = false, bool erode = false) {
@@ -732,7 +736,7 @@ static int assemble(Solver &S, int zeroStrain, bool prepared = false, bool erode
     S.mark(NF_GROUP_ELEMENT, true);
     if (d.mixed) {
         if (!prepared) n += launch_prepare_mixed(S, zeroStrain);
-        n += launch_element_mixed(S, zeroStrain);
+        n += launch_element_mixed(S, zeroStrain, erode);
     } else if (d.E > 0) {
         if (d.full) {
             k_element_full<<<grid_for(d.E, BLOCK), BLOCK, 0, st>>>(d, zeroStrain);

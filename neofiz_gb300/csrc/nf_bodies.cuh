@@ -4,6 +4,7 @@
 #pragma once
 
 #include "nf_internal.h"
+#include "nf_fpconv.h"
 
 namespace nf {
 
@@ -108,11 +109,13 @@ static __device__ __forceinline__ void nodal_node(const Dev &d, int i, const Nod
             pr = x0.x;
             pz = x0.y;
         }
-        const double cr = x0.x + u.x, cz = x0.y + u.y;
-        const float prh = (float)pr, pzh = (float)pz, crh = (float)cr, czh = (float)cz;
-        geo.pMid[geo.base + i] = make_float4(prh, (float)(pr - (double)prh), pzh, (float)(pz - (double)pzh));
-        if (geo.pCur) geo.pCur[geo.base + i] = make_float4(crh, (float)(cr - (double)crh), czh, (float)(cz - (double)czh));
-        geo.vdt[geo.base + i] = make_float2((float)(v.x * dt), (float)(v.y * dt));
+        const float2 sr = nf_split(pr), sz = nf_split(pz);
+        geo.pMid[geo.base + i] = make_float4(sr.x, sr.y, sz.x, sz.y);
+        if (geo.pCur) {
+            const float2 qr = nf_split(x0.x + u.x), qz = nf_split(x0.y + u.y);
+            geo.pCur[geo.base + i] = make_float4(qr.x, qr.y, qz.x, qz.y);
+        }
+        geo.vdt[geo.base + i] = make_float2(nf_narrow(v.x * dt), nf_narrow(v.y * dt));
     }
 }
 
@@ -130,12 +133,13 @@ static __device__ __forceinline__ void prepare_node(const Dev &d, int i, double 
         pr = x.x;
         pz = x.y;
     }
-    const double cr = x.x + u.x, cz = x.y + u.y;
-    const float prh = (float)pr, pzh = (float)pz, crh = (float)cr, czh = (float)cz;
-    geo.pMid[geo.base + i] = make_float4(prh, (float)(pr - (double)prh), pzh, (float)(pz - (double)pzh));
-    if (geo.pCur)
-        geo.pCur[geo.base + i] = make_float4(crh, (float)(cr - (double)crh), czh, (float)(cz - (double)czh));
-    geo.vdt[geo.base + i] = make_float2((float)(v.x * sdt), (float)(v.y * sdt));
+    const float2 sr = nf_split(pr), sz = nf_split(pz);
+    geo.pMid[geo.base + i] = make_float4(sr.x, sr.y, sz.x, sz.y);
+    if (geo.pCur) {
+        const float2 qr = nf_split(x.x + u.x), qz = nf_split(x.y + u.y);
+        geo.pCur[geo.base + i] = make_float4(qr.x, qr.y, qz.x, qz.y);
+    }
+    geo.vdt[geo.base + i] = make_float2(nf_narrow(v.x * sdt), nf_narrow(v.y * sdt));
 }
 
 // reducedIntegration, ExplicitSolver.java:1373-1504, for element e: B at the centroid, strain
@@ -763,16 +767,32 @@ static __device__ __forceinline__ double2 gather_node(const Dev &d, int n) {
     return make_double2(sr + m * d.gravR, sz + m * d.gravZ);
 }
 
-// The same gather of float contributions into FP64 sums (the mixed form).
+// The same gather of float contributions into FP64 sums (the mixed form), four slots at a
+// time like gather_node. Each float is widened to double by integer arithmetic (exact, the
+// value the conversion gives): only the sums use the FP64 pipe.
 static __device__ __forceinline__ double2 gather_node_f32(const Dev &d, int n) {
     double sr = 0.0, sz = 0.0;
     const int end = d.nodeSlotStart[n + 1];
-    for (int k = d.nodeSlotStart[n]; k < end; k++) {
-        const int slot = d.nodeSlot[k];
-        sr += (double)d.contribF[slot];
-        sz += (double)d.contribF[slot + 4];
-    }
     const double m = d.mass[n];
+    for (int k = d.nodeSlotStart[n]; k < end; k += 4) {
+        const int cnt = end - k < 4 ? end - k : 4;
+        int slot[4];
+        float vr[4], vz[4];
+#pragma unroll
+        for (int j = 0; j < 4; j++) slot[j] = j < cnt ? d.nodeSlot[k + j] : 0;
+#pragma unroll
+        for (int j = 0; j < 4; j++) {
+            vr[j] = j < cnt ? d.contribF[slot[j]] : 0.0f;
+            vz[j] = j < cnt ? d.contribF[slot[j] + 4] : 0.0f;
+        }
+#pragma unroll
+        for (int j = 0; j < 4; j++) {
+            if (j < cnt) {
+                sr += nf_widen(vr[j]);
+                sz += nf_widen(vz[j]);
+            }
+        }
+    }
     return make_double2(sr + m * d.gravR, sz + m * d.gravZ);
 }
 

@@ -421,7 +421,7 @@ void launch_material_points(const MatDev &m, int count, double *sig, double *bac
 // Launchers (k_mixed.cu)
 int launch_prepare_mixed(Solver &S, int zeroStrain);
 int launch_erode_mixed(Solver &S);
-int launch_element_mixed(Solver &S, int zeroStrain);
+int launch_element_mixed(Solver &S, int zeroStrain, bool erode);
 int launch_pressure_mixed(Solver &S);
 int launch_gather_mixed(Solver &S);
 void launch_convert_state(Solver &S, bool toFloat, int what);
