@@ -1,13 +1,13 @@
 // nf_fpconv.h -- float <-> double conversions in 32-bit integer arithmetic, bit for bit the
 // IEEE round-to-nearest-even conversions.
 //
-// On GB300 a conversion between float and double costs about what an FP64 operation does: the
-// mixed form's gather, which converts each float contribution before adding it in double, took
-// 49 us a step on a 1M-quad scene where the FP64 gather, reading twice the bytes, took 33 us,
-// and 31 us with the widening below. The mixed form converts about twenty values per node and
-// step (a node's positions as float pairs and v dt, and its force contributions), so those
-// conversions outweighed the FP32 element arithmetic. These forms take a few 32-bit integer
-// operations each.
+// On GB300 a conversion between float and double issues on the FP64 pipe, like an FP64 add: the
+// mixed form's gather, which widened each float contribution before adding it in double, ran
+// half its FP64-pipe instructions as conversions, and took 49 us a step on a 1M-quad scene where
+// the FP64 gather, reading twice the bytes, took 33 us (31 us with the widening below). The
+// mixed form converted about twenty values per node and step (a node's positions as float pairs
+// and v dt, and its force contributions). These forms take a few 32-bit integer operations
+// each.
 //
 // Each function returns the bit pattern the conversion gives. The split and the narrowing cover
 // the ranges the geometry of a scene lives in and return false outside them (the caller then
