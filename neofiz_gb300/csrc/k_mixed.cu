@@ -3,9 +3,10 @@
 // gather, contact and every audit stay FP64.
 //
 // The element kernel never touches FP64. Absolute coordinates in FP32 would lose the element
-// geometry (a 0.05 mm element 20 mm from the origin keeps only ~5 significant digits), so a
-// per-node kernel (k_prepare_mixed, FP64) writes each node's mid-step and current positions as
-// a pair of floats (hi = fl(P), lo = fl(P - hi)); an element forms its edge vectors as
+// geometry (a 0.05 mm element 20 mm from the origin keeps only ~5 significant digits), so the
+// nodal update (k_prepare_mixed before the first step) writes each node's mid-step and current
+// positions as a pair of floats (hi = fl(P), lo = fl(P - hi), split by integer arithmetic in
+// nf_fpconv.h with the conversions' bits); an element forms its edge vectors as
 // (hi_i - hi_0) + (lo_i - lo_0), which is exact in the first term (Sterbenz) and rounds once,
 // i.e. the difference to FP32 precision. The element kernel restates reducedIntegration
 // (ExplicitSolver.java:1373-1504) and fullIntegration (:1219-1339) in float on those
